@@ -1,0 +1,307 @@
+"""Benchmark of the GB300 line raytrace on the large band workload.
+
+Workload (one step): the 400x200 (r, theta) disk with seeded +-10% lognormal per-cell
+perturbations of T and rho, 20 ro-vibrational lines (P and R branch, J=1..10) x 200
+channels (+-24.875 km/s), circular image of 1000 rings x 256 azimuths (+1 central beam),
+inclinations 20 and 60 degrees: 40 spectra, 2.048e9 ray-channels. Synthetic inputs
+(radlite_gb300.synth); FP64 geometry, FP32 transfer.
+
+  value   ray-channels/s with the model resident on the device, timed with CUDA events on
+          the library's stream (geometry + walk + reduction of both inclinations)
+  e2e     the same metric through the C ABI from host arrays: model upload, both
+          inclinations and the spectra read back, wall clock
+  --impl reference   the reference algorithm on the host cores: the FP64 C restatement of
+          RADLite's Fortran raytrace (the Fortran itself does not compile here), one
+          process per core, on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ray-channels/s & spectra/s at 1e-4 rel err: plain vs batched+adjoint, 1 GB300"
+UNIT = "ray-channels/s"
+INCLS = (20.0, 60.0)
+# per formal-solution step: minimal FP32-pipe instructions and MUFU operations of the
+# linear-source step with a Gaussian profile (Doppler offset, profile, emissivity and
+# extinction, optical depth, exponential coefficients, bracket, intensity update)
+BUDGET_FP32 = 19
+BUDGET_MUFU = 3
+
+
+def workload():
+    from radlite_gb300 import synth
+    cfg = synth.config_by_name("band_large")
+    return cfg, synth.model_arrays(cfg)
+
+
+def camera(cfg, incl):
+    return dict(incl_deg=incl, nphi=cfg.nphi, dbdr=cfg.dbdr, nrrayextra=cfg.nrrextra, vmax=cfg.vmax, dv=cfg.dv,
+                ilinestart=cfg.ilinestart, nlines=cfg.nlines)
+
+
+class Clocks:
+    """Samples SM clocks and throttle reasons with nvidia-smi during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device, self.rows, self.proc = device, [], None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait(timeout=5)
+
+    def summary(self):
+        sm = [float(r[0]) for r in self.rows if r and r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if len(r) > 1 and r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for i, n in enumerate(names):
+                if len(r) > 4 + i and r[4 + i].lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------------------------
+# CPU side: the oracle on a bounded sample (one process per core)
+# ------------------------------------------------------------------------------------
+def _cpu_worker(args):
+    d, iline, rays = args
+    from oracle import pyoracle
+    o = pyoracle.Oracle(d)
+    t0 = time.perf_counter()
+    n = 0
+    for r in rays:
+        o.line_image(iline, int(r), int(r) + 1)
+        n += o.nfr
+    return n, time.perf_counter() - t0
+
+
+def cpu_sample(cfg, stride, procs, tmpdir):
+    from radlite_gb300 import synth
+    import numpy as np
+    d = os.path.join(tmpdir, "band_large_i20")
+    if not os.path.exists(os.path.join(d, "radlite.inp")):
+        synth.write_model(synth.config_by_name("band_large", incl_deg=INCLS[0]), d)
+    from oracle import pyoracle
+    pyoracle.build()
+    nrays = 1 + (abs(cfg.nrrextra) + 10 + cfg.dbdr * (cfg.nr - 1)) * cfg.nphi
+    rays = np.arange(0, nrays, stride)
+    parts = [(d, cfg.ilinestart, rays[i::procs]) for i in range(procs)]
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(procs) as pool:
+        t0 = time.perf_counter()
+        res = pool.map(_cpu_worker, parts)
+        wall = time.perf_counter() - t0
+    n = sum(r[0] for r in res)
+    busy = max(r[1] for r in res)
+    return {"ray_channels": n, "rays": len(rays), "compute_s": busy, "wall_s": wall, "value": n / busy}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return world, rank, local, dist
+
+
+def reference_arm(args):
+    world, rank, _, dist = dist_setup()
+    if rank != 0:
+        return 0
+    cfg, _ = workload()
+    procs = os.cpu_count() or 1
+    stride = args.cpu_stride
+    with tempfile.TemporaryDirectory() as tmp:
+        vals = []
+        for i in range(args.warmup + args.steps):
+            s = cpu_sample(cfg, stride, procs, tmp)
+            if i >= args.warmup:
+                vals.append(s)
+    v = statistics.median(x["value"] for x in vals)
+    ms = statistics.median(x["compute_s"] for x in vals) * 1e3
+    sample = (f"band_large line {cfg.ilinestart} (of 20), incl {INCLS[0]:.0f} deg, every {stride}th ray "
+              f"({vals[0]['rays']} rays x 200 channels) per step")
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator in the reference file formats)",
+            "config": {"workload": "band_large: 400x200 disk, 20 band lines x 200 channels, 1000x256 rays, "
+                                   "incl 20+60 deg (bounded CPU sample)"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": procs, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "the reference Fortran cannot be compiled on this image (no Fortran compiler); timed is the "
+                    "FP64 C restatement of its raytrace (oracle/), one process per host core"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def load_traffic():
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(p) as fh:
+            return json.load(fh)
+    except (OSError, ValueError):
+        return {}
+
+
+def ours(args):
+    import numpy as np
+    import radlite_gb300 as rl
+    world, rank, local, dist = dist_setup()
+    cfg, arr = workload()
+    ctx = rl.Context(local)
+    peaks = ctx.measure_peaks()
+    m = ctx.load_arrays(arr, camera(cfg, INCLS[0]))
+
+    def step(model):
+        st_all = []
+        spectra = []
+        for inc in INCLS:
+            model.set_camera(inc, cfg.nphi, cfg.dbdr, cfg.nrrextra)
+            f, st = model.spectra(cfg.ilinestart, cfg.nlines, stats=True)
+            spectra.append(f)
+            st_all.append(st)
+        return spectra, st_all
+
+    for _ in range(args.warmup):
+        step(m)
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    dev_ms, walk_ms, steps_fs, integ = [], [], 0, 0
+    with Clocks(local) as clk:
+        for _ in range(args.steps):
+            _, sts = step(m)
+            dev_ms.append(sum(s["geometry_ms"] + s["upload_ms"] + s["walk_ms"] + s["reduce_ms"] for s in sts))
+            walk_ms.append(sum(s["walk_ms"] for s in sts))
+            steps_fs = sum(s["steps"] for s in sts)
+            integ = sum(s["integrated"] for s in sts)
+    wall = (time.perf_counter() - t0) / args.steps
+    ms = sum(dev_ms) / len(dev_ms)
+    if dist:
+        import torch
+        t = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    nrays = 1 + (abs(cfg.nrrextra) + 10 + cfg.dbdr * (cfg.nr - 1)) * cfg.nphi
+    nfr = int(2.0 * cfg.vmax / cfg.dv + 1)
+    rc_per_step = nrays * nfr * cfg.nlines * len(INCLS)
+    value = world * rc_per_step / (ms * 1e-3)
+    spectra_s = world * cfg.nlines * len(INCLS) / (ms * 1e-3)
+    # roofline of the walk kernel (dominant): FP32 / MUFU issue with the per-step budget
+    wk = sum(walk_ms) / len(walk_ms) * 1e-3
+    t_fp = steps_fs * BUDGET_FP32 / peaks["ffma_per_s"]
+    t_mu = steps_fs * BUDGET_MUFU / peaks["ex2_per_s"]
+    bound_mufu = t_mu >= t_fp
+    achieved = (steps_fs * (BUDGET_MUFU if bound_mufu else BUDGET_FP32)) / wk
+    peak = peaks["ex2_per_s"] if bound_mufu else peaks["ffma_per_s"]
+    traffic = load_traffic().get("k_walk_dram_bytes_per_launch")
+    # e2e: through the C ABI from host arrays, wall clock, copies included
+    e2e_t, h2d, d2h = [], 0, 0
+    for i in range(max(1, min(args.steps, 3))):
+        t1 = time.perf_counter()
+        m2 = ctx.load_arrays(arr, camera(cfg, INCLS[0]))
+        spectra, sts = step(m2)
+        e2e_t.append(time.perf_counter() - t1)
+        h2d = sum(s["h2d_bytes"] for s in sts)
+        d2h = sum(s["d2h_bytes"] for s in sts)
+        m2.free()
+    e2e = world * rc_per_step / statistics.median(e2e_t)
+    # accuracy at full size: FP32 vs FP64 of the first line at the first inclination
+    rel = None
+    if not args.no_verify:
+        m.set_camera(INCLS[0], cfg.nphi, cfg.dbdr, cfg.nrrextra)
+        f32 = m.spectra(cfg.ilinestart, 1)[0]
+        m.set_precision(1)
+        f64 = m.spectra(cfg.ilinestart, 1)[0]
+        m.set_precision(0)
+        sel = f64 > 1e-3 * f64.max()
+        rel = float(np.max(np.abs(f32[sel] - f64[sel]) / np.abs(f64[sel])))
+    out = None
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu:
+            with tempfile.TemporaryDirectory() as tmp:
+                s = cpu_sample(cfg, args.cpu_stride, os.cpu_count() or 1, tmp)
+            cpu = {"value": s["value"], "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+                   "sample": f"band_large line {cfg.ilinestart}, incl {INCLS[0]:.0f} deg, every {args.cpu_stride}th "
+                             f"ray ({s['rays']} rays x {nfr} channels), FP64 C restatement, one process per core"}
+        out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": ms, "wall_ms_per_step": wall * 1e3,
+               "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32 (fp64 geometry)",
+               "data": "synthetic (seeded generator in the reference file formats)",
+               "config": {"workload": "band_large: 400x200 disk (+-10% lognormal T, rho), 20 band lines x 200 "
+                                      "channels, 1000x256+1 rays, incl 20+60 deg",
+                          "l2": "inputs larger than L2 (node records ~10 GB per inclination)",
+                          "ray_channels_per_step": rc_per_step, "spectra_per_step": cfg.nlines * len(INCLS)},
+               "spectra_per_s": spectra_s,
+               "formal_solution_steps_per_step": steps_fs, "integrated_ray_channels_per_step": integ,
+               "rel_err_fp32_vs_fp64": rel,
+               "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+               "roofline": {"bound": "mufu_issue" if bound_mufu else "fp32_issue", "achieved": achieved / 1e12,
+                            "peak": peak / 1e12, "unit": "Tops/s", "frac": achieved / peak, "traffic": traffic,
+                            "kernel": "k_walk<float>", "walk_ms_per_step": wk * 1e3,
+                            "budget_per_step": {"fp32": BUDGET_FP32, "mufu": BUDGET_MUFU},
+                            "peaks_measured": peaks},
+               "cpu_baseline": cpu,
+               "clocks": clk.summary(),
+               "gpu_launches": args.steps * len(INCLS) * 4}
+        print(json.dumps(out), flush=True)
+    m.free()
+    ctx.close()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-stride", type=int, default=16)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-verify", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    return reference_arm(args) if args.impl == "reference" else ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,131 @@
+/*
+ * rlgpu.h -- C ABI of the GB300 line raytrace, a drop-in for RADLite's raytrace step.
+ *
+ * Reference interfaces replaced (RADLITE/ of pontoppi/radlite):
+ *   - the process/file boundary: the RADlite executable run in a directory holding the
+ *     input files, writing linespectrum_<mol>.dat and radlite.success
+ *     (main.F:26-71; drivers pyradlite/pyradlite/radlite.py:592-595, PRO/line_run.pro:173)
+ *     -> rl_run_dir()
+ *   - the in-process per-line call `call calc_line_spectrum(iln, linespec_distance,
+ *     main_passbwidth, main_passbnfr)` (main.F:1043-1049, telescope.F:1465-1654), whose
+ *     result is the COMMON array spec_flux_observer(1:nfr) (telescope.F:1433)
+ *     -> rl_line_spectrum() / rl_spectra()
+ *   - the input readers (setup.F, grid.F, dust.F, star.F, line.F readers)
+ *     -> rl_load_dir(); in-memory arrays of the same content -> rl_load_arrays()
+ *   - the circular image (imcir_int, telescope.F:339-631; SAVE_IMCIR dump
+ *     telescope.F:1348-1373) -> rl_line_image()
+ *
+ * Conventions: every call returns 0 on success and a negative code on failure, with a
+ * message available from rl_last_error(); the library never exits the process. Buffers
+ * are owned by the caller and live in host memory; device memory is owned by the library
+ * behind the opaque handles. A handle is used by one host thread at a time.
+ */
+#ifndef RLGPU_H
+#define RLGPU_H
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct rl_ctx rl_ctx;
+typedef struct rl_model rl_model;
+
+enum { RL_OK = 0, RL_ERR_ARG = -1, RL_ERR_IO = -2, RL_ERR_CUDA = -3, RL_ERR_GEOMETRY = -4, RL_ERR_STATE = -5 };
+enum { RL_FP32 = 0, RL_FP64 = 1 };
+
+typedef struct rl_stats {
+  unsigned long long steps;        /* formal-solution steps incl. sub-steps (qdr_src_2 calls) */
+  unsigned long long integrated;   /* (ray, channel, line) triples integrated */
+  unsigned long long node_visits;  /* integrated triples x nodes of their ray */
+  unsigned long long ray_channels; /* rays x channels x lines written to the image */
+  double geometry_ms, walk_ms, reduce_ms, upload_ms, total_ms;
+  int nrays, nfr, kmax, nlines;
+  unsigned long long h2d_bytes, d2h_bytes;   /* host<->device copies made by the call */
+} rl_stats;
+
+typedef struct rl_model_info {
+  int nr, nth, nlev, nlines_mol, nlines_spec, ilinestart, nfr, nphi, dbdr, nrrayextra, nrays, nrings;
+  int outer_bc, starpump, line_dust, precision;
+  double incl_deg, vmax, dv, rstar, aksmax;
+} rl_model_info;
+
+/* In-memory model: the content of the input files as arrays (cgs units as in the files).
+   Cell arrays are indexed (ir-1)*nth + (it-1) over the stored upper half of the grid. */
+typedef struct rl_model_arrays {
+  int nr, nth;
+  const double* radius;     /* [nr]   radius.inp */
+  const double* theta;      /* [nth]  theta.inp (0 .. pi/2, mirrored about the equator) */
+  const double* rho;        /* [ncell] gas density (density.inp) */
+  const double* abund;      /* [ncell] molecular abundance (abundance.inp) */
+  const double* width;      /* [ncell] local line width [km/s] (turbulence.inp) */
+  const double* vel;        /* [ncell*3] v_r, v_theta, v_phi [cm/s] (velocity.inp) */
+  int nlev;
+  const double* pop;        /* [ncell*nlev] level populations (levelpop_<mol>.dat) */
+  int nlines_mol;
+  const int* lev_up;        /* [nlines_mol] 1-based (moldata.dat) */
+  const int* lev_low;
+  const double* aud;        /* [nlines_mol] Einstein A [1/s] */
+  const double* energy_cm;  /* [nlev] level energies [1/cm] */
+  const double* gdeg;       /* [nlev] statistical weights */
+  double umass;             /* mean molecular weight (line.inp) */
+  int line_dust;            /* include dust in the lines (radlite.inp) */
+  int ncont;                /* frequency.inp */
+  const double* freq;       /* [ncont] */
+  const double* dust_rho;   /* [ncell] one species, one size (dustdens.inp) */
+  const double* dust_temp;  /* [ncell] (dusttemp_final.dat) */
+  const double* kappa_abs;  /* [ncont] (dustopac_1.inp) */
+  const double* kappa_scat; /* [ncont] */
+  double rstar;             /* starinfo.inp [cm] */
+  const double* star_flux_1pc; /* [ncont] F_nu at 1 pc (starspectrum.inp) or NULL (no star pumping) */
+  int outer_bc;             /* 0 black, 2 microwave background */
+  double incl_deg;          /* linespectrum.inp */
+  int nphi, dbdr, nrrayextra;  /* radlite.inp circular image */
+  double vmax, dv, radvelo; /* passband half width, sampling, radial velocity [km/s] */
+  int ilinestart, nlines_spec;
+  const char* molname;      /* output file tag: linespectrum_<molname>.dat */
+} rl_model_arrays;
+
+int rl_create(rl_ctx** ctx, int device);
+int rl_destroy(rl_ctx* ctx);
+/* Copies the last error message of the context (or of the process for a NULL context). */
+int rl_last_error(rl_ctx* ctx, char* buf, size_t len);
+
+int rl_load_dir(rl_ctx* ctx, const char* dir, rl_model** model);
+int rl_load_arrays(rl_ctx* ctx, const rl_model_arrays* arrays, rl_model** model);
+int rl_model_free(rl_model* model);
+int rl_model_get_info(rl_model* model, rl_model_info* info);
+
+/* Camera override (radlite.inp / linespectrum.inp values are the default). */
+int rl_set_camera(rl_model* model, double incl_deg, int nphi, int dbdr, int nrrayextra);
+/* RL_FP32 (default): FP64 geometry, FP32 transfer. RL_FP64: FP64 throughout. */
+int rl_set_precision(rl_model* model, int precision);
+
+/* F_nu at 1 pc of line `iline` (1-based line of moldata.dat), channel order of the
+   passband (ascending frequency), like spec_flux_observer after calc_line_spectrum.
+   velo_out (may be NULL) receives the output-file velocities [km/s]. */
+int rl_line_spectrum(rl_model* model, int iline, double* flux_out, double* velo_out, rl_stats* stats);
+/* Lines iline0 .. iline0+nlines-1 in one launch; flux_out is [nlines][nfr]. */
+int rl_spectra(rl_model* model, int iline0, int nlines, double* flux_out, rl_stats* stats);
+/* Circular image of one line: [nrays][nfr] intensities (ray 0 = central beam, then
+   rings from the inside out, azimuth fastest), as imcir_int. */
+int rl_line_image(rl_model* model, int iline, double* image_out, rl_stats* stats);
+
+/* The RADlite executable's work in `dir`: read the inputs, render the lines requested by
+   linespectrum.inp, write linespectrum_<mol>.dat and radlite.success. */
+int rl_run_dir(const char* dir, int device, rl_stats* stats);
+
+/* Node list of one ray as the geometry kernel produces it (inspection and tests):
+   returns the node count (may exceed cap; arrays receive min(count, cap) entries). */
+int rl_debug_trajectory(rl_model* model, int iray, int cap, double* s, double* r, double* theta, double* mu,
+                        double* dvmu, int* icr, int* ir, int* it);
+
+/* Measured throughput of the two pipes that bound the formal solution: FP32 FFMA
+   instructions per second (lane operations) and MUFU ex2 operations per second over the
+   whole device. Roofline denominators; no counterpart in the reference. */
+int rl_measure_peaks(rl_ctx* ctx, double* ffma_per_s, double* ex2_per_s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

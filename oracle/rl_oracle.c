@@ -110,6 +110,11 @@ static int tok_d(const char* t, double* v) {
     for (char* q = b; *q; q++) if (*q == 'd' || *q == 'D') *q = 'e';
     char* e; *v = strtod(b, &e);
     if (e == b) return fail("not a number: '%s'", t);
+    if (*e == '+' || *e == '-') {   /* Fortran exponent without a letter */
+        char* e2; long ex = strtol(e, &e2, 10);
+        if (e2 != e + 1 && *e2 == 0) { *v *= pow(10.0, (double)ex); return 0; }
+    }
+    if (*e != 0) return fail("not a number: '%s'", t);
     return 0;
 }
 static int rd_d(frec* f, double* v) { char t[1][96]; if (fr_list(f, 1, t)) return -1; return tok_d(t[0], v); }
@@ -520,6 +525,10 @@ static int read_model(const char* dir, rlo_model* m) {
         int fnr; char fn[200];
         if (fr_open(&f, dir, "levelpop.info")) return -1;
         if (rd_i(&f, &fnr)) return -1;
+        if (fnr == -3) {   /* line.F:847-870 */
+            if (rd_s(&f, s, sizeof s)) return -1;
+            if (strncmp(s, "levelpop_", 9) != 0 || !strstr(s + 9, ".dat")) return fail("levelpop.info: bad file name '%s'", s);
+        }
         fr_close(&f);
         if (fnr == -1) strcpy(fn, "levelpop.dat");
         else if (fnr == -2) strcpy(fn, "levelpop_final.dat");

@@ -1,0 +1,291 @@
+"""GB300-native line raytrace for RADLite models (drop-in for the RADlite raytrace step).
+
+The compute path is the in-tree CUDA library ``_lib/librlgpu.so`` (sm_103a kernels behind
+the C ABI of ``include/rlgpu.h``). This module is a thin ctypes binding over that ABI that
+mirrors the reference's entry points:
+
+  run_dir(dir)                    the RADlite executable run in a working directory
+                                  (RADLITE/main.F:26-71): writes linespectrum_<mol>.dat
+  Model.calc_line_spectrum(iline) calc_line_spectrum (RADLITE/telescope.F:1465-1654):
+                                  F_nu at 1 pc over the passband (spec_flux_observer)
+  Model.line_image(iline)         the circular image imcir_int (telescope.F:339-631)
+
+There is no CPU fallback: importing works without a GPU, but every call that computes
+needs the built library and a CUDA device and raises otherwise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "librlgpu.so")
+EXE_PATH = os.path.join(_HERE, "_lib", "RADlite_gpu")
+
+RL_FP32, RL_FP64 = 0, 1
+
+
+class RLError(RuntimeError):
+    pass
+
+
+class Stats(C.Structure):
+    _fields_ = [("steps", C.c_ulonglong), ("integrated", C.c_ulonglong), ("node_visits", C.c_ulonglong),
+                ("ray_channels", C.c_ulonglong), ("geometry_ms", C.c_double), ("walk_ms", C.c_double),
+                ("reduce_ms", C.c_double), ("upload_ms", C.c_double), ("total_ms", C.c_double),
+                ("nrays", C.c_int), ("nfr", C.c_int), ("kmax", C.c_int), ("nlines", C.c_int),
+                ("h2d_bytes", C.c_ulonglong), ("d2h_bytes", C.c_ulonglong)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class ModelInfo(C.Structure):
+    _fields_ = [(n, C.c_int) for n in ("nr", "nth", "nlev", "nlines_mol", "nlines_spec", "ilinestart", "nfr",
+                                       "nphi", "dbdr", "nrrayextra", "nrays", "nrings", "outer_bc", "starpump",
+                                       "line_dust", "precision")] + \
+               [(n, C.c_double) for n in ("incl_deg", "vmax", "dv", "rstar", "aksmax")]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_D = C.POINTER(C.c_double)
+_I = C.POINTER(C.c_int)
+
+
+class ModelArrays(C.Structure):
+    _fields_ = [("nr", C.c_int), ("nth", C.c_int), ("radius", _D), ("theta", _D), ("rho", _D), ("abund", _D),
+                ("width", _D), ("vel", _D), ("nlev", C.c_int), ("pop", _D), ("nlines_mol", C.c_int),
+                ("lev_up", _I), ("lev_low", _I), ("aud", _D), ("energy_cm", _D), ("gdeg", _D),
+                ("umass", C.c_double), ("line_dust", C.c_int), ("ncont", C.c_int), ("freq", _D),
+                ("dust_rho", _D), ("dust_temp", _D), ("kappa_abs", _D), ("kappa_scat", _D),
+                ("rstar", C.c_double), ("star_flux_1pc", _D), ("outer_bc", C.c_int), ("incl_deg", C.c_double),
+                ("nphi", C.c_int), ("dbdr", C.c_int), ("nrrayextra", C.c_int), ("vmax", C.c_double),
+                ("dv", C.c_double), ("radvelo", C.c_double), ("ilinestart", C.c_int), ("nlines_spec", C.c_int),
+                ("molname", C.c_char_p)]
+
+
+EXPORTS = ["rl_create", "rl_destroy", "rl_last_error", "rl_load_dir", "rl_load_arrays", "rl_model_free",
+           "rl_model_get_info", "rl_set_camera", "rl_set_precision", "rl_line_spectrum", "rl_spectra",
+           "rl_line_image", "rl_run_dir", "rl_debug_trajectory", "rl_measure_peaks"]
+
+_lib = None
+
+
+def lib():
+    """The loaded CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RLError(f"{LIB_PATH} is missing: build it with radlite_gb300.build.build() (no CPU fallback)")
+        L = C.CDLL(LIB_PATH)
+        vp = C.c_void_p
+        L.rl_create.argtypes = [C.POINTER(vp), C.c_int]
+        L.rl_destroy.argtypes = [vp]
+        L.rl_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
+        L.rl_load_dir.argtypes = [vp, C.c_char_p, C.POINTER(vp)]
+        L.rl_load_arrays.argtypes = [vp, C.POINTER(ModelArrays), C.POINTER(vp)]
+        L.rl_model_free.argtypes = [vp]
+        L.rl_model_get_info.argtypes = [vp, C.POINTER(ModelInfo)]
+        L.rl_set_camera.argtypes = [vp, C.c_double, C.c_int, C.c_int, C.c_int]
+        L.rl_set_precision.argtypes = [vp, C.c_int]
+        L.rl_line_spectrum.argtypes = [vp, C.c_int, _D, _D, C.POINTER(Stats)]
+        L.rl_spectra.argtypes = [vp, C.c_int, C.c_int, _D, C.POINTER(Stats)]
+        L.rl_line_image.argtypes = [vp, C.c_int, _D, C.POINTER(Stats)]
+        L.rl_run_dir.argtypes = [C.c_char_p, C.c_int, C.POINTER(Stats)]
+        L.rl_debug_trajectory.argtypes = [vp, C.c_int, C.c_int, _D, _D, _D, _D, _D, _I, _I, _I]
+        L.rl_measure_peaks.argtypes = [vp, _D, _D]
+        _lib = L
+    return _lib
+
+
+def _err(ctx=None) -> str:
+    buf = C.create_string_buffer(2048)
+    lib().rl_last_error(ctx, buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+def _check(rc, ctx=None):
+    if rc < 0:
+        raise RLError(_err(ctx))
+    return rc
+
+
+def _dp(a):
+    return a.ctypes.data_as(_D)
+
+
+class Context:
+    """One CUDA device with its stream (rl_ctx)."""
+
+    def __init__(self, device: int = 0):
+        self.h = C.c_void_p()
+        _check(lib().rl_create(C.byref(self.h), device))
+
+    def close(self):
+        if self.h:
+            lib().rl_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def measure_peaks(self) -> dict:
+        """Measured FP32 FFMA and MUFU ex2 throughput of the device (lane ops per second)."""
+        a, b = C.c_double(), C.c_double()
+        _check(lib().rl_measure_peaks(self.h, C.byref(a), C.byref(b)), self.h)
+        return {"ffma_per_s": a.value, "ex2_per_s": b.value}
+
+    def load_dir(self, path: str) -> "Model":
+        h = C.c_void_p()
+        _check(lib().rl_load_dir(self.h, os.fsencode(path), C.byref(h)), self.h)
+        return Model(self, h)
+
+    def load_arrays(self, arrays: dict, camera: dict) -> "Model":
+        """Model from in-memory arrays (the content of the input files, see synth.model_arrays)."""
+        keep = []
+
+        def arr(x, dt=np.float64):
+            a = np.ascontiguousarray(x, dtype=dt)
+            keep.append(a)
+            return a.ctypes.data_as(_D if dt == np.float64 else _I)
+
+        f = arrays
+        cell = lambda a: np.asarray(a).T.ravel()   # [nt, nr] -> (ir-1)*nth + (it-1)
+        nt, nr = f["rho"].shape
+        pop = f["pop"].transpose(2, 1, 0).reshape(nr * nt, -1)
+        vel = np.stack([cell(f["vel"][0]), cell(f["vel"][1]), cell(f["vel"][2])], axis=1)
+        lines = f["lines"]
+        a = ModelArrays()
+        a.nr, a.nth = nr, nt
+        a.radius, a.theta = arr(f["r"]), arr(f["theta"])
+        a.rho, a.abund, a.width = arr(cell(f["rho"])), arr(cell(f["abund"])), arr(cell(f["width"]))
+        a.vel = arr(vel)
+        a.nlev = pop.shape[1]
+        a.pop = arr(pop)
+        a.nlines_mol = len(lines)
+        a.lev_up = arr([u for u, _, _ in lines], np.int32)
+        a.lev_low = arr([l for _, l, _ in lines], np.int32)
+        a.aud = arr([float(f"{A:.3e}") for _, _, A in lines])
+        a.energy_cm = arr(np.round(f["E"], 4))
+        a.gdeg = arr(f["g"])
+        a.umass = 2.3
+        a.line_dust = 1
+        a.ncont = len(f["freq"])
+        a.freq = arr(f["freq"])
+        a.dust_rho, a.dust_temp = arr(cell(f["dust_rho"])), arr(cell(f["dust_temp"]))
+        a.kappa_abs, a.kappa_scat = arr(f["kappa_abs"]), arr(f["kappa_scat"])
+        a.rstar = f["rstar"]
+        a.star_flux_1pc = arr(f["star_flux_1pc"]) if camera.get("starpump", 1) else C.cast(None, _D)
+        a.outer_bc = camera.get("outer_bc", 0)
+        a.incl_deg = camera["incl_deg"]
+        a.nphi, a.dbdr, a.nrrayextra = camera["nphi"], camera["dbdr"], camera["nrrayextra"]
+        a.vmax, a.dv, a.radvelo = camera["vmax"], camera["dv"], camera.get("radvelo", 0.0)
+        a.ilinestart, a.nlines_spec = camera["ilinestart"], camera["nlines"]
+        a.molname = camera.get("molname", "moldata").encode()
+        h = C.c_void_p()
+        _check(lib().rl_load_arrays(self.h, C.byref(a), C.byref(h)), self.h)
+        return Model(self, h)
+
+
+class Model:
+    """A loaded RADLite model on the GPU (rl_model)."""
+
+    def __init__(self, ctx: Context, h):
+        self.ctx, self.h = ctx, h
+
+    def free(self):
+        if self.h:
+            lib().rl_model_free(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def info(self) -> dict:
+        i = ModelInfo()
+        _check(lib().rl_model_get_info(self.h, C.byref(i)))
+        return i.as_dict()
+
+    @property
+    def _ch(self):
+        return self.ctx.h if self.ctx is not None else None
+
+    def set_camera(self, incl_deg, nphi, dbdr, nrrayextra):
+        _check(lib().rl_set_camera(self.h, incl_deg, nphi, dbdr, nrrayextra), self._ch)
+
+    def set_precision(self, precision: int):
+        _check(lib().rl_set_precision(self.h, precision), self._ch)
+
+    def calc_line_spectrum(self, iline: int, stats: bool = False):
+        """F_nu at 1 pc over the passband of line `iline` (1-based, moldata.dat order)."""
+        n = self.info()["nfr"]
+        flux, velo = np.zeros(n), np.zeros(n)
+        st = Stats()
+        _check(lib().rl_line_spectrum(self.h, iline, _dp(flux), _dp(velo), C.byref(st)), self._ch)
+        return (flux, velo, st.as_dict()) if stats else (flux, velo)
+
+    def spectra(self, iline0: int, nlines: int, stats: bool = False):
+        n = self.info()["nfr"]
+        flux = np.zeros((nlines, n))
+        st = Stats()
+        _check(lib().rl_spectra(self.h, iline0, nlines, _dp(flux), C.byref(st)), self._ch)
+        return (flux, st.as_dict()) if stats else flux
+
+    def line_image(self, iline: int):
+        info = self.info()
+        img = np.zeros((info["nrays"], info["nfr"]))
+        st = Stats()
+        _check(lib().rl_line_image(self.h, iline, _dp(img), C.byref(st)), self._ch)
+        return img
+
+    def trajectory(self, iray: int, cap: int = 8192) -> dict:
+        out = {k: np.zeros(cap) for k in ("s", "r", "theta", "mu", "dvmu")}
+        iv = {k: np.zeros(cap, dtype=np.int32) for k in ("icr", "ir", "it")}
+        n = _check(lib().rl_debug_trajectory(self.h, iray, cap, *(_dp(out[k]) for k in ("s", "r", "theta", "mu", "dvmu")),
+                                             *(iv[k].ctypes.data_as(_I) for k in ("icr", "ir", "it"))), self._ch)
+        n = min(n, cap)
+        res = {k: v[:n] for k, v in out.items()}
+        res.update({k: v[:n] for k, v in iv.items()})
+        return res
+
+
+def load_dir_host(path: str) -> "Model":
+    """Parse a model directory without a device (host-side checks of the input files)."""
+    h = C.c_void_p()
+    _check(lib().rl_load_dir(None, os.fsencode(path), C.byref(h)))
+    return Model(None, h)
+
+
+def run_dir(path: str, device: int = 0) -> dict:
+    """Render the lines requested by linespectrum.inp in `path`, like the RADlite executable."""
+    st = Stats()
+    rc = lib().rl_run_dir(os.fsencode(path), device, C.byref(st))
+    if rc < 0:
+        raise RLError(_err())
+    return st.as_dict()
+
+
+def read_spectrum_file(path: str):
+    """Parse linespectrum_<mol>.dat (the reference's output layout) into a list of dicts."""
+    with open(path) as fh:
+        lines = fh.read().split("\n")
+    nlines = int(lines[4])
+    out, i = [], 6
+    for _ in range(nlines):
+        up, lo = (int(x) for x in lines[i + 2].split())
+        freq = float(lines[i + 3].replace("E", "e") if not lines[i + 3].startswith(".") else "0" + lines[i + 3])
+        n = int(lines[i + 5])
+        rows = np.array([[float(v) for v in r.split()] for r in lines[i + 7:i + 7 + n]])
+        out.append({"up": up, "low": lo, "freq": freq, "velo": rows[:, 0], "flux": rows[:, 1]})
+        i += 7 + n - 1
+    return out

@@ -1,0 +1,647 @@
+// rl_capi.cpp -- the C ABI (include/rlgpu.h): device residency, camera geometry cache,
+// per-line table upload, kernel orchestration on one stream, and the directory runner.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <type_traits>
+#include <string>
+#include <vector>
+
+#include "../../include/rlgpu.h"
+#include "rl_device.h"
+#include "rl_geometry.cuh"
+#include "rl_host.h"
+
+namespace rl {
+template <typename T>
+cudaError_t launch_geometry(const GeoParams& p, const NodeBuf<T>& nb, int ray0, int nray, TrajDebug* dbg,
+                            cudaStream_t s);
+template <typename T>
+cudaError_t launch_walk(const WalkParams<T>& P, int cpl, int nsm, cudaStream_t s);
+template <typename T>
+cudaError_t launch_reduce(const ReduceParams& p, const T* img, double* ring, double* flux, cudaStream_t s);
+cudaError_t measure_peaks(int nsm, cudaStream_t st, double* ffma_per_s, double* ex2_per_s);
+}  // namespace rl
+
+using namespace rl;
+
+namespace {
+thread_local std::string g_last_error;
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t n = 0;
+  ~DevBuf() { if (p) cudaFree(p); }
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= n && p) return cudaSuccess;
+    if (p) { cudaFree(p); p = nullptr; n = 0; }
+    cudaError_t e = cudaMalloc(&p, bytes ? bytes : 16);
+    if (e == cudaSuccess) n = bytes;
+    return e;
+  }
+  template <typename T> T* as() const { return static_cast<T*>(p); }
+};
+}  // namespace
+
+struct rl_ctx {
+  int device = 0, nsm = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[6] = {};
+  std::string err;
+};
+
+struct rl_model {
+  rl_ctx* ctx = nullptr;
+  Model m;
+  int precision = RL_FP32;
+  // camera request
+  double incl_rad = 0.0;
+  int nphi = 0, dbdr = 1, nrext = 0;
+  // device copies of the grid and cell fields (uploaded once)
+  bool grid_ready = false;
+  DevBuf dR, dTH, dtan2, dvel, dlw;
+  // camera geometry cache
+  bool geo_ready = false;
+  int geo_prec = -1;
+  Camera cam;
+  DevBuf dx0, dz0, dri;
+  DevBuf nb_nn, nb_st, nb_ds, nb_dvf, nb_vl, nb_dvs, nb_lw, nb_wr, nb_wt, nb_c00, nb_misc;
+  int kmax = 0;
+  // per-line tables of the last line range (reused while the range and precision match)
+  int tab_line0 = -1, tab_nl = 0, tab_prec = -1;
+  std::vector<double> tab_scale;
+  // per-call buffers
+  DevBuf dtab, dnsum, dwch, dvelo, dstar, dlc, dimg, dring, dflux, dscale, dcnt, dwork, derr;
+};
+
+static int set_err(rl_ctx* c, int code, const std::string& msg) {
+  g_last_error = msg;
+  if (c) c->err = msg;
+  return code;
+}
+#define CUDA_TRY(call)                                                                      \
+  do {                                                                                      \
+    cudaError_t e_ = (call);                                                                \
+    if (e_ != cudaSuccess)                                                                  \
+      return set_err(ctx, RL_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+static thread_local unsigned long long g_h2d = 0, g_d2h = 0;   // per call, reset by the entry points
+static cudaError_t h2d(void* dst, const void* src, size_t n, cudaStream_t s) {
+  g_h2d += n;
+  return cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, s);
+}
+static cudaError_t d2h(void* dst, const void* src, size_t n, cudaStream_t s) {
+  g_d2h += n;
+  return cudaMemcpyAsync(dst, src, n, cudaMemcpyDeviceToHost, s);
+}
+
+static void camera_defaults(rl_model* md) {
+  md->incl_rad = md->m.incl_rad;
+  md->nphi = md->m.nphi;
+  md->dbdr = md->m.dbdr;
+  md->nrext = md->m.nrext;
+}
+
+static int upload_grid(rl_model* md) {
+  rl_ctx* ctx = md->ctx;
+  if (md->grid_ready) return 0;
+  const Model& m = md->m;
+  std::vector<double> tan2(m.nth + 1, 0.0);
+  for (int iy = 1; iy <= m.nth; iy++) { const double t = std::tan(m.TH[iy + 1]); tan2[iy] = t * t; }
+  CUDA_TRY(md->dR.ensure(sizeof(double) * m.R.size()));
+  CUDA_TRY(md->dTH.ensure(sizeof(double) * m.TH.size()));
+  CUDA_TRY(md->dtan2.ensure(sizeof(double) * tan2.size()));
+  CUDA_TRY(md->dvel.ensure(sizeof(double) * m.vel.size()));
+  CUDA_TRY(md->dlw.ensure(sizeof(double) * m.lw.size()));
+  cudaStream_t s = ctx->stream;
+  CUDA_TRY(h2d(md->dR.p, m.R.data(), sizeof(double) * m.R.size(), s));
+  CUDA_TRY(h2d(md->dTH.p, m.TH.data(), sizeof(double) * m.TH.size(), s));
+  CUDA_TRY(h2d(md->dtan2.p, tan2.data(), sizeof(double) * tan2.size(), s));
+  CUDA_TRY(h2d(md->dvel.p, m.vel.data(), sizeof(double) * m.vel.size(), s));
+  CUDA_TRY(h2d(md->dlw.p, m.lw.data(), sizeof(double) * m.lw.size(), s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  md->grid_ready = true;
+  return 0;
+}
+
+template <typename T>
+static NodeBuf<T> node_view(rl_model* md) {
+  NodeBuf<T> nb;
+  nb.nrays = md->cam.nrays;
+  nb.kmax = md->kmax;
+  nb.nnodes = md->nb_nn.as<int>();
+  nb.status = md->nb_st.as<int>();
+  nb.ds = md->nb_ds.as<T>();
+  nb.dvf = md->nb_dvf.as<float>();
+  nb.vl = md->nb_vl.as<T>();
+  nb.dvseg = md->nb_dvs.as<T>();
+  nb.lw = md->nb_lw.as<T>();
+  nb.wr = md->nb_wr.as<T>();
+  nb.wt = md->nb_wt.as<T>();
+  nb.c00 = md->nb_c00.as<int>();
+  nb.misc = md->nb_misc.as<unsigned>();
+  return nb;
+}
+
+static GeoParams geo_params(rl_model* md) {
+  GeoParams p;
+  const Model& m = md->m;
+  p.nr = m.nr; p.nth = m.nth; p.ny = m.ny; p.rstar = m.rstar; p.theta0 = md->cam.theta0;
+  p.R = md->dR.as<double>(); p.TH = md->dTH.as<double>(); p.tan2 = md->dtan2.as<double>();
+  p.vel = md->dvel.as<double>(); p.lw = md->dlw.as<double>();
+  p.x0 = md->dx0.as<double>(); p.z0 = md->dz0.as<double>();
+  return p;
+}
+
+template <typename T>
+static int build_geometry(rl_model* md, rl_stats* st) {
+  rl_ctx* ctx = md->ctx;
+  cudaStream_t s = ctx->stream;
+  if (md->geo_ready && md->geo_prec == md->precision) return 0;
+  int rc = upload_grid(md);
+  if (rc) return rc;
+  std::string err;
+  if (setup_camera(md->m, md->incl_rad, md->nphi, md->dbdr, md->nrext, md->cam, err))
+    return set_err(ctx, RL_ERR_ARG, err);
+  const Camera& cam = md->cam;
+  md->kmax = rlg::max_nodes(md->m.nr, md->m.nth);
+  const size_t nn = (size_t)cam.nrays * md->kmax;
+  CUDA_TRY(md->dx0.ensure(sizeof(double) * cam.nrays));
+  CUDA_TRY(md->dz0.ensure(sizeof(double) * cam.nrays));
+  CUDA_TRY(md->dri.ensure(sizeof(double) * cam.ri.size()));
+  CUDA_TRY(md->nb_nn.ensure(sizeof(int) * cam.nrays));
+  CUDA_TRY(md->nb_st.ensure(sizeof(int) * cam.nrays));
+  CUDA_TRY(md->nb_ds.ensure(sizeof(T) * nn));
+  CUDA_TRY(md->nb_dvf.ensure(sizeof(float) * nn));
+  CUDA_TRY(md->nb_vl.ensure(sizeof(T) * nn));
+  CUDA_TRY(md->nb_dvs.ensure(sizeof(T) * nn));
+  CUDA_TRY(md->nb_lw.ensure(sizeof(T) * nn));
+  CUDA_TRY(md->nb_wr.ensure(sizeof(T) * nn));
+  CUDA_TRY(md->nb_wt.ensure(sizeof(T) * nn));
+  CUDA_TRY(md->nb_c00.ensure(sizeof(int) * nn));
+  CUDA_TRY(md->nb_misc.ensure(sizeof(unsigned) * nn));
+  CUDA_TRY(h2d(md->dx0.p, cam.x0.data(), sizeof(double) * cam.nrays, s));
+  CUDA_TRY(h2d(md->dz0.p, cam.z0.data(), sizeof(double) * cam.nrays, s));
+  CUDA_TRY(h2d(md->dri.p, cam.ri.data(), sizeof(double) * cam.ri.size(), s));
+  CUDA_TRY(cudaEventRecord(ctx->ev[0], s));
+  CUDA_TRY(launch_geometry<T>(geo_params(md), node_view<T>(md), 0, cam.nrays, nullptr, s));
+  CUDA_TRY(cudaEventRecord(ctx->ev[1], s));
+  std::vector<int> status(cam.nrays);
+  CUDA_TRY(d2h(status.data(), md->nb_st.p, sizeof(int) * cam.nrays, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
+  if (st) st->geometry_ms += ms;
+  for (int r = 0; r < cam.nrays; r++)
+    if (status[r] != 0)
+      return set_err(ctx, RL_ERR_GEOMETRY, "geometry: ray " + std::to_string(r) + " failed with status " + std::to_string(status[r]));
+  md->geo_ready = true;
+  md->geo_prec = md->precision;
+  return 0;
+}
+
+template <typename T>
+static int run_lines(rl_model* md, int iline0, int nl, double* flux_out, double* image_out, rl_stats* st) {
+  rl_ctx* ctx = md->ctx;
+  cudaStream_t s = ctx->stream;
+  const Model& m = md->m;
+  if (nl < 1 || iline0 < 1 || iline0 + nl - 1 > (int)m.lfreq.size())
+    return set_err(ctx, RL_ERR_ARG, "line range outside the molecule's line list");
+  int rc = build_geometry<T>(md, st);
+  if (rc) return rc;
+  const Camera& cam = md->cam;
+  const int ncell = m.ncell(), nfr = m.nfr;
+  // per-line tables (built on the host in FP64, kept on the device between calls)
+  const bool cached = md->tab_line0 == iline0 && md->tab_nl == nl && md->tab_prec == md->precision;
+  std::vector<T> tab, nsum, wch, star;
+  std::vector<double> velo, scale = md->tab_scale;
+  std::vector<LineConst<T>> lc;
+  const bool scaled = std::is_same<T, float>::value;
+  if (!cached) {
+    tab.resize((size_t)nl * ncell * 4); nsum.resize((size_t)nl * ncell); wch.resize((size_t)nl * nfr);
+    star.resize((size_t)nl * nfr); velo.resize((size_t)nl * nfr); scale.assign(nl, 1.0); lc.resize(nl);
+    md->tab_line0 = -1;
+  }
+  for (int l = 0; l < nl && !cached; l++) {
+    LinePrep lp;
+    std::string err;
+    if (prepare_line(m, iline0 + l, scaled, lp, err)) return set_err(ctx, RL_ERR_ARG, err);
+    for (size_t i = 0; i < (size_t)ncell * 4; i++) tab[(size_t)l * ncell * 4 + i] = (T)lp.tab[i];
+    for (int c = 0; c < ncell; c++) nsum[(size_t)l * ncell + c] = (T)lp.nsum[c];
+    for (int k = 0; k < nfr; k++) {
+      wch[(size_t)l * nfr + k] = (T)lp.wch[k];
+      star[(size_t)l * nfr + k] = (T)lp.star[k];
+      velo[(size_t)l * nfr + k] = lp.velo[k];
+    }
+    lc[l].cphi = (T)lp.cphi;
+    lc[l].istart = (T)lp.istart;
+    lc[l].scale = lp.scale;
+    scale[l] = lp.scale;
+  }
+  const size_t nimg = (size_t)nl * cam.nrays * nfr;
+  if (!cached) {
+    CUDA_TRY(md->dtab.ensure(sizeof(T) * tab.size()));
+    CUDA_TRY(md->dnsum.ensure(sizeof(T) * nsum.size()));
+    CUDA_TRY(md->dwch.ensure(sizeof(T) * wch.size()));
+    CUDA_TRY(md->dstar.ensure(sizeof(T) * star.size()));
+    CUDA_TRY(md->dvelo.ensure(sizeof(double) * velo.size()));
+    CUDA_TRY(md->dlc.ensure(sizeof(LineConst<T>) * lc.size()));
+    CUDA_TRY(md->dscale.ensure(sizeof(double) * nl));
+  }
+  CUDA_TRY(md->dimg.ensure(sizeof(T) * nimg));
+  CUDA_TRY(md->dring.ensure(sizeof(double) * (size_t)nl * (cam.nrr + 1) * nfr));
+  CUDA_TRY(md->dflux.ensure(sizeof(double) * (size_t)nl * nfr));
+  CUDA_TRY(md->dcnt.ensure(sizeof(unsigned long long) * 4));
+  CUDA_TRY(md->dwork.ensure(sizeof(int)));
+  CUDA_TRY(md->derr.ensure(sizeof(int)));
+  CUDA_TRY(cudaEventRecord(ctx->ev[0], s));
+  if (!cached) {
+    CUDA_TRY(h2d(md->dtab.p, tab.data(), sizeof(T) * tab.size(), s));
+    CUDA_TRY(h2d(md->dnsum.p, nsum.data(), sizeof(T) * nsum.size(), s));
+    CUDA_TRY(h2d(md->dwch.p, wch.data(), sizeof(T) * wch.size(), s));
+    CUDA_TRY(h2d(md->dstar.p, star.data(), sizeof(T) * star.size(), s));
+    CUDA_TRY(h2d(md->dvelo.p, velo.data(), sizeof(double) * velo.size(), s));
+    CUDA_TRY(h2d(md->dlc.p, lc.data(), sizeof(LineConst<T>) * lc.size(), s));
+    CUDA_TRY(h2d(md->dscale.p, scale.data(), sizeof(double) * nl, s));
+  }
+  CUDA_TRY(cudaMemsetAsync(md->dcnt.p, 0, sizeof(unsigned long long) * 4, s));
+  CUDA_TRY(cudaMemsetAsync(md->dwork.p, 0, sizeof(int), s));
+  CUDA_TRY(cudaMemsetAsync(md->derr.p, 0, sizeof(int), s));
+  CUDA_TRY(cudaEventRecord(ctx->ev[1], s));
+  WalkParams<T> P;
+  P.nb = node_view<T>(md);
+  P.nth = m.nth; P.ncell = ncell; P.nlines = nl; P.nfr = nfr; P.nitems = nl * cam.nrays;
+  P.tab = md->dtab.as<T>(); P.nsum = md->dnsum.as<T>(); P.wch = md->dwch.as<T>(); P.velo = md->dvelo.as<double>();
+  P.star = md->dstar.as<T>(); P.lc = md->dlc.as<LineConst<T>>();
+  P.aksmax_c = m.aksmax / 2.99792458e5;
+  P.kq = (T)(3.33567e-6 * 2.99792458e5);
+  P.fstar = (T)((m.rstar / cam.ri[1]) * (m.rstar / cam.ri[1]));
+  P.img = md->dimg.as<T>();
+  P.counters = md->dcnt.as<unsigned long long>();
+  P.work = md->dwork.as<int>();
+  P.err = md->derr.as<int>();
+  if (cam.ri[1] < m.rstar) return set_err(ctx, RL_ERR_ARG, "central beam smaller than the star");
+  const int need = (nfr + 31) / 32;
+  const int cpl = need <= 1 ? 1 : need <= 2 ? 2 : need <= 4 ? 4 : 8;
+  CUDA_TRY(launch_walk<T>(P, cpl, ctx->nsm, s));
+  CUDA_TRY(cudaEventRecord(ctx->ev[2], s));
+  ReduceParams rp;
+  rp.nrays = cam.nrays; rp.nfr = nfr; rp.nphi = cam.nphi; rp.nrr = cam.nrr; rp.nlines = nl;
+  rp.ri = md->dri.as<double>(); rp.dist2 = 3.08572e18 * 3.08572e18; rp.scale = md->dscale.as<double>();
+  CUDA_TRY(launch_reduce<T>(rp, md->dimg.as<T>(), md->dring.as<double>(), md->dflux.as<double>(), s));
+  CUDA_TRY(cudaEventRecord(ctx->ev[3], s));
+  if (flux_out)
+    CUDA_TRY(d2h(flux_out, md->dflux.p, sizeof(double) * (size_t)nl * nfr, s));
+  unsigned long long cnt[4] = {0, 0, 0, 0};
+  int kerr = 0;
+  CUDA_TRY(d2h(cnt, md->dcnt.p, sizeof(cnt), s));
+  CUDA_TRY(d2h(&kerr, md->derr.p, sizeof(int), s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  if (image_out) {
+    std::vector<T> img(nimg);
+    g_d2h += sizeof(T) * nimg;
+    CUDA_TRY(cudaMemcpy(img.data(), md->dimg.p, sizeof(T) * nimg, cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < nimg; i++) image_out[i] = (double)img[i] * scale[i / ((size_t)cam.nrays * nfr)];
+  }
+  if (!cached) {
+    md->tab_line0 = iline0; md->tab_nl = nl; md->tab_prec = md->precision; md->tab_scale = scale;
+  }
+  if (kerr != 0) return set_err(ctx, RL_ERR_GEOMETRY, "walk: error code " + std::to_string(kerr));
+  if (st) {
+    float a = 0, b = 0, c = 0;
+    cudaEventElapsedTime(&a, ctx->ev[0], ctx->ev[1]);
+    cudaEventElapsedTime(&b, ctx->ev[1], ctx->ev[2]);
+    cudaEventElapsedTime(&c, ctx->ev[2], ctx->ev[3]);
+    st->upload_ms += a; st->walk_ms += b; st->reduce_ms += c;
+    st->steps += cnt[0]; st->integrated += cnt[1]; st->node_visits += cnt[2];
+    st->ray_channels += (unsigned long long)cam.nrays * nfr * nl;
+    st->nrays = cam.nrays; st->nfr = nfr; st->kmax = md->kmax; st->nlines += nl;
+  }
+  return 0;
+}
+
+static int dispatch_lines(rl_model* md, int iline0, int nl, double* flux, double* image, rl_stats* st) {
+  g_h2d = 0; g_d2h = 0;
+  const int rc = md->precision == RL_FP64 ? run_lines<double>(md, iline0, nl, flux, image, st)
+                                          : run_lines<float>(md, iline0, nl, flux, image, st);
+  if (st) { st->h2d_bytes += g_h2d; st->d2h_bytes += g_d2h; }
+  return rc;
+}
+
+extern "C" {
+
+int rl_create(rl_ctx** out, int device) {
+  if (!out) return set_err(nullptr, RL_ERR_ARG, "rl_create: null output");
+  *out = nullptr;
+  std::unique_ptr<rl_ctx> c(new rl_ctx);
+  c->device = device;
+  rl_ctx* ctx = c.get();
+  CUDA_TRY(cudaSetDevice(device));
+  CUDA_TRY(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device));
+  CUDA_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  for (auto& e : c->ev) CUDA_TRY(cudaEventCreate(&e));
+  *out = c.release();
+  return 0;
+}
+
+int rl_destroy(rl_ctx* ctx) {
+  if (!ctx) return 0;
+  cudaSetDevice(ctx->device);
+  for (auto& e : ctx->ev) if (e) cudaEventDestroy(e);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return 0;
+}
+
+int rl_last_error(rl_ctx* ctx, char* buf, size_t len) {
+  const std::string& e = ctx ? ctx->err : g_last_error;
+  if (buf && len) { std::snprintf(buf, len, "%s", e.c_str()); }
+  return (int)e.size();
+}
+
+int rl_load_dir(rl_ctx* ctx, const char* dir, rl_model** out) {
+  if (!dir || !out) return set_err(ctx, RL_ERR_ARG, "rl_load_dir: null argument");
+  *out = nullptr;
+  std::unique_ptr<rl_model> md(new rl_model);
+  md->ctx = ctx;
+  std::string err;
+  if (load_dir(dir, md->m, err)) return set_err(ctx, RL_ERR_IO, err);
+  camera_defaults(md.get());
+  *out = md.release();
+  return 0;
+}
+
+int rl_load_arrays(rl_ctx* ctx, const rl_model_arrays* a, rl_model** out) {
+  if (!a || !out) return set_err(ctx, RL_ERR_ARG, "rl_load_arrays: null argument");
+  *out = nullptr;
+  if (a->nr < 3 || a->nth < 2 || a->nlev < 2 || a->nlines_mol < 1 || !a->radius || !a->theta || !a->rho ||
+      !a->abund || !a->width || !a->vel || !a->pop || !a->lev_up || !a->lev_low || !a->aud || !a->energy_cm ||
+      !a->gdeg)
+    return set_err(ctx, RL_ERR_ARG, "rl_load_arrays: missing or inconsistent arrays");
+  if (a->line_dust && (a->ncont < 2 || !a->freq || !a->dust_rho || !a->dust_temp || !a->kappa_abs || !a->kappa_scat))
+    return set_err(ctx, RL_ERR_ARG, "rl_load_arrays: dust arrays required with line_dust");
+  std::unique_ptr<rl_model> md(new rl_model);
+  md->ctx = ctx;
+  Model& m = md->m;
+  m.nr = a->nr; m.nth = a->nth; m.ny = 2 * a->nth;
+  const int ncell = m.ncell();
+  m.R.assign(m.nr + 4, 0.0);
+  for (int i = 0; i < m.nr; i++) m.R[i + 2] = a->radius[i];
+  auto R = [&](int ix) -> double& { return m.R[ix + 1]; };
+  R(0) = R(1) * R(1) / R(2); R(-1) = R(0) * R(0) / R(1);
+  R(m.nr + 1) = R(m.nr) * R(m.nr) / R(m.nr - 1); R(m.nr + 2) = R(m.nr + 1) * R(m.nr + 1) / R(m.nr);
+  for (int ix = 1; ix < m.nr; ix++)
+    if (!(R(ix + 1) > R(ix)) || R(ix + 1) / R(ix) - 1.0 < 1.0e-6)
+      return set_err(ctx, RL_ERR_ARG, "rl_load_arrays: radii must increase by more than the telescope safety number");
+  m.TH.assign(m.ny + 4, 0.0);
+  for (int i = 0; i < m.nth; i++) {
+    if (a->theta[i] < 0.0 || a->theta[i] > 1.5707963268) return set_err(ctx, RL_ERR_ARG, "rl_load_arrays: theta outside [0, pi/2]");
+    m.TH[i + 2] = a->theta[i];
+  }
+  auto T = [&](int iy) -> double& { return m.TH[iy + 1]; };
+  for (int iy = 1; iy <= m.nth; iy++) T(2 * m.nth + 1 - iy) = 3.14159265359 - T(iy);
+  T(0) = -T(1); T(-1) = -T(2);
+  const double twopi_f = (double)(2.0f * 3.1415926f);
+  T(m.ny + 1) = twopi_f - T(m.ny); T(m.ny + 2) = twopi_f - T(m.ny - 1);
+  m.rho.assign(a->rho, a->rho + ncell);
+  m.abun.assign(a->abund, a->abund + ncell);
+  m.lw.assign(a->width, a->width + ncell);
+  m.vel.assign(a->vel, a->vel + 3 * (size_t)ncell);
+  m.nlev = a->nlev;
+  m.pop.assign(a->pop, a->pop + (size_t)ncell * a->nlev);
+  m.Ecm.assign(a->energy_cm, a->energy_cm + a->nlev);
+  m.gdeg.assign(a->gdeg, a->gdeg + a->nlev);
+  m.lup.assign(a->lev_up, a->lev_up + a->nlines_mol);
+  m.ldn.assign(a->lev_low, a->lev_low + a->nlines_mol);
+  m.Aud.assign(a->aud, a->aud + a->nlines_mol);
+  m.lfreq.resize(a->nlines_mol);
+  for (int i = 0; i < a->nlines_mol; i++) {
+    if (m.lup[i] < 1 || m.ldn[i] < 1 || m.lup[i] > m.nlev || m.ldn[i] > m.nlev || m.lup[i] <= m.ldn[i])
+      return set_err(ctx, RL_ERR_ARG, "rl_load_arrays: invalid line levels");
+    m.lfreq[i] = 1.509160e26 * (1.986468498e-16 * m.Ecm[m.lup[i] - 1] - 1.986468498e-16 * m.Ecm[m.ldn[i] - 1]);
+    if (!(m.lfreq[i] > 0.0)) return set_err(ctx, RL_ERR_ARG, "rl_load_arrays: non-positive line frequency");
+  }
+  m.umass = a->umass;
+  m.line_dust = a->line_dust;
+  m.ncont = a->ncont;
+  if (a->ncont > 0 && a->freq) m.cnu.assign(a->freq, a->freq + a->ncont);
+  if (m.line_dust) {
+    m.nspec = 1;
+    m.nsize.assign(1, 1);
+    m.drho.assign(a->dust_rho, a->dust_rho + ncell);
+    m.dtemp.assign((size_t)4 * ncell, 0.0);
+    std::copy(a->dust_temp, a->dust_temp + ncell, m.dtemp.begin());
+    m.kabs.assign((size_t)4 * m.ncont, 0.0);
+    m.ksca.assign((size_t)4 * m.ncont, 0.0);
+    std::copy(a->kappa_abs, a->kappa_abs + m.ncont, m.kabs.begin());
+    std::copy(a->kappa_scat, a->kappa_scat + m.ncont, m.ksca.begin());
+  }
+  m.rstar = a->rstar;
+  m.starcont.assign(std::max(m.ncont, 0), 0.0);
+  m.starpump = a->star_flux_1pc ? 1 : 0;
+  if (a->star_flux_1pc)
+    for (int i = 0; i < m.ncont; i++) m.starcont[i] = 3.0308410e36 * a->star_flux_1pc[i] / (m.rstar * m.rstar);
+  m.outer_bc = a->outer_bc;
+  if (m.outer_bc != 0 && m.outer_bc != 2) return set_err(ctx, RL_ERR_ARG, "rl_load_arrays: outer boundary 0 or 2");
+  m.incl_rad = a->incl_deg * 0.0174532925199;
+  m.nphi = a->nphi; m.dbdr = a->dbdr; m.nrext = a->nrrayextra;
+  m.vmax = a->vmax; m.dv = a->dv; m.radvelo = a->radvelo;
+  m.ilstart = a->ilinestart; m.nlspec = a->nlines_spec; m.style = 1;
+  m.molname = a->molname ? a->molname : "moldata";
+  m.molfile = m.molname + ".dat";
+  finish_model(m);
+  if (m.nfr < 2) return set_err(ctx, RL_ERR_ARG, "rl_load_arrays: passband needs at least 2 channels");
+  if (m.ilstart < 1 || m.ilstart + m.nlspec - 1 > a->nlines_mol) return set_err(ctx, RL_ERR_ARG, "rl_load_arrays: line range");
+  camera_defaults(md.get());
+  *out = md.release();
+  return 0;
+}
+
+int rl_model_free(rl_model* md) {
+  if (!md) return 0;
+  if (md->ctx) cudaSetDevice(md->ctx->device);
+  delete md;
+  return 0;
+}
+
+int rl_model_get_info(rl_model* md, rl_model_info* info) {
+  if (!md || !info) return set_err(nullptr, RL_ERR_ARG, "rl_model_get_info: null argument");
+  const Model& m = md->m;
+  std::memset(info, 0, sizeof *info);
+  info->nr = m.nr; info->nth = m.nth; info->nlev = m.nlev; info->nlines_mol = (int)m.lfreq.size();
+  info->nlines_spec = m.nlspec; info->ilinestart = m.ilstart; info->nfr = m.nfr; info->nphi = md->nphi;
+  info->dbdr = md->dbdr; info->nrrayextra = md->nrext;
+  info->nrings = std::abs(md->nrext) + 10 + md->dbdr * (m.nr - 1);
+  info->nrays = 1 + info->nrings * md->nphi;
+  info->outer_bc = m.outer_bc; info->starpump = m.starpump; info->line_dust = m.line_dust;
+  info->precision = md->precision;
+  info->incl_deg = md->incl_rad * 57.2957795132; info->vmax = m.vmax; info->dv = m.dv; info->rstar = m.rstar;
+  info->aksmax = m.aksmax;
+  return 0;
+}
+
+int rl_set_camera(rl_model* md, double incl_deg, int nphi, int dbdr, int nrrayextra) {
+  if (!md) return set_err(nullptr, RL_ERR_ARG, "rl_set_camera: null model");
+  rl_ctx* ctx = md->ctx;
+  if (md->incl_rad == incl_deg * 0.0174532925199 && md->nphi == nphi && md->dbdr == dbdr && md->nrext == nrrayextra)
+    return 0;
+  if (nphi < 1 || dbdr < 1 || nrrayextra == 0 || incl_deg == 0.0)
+    return set_err(ctx, RL_ERR_ARG, "rl_set_camera: need nphi>0, dbdr>0, nrrayextra!=0, inclination!=0");
+  md->incl_rad = incl_deg * 0.0174532925199;
+  md->nphi = nphi; md->dbdr = dbdr; md->nrext = nrrayextra;
+  md->geo_ready = false;
+  return 0;
+}
+
+int rl_set_precision(rl_model* md, int precision) {
+  if (!md) return set_err(nullptr, RL_ERR_ARG, "rl_set_precision: null model");
+  if (precision != RL_FP32 && precision != RL_FP64) return set_err(md->ctx, RL_ERR_ARG, "rl_set_precision: RL_FP32 or RL_FP64");
+  if (precision != md->precision) md->geo_ready = false;
+  md->precision = precision;
+  return 0;
+}
+
+int rl_line_spectrum(rl_model* md, int iline, double* flux_out, double* velo_out, rl_stats* st) {
+  if (!md || !flux_out) return set_err(nullptr, RL_ERR_ARG, "rl_line_spectrum: null argument");
+  rl_ctx* ctx = md->ctx;
+  if (!ctx) return set_err(nullptr, RL_ERR_STATE, "model was loaded without a device context");
+  CUDA_TRY(cudaSetDevice(ctx->device));
+  if (st) std::memset(st, 0, sizeof *st);
+  int rc = dispatch_lines(md, iline, 1, flux_out, nullptr, st);
+  if (rc) return rc;
+  if (velo_out) {
+    const Model& m = md->m;
+    const double lf = m.lfreq[iline - 1], nu0 = std::fabs(lf);
+    const double passb = 3.33567e-6 * nu0 * m.vmax, dnu = 2.0 * passb / (m.nfr - 1.0);
+    for (int k = 0; k < m.nfr; k++) velo_out[k] = -2.99792458e5 * ((nu0 + (-passb + k * dnu)) - lf) / lf + m.radvelo;
+  }
+  return 0;
+}
+
+int rl_spectra(rl_model* md, int iline0, int nlines, double* flux_out, rl_stats* st) {
+  if (!md || !flux_out) return set_err(nullptr, RL_ERR_ARG, "rl_spectra: null argument");
+  rl_ctx* ctx = md->ctx;
+  if (!ctx) return set_err(nullptr, RL_ERR_STATE, "model was loaded without a device context");
+  CUDA_TRY(cudaSetDevice(ctx->device));
+  if (st) std::memset(st, 0, sizeof *st);
+  return dispatch_lines(md, iline0, nlines, flux_out, nullptr, st);
+}
+
+int rl_line_image(rl_model* md, int iline, double* image_out, rl_stats* st) {
+  if (!md || !image_out) return set_err(nullptr, RL_ERR_ARG, "rl_line_image: null argument");
+  rl_ctx* ctx = md->ctx;
+  if (!ctx) return set_err(nullptr, RL_ERR_STATE, "model was loaded without a device context");
+  CUDA_TRY(cudaSetDevice(ctx->device));
+  if (st) std::memset(st, 0, sizeof *st);
+  return dispatch_lines(md, iline, 1, nullptr, image_out, st);
+}
+
+int rl_run_dir(const char* dir, int device, rl_stats* st) {
+  rl_ctx* ctx = nullptr;
+  int rc = rl_create(&ctx, device);
+  if (rc) return rc;
+  rl_model* md = nullptr;
+  rc = rl_load_dir(ctx, dir, &md);
+  if (rc == 0) {
+    const Model& m = md->m;
+    std::vector<double> flux((size_t)m.nlspec * m.nfr);
+    if (st) std::memset(st, 0, sizeof *st);
+    rc = dispatch_lines(md, m.ilstart, m.nlspec, flux.data(), nullptr, st);
+    if (rc == 0) {
+      std::vector<int> lines;
+      for (int i = 0; i < m.nlspec; i++) lines.push_back(m.ilstart + i);
+      std::string err;
+      if (write_spectrum_file(std::string(dir) + "/linespectrum_" + m.molname + ".dat", m, md->cam, lines, flux, err))
+        rc = set_err(ctx, RL_ERR_IO, err);
+      else {
+        FILE* fp = std::fopen((std::string(dir) + "/radlite.success").c_str(), "w");
+        if (fp) { std::fprintf(fp, " 1\n"); std::fclose(fp); }
+      }
+    }
+  }
+  if (rc) g_last_error = ctx->err;
+  rl_model_free(md);
+  rl_destroy(ctx);
+  return rc;
+}
+
+int rl_measure_peaks(rl_ctx* ctx, double* ffma_per_s, double* ex2_per_s) {
+  if (!ctx || !ffma_per_s || !ex2_per_s) return set_err(ctx, RL_ERR_ARG, "rl_measure_peaks: null argument");
+  CUDA_TRY(cudaSetDevice(ctx->device));
+  CUDA_TRY(measure_peaks(ctx->nsm, ctx->stream, ffma_per_s, ex2_per_s));
+  return 0;
+}
+
+int rl_debug_trajectory(rl_model* md, int iray, int cap, double* s, double* r, double* th, double* mu, double* dvmu,
+                        int* icr, int* ir, int* it) {
+  if (!md) return set_err(nullptr, RL_ERR_ARG, "rl_debug_trajectory: null model");
+  rl_ctx* ctx = md->ctx;
+  if (!ctx) return set_err(nullptr, RL_ERR_STATE, "model was loaded without a device context");
+  CUDA_TRY(cudaSetDevice(ctx->device));
+  int rc = upload_grid(md);
+  if (rc) return rc;
+  std::string err;
+  Camera cam;
+  if (setup_camera(md->m, md->incl_rad, md->nphi, md->dbdr, md->nrext, cam, err)) return set_err(ctx, RL_ERR_ARG, err);
+  if (iray < 0 || iray >= cam.nrays) return set_err(ctx, RL_ERR_ARG, "rl_debug_trajectory: ray index out of range");
+  if (cap < 0) return set_err(ctx, RL_ERR_ARG, "rl_debug_trajectory: negative capacity");
+  const int kmax = rlg::max_nodes(md->m.nr, md->m.nth);
+  cudaStream_t st = ctx->stream;
+  DevBuf bx0, bz0, bnn, bst, bds, bdvf, bvl, bdvs, blw, bwr, bwt, bc00, bmisc, dbg, arr;
+  CUDA_TRY(bx0.ensure(sizeof(double))); CUDA_TRY(bz0.ensure(sizeof(double)));
+  CUDA_TRY(bnn.ensure(sizeof(int))); CUDA_TRY(bst.ensure(sizeof(int)));
+  CUDA_TRY(bds.ensure(sizeof(double) * kmax)); CUDA_TRY(bdvf.ensure(sizeof(float) * kmax));
+  CUDA_TRY(bvl.ensure(sizeof(double) * kmax)); CUDA_TRY(bdvs.ensure(sizeof(double) * kmax));
+  CUDA_TRY(blw.ensure(sizeof(double) * kmax)); CUDA_TRY(bwr.ensure(sizeof(double) * kmax));
+  CUDA_TRY(bwt.ensure(sizeof(double) * kmax)); CUDA_TRY(bc00.ensure(sizeof(int) * kmax));
+  CUDA_TRY(bmisc.ensure(sizeof(unsigned) * kmax));
+  const size_t per = (size_t)kmax;
+  CUDA_TRY(arr.ensure((sizeof(double) * 5 + sizeof(int) * 3) * per));
+  CUDA_TRY(dbg.ensure(sizeof(TrajDebug)));
+  TrajDebug h;
+  char* base = arr.as<char>();
+  h.s = (double*)base; h.r = h.s + per; h.th = h.r + per; h.mu = h.th + per; h.dvmu = h.mu + per;
+  h.icr = (int*)(h.dvmu + per); h.ir = h.icr + per; h.it = h.ir + per; h.cap = kmax;
+  CUDA_TRY(h2d(dbg.p, &h, sizeof h, st));
+  CUDA_TRY(h2d(bx0.p, &cam.x0[iray], sizeof(double), st));
+  CUDA_TRY(h2d(bz0.p, &cam.z0[iray], sizeof(double), st));
+  GeoParams p;
+  const Model& m = md->m;
+  p.nr = m.nr; p.nth = m.nth; p.ny = m.ny; p.rstar = m.rstar; p.theta0 = cam.theta0;
+  p.R = md->dR.as<double>(); p.TH = md->dTH.as<double>(); p.tan2 = md->dtan2.as<double>();
+  p.vel = md->dvel.as<double>(); p.lw = md->dlw.as<double>(); p.x0 = bx0.as<double>(); p.z0 = bz0.as<double>();
+  NodeBuf<double> nb;
+  nb.nrays = 1; nb.kmax = kmax; nb.nnodes = bnn.as<int>(); nb.status = bst.as<int>();
+  nb.ds = bds.as<double>(); nb.dvf = bdvf.as<float>(); nb.vl = bvl.as<double>(); nb.dvseg = bdvs.as<double>();
+  nb.lw = blw.as<double>(); nb.wr = bwr.as<double>(); nb.wt = bwt.as<double>(); nb.c00 = bc00.as<int>();
+  nb.misc = bmisc.as<unsigned>();
+  CUDA_TRY(launch_geometry<double>(p, nb, 0, 1, dbg.as<TrajDebug>(), st));
+  int n = 0, status = 0;
+  CUDA_TRY(d2h(&n, bnn.p, sizeof(int), st));
+  CUDA_TRY(d2h(&status, bst.p, sizeof(int), st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  if (status != 0) return set_err(ctx, RL_ERR_GEOMETRY, "geometry status " + std::to_string(status));
+  const int c = std::min(n, cap);
+  std::vector<double> hd(5 * per);
+  std::vector<int> hi(3 * per);
+  CUDA_TRY(cudaMemcpy(hd.data(), h.s, sizeof(double) * 5 * per, cudaMemcpyDeviceToHost));
+  CUDA_TRY(cudaMemcpy(hi.data(), h.icr, sizeof(int) * 3 * per, cudaMemcpyDeviceToHost));
+  for (int k = 0; k < c; k++) {
+    if (s) s[k] = hd[k];
+    if (r) r[k] = hd[per + k];
+    if (th) th[k] = hd[2 * per + k];
+    if (mu) mu[k] = hd[3 * per + k];
+    if (dvmu) dvmu[k] = hd[4 * per + k];
+    if (icr) icr[k] = hi[k];
+    if (ir) ir[k] = hi[per + k];
+    if (it) it[k] = hi[2 * per + k];
+  }
+  return n;
+}
+
+}  // extern "C"

@@ -1,0 +1,84 @@
+// rl_device.h -- plain structs shared by the host orchestration and the CUDA kernels.
+#pragma once
+#include <stddef.h>
+#include <stdint.h>
+
+namespace rl {
+
+// Per-node flag bits in NodeBuf::misc (bits 0-15: theta-corner offset + 32768,
+// bits 16-17: radial-corner offset + 1).
+constexpr unsigned kFlagHole = 1u << 20;   // segment ending here lies in the central hole
+constexpr unsigned kFlagIr1 = 1u << 21;    // node on the innermost radial cell (ir == 1)
+constexpr int kIcrShift = 18;              // bits 18-19: crossing type 1..3
+
+// Node records of all rays of one camera, row-major by ray (row stride kmax).
+template <typename T>
+struct NodeBuf {
+  int nrays = 0, kmax = 0;
+  int* nnodes = nullptr;       // [nrays]
+  int* status = nullptr;       // [nrays] geometry status (0 = fine)
+  T* ds = nullptr;             // s_k - s_{k-1} (0 at k=0 and in the central hole)
+  float* dvf = nullptr;        // (float) projected velocity / c  (window test)
+  T* vl = nullptr;             // projected velocity in passband units (dvmu / 3.33567e-6)
+  T* dvseg = nullptr;          // vl_k - vl_{k-1}, formed in FP64
+  T* lw = nullptr;             // interpolated line width [km/s]
+  T* wr = nullptr;             // radial interpolation weight
+  T* wt = nullptr;             // theta interpolation weight
+  int* c00 = nullptr;          // cell index of the base corner
+  unsigned* misc = nullptr;    // corner offsets, crossing type, flags
+};
+
+// Debug copy of one ray's trajectory (filled only by the debug geometry launch).
+struct TrajDebug {
+  double* s; double* r; double* th; double* mu; double* dvmu; int* icr; int* ir; int* it;
+  int cap;
+};
+
+struct GeoParams {
+  int nr, nth, ny;
+  double rstar, theta0;
+  const double* R;      // [nr+4]
+  const double* TH;     // [ny+4]
+  const double* tan2;   // [nth+1]
+  const double* vel;    // [ncell*3]
+  const double* lw;     // [ncell]
+  const double* x0;     // [nrays]
+  const double* z0;     // [nrays]
+};
+
+// Per-line constants of the walk.
+template <typename T>
+struct LineConst {
+  T cphi;       // 0.56419583546 / (3.33567e-6 * nu0): profile normalisation times lwav
+  T istart;     // outer-boundary start intensity (scaled)
+  double scale; // intensity scale: spectrum = scale * sum
+};
+
+template <typename T>
+struct WalkParams {
+  NodeBuf<T> nb;
+  int nth, ncell;
+  int nlines, nfr, nitems;
+  const T* tab;              // [nlines][ncell][4] = {j-factor, alpha-factor, dust j, dust alpha}
+  const T* nsum;             // [nlines][ncell] N_up + N_low (window threshold)
+  const T* wch;              // [nlines][nfr] channel velocity in passband units
+  const double* velo;        // [nlines][nfr] dnu/nu0 (window test)
+  const T* star;             // [nlines][nfr] scaled stellar intensity
+  const LineConst<T>* lc;    // [nlines]
+  double aksmax_c;           // max line width / c
+  T kq;                      // 3.33567e-6 * 2.99792458e5
+  T fstar;                   // (R*/ri(1))^2 for the central beam
+  T* img;                    // [nlines][nrays][nfr]
+  unsigned long long* counters;   // [0] steps, [1] integrated channels, [2] node visits
+  int* work;                 // dynamic work counter
+  int* err;                  // first error code
+};
+
+struct ReduceParams {
+  int nrays, nfr, nphi, nrr, nlines;
+  const double* ri;          // [nrr+2] ring edges
+  double dist2;              // distance^2 [cm^2]
+  const double* scale;       // [nlines]
+};
+
+}  // namespace rl

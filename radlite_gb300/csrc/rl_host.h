@@ -1,0 +1,69 @@
+// rl_host.h -- host-side model of one RADLite working directory.
+#pragma once
+#include <string>
+#include <vector>
+
+namespace rl {
+
+// Everything the line raytrace reads from the reference's input files.
+struct Model {
+  // spatial grid: R(ix) = R[ix+1] (ix=-1..nr+2), TH(iy) = TH[iy+1] (iy=-1..ny+2)
+  int nr = 0, nth = 0, ny = 0;
+  std::vector<double> R, TH;
+  // cells of the stored (upper) half, index (ir-1)*nth + (it-1)
+  std::vector<double> rho, abun, lw, vel;   // vel: 3 per cell (v_r, v_theta, v_phi) [cm/s]
+  int nspec = 0;
+  std::vector<int> nsize;                   // sizes per species
+  std::vector<double> drho;                 // [spec][cell]
+  std::vector<double> dtemp;                // [spec][4][cell]
+  int ncont = 0;                            // frequency.inp
+  std::vector<double> cnu;                  // [ncont]
+  std::vector<double> kabs, ksca;           // [spec][4][ncont]
+  std::vector<double> scat;                 // [ncont][cell] (empty if absent)
+  int nlev = 0;
+  std::vector<double> pop;                  // [cell][nlev]
+  // molecule
+  std::string molname, molfile;
+  std::vector<double> Ecm, gdeg;            // [nlev_mol]
+  std::vector<int> lup, ldn;                // 1-based level indices per line
+  std::vector<double> Aud, lfreq;           // per line
+  double umass = 2.3;
+  // star and boundaries
+  double rstar = 0.0;
+  std::vector<double> starcont;             // intensity at the stellar surface on cnu
+  int starpump = 0, outer_bc = 0, line_dust = 1;
+  // camera and passband (radlite.inp, linespectrum.inp)
+  double incl_rad = 0.0;
+  int nphi = 0, dbdr = 1, nrext = 0;
+  double vmax = 0.0, dv = 0.0, radvelo = 0.0;
+  int nlspec = 0, ilstart = 1, style = 1, nfr = 0;
+  double aksmax = 0.0;
+  int ncell() const { return nr * nth; }
+};
+
+// The reference's camera: the circular-image ray family (telescope.F:715-1191).
+struct Camera {
+  double incl_rad = 0.0;   // after the small-angle clamp
+  double theta0 = 0.0;
+  int nphi = 0, nrr = 0, nrays = 0;
+  std::vector<double> x0, z0;   // [nrays], ray 0 = central beam
+  std::vector<double> rays_r;   // [nrr+1]
+  std::vector<double> ri;       // [nrr+2] ring edges
+};
+
+// Per-line constants and cell tables (line.F:427-545, 1708-1823, 3502-3677, 3797-3845).
+struct LinePrep {
+  double lfreq = 0.0, nu0 = 0.0, Bud = 0.0, Bdu = 0.0, scale = 1.0, istart = 0.0, cphi = 0.0;
+  std::vector<double> dnu, velo, wch, star;    // [nfr]
+  std::vector<double> tab;                     // [ncell][4] jfac/scale, afac, jd/scale, ad
+  std::vector<double> nsum;                    // [ncell]
+};
+
+int load_dir(const std::string& dir, Model& m, std::string& err);
+int setup_camera(const Model& m, double incl_rad, int nphi, int dbdr, int nrext, Camera& cam, std::string& err);
+int prepare_line(const Model& m, int iline, bool scaled, LinePrep& lp, std::string& err);
+void finish_model(Model& m);   // derived quantities (aksmax, passband channel count)
+int write_spectrum_file(const std::string& path, const Model& m, const Camera& cam,
+                        const std::vector<int>& lines, const std::vector<double>& flux, std::string& err);
+
+}  // namespace rl

@@ -1,0 +1,29 @@
+// Test-only harness: the product's ray/grid geometry (rl_geometry.cuh) compiled for the
+// host, so its node lists and interpolation corners can be checked against the oracle
+// without a GPU. Not part of the library.
+#include <cmath>
+#include "../radlite_gb300/csrc/rl_geometry.cuh"
+
+namespace {
+struct Collect {
+  int cap, n;
+  double *s, *r, *th, *mu;
+  int *icr, *ir, *it;
+  bool operator()(const rlg::Node& nd) {
+    if (n >= cap) return false;
+    s[n] = nd.s; r[n] = nd.r; th[n] = nd.th; mu[n] = nd.mu; icr[n] = nd.icr; ir[n] = nd.ir; it[n] = nd.it;
+    n++;
+    return true;
+  }
+};
+}  // namespace
+
+extern "C" int geom_trace(int nr, int nth, const double* R, const double* TH, const double* tan2, double rstar,
+                          double x0, double z0, double theta0, int cap, double* s, double* r, double* th, double* mu,
+                          int* icr, int* ir, int* it, int* status) {
+  rlg::Grid g;
+  g.R = R; g.TH = TH; g.tan2 = tan2; g.nr = nr; g.nth = nth; g.ny = 2 * nth; g.rstar = rstar;
+  Collect c{cap, 0, s, r, th, mu, icr, ir, it};
+  *status = rlg::trace(g, x0, z0, theta0, c);
+  return c.n;
+}

@@ -1,0 +1,58 @@
+"""The C-ABI library loads and exports every entry point that include/rlgpu.h declares;
+host-side parsing of the input files works without a device."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared():
+    src = open(os.path.join(ROOT, "include", "rlgpu.h")).read()
+    return sorted(set(re.findall(r"^\s*int\s+(rl_\w+)\s*\(", src, flags=re.M)))
+
+
+def test_header_symbols_exported(gpu_lib):
+    L = gpu_lib.lib()
+    names = declared()
+    assert len(names) >= 14
+    for n in names:
+        assert hasattr(L, n), f"{n} declared in rlgpu.h but not exported"
+    assert sorted(gpu_lib.EXPORTS) == names
+
+
+def test_host_only_load_matches_files(gpu_lib, model_dir, oracle_lib):
+    d = model_dir("tiny_band")
+    m = gpu_lib.load_dir_host(d)
+    info = m.info()
+    o = oracle_lib.Oracle(d)
+    assert (info["nr"], info["nth"], info["nfr"], info["nrays"]) == (o.nr, o.nth, o.nfr, o.nrays)
+    assert info["nlines_spec"] == o.nlines_spec and info["ilinestart"] == o.ilinestart
+    assert abs(info["aksmax"] - o.aksmax) <= 1e-12 * o.aksmax
+    with pytest.raises(gpu_lib.RLError, match="device context"):
+        m.calc_line_spectrum(1)
+
+
+@pytest.mark.parametrize("fname,mutate,msg", [
+    ("radius.inp", lambda t: "\n".join(t.split("\n")[:10]), "end of file"),
+    ("theta.inp", lambda t: t.replace("       1\n", "       0\n", 1), "mirroring"),
+    ("density.inp", lambda t: "3\t3\t1\n" + t.split("\n", 1)[1], "inconsistent"),
+    ("levelpop.info", lambda t: "-3\nwrongname.dat\n0", "levelpop.info"),
+    ("levelpop.info", lambda t: "-1\n", "cannot open"),
+    ("linespectrum.inp", lambda t: t.replace("0       Command", "2       Command"), "only the line spectrum"),
+    ("radlite.inp", lambda t: t.replace("-551", "-500"), "setup type"),
+    ("moldata.dat", lambda t: t.replace("    4    3", "    3    4"), "invalid levels"),
+    ("velocity.inp", lambda t: t.replace("e+", "x+", 1), "not a number"),
+])
+def test_malformed_inputs_rejected(gpu_lib, tmp_path, fname, mutate, msg):
+    from radlite_gb300 import synth
+    d = synth.write_model(synth.config_by_name("tiny_line"), str(tmp_path / "m"))
+    p = os.path.join(d, fname)
+    txt = open(p).read()
+    new = mutate(txt)
+    assert new != txt
+    open(p, "w").write(new)
+    with pytest.raises(gpu_lib.RLError, match=msg):
+        gpu_lib.load_dir_host(d)
