@@ -288,8 +288,26 @@ def ours(args):
     return 0
 
 
+def profile_case(args):
+    """One pass of a named workload (geometry, walk, reduction), for profiler captures."""
+    import radlite_gb300 as rl
+    from radlite_gb300 import synth
+    cfg = synth.config_by_name(args.workload)
+    arr = synth.model_arrays(cfg)
+    ctx = rl.Context(0)
+    m = ctx.load_arrays(arr, camera(cfg, cfg.incl_deg))
+    f, st = m.spectra(cfg.ilinestart, cfg.nlines, stats=True)
+    print(json.dumps({"workload": args.workload, "steps": st["steps"], "walk_ms": st["walk_ms"],
+                      "geometry_ms": st["geometry_ms"], "nrays": st["nrays"], "nlines": st["nlines"]}), flush=True)
+    m.free()
+    ctx.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--profile", action="store_true", help="one pass of --workload (profiler captures)")
+    ap.add_argument("--workload", default="adjoint_disk")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
@@ -300,6 +318,8 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.profile:
+        return profile_case(args)
     return reference_arm(args) if args.impl == "reference" else ours(args)
 
 

@@ -28,6 +28,7 @@ cudaError_t measure_peaks(int nsm, cudaStream_t st, double* ffma_per_s, double* 
 }  // namespace rl
 
 using namespace rl;
+static constexpr int kWalkGroup = 8;   // lines per walk work item (k_walk's kGroup)
 
 namespace {
 thread_local std::string g_last_error;
@@ -231,8 +232,15 @@ static int run_lines(rl_model* md, int iline0, int nl, double* flux_out, double*
     LinePrep lp;
     std::string err;
     if (prepare_line(m, iline0 + l, scaled, lp, err)) return set_err(ctx, RL_ERR_ARG, err);
-    for (size_t i = 0; i < (size_t)ncell * 4; i++) tab[(size_t)l * ncell * 4 + i] = (T)lp.tab[i];
-    for (int c = 0; c < ncell; c++) nsum[(size_t)l * ncell + c] = (T)lp.nsum[c];
+    // cell-major, line-minor: the corners of one node for consecutive lines are contiguous.
+    // The line factors carry the profile normalisation (phi = cphi / lwav * e^{-u^2}).
+    for (int c = 0; c < ncell; c++) {
+      tab[((size_t)c * nl + l) * 4 + 0] = (T)(lp.tab[4 * (size_t)c + 0] * lp.cphi);
+      tab[((size_t)c * nl + l) * 4 + 1] = (T)(lp.tab[4 * (size_t)c + 1] * lp.cphi);
+      tab[((size_t)c * nl + l) * 4 + 2] = (T)lp.tab[4 * (size_t)c + 2];
+      tab[((size_t)c * nl + l) * 4 + 3] = (T)lp.tab[4 * (size_t)c + 3];
+      nsum[(size_t)c * nl + l] = (T)lp.nsum[c];
+    }
     for (int k = 0; k < nfr; k++) {
       wch[(size_t)l * nfr + k] = (T)lp.wch[k];
       star[(size_t)l * nfr + k] = (T)lp.star[k];
@@ -275,7 +283,9 @@ static int run_lines(rl_model* md, int iline0, int nl, double* flux_out, double*
   CUDA_TRY(cudaEventRecord(ctx->ev[1], s));
   WalkParams<T> P;
   P.nb = node_view<T>(md);
-  P.nth = m.nth; P.ncell = ncell; P.nlines = nl; P.nfr = nfr; P.nitems = nl * cam.nrays;
+  P.nth = m.nth; P.ncell = ncell; P.nlines = nl; P.nfr = nfr;
+  P.nitems = ((nl + kWalkGroup - 1) / kWalkGroup) * cam.nrays;   // (line group, ray) work items
+  if (nfr >= 2048) return set_err(ctx, RL_ERR_ARG, "at most 2047 channels per line are supported");
   P.tab = md->dtab.as<T>(); P.nsum = md->dnsum.as<T>(); P.wch = md->dwch.as<T>(); P.velo = md->dvelo.as<double>();
   P.star = md->dstar.as<T>(); P.lc = md->dlc.as<LineConst<T>>();
   P.aksmax_c = m.aksmax / 2.99792458e5;
@@ -286,7 +296,8 @@ static int run_lines(rl_model* md, int iline0, int nl, double* flux_out, double*
   P.work = md->dwork.as<int>();
   P.err = md->derr.as<int>();
   if (cam.ri[1] < m.rstar) return set_err(ctx, RL_ERR_ARG, "central beam smaller than the star");
-  const int need = (nfr + 31) / 32;
+  // slots per lane: enough for every (line, channel) pair of a line group in one tile
+  const int need = (std::min(nl, kWalkGroup) * nfr + 31) / 32;
   const int cpl = need <= 1 ? 1 : need <= 2 ? 2 : need <= 4 ? 4 : 8;
   CUDA_TRY(launch_walk<T>(P, cpl, ctx->nsm, s));
   CUDA_TRY(cudaEventRecord(ctx->ev[2], s));

@@ -128,21 +128,24 @@ template <> struct Math<float> {
     return y;
   }
   static __device__ __forceinline__ float div(float a, float b) { return __fdiv_rn(a, b); }
-  // Formal-solution coefficients for optical depth d > 1e-6:
-  //   x = e^{-d}, e0 = 1 - x, b = (d - e0)/d, a = e0 - b.
-  // Below d = 0.7 the FP32 cancellation in d - e0 is avoided with Taylor series.
+  // Formal-solution coefficients for optical depth d (qdr_src_2, transfer.F:1517-1528):
+  //   d > 1e-6:  x = e^{-d}, e0 = 1 - x, b = (d - e0)/d, a = e0 - b
+  //   else:      a = b = d/2, x = 1 - d
+  // Evaluated without branches (both forms, then selects) so that independent channels
+  // interleave. Below d = 0.25 b comes from its Taylor series (the FP32 difference d - e0
+  // cancels there) and e0 = d (1 - b); above, e^{-d} on the MUFU pipe.
   static __device__ __forceinline__ void coeffs(float d, float& x, float& a, float& b) {
-    if (d < 0.7f) {
-      const float e0 = d * (1.f - d * (0.5f - d * (1.f / 6.f - d * (1.f / 24.f - d * (1.f / 120.f - d * (1.f / 720.f - d * (1.f / 5040.f - d * (1.f / 40320.f - d * (1.f / 362880.f)))))))));
-      b = d * (0.5f - d * (1.f / 6.f - d * (1.f / 24.f - d * (1.f / 120.f - d * (1.f / 720.f - d * (1.f / 5040.f - d * (1.f / 40320.f - d * (1.f / 362880.f - d * (1.f / 3628800.f)))))))));
-      x = 1.f - e0;
-      a = e0 - b;
-    } else {
-      x = expneg(d);
-      const float e0 = 1.f - x;
-      b = (d - e0) * rcp(d);
-      a = e0 - b;
-    }
+    const float bs = d * (0.5f - d * (1.f / 6.f - d * (1.f / 24.f - d * (1.f / 120.f - d * (1.f / 720.f - d * (1.f / 5040.f))))));
+    const float e0s = d - d * bs;
+    const float xd = expneg(d);
+    const float e0d = 1.f - xd;
+    const float bd = (d - e0d) * rcp(d);
+    const bool ser = d < 0.25f, tiny = !(d > 1.0e-6f);
+    const float e0 = ser ? e0s : e0d;
+    b = ser ? bs : bd;
+    x = ser ? 1.f - e0s : xd;
+    a = e0 - b;
+    if (tiny) { a = 0.5f * d; b = a; x = 1.f - d; }
   }
 };
 
@@ -151,11 +154,15 @@ template <> struct Math<double> {
   static __device__ __forceinline__ double rcp(double x) { return 1.0 / x; }
   static __device__ __forceinline__ double div(double a, double b) { return a / b; }
   static __device__ __forceinline__ void coeffs(double d, double& x, double& a, double& b) {
-    x = exp(-d);
-    const double e0 = 1.0 - x;
-    const double e1 = d - e0;
-    b = e1 / d;
-    a = e0 - b;
+    if (d > 1.0e-6) {
+      x = exp(-d);
+      const double e0 = 1.0 - x;
+      const double e1 = d - e0;
+      b = e1 / d;
+      a = e0 - b;
+    } else {
+      a = 0.5 * d; b = a; x = 1.0 - d;
+    }
   }
 };
 
@@ -172,11 +179,7 @@ __device__ __forceinline__ void formal(T& I, T j0, T a0, T S0, T j1, T a1, T S1,
   const T dtau = (a0 + a1) * hds;
   const T theo = (j0 + j1) * hds;
   T x, a, b;
-  if (dtau > (T)1.0e-6) {
-    Math<T>::coeffs(dtau, x, a, b);
-  } else {
-    a = (T)0.5 * dtau; b = a; x = (T)1 - dtau;
-  }
+  Math<T>::coeffs(dtau, x, a, b);
   const T src1 = a0 > (T)0 ? S0 : (a1 > (T)0 ? S1 : (T)0);
   const T src2 = a1 > (T)0 ? S1 : (a0 > (T)0 ? S0 : (T)0);
   T q = dtau > (T)1.0e-9f ? a * src1 + b * src2 : theo;
@@ -195,11 +198,32 @@ __device__ __forceinline__ void point_state(const Pt<T>& p, T phi, T& j, T& a, T
   S = a > (T)0 ? j * Math<T>::rcp(a) : (T)0;
 }
 
+// Lines sharing one ray per work item. The integrated (line, channel) pairs of all of
+// them are packed densely over the 32 lanes x C slots of the warp.
+constexpr int kGroup = 8;
+constexpr int kChBits = 11;               // channel index bits of a packed (line, channel)
+constexpr int kMaxChannels = 1 << kChBits;
+
+template <typename T>
+struct alignas(16) LineVals { T jf, af, jd, ad; };
+
+// Per-warp staging of one 32-node chunk; entry 0 carries the last node of the previous
+// chunk, entries 1..32 the nodes of this chunk.
 template <typename T>
 struct WarpStage {
-  T jf[32], af[32], jd[32], ad[32], vl[32];
-  T hds[32], ds[32], rlw[32], nrm[32], dvs[32], q[32], ids[32];
-  unsigned flags[32];
+  LineVals<T> lv[kGroup][33];
+  T vl[33], hds[33], ds[33], rlw[33], q[33], ids[33], dvs[33];
+  unsigned flags[33];
+  T contv[kGroup];
+  float mn[kGroup], mx[kGroup];
+  int cont_ch[kGroup];
+};
+
+// Per-lane state of the walk slots between chunks and slot pairs.
+template <typename T, int C>
+struct SlotState {
+  T I[C][32], j0[C][32], a0[C][32], S0[C][32], w[C][32];
+  int ll[C][32];
 };
 
 __device__ __forceinline__ unsigned lanemask_lt() {
@@ -209,80 +233,187 @@ __device__ __forceinline__ unsigned lanemask_lt() {
 }
 
 template <typename T>
-__device__ __forceinline__ void load_corners(const T* __restrict__ tab, int c00, unsigned misc, int nth, T wr, T wt,
-                                             T& jf, T& af, T& jd, T& ad) {
+__device__ __forceinline__ LineVals<T> ld_lv(const T* p) {
+  LineVals<T> v;
+  if constexpr (sizeof(T) == 4) {
+    const float4 q = __ldg(reinterpret_cast<const float4*>(p));
+    v.jf = q.x; v.af = q.y; v.jd = q.z; v.ad = q.w;
+  } else {
+    const double2 a = __ldg(reinterpret_cast<const double2*>(p));
+    const double2 b = __ldg(reinterpret_cast<const double2*>(p) + 1);
+    v.jf = a.x; v.af = a.y; v.jd = b.x; v.ad = b.y;
+  }
+  return v;
+}
+
+struct Corners { int c00, c01, c10, c11; };
+__device__ __forceinline__ Corners corners(int c00, unsigned misc, int nth) {
   const int dto = (int)(misc & 0xFFFFu) - 32768;
   const int dro = (int)((misc >> 16) & 3u) - 1;
-  const int c01 = c00 + dto, c10 = c00 + dro * nth, c11 = c10 + dto;
-  T v00[4], v01[4] = {0, 0, 0, 0}, v10[4] = {0, 0, 0, 0}, v11[4] = {0, 0, 0, 0};
-#pragma unroll
-  for (int i = 0; i < 4; i++) v00[i] = __ldg(&tab[4 * (size_t)c00 + i]);
-  if (wt != (T)0) {
-#pragma unroll
-    for (int i = 0; i < 4; i++) v01[i] = __ldg(&tab[4 * (size_t)c01 + i]);
-  }
+  Corners c;
+  c.c00 = c00; c.c01 = c00 + dto; c.c10 = c00 + dro * nth; c.c11 = c.c10 + dto;
+  return c;
+}
+
+// bilinear interpolation with the reference's weighting; zero-weight corners not read
+template <typename T>
+__device__ __forceinline__ LineVals<T> interp_lv(const T* __restrict__ tab, const Corners& c, int nl, int l, T wr,
+                                                 T wt) {
+  const LineVals<T> z = {0, 0, 0, 0};
+  const LineVals<T> v00 = ld_lv(tab + 4 * ((size_t)c.c00 * nl + l));
+  const LineVals<T> v01 = wt != (T)0 ? ld_lv(tab + 4 * ((size_t)c.c01 * nl + l)) : z;
+  LineVals<T> v10 = z, v11 = z;
   if (wr != (T)0) {
-#pragma unroll
-    for (int i = 0; i < 4; i++) v10[i] = __ldg(&tab[4 * (size_t)c10 + i]);
-    if (wt != (T)0) {
-#pragma unroll
-      for (int i = 0; i < 4; i++) v11[i] = __ldg(&tab[4 * (size_t)c11 + i]);
-    }
+    v10 = ld_lv(tab + 4 * ((size_t)c.c10 * nl + l));
+    if (wt != (T)0) v11 = ld_lv(tab + 4 * ((size_t)c.c11 * nl + l));
   }
-  T out[4];
-#pragma unroll
-  for (int i = 0; i < 4; i++)
-    out[i] = ((T)1 - wr) * (((T)1 - wt) * v00[i] + wt * v01[i]) + wr * (((T)1 - wt) * v10[i] + wt * v11[i]);
-  jf = out[0]; af = out[1]; jd = out[2]; ad = out[3];
+  const T ar = (T)1 - wr, at = (T)1 - wt;
+  LineVals<T> o;
+  o.jf = ar * (at * v00.jf + wt * v01.jf) + wr * (at * v10.jf + wt * v11.jf);
+  o.af = ar * (at * v00.af + wt * v01.af) + wr * (at * v10.af + wt * v11.af);
+  o.jd = ar * (at * v00.jd + wt * v01.jd) + wr * (at * v10.jd + wt * v11.jd);
+  o.ad = ar * (at * v00.ad + wt * v01.ad) + wr * (at * v10.ad + wt * v11.ad);
+  return o;
 }
 
 template <typename T>
-__device__ __forceinline__ T load_nsum(const T* __restrict__ ns, int c00, unsigned misc, int nth, T wr, T wt) {
-  const int dto = (int)(misc & 0xFFFFu) - 32768;
-  const int dro = (int)((misc >> 16) & 3u) - 1;
-  const int c01 = c00 + dto, c10 = c00 + dro * nth, c11 = c10 + dto;
-  const T v00 = __ldg(&ns[c00]);
-  const T v01 = wt != (T)0 ? __ldg(&ns[c01]) : (T)0;
+__device__ __forceinline__ T interp_1(const T* __restrict__ v, const Corners& c, int nl, int l, T wr, T wt) {
+  const T v00 = __ldg(&v[(size_t)c.c00 * nl + l]);
+  const T v01 = wt != (T)0 ? __ldg(&v[(size_t)c.c01 * nl + l]) : (T)0;
   T v10 = 0, v11 = 0;
-  if (wr != (T)0) { v10 = __ldg(&ns[c10]); if (wt != (T)0) v11 = __ldg(&ns[c11]); }
+  if (wr != (T)0) {
+    v10 = __ldg(&v[(size_t)c.c10 * nl + l]);
+    if (wt != (T)0) v11 = __ldg(&v[(size_t)c.c11 * nl + l]);
+  }
   return ((T)1 - wr) * (((T)1 - wt) * v00 + wt * v01) + wr * (((T)1 - wt) * v10 + wt * v11);
 }
 
-// Walk all channels held by this lane over the ray. Returns the formal-solution
-// step count of the lane.
+template <typename T>
+struct SlotOutT { T I, j0, a0, S0; int steps; };
+
+// Segment with a state reset (first segment, central hole, star) or with SUBGRID
+// refinement (line.F:4703-4833): interior points i = ia..ib of the 31-point grid over
+// [s_c - 3 l, s_c + 3 l] strictly inside (0, ds), then the segment end. Kept out of line:
+// it is rare, and inlining it per slot overflows the instruction cache.
+template <typename T>
+__device__ __noinline__ SlotOutT<T> slot_slow(bool init, bool sub, T w, LineVals<T> v0, LineVals<T> v1, T vl0,
+                                               T vl1, T rl, T hds, T q, T dsf, T dvs, T ids, T I, T j0, T a0, T S0) {
+  const Pt<T> p0 = {v0.jd, v0.ad, v0.jf, v0.af, vl0};
+  const Pt<T> p1 = {v1.jd, v1.ad, v1.jf, v1.af, vl1};
+  if (init) {
+    const T ph0 = profile(w, vl0, rl, rl);
+    point_state(p0, ph0, j0, a0, S0);
+  }
+  int ia = 1, ib = 0;
+  T sleft = 0, lg = 0;
+  if (sub) {
+    const T s_c = dsf * (w - vl0) / dvs;
+    const T dls = dsf / q;
+    const T sright = s_c + (T)3 * dls;
+    sleft = s_c - (T)3 * dls;
+    if (sright > (T)0 && sleft < dsf) {
+      lg = (sright - sleft) / (T)30;
+      ia = 0;
+      if (!(sleft > (T)0)) {
+        ia = (int)((-sleft) / lg);
+        ia = ia < 0 ? 0 : (ia > 31 ? 31 : ia);
+        while (ia > 0 && sleft + (T)(ia - 1) * lg > (T)0) ia--;
+        while (ia <= 30 && !(sleft + (T)ia * lg > (T)0)) ia++;
+      }
+      ib = 30;
+      if (!(sleft + (T)30 * lg < dsf)) {
+        ib = (int)((dsf - sleft) / lg);
+        ib = ib < -1 ? -1 : (ib > 30 ? 30 : ib);
+        while (ib < 30 && sleft + (T)(ib + 1) * lg < dsf) ib++;
+        while (ib >= 0 && !(sleft + (T)ib * lg < dsf)) ib--;
+      }
+    }
+  }
+  int steps = 0;
+  T sp = 0;
+  for (int i = ia; i <= ib + 1; i++) {
+    T s;
+    Pt<T> pq;
+    if (i <= ib) {
+      s = sleft + (T)i * lg;
+      const T e = s * ids, ep = (T)1 - e;
+      pq.jd = ep * p0.jd + e * p1.jd; pq.ad = ep * p0.ad + e * p1.ad;
+      pq.jf = ep * p0.jf + e * p1.jf; pq.af = ep * p0.af + e * p1.af;
+      pq.vl = ep * p0.vl + e * p1.vl;
+    } else {
+      s = dsf; pq = p1;
+    }
+    const T ph = profile(w, pq.vl, rl, rl);
+    T j1, a1, S1;
+    point_state(pq, ph, j1, a1, S1);
+    const T h = (ia <= ib) ? (T)0.5 * (s - sp) : hds;
+    formal(I, j0, a0, S0, j1, a1, S1, h);
+    j0 = j1; a0 = a1; S0 = S1;
+    sp = s;
+    steps++;
+  }
+  SlotOutT<T> o;
+  o.I = I; o.j0 = j0; o.a0 = a0; o.S0 = S0; o.steps = steps;
+  return o;
+}
+
+// Formal solution of the (line, channel) pairs list[0..nt) of lines l0.. of one ray.
+// The per-line tables carry the profile normalisation 0.56419583546/(3.33567e-6 nu0), so
+// the profile of every slot is rlw * exp(-u^2) with the node's shared 1/linewidth.
+// Work order: per 32-node chunk, per pair of slots (two independent channels per lane),
+// all nodes of the chunk; the slot state lives in shared memory between pairs.
 template <typename T, int C>
-__device__ long long walk_ray(const WalkParams<T>& P, WarpStage<T>& S, int line, int ray, int K,
-                              const short* list, int nint, T (&I)[C], int lane) {
+__device__ long long walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<T, C>& SS, int ray, int K,
+                              int l0, int gl, const unsigned short* list, int nt, int lane) {
   const NodeBuf<T>& nb = P.nb;
   const size_t row = (size_t)ray * nb.kmax;
-  const T* tab = P.tab + (size_t)line * P.ncell * 4;
-  const LineConst<T> lc = P.lc[line];
-  const T* wch = P.wch + (size_t)line * P.nfr;
-  const T* star = P.star + (size_t)line * P.nfr;
-  const int nslot = (nint + 31) >> 5;
-  T w[C], j0[C], a0[C], S0[C];
-  int ch[C];
-#pragma unroll
-  for (int j = 0; j < C; j++) {
+  const int nl = P.nlines;
+  const int nslot = (nt + 31) >> 5;
+  const int npair = (nslot + 1) >> 1;
+  for (int j = 0; j < 2 * npair && j < C; j++) {
     const int idx = j * 32 + lane;
-    ch[j] = idx < nint ? list[idx] : -1;
-    w[j] = ch[j] >= 0 ? wch[ch[j]] : (T)0;
-    I[j] = lc.istart;
-    j0[j] = 0; a0[j] = 0; S0[j] = 0;
+    int L = -1;
+    T w = 0, I = 0;
+    if (idx < nt) {
+      const unsigned e = list[idx];
+      L = (int)(e >> kChBits);
+      w = P.wch[(size_t)(l0 + L) * P.nfr + (e & (kMaxChannels - 1))];
+      I = P.lc[l0 + L].istart;
+    }
+    SS.ll[j][lane] = L; SS.w[j][lane] = w; SS.I[j][lane] = I;
+    SS.j0[j][lane] = 0; SS.a0[j][lane] = 0; SS.S0[j][lane] = 0;
+  }
+  // central beam: the node where the ray first reaches the innermost cell mixes in the
+  // star (telescope.F:4166-4191)
+  int star_node = -1;
+  if (ray == 0) {
+    for (int kb = 0; kb < K && star_node < 0; kb += 32) {
+      const int k = kb + lane;
+      const bool f = k >= 1 && k < K && (nb.misc[row + k] & kFlagIr1);
+      const unsigned m = __ballot_sync(0xffffffffu, f);
+      if (m) star_node = kb + __ffs(m) - 1;
+    }
   }
   long long steps = 0;
-  Pt<T> p0 = {0, 0, 0, 0, 0};
   T lw_last = 0;
-  bool init = true, star_done = false;
   for (int kb = 0; kb < K; kb += 32) {
+    if (kb > 0) {   // carry the last node of the previous chunk into entry 0
+      if (lane == 0) {
+        S.vl[0] = S.vl[32]; S.hds[0] = S.hds[32]; S.ds[0] = S.ds[32]; S.rlw[0] = S.rlw[32];
+        S.q[0] = S.q[32]; S.ids[0] = S.ids[32]; S.dvs[0] = S.dvs[32]; S.flags[0] = S.flags[32];
+      }
+      if (lane < gl) S.lv[lane][0] = S.lv[lane][32];
+      __syncwarp();
+    }
     const int k = kb + lane;
-    T jf = 0, af = 0, jd = 0, ad = 0, vl = 0, ds = 0, dvs = 0, lwk = 0;
+    T vl = 0, ds = 0, dvs = 0, lwk = 0;
     unsigned misc = 0;
     if (k < K) {
       const size_t o = row + k;
       const T wr = nb.wr[o], wt = nb.wt[o];
       misc = nb.misc[o];
-      load_corners(tab, nb.c00[o], misc, P.nth, wr, wt, jf, af, jd, ad);
+      const Corners c = corners(nb.c00[o], misc, P.nth);
+      for (int l = 0; l < gl; l++) S.lv[l][lane + 1] = interp_lv(P.tab, c, nl, l0 + l, wr, wt);
       vl = nb.vl[o]; ds = nb.ds[o]; dvs = nb.dvseg[o]; lwk = nb.lw[o];
     }
     T lwp = __shfl_up_sync(0xffffffffu, lwk, 1);
@@ -290,81 +421,72 @@ __device__ long long walk_ray(const WalkParams<T>& P, WarpStage<T>& S, int line,
     lw_last = __shfl_sync(0xffffffffu, lwk, 31);
     const T lwav = (T)0.5 * (lwp + lwk);
     const T rlw = lwav > (T)0 ? Math<T>::div((T)1, lwav) : (T)0;
-    const T qv = (dvs < (T)0 ? -dvs : dvs) * P.kq * rlw;
-    S.jf[lane] = jf; S.af[lane] = af; S.jd[lane] = jd; S.ad[lane] = ad; S.vl[lane] = vl;
-    S.hds[lane] = (T)0.5 * ds; S.ds[lane] = ds; S.rlw[lane] = rlw; S.nrm[lane] = lc.cphi * rlw;
-    S.dvs[lane] = dvs; S.q[lane] = qv; S.ids[lane] = ds > (T)0 ? Math<T>::div((T)1, ds) : (T)0;
-    S.flags[lane] = misc;
+    S.vl[lane + 1] = vl; S.hds[lane + 1] = (T)0.5 * ds; S.ds[lane + 1] = ds; S.rlw[lane + 1] = rlw;
+    S.q[lane + 1] = (dvs < (T)0 ? -dvs : dvs) * P.kq * rlw;
+    S.ids[lane + 1] = ds > (T)0 ? Math<T>::div((T)1, ds) : (T)0;
+    S.dvs[lane + 1] = dvs;
+    S.flags[lane + 1] = misc;
     __syncwarp();
     const int nn = min(32, K - kb);
-    for (int n = 0; n < nn; n++) {
-      const Pt<T> p1 = {S.jd[n], S.ad[n], S.jf[n], S.af[n], S.vl[n]};
-      if (kb + n == 0) { p0 = p1; continue; }
-      const unsigned fl = S.flags[n];
-      if (fl & kFlagHole) init = true;
-      if (ray == 0 && (fl & kFlagIr1) && !star_done) {
-#pragma unroll
-        for (int j = 0; j < C; j++)
-          if (j < nslot && ch[j] >= 0) I[j] = ((T)1 - P.fstar) * I[j] + P.fstar * star[ch[j]];
-        star_done = true;
-        init = true;
+    const int n0 = kb == 0 ? 1 : 0;   // node 0 of the ray starts the walk
+    for (int pp = 0; pp < npair; pp++) {
+      const int ja = 2 * pp, jb = ja + 1;
+      const bool hb = jb < C;
+      T Ia = SS.I[ja][lane], j0a = SS.j0[ja][lane], a0a = SS.a0[ja][lane], S0a = SS.S0[ja][lane];
+      const T wa = SS.w[ja][lane];
+      const int La = SS.ll[ja][lane];
+      T Ib = 0, j0b = 0, a0b = 0, S0b = 0, wb = 0;
+      int Lb = -1;
+      if (hb) {
+        Ib = SS.I[jb][lane]; j0b = SS.j0[jb][lane]; a0b = SS.a0[jb][lane]; S0b = SS.S0[jb][lane];
+        wb = SS.w[jb][lane]; Lb = SS.ll[jb][lane];
       }
-      const T rlw = S.rlw[n], nrm = S.nrm[n], hds = S.hds[n], q = S.q[n];
-      const bool sub = (T)6 * q > (T)1;
-#pragma unroll
-      for (int j = 0; j < C; j++) {
-        if (j >= nslot) break;
-        if (ch[j] < 0) continue;
-        if (init) {
-          const T ph0 = profile(w[j], p0.vl, rlw, nrm);
-          point_state(p0, ph0, j0[j], a0[j], S0[j]);
+      const int la = La < 0 ? 0 : La, lb = Lb < 0 ? 0 : Lb;
+      const int va = La >= 0 ? 1 : 0, vb = Lb >= 0 ? 1 : 0;
+      for (int n = n0; n < nn; n++) {
+        const int g = kb + n;
+        const unsigned fl = S.flags[n + 1];
+        bool init = g == 1 || (fl & kFlagHole);
+        if (g == star_node) {
+          if (La >= 0) Ia = ((T)1 - P.fstar) * Ia + P.fstar * P.star[(size_t)(l0 + La) * P.nfr + (list[ja * 32 + lane] & (kMaxChannels - 1))];
+          if (Lb >= 0) Ib = ((T)1 - P.fstar) * Ib + P.fstar * P.star[(size_t)(l0 + Lb) * P.nfr + (list[jb * 32 + lane] & (kMaxChannels - 1))];
+          init = true;
         }
-        bool done = false;
-        if (sub) {
-          const T dsf = S.ds[n];
-          const T s_c = dsf * (w[j] - p0.vl) / S.dvs[n];
-          const T dls = dsf / q;
-          const T sright = s_c + (T)3 * dls, sleft = s_c - (T)3 * dls;
-          if (sright > (T)0 && sleft < dsf) {
-            const T lg = (sright - sleft) / (T)30;
-            const T ids = S.ids[n];
-            T sp = 0;
-            for (int i = 0; i <= 31; i++) {
-              T s, e;
-              Pt<T> pq;
-              if (i < 31) {
-                s = sleft + (T)i * lg;
-                if (!(s > (T)0 && s < dsf)) continue;
-                e = s * ids;
-                const T ep = (T)1 - e;
-                pq.jd = ep * p0.jd + e * p1.jd; pq.ad = ep * p0.ad + e * p1.ad;
-                pq.jf = ep * p0.jf + e * p1.jf; pq.af = ep * p0.af + e * p1.af;
-                pq.vl = ep * p0.vl + e * p1.vl;
-              } else {
-                s = dsf; pq = p1;
-              }
-              const T ph = profile(w[j], pq.vl, rlw, nrm);
-              T j1, a1, S1;
-              point_state(pq, ph, j1, a1, S1);
-              formal(I[j], j0[j], a0[j], S0[j], j1, a1, S1, (T)0.5 * (s - sp));
-              j0[j] = j1; a0[j] = a1; S0[j] = S1;
-              sp = s;
-              steps++;
-            }
-            done = true;
+        const T vl1 = S.vl[n + 1], rl = S.rlw[n + 1], hds = S.hds[n + 1], q = S.q[n + 1];
+        const bool sub = (T)6 * q > (T)1;
+        const LineVals<T> v1a = S.lv[la][n + 1];
+        const LineVals<T> v1b = S.lv[lb][n + 1];
+        if (!init && !sub) {
+          T j1, a1, S1;
+          {
+            const Pt<T> p1 = {v1a.jd, v1a.ad, v1a.jf, v1a.af, vl1};
+            point_state(p1, profile(wa, vl1, rl, rl), j1, a1, S1);
+            formal(Ia, j0a, a0a, S0a, j1, a1, S1, hds);
+            j0a = j1; a0a = a1; S0a = S1;
+          }
+          {
+            const Pt<T> p1 = {v1b.jd, v1b.ad, v1b.jf, v1b.af, vl1};
+            point_state(p1, profile(wb, vl1, rl, rl), j1, a1, S1);
+            formal(Ib, j0b, a0b, S0b, j1, a1, S1, hds);
+            j0b = j1; a0b = a1; S0b = S1;
+          }
+          steps += va + vb;
+        } else {
+          const T vl0 = S.vl[n], dsf = S.ds[n + 1], dvs = S.dvs[n + 1], ids = S.ids[n + 1];
+          if (La >= 0) {
+            const SlotOutT<T> o = slot_slow<T>(init, sub, wa, S.lv[la][n], v1a, vl0, vl1, rl, hds, q, dsf, dvs, ids,
+                                               Ia, j0a, a0a, S0a);
+            Ia = o.I; j0a = o.j0; a0a = o.a0; S0a = o.S0; steps += o.steps;
+          }
+          if (Lb >= 0) {
+            const SlotOutT<T> o = slot_slow<T>(init, sub, wb, S.lv[lb][n], v1b, vl0, vl1, rl, hds, q, dsf, dvs, ids,
+                                               Ib, j0b, a0b, S0b);
+            Ib = o.I; j0b = o.j0; a0b = o.a0; S0b = o.S0; steps += o.steps;
           }
         }
-        if (!done) {
-          const T ph = profile(w[j], p1.vl, rlw, nrm);
-          T j1, a1, S1;
-          point_state(p1, ph, j1, a1, S1);
-          formal(I[j], j0[j], a0[j], S0[j], j1, a1, S1, hds);
-          j0[j] = j1; a0[j] = a1; S0[j] = S1;
-          steps++;
-        }
       }
-      init = false;
-      p0 = p1;
+      SS.I[ja][lane] = Ia; SS.j0[ja][lane] = j0a; SS.a0[ja][lane] = a0a; SS.S0[ja][lane] = S0a;
+      if (hb) { SS.I[jb][lane] = Ib; SS.j0[jb][lane] = j0b; SS.a0[jb][lane] = a0b; SS.S0[jb][lane] = S0b; }
     }
     __syncwarp();
   }
@@ -372,145 +494,170 @@ __device__ long long walk_ray(const WalkParams<T>& P, WarpStage<T>& S, int line,
 }
 
 template <typename T, int C>
-__global__ void __launch_bounds__(256) k_walk(WalkParams<T> P) {
+__global__ void __launch_bounds__(128) k_walk(WalkParams<T> P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  const int nfrp = (P.nfr + 7) & ~7;
+  const int cap = kGroup * P.nfr;
+  const int capp = (cap + 7) & ~7;
   WarpStage<T>* stages = reinterpret_cast<WarpStage<T>*>(smem_raw);
-  short* lists = reinterpret_cast<short*>(smem_raw + sizeof(WarpStage<T>) * nw);
+  SlotState<T, C>* sstates = reinterpret_cast<SlotState<T, C>*>(smem_raw + sizeof(WarpStage<T>) * nw);
+  unsigned short* lists =
+      reinterpret_cast<unsigned short*>(smem_raw + (sizeof(WarpStage<T>) + sizeof(SlotState<T, C>)) * nw);
   WarpStage<T>& S = stages[wib];
-  short* list = lists + (size_t)wib * nfrp;
-  __shared__ T cont_val[8];
+  SlotState<T, C>& SS = sstates[wib];
+  unsigned short* list = lists + (size_t)wib * capp;
   unsigned long long st_steps = 0, st_int = 0, st_nodes = 0;
   const NodeBuf<T>& nb = P.nb;
+  const int nl = P.nlines;
+  const int ngroups = (nl + kGroup - 1) / kGroup;
   for (;;) {
     int item = 0;
     if (lane == 0) item = atomicAdd(P.work, 1);
     item = __shfl_sync(0xffffffffu, item, 0);
     if (item >= P.nitems) break;
-    const int line = item / nb.nrays, ray = item - line * nb.nrays;
+    const int g = item / nb.nrays, ray = item - g * nb.nrays;
+    const int l0 = g * kGroup, gl = min(kGroup, nl - l0);
     const int K = nb.nnodes[ray];
     if (nb.status[ray] != 0 || K < 1) {
       if (lane == 0) atomicCAS(P.err, 0, 100 + nb.status[ray]);
       continue;
     }
     const size_t row = (size_t)ray * nb.kmax;
-    const double* velo = P.velo + (size_t)line * P.nfr;
-    // 1. velocity window of the ray from node projected velocities (telescope.F:4265-4270)
-    double lo = -1e300, hi = 1e300;
+    // 1. velocity window of the ray per line (telescope.F:4265-4270): node projected
+    //    velocities where N_up + N_low exceeds 1e-3, nodes 0 .. K-2
+    float mn[kGroup], mx[kGroup];
+#pragma unroll
+    for (int l = 0; l < kGroup; l++) { mn[l] = 1.0f; mx[l] = -1.0f; }
+    __syncwarp();
     if (ray != 0) {
-      float mn = 1.0f, mx = -1.0f;
-      const T* ns = P.nsum + (size_t)line * P.ncell;
       for (int k = lane; k < K - 1; k += 32) {
         const size_t o = row + k;
-        const T n = load_nsum(ns, nb.c00[o], nb.misc[o], P.nth, nb.wr[o], nb.wt[o]);
-        if (n > (T)1.0e-3) { const float d = nb.dvf[o]; mn = fminf(mn, d); mx = fmaxf(mx, d); }
+        const T wr = nb.wr[o], wt = nb.wt[o];
+        const Corners c = corners(nb.c00[o], nb.misc[o], P.nth);
+        const float d = nb.dvf[o];
+#pragma unroll
+        for (int l = 0; l < kGroup; l++) {
+          if (l < gl && interp_1(P.nsum, c, nl, l0 + l, wr, wt) > (T)1.0e-3) {
+            mn[l] = fminf(mn[l], d); mx[l] = fmaxf(mx[l], d);
+          }
+        }
       }
 #pragma unroll
-      for (int off = 16; off > 0; off >>= 1) {
-        mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, off));
-        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+      for (int l = 0; l < kGroup; l++) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+          mn[l] = fminf(mn[l], __shfl_xor_sync(0xffffffffu, mn[l], off));
+          mx[l] = fmaxf(mx[l], __shfl_xor_sync(0xffffffffu, mx[l], off));
+        }
       }
-      lo = (double)mn - 2.0 * P.aksmax_c;
-      hi = (double)mx + 2.0 * P.aksmax_c;
     }
-    // 2. channels to integrate: channel 1, the in-window channels, and the channel that
-    //    supplies the continuum for the rest (telescope.F:541-613)
-    int nint = 0, cont_ch = -1;
-    bool in0 = true;
-    if (ray != 0) in0 = velo[0] <= hi && velo[0] >= lo;
-    if (ray != 0 && !in0) cont_ch = 0;
-    for (int cb = 0; cb < P.nfr; cb += 32) {
-      const int c = cb + lane;
-      const bool valid = c < P.nfr;
-      const bool in = valid && (ray == 0 || (velo[c] <= hi && velo[c] >= lo));
-      if (cont_ch < 0 && ray != 0) {
-        const unsigned outm = __ballot_sync(0xffffffffu, valid && !in && c >= 1);
-        if (outm) cont_ch = cb + __ffs(outm) - 1;
-      }
-      const bool take = valid && (c == 0 || in || c == cont_ch);
-      const unsigned m = __ballot_sync(0xffffffffu, take);
-      if (take) list[nint + __popc(m & lanemask_lt())] = (short)c;
-      nint += __popc(m);
+    if (lane == 0) {
+#pragma unroll
+      for (int l = 0; l < kGroup; l++) { S.mn[l] = mn[l]; S.mx[l] = mx[l]; }
     }
     __syncwarp();
-    // 3. formal solution of the selected channels, in tiles of 32*C channels
-    T* img = P.img + ((size_t)line * nb.nrays + ray) * P.nfr;
-    T contv = 0;
+    // 2. (line, channel) pairs to integrate: channel 1, the in-window channels and the
+    //    channel that supplies the continuum of the others (telescope.F:541-613)
+    int nint = 0;
+    for (int l = 0; l < gl; l++) {
+      int cc = -1;
+      const double* velo = P.velo + (size_t)(l0 + l) * P.nfr;
+      const double lo = (double)S.mn[l] - 2.0 * P.aksmax_c, hi = (double)S.mx[l] + 2.0 * P.aksmax_c;
+      if (ray != 0 && !(velo[0] <= hi && velo[0] >= lo)) cc = 0;
+      for (int cb = 0; cb < P.nfr; cb += 32) {
+        const int c = cb + lane;
+        const bool valid = c < P.nfr;
+        const bool in = valid && (ray == 0 || (velo[c] <= hi && velo[c] >= lo));
+        if (cc < 0 && ray != 0) {
+          const unsigned outm = __ballot_sync(0xffffffffu, valid && !in && c >= 1);
+          if (outm) cc = cb + __ffs(outm) - 1;
+        }
+        const bool take = valid && (c == 0 || in || c == cc);
+        const unsigned m = __ballot_sync(0xffffffffu, take);
+        if (take) list[nint + __popc(m & lanemask_lt())] = (unsigned short)((l << kChBits) | c);
+        nint += __popc(m);
+      }
+      if (lane == 0) S.cont_ch[l] = cc;
+    }
+    __syncwarp();
+    // 3. formal solution of the selected pairs, in tiles of 32*C
     for (int tb = 0; tb < nint; tb += 32 * C) {
       const int nt = min(32 * C, nint - tb);
-      T I[C];
-      st_steps += walk_ray<T, C>(P, S, line, ray, K, list + tb, nt, I, lane);
-#pragma unroll
+      st_steps += walk_ray<T, C>(P, S, SS, ray, K, l0, gl, list + tb, nt, lane);
       for (int j = 0; j < C; j++) {
         const int idx = j * 32 + lane;
         if (idx < nt) {
-          const int c = list[tb + idx];
-          img[c] = I[j];
-          if (c == cont_ch) cont_val[wib] = I[j];
+          const unsigned e = list[tb + idx];
+          const int l = (int)(e >> kChBits), c = (int)(e & (kMaxChannels - 1));
+          const T Iv = SS.I[j][lane];
+          P.img[((size_t)(l0 + l) * nb.nrays + ray) * P.nfr + c] = Iv;
+          if (c == S.cont_ch[l]) S.contv[l] = Iv;
         }
       }
     }
     st_int += nint;
     st_nodes += (unsigned long long)nint * K;
     __syncwarp();
-    if (cont_ch >= 0) contv = cont_val[wib];
-    // 4. continuum copy for the rest of the channels
-    if (cont_ch >= 0) {
+    // 4. continuum copy for the other channels of each line
+    for (int l = 0; l < gl; l++) {
+      const int cc = S.cont_ch[l];
+      if (cc < 0) continue;
+      const double* velo = P.velo + (size_t)(l0 + l) * P.nfr;
+      const double lo = (double)S.mn[l] - 2.0 * P.aksmax_c, hi = (double)S.mx[l] + 2.0 * P.aksmax_c;
+      T* img = P.img + ((size_t)(l0 + l) * nb.nrays + ray) * P.nfr;
+      const T contv = S.contv[l];
       if (contv != (T)0) {
         for (int c = lane; c < P.nfr; c += 32) {
           const bool in = velo[c] <= hi && velo[c] >= lo;
-          if (!(c == 0 || in || c == cont_ch)) img[c] = contv;
+          if (!(c == 0 || in || c == cc)) img[c] = contv;
         }
-      } else {
-        // a zero continuum is recomputed channel by channel in the reference: integrate
-        // every remaining out-of-window channel, then apply its sequential copy rule
-        int n2 = 0;
-        for (int cb = 0; cb < P.nfr; cb += 32) {
-          const int c = cb + lane;
-          const bool valid = c < P.nfr;
-          const bool take = valid && !(c == 0 || (velo[c] <= hi && velo[c] >= lo) || c == cont_ch);
-          const unsigned m = __ballot_sync(0xffffffffu, take);
-          if (take) list[n2 + __popc(m & lanemask_lt())] = (short)c;
-          n2 += __popc(m);
-        }
-        __syncwarp();
-        for (int tb = 0; tb < n2; tb += 32 * C) {
-          const int nt = min(32 * C, n2 - tb);
-          T I[C];
-          st_steps += walk_ray<T, C>(P, S, line, ray, K, list + tb, nt, I, lane);
-#pragma unroll
-          for (int j = 0; j < C; j++) {
-            const int idx = j * 32 + lane;
-            if (idx < nt) img[list[tb + idx]] = I[j];
-          }
-        }
-        st_int += n2;
-        st_nodes += (unsigned long long)n2 * K;
-        __syncwarp();
-        if (lane == 0) {
-          T cur = 0;
-          bool have = false;
-          for (int c = 0; c < P.nfr; c++) {
-            const bool in = velo[c] <= hi && velo[c] >= lo;
-            if (c != cont_ch && (c == 0 || in)) continue;
-            if (have) img[c] = cur;
-            else if (img[c] != (T)0) { cur = img[c]; have = true; }
-          }
+        continue;
+      }
+      // a zero continuum is recomputed channel by channel in the reference: integrate
+      // every other out-of-window channel, then apply its sequential copy rule
+      int n2 = 0;
+      for (int cb = 0; cb < P.nfr; cb += 32) {
+        const int c = cb + lane;
+        const bool valid = c < P.nfr;
+        const bool take = valid && !(c == 0 || (velo[c] <= hi && velo[c] >= lo) || c == cc);
+        const unsigned m = __ballot_sync(0xffffffffu, take);
+        if (take) list[n2 + __popc(m & lanemask_lt())] = (unsigned short)((l << kChBits) | c);
+        n2 += __popc(m);
+      }
+      __syncwarp();
+      for (int tb = 0; tb < n2; tb += 32 * C) {
+        const int nt = min(32 * C, n2 - tb);
+        st_steps += walk_ray<T, C>(P, S, SS, ray, K, l0, gl, list + tb, nt, lane);
+        for (int j = 0; j < C; j++) {
+          const int idx = j * 32 + lane;
+          if (idx < nt) img[list[tb + idx] & (kMaxChannels - 1)] = SS.I[j][lane];
         }
       }
+      st_int += n2;
+      st_nodes += (unsigned long long)n2 * K;
+      __syncwarp();
+      if (lane == 0) {
+        T cur = 0;
+        bool have = false;
+        for (int c = 0; c < P.nfr; c++) {
+          const bool in = velo[c] <= hi && velo[c] >= lo;
+          if (c != cc && (c == 0 || in)) continue;
+          if (have) img[c] = cur;
+          else if (img[c] != (T)0) { cur = img[c]; have = true; }
+        }
+      }
+      __syncwarp();
     }
     __syncwarp();
   }
 #pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    st_steps += __shfl_xor_sync(0xffffffffu, st_steps, off);
-  }
+  for (int off = 16; off > 0; off >>= 1) st_steps += __shfl_xor_sync(0xffffffffu, st_steps, off);
   if (lane == 0) {
     atomicAdd(&P.counters[0], st_steps);
     atomicAdd(&P.counters[1], st_int);
     atomicAdd(&P.counters[2], st_nodes);
   }
+  (void)ngroups;
 }
 
 // ------------------------------------------------------------------------------------
@@ -630,9 +777,10 @@ cudaError_t launch_geometry(const GeoParams& p, const NodeBuf<T>& nb, int ray0, 
 
 template <typename T, int C>
 static cudaError_t launch_walk_c(const WalkParams<T>& P, int nsm, cudaStream_t s) {
-  const int warps = 8, threads = warps * 32;
-  const int nfrp = (P.nfr + 7) & ~7;
-  const size_t smem = sizeof(WarpStage<T>) * warps + sizeof(short) * (size_t)nfrp * warps;
+  const int warps = 4, threads = warps * 32;
+  const int capp = (kGroup * P.nfr + 7) & ~7;
+  const size_t smem = (sizeof(WarpStage<T>) + sizeof(SlotState<T, C>)) * warps +
+                      sizeof(unsigned short) * (size_t)capp * warps;
   cudaError_t e = cudaFuncSetAttribute(k_walk<T, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
