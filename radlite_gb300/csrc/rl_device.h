@@ -9,6 +9,8 @@ namespace rl {
 // bits 16-17: radial-corner offset + 1).
 constexpr unsigned kFlagHole = 1u << 20;   // segment ending here lies in the central hole
 constexpr unsigned kFlagIr1 = 1u << 21;    // node on the innermost radial cell (ir == 1)
+constexpr unsigned kFlagInit = 1u << 22;   // (walk) the segment ending here restarts the line state
+constexpr unsigned kFlagSub = 1u << 23;    // (walk) the segment ending here may need sub-steps
 constexpr int kIcrShift = 18;              // bits 18-19: crossing type 1..3
 
 // Node records of all rays of one camera, row-major by ray (row stride kmax).

@@ -135,21 +135,32 @@ template <> struct Math<float> {
   // interleave. Below d = 0.25 b comes from its Taylor series (the FP32 difference d - e0
   // cancels there) and e0 = d (1 - b); above, e^{-d} on the MUFU pipe.
   static __device__ __forceinline__ void coeffs(float d, float& x, float& a, float& b) {
-    const float bs = d * (0.5f - d * (1.f / 6.f - d * (1.f / 24.f - d * (1.f / 120.f - d * (1.f / 720.f - d * (1.f / 5040.f))))));
-    const float e0s = d - d * bs;
-    const float xd = expneg(d);
-    const float e0d = 1.f - xd;
-    const float bd = (d - e0d) * rcp(d);
-    const bool ser = d < 0.25f, tiny = !(d > 1.0e-6f);
-    const float e0 = ser ? e0s : e0d;
-    b = ser ? bs : bd;
-    x = ser ? 1.f - e0s : xd;
+    float xs, as, bs, xd, ad, bd;
+    series(d, xs, as, bs);
+    direct(d, xd, ad, bd);
+    const bool ser = d < 0.25f;
+    x = ser ? xs : xd; a = ser ? as : ad; b = ser ? bs : bd;
+  }
+  // d < 0.25: b from its Taylor series, e0 = d (1 - b), x = 1 - e0. Below d = 1e-6 the
+  // reference uses a = b = d/2, x = 1 - d; the series agrees with that to O(d^2), below
+  // FP32 resolution, so FP32 needs no separate branch.
+  static __device__ __forceinline__ void series(float d, float& x, float& a, float& b) {
+    b = d * (0.5f - d * (1.f / 6.f - d * (1.f / 24.f - d * (1.f / 120.f - d * (1.f / 720.f - d * (1.f / 5040.f))))));
+    const float e0 = d - d * b;
+    x = 1.f - e0;
     a = e0 - b;
-    if (tiny) { a = 0.5f * d; b = a; x = 1.f - d; }
+  }
+  static __device__ __forceinline__ void direct(float d, float& x, float& a, float& b) {
+    x = expneg(d);
+    const float e0 = 1.f - x;
+    b = (d - e0) * rcp(d);
+    a = e0 - b;
   }
 };
 
 template <> struct Math<double> {
+  static __device__ __forceinline__ void series(double d, double& x, double& a, double& b) { coeffs(d, x, a, b); }
+  static __device__ __forceinline__ void direct(double d, double& x, double& a, double& b) { coeffs(d, x, a, b); }
   static __device__ __forceinline__ double expneg(double x) { return exp(-x); }
   static __device__ __forceinline__ double rcp(double x) { return 1.0 / x; }
   static __device__ __forceinline__ double div(double a, double b) { return a / b; }
@@ -201,6 +212,7 @@ __device__ __forceinline__ void point_state(const Pt<T>& p, T phi, T& j, T& a, T
 // Lines sharing one ray per work item. The integrated (line, channel) pairs of all of
 // them are packed densely over the 32 lanes x C slots of the warp.
 constexpr int kGroup = 8;
+constexpr int kPass = 4;                  // slots walked together (independent chains per lane)
 constexpr int kChBits = 11;               // channel index bits of a packed (line, channel)
 constexpr int kMaxChannels = 1 << kChBits;
 
@@ -212,11 +224,19 @@ struct alignas(16) LineVals { T jf, af, jd, ad; };
 template <typename T>
 struct WarpStage {
   LineVals<T> lv[kGroup][33];
-  T vl[33], hds[33], ds[33], rlw[33], q[33], ids[33], dvs[33];
+  T vl[33], hds[33], ds[33], rlw[33], q[33], ids[33], dvs[33], idvs[33], hw3[33], lg[33], ilg[33];
   unsigned flags[33];
   T contv[kGroup];
   float mn[kGroup], mx[kGroup];
   int cont_ch[kGroup];
+};
+
+// Compacted SUBGRID work of one segment: the (slot, lane) channels whose refined window
+// overlaps the segment, processed one per lane.
+template <typename T>
+struct SubWork {
+  T I[128], j0[128], a0[128], S0[128], w[128];
+  unsigned char l[128];
 };
 
 // Per-lane state of the walk slots between chunks and slot pairs.
@@ -357,20 +377,69 @@ __device__ __noinline__ SlotOutT<T> slot_slow(bool init, bool sub, T w, LineVals
   return o;
 }
 
+// SUBGRID refinement of one (line, channel) over one segment whose refined window
+// overlaps it: interior points ia..ib of the grid s_i = sleft + i*lg, i = 0..30, that lie
+// strictly inside (0, ds), then the segment end (line.F:4769-4821). Called for those
+// channels only.
+template <typename T>
+__device__ __noinline__ SlotOutT<T> slot_sub(T w, LineVals<T> v0, LineVals<T> v1, T vl0, T vl1, T rl, T dsf, T ids,
+                                              T sleft, T lg, T ilg, T I, T j0, T a0, T S0) {
+  int ia = 0;
+  if (!(sleft > (T)0)) {
+    ia = (int)(-sleft * ilg);
+    ia = ia < 0 ? 0 : (ia > 31 ? 31 : ia);
+    while (ia > 0 && sleft + (T)(ia - 1) * lg > (T)0) ia--;
+    while (ia <= 30 && !(sleft + (T)ia * lg > (T)0)) ia++;
+  }
+  int ib = 30;
+  if (!(sleft + (T)30 * lg < dsf)) {
+    ib = (int)((dsf - sleft) * ilg);
+    ib = ib < -1 ? -1 : (ib > 30 ? 30 : ib);
+    while (ib < 30 && sleft + (T)(ib + 1) * lg < dsf) ib++;
+    while (ib >= 0 && !(sleft + (T)ib * lg < dsf)) ib--;
+  }
+  int steps = 0;
+  T sp = 0;
+  for (int i = ia; i <= ib + 1; i++) {
+    T s;
+    Pt<T> pq;
+    if (i <= ib) {
+      s = sleft + (T)i * lg;
+      const T e = s * ids, ep = (T)1 - e;
+      pq.jd = ep * v0.jd + e * v1.jd; pq.ad = ep * v0.ad + e * v1.ad;
+      pq.jf = ep * v0.jf + e * v1.jf; pq.af = ep * v0.af + e * v1.af;
+      pq.vl = ep * vl0 + e * vl1;
+    } else {
+      s = dsf;
+      pq.jd = v1.jd; pq.ad = v1.ad; pq.jf = v1.jf; pq.af = v1.af; pq.vl = vl1;
+    }
+    const T ph = profile(w, pq.vl, rl, rl);
+    T j1, a1, S1;
+    point_state(pq, ph, j1, a1, S1);
+    formal(I, j0, a0, S0, j1, a1, S1, (T)0.5 * (s - sp));
+    j0 = j1; a0 = a1; S0 = S1;
+    sp = s;
+    steps++;
+  }
+  SlotOutT<T> o;
+  o.I = I; o.j0 = j0; o.a0 = a0; o.S0 = S0; o.steps = steps;
+  return o;
+}
+
 // Formal solution of the (line, channel) pairs list[0..nt) of lines l0.. of one ray.
 // The per-line tables carry the profile normalisation 0.56419583546/(3.33567e-6 nu0), so
 // the profile of every slot is rlw * exp(-u^2) with the node's shared 1/linewidth.
 // Work order: per 32-node chunk, per pair of slots (two independent channels per lane),
 // all nodes of the chunk; the slot state lives in shared memory between pairs.
 template <typename T, int C>
-__device__ long long walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<T, C>& SS, int ray, int K,
-                              int l0, int gl, const unsigned short* list, int nt, int lane) {
+__device__ long long walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<T, C>& SS, SubWork<T>& SW, int ray,
+                              int K, int l0, int gl, const unsigned short* list, int nt, int lane) {
   const NodeBuf<T>& nb = P.nb;
   const size_t row = (size_t)ray * nb.kmax;
   const int nl = P.nlines;
   const int nslot = (nt + 31) >> 5;
-  const int npair = (nslot + 1) >> 1;
-  for (int j = 0; j < 2 * npair && j < C; j++) {
+  const int npass = (nslot + kPass - 1) / kPass;
+  for (int j = 0; j < kPass * npass && j < C; j++) {
     const int idx = j * 32 + lane;
     int L = -1;
     T w = 0, I = 0;
@@ -401,6 +470,7 @@ __device__ long long walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState
       if (lane == 0) {
         S.vl[0] = S.vl[32]; S.hds[0] = S.hds[32]; S.ds[0] = S.ds[32]; S.rlw[0] = S.rlw[32];
         S.q[0] = S.q[32]; S.ids[0] = S.ids[32]; S.dvs[0] = S.dvs[32]; S.flags[0] = S.flags[32];
+        S.idvs[0] = S.idvs[32]; S.hw3[0] = S.hw3[32]; S.lg[0] = S.lg[32]; S.ilg[0] = S.ilg[32];
       }
       if (lane < gl) S.lv[lane][0] = S.lv[lane][32];
       __syncwarp();
@@ -425,68 +495,159 @@ __device__ long long walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState
     S.q[lane + 1] = (dvs < (T)0 ? -dvs : dvs) * P.kq * rlw;
     S.ids[lane + 1] = ds > (T)0 ? Math<T>::div((T)1, ds) : (T)0;
     S.dvs[lane + 1] = dvs;
-    S.flags[lane + 1] = misc;
+    {
+      // refined window half width 3 l = 3 ds/q and the spacing of its 31-point grid
+      const T qv = S.q[lane + 1];
+      const T dls = qv > (T)0 ? Math<T>::div(ds, qv) : (T)0;
+      S.idvs[lane + 1] = dvs != (T)0 ? Math<T>::div((T)1, dvs) : (T)0;
+      S.hw3[lane + 1] = (T)3 * dls;
+      S.lg[lane + 1] = (T)6 * dls / (T)30;
+      S.ilg[lane + 1] = dls > (T)0 ? Math<T>::div((T)30, (T)6 * dls) : (T)0;
+    }
+    {
+      unsigned f = misc;
+      if (k == 1 || (misc & kFlagHole) || k == star_node) f |= kFlagInit;
+      if ((T)6 * S.q[lane + 1] > (T)1) f |= kFlagSub;
+      S.flags[lane + 1] = f;
+    }
     __syncwarp();
     const int nn = min(32, K - kb);
     const int n0 = kb == 0 ? 1 : 0;   // node 0 of the ray starts the walk
-    for (int pp = 0; pp < npair; pp++) {
-      const int ja = 2 * pp, jb = ja + 1;
-      const bool hb = jb < C;
-      T Ia = SS.I[ja][lane], j0a = SS.j0[ja][lane], a0a = SS.a0[ja][lane], S0a = SS.S0[ja][lane];
-      const T wa = SS.w[ja][lane];
-      const int La = SS.ll[ja][lane];
-      T Ib = 0, j0b = 0, a0b = 0, S0b = 0, wb = 0;
-      int Lb = -1;
-      if (hb) {
-        Ib = SS.I[jb][lane]; j0b = SS.j0[jb][lane]; a0b = SS.a0[jb][lane]; S0b = SS.S0[jb][lane];
-        wb = SS.w[jb][lane]; Lb = SS.ll[jb][lane];
+    for (int pq = 0; pq < npass; pq++) {
+      T I[kPass], j0[kPass], a0[kPass], S0[kPass], w[kPass];
+      int Ls[kPass], lsl[kPass];
+      int nv = 0;
+#pragma unroll
+      for (int u = 0; u < kPass; u++) {
+        const int j = kPass * pq + u;
+        if (j < C) {
+          I[u] = SS.I[j][lane]; j0[u] = SS.j0[j][lane]; a0[u] = SS.a0[j][lane]; S0[u] = SS.S0[j][lane];
+          w[u] = SS.w[j][lane]; Ls[u] = SS.ll[j][lane];
+        } else {
+          I[u] = 0; j0[u] = 0; a0[u] = 0; S0[u] = 0; w[u] = 0; Ls[u] = -1;
+        }
+        lsl[u] = Ls[u] < 0 ? 0 : Ls[u];
+        nv += Ls[u] >= 0 ? 1 : 0;
       }
-      const int la = La < 0 ? 0 : La, lb = Lb < 0 ? 0 : Lb;
-      const int va = La >= 0 ? 1 : 0, vb = Lb >= 0 ? 1 : 0;
       for (int n = n0; n < nn; n++) {
         const int g = kb + n;
         const unsigned fl = S.flags[n + 1];
-        bool init = g == 1 || (fl & kFlagHole);
         if (g == star_node) {
-          if (La >= 0) Ia = ((T)1 - P.fstar) * Ia + P.fstar * P.star[(size_t)(l0 + La) * P.nfr + (list[ja * 32 + lane] & (kMaxChannels - 1))];
-          if (Lb >= 0) Ib = ((T)1 - P.fstar) * Ib + P.fstar * P.star[(size_t)(l0 + Lb) * P.nfr + (list[jb * 32 + lane] & (kMaxChannels - 1))];
-          init = true;
+#pragma unroll
+          for (int u = 0; u < kPass; u++)
+            if (Ls[u] >= 0)
+              I[u] = ((T)1 - P.fstar) * I[u] +
+                     P.fstar * P.star[(size_t)(l0 + Ls[u]) * P.nfr + (list[(kPass * pq + u) * 32 + lane] & (kMaxChannels - 1))];
         }
-        const T vl1 = S.vl[n + 1], rl = S.rlw[n + 1], hds = S.hds[n + 1], q = S.q[n + 1];
-        const bool sub = (T)6 * q > (T)1;
-        const LineVals<T> v1a = S.lv[la][n + 1];
-        const LineVals<T> v1b = S.lv[lb][n + 1];
-        if (!init && !sub) {
-          T j1, a1, S1;
-          {
-            const Pt<T> p1 = {v1a.jd, v1a.ad, v1a.jf, v1a.af, vl1};
-            point_state(p1, profile(wa, vl1, rl, rl), j1, a1, S1);
-            formal(Ia, j0a, a0a, S0a, j1, a1, S1, hds);
-            j0a = j1; a0a = a1; S0a = S1;
+        const T vl1 = S.vl[n + 1], rl = S.rlw[n + 1], hds = S.hds[n + 1];
+        if (!(fl & kFlagInit)) {
+          // SUBGRID window test of the reference (line.F:4733-4742): slots whose refined
+          // window [s_c - 3l, s_c + 3l] overlaps (0, ds) keep their state here and are
+          // refined below; all others take one formal-solution step
+          bool ov[kPass];
+          bool any = false;
+#pragma unroll
+          for (int u = 0; u < kPass; u++) ov[u] = false;
+          if (fl & kFlagSub) {
+            const T vl0 = S.vl[n], dsf = S.ds[n + 1], hw3 = S.hw3[n + 1];
+#pragma unroll
+            for (int u = 0; u < kPass; u++) {
+              const T s_c = sizeof(T) == 8 ? dsf * (w[u] - vl0) / S.dvs[n + 1] : dsf * (w[u] - vl0) * S.idvs[n + 1];
+              ov[u] = Ls[u] >= 0 && (s_c + hw3 > (T)0) && (s_c - hw3 < dsf);
+              any = any || ov[u];
+            }
+            any = __any_sync(0xffffffffu, any);
           }
-          {
-            const Pt<T> p1 = {v1b.jd, v1b.ad, v1b.jf, v1b.af, vl1};
-            point_state(p1, profile(wb, vl1, rl, rl), j1, a1, S1);
-            formal(Ib, j0b, a0b, S0b, j1, a1, S1, hds);
-            j0b = j1; a0b = a1; S0b = S1;
+          T j1[kPass], a1[kPass], S1[kPass], dt[kPass], th[kPass];
+          bool ser_all = true, dir_all = true;
+#pragma unroll
+          for (int u = 0; u < kPass; u++) {
+            const LineVals<T> v = S.lv[lsl[u]][n + 1];
+            const T ph = profile(w[u], vl1, rl, rl);
+            j1[u] = v.jd + v.jf * ph;
+            a1[u] = v.ad + v.af * ph;
+            S1[u] = a1[u] > (T)0 ? j1[u] * Math<T>::rcp(a1[u]) : (T)0;
+            dt[u] = (a0[u] + a1[u]) * hds;
+            th[u] = (j0[u] + j1[u]) * hds;
+            const bool ser = dt[u] < (T)0.25;
+            ser_all = ser_all && ser;
+            dir_all = dir_all && !ser;
           }
-          steps += va + vb;
+          ser_all = __all_sync(0xffffffffu, ser_all);
+          dir_all = __all_sync(0xffffffffu, dir_all);
+          T x[kPass], ca[kPass], cb[kPass];
+          if (ser_all) {
+#pragma unroll
+            for (int u = 0; u < kPass; u++) Math<T>::series(dt[u], x[u], ca[u], cb[u]);
+          } else if (dir_all) {
+#pragma unroll
+            for (int u = 0; u < kPass; u++) Math<T>::direct(dt[u], x[u], ca[u], cb[u]);
+          } else {
+#pragma unroll
+            for (int u = 0; u < kPass; u++) Math<T>::coeffs(dt[u], x[u], ca[u], cb[u]);
+          }
+#pragma unroll
+          for (int u = 0; u < kPass; u++) {
+            const T src1 = a0[u] > (T)0 ? S0[u] : S1[u];
+            const T src2 = a1[u] > (T)0 ? S1[u] : S0[u];
+            T qv = dt[u] > (T)1.0e-9f ? ca[u] * src1 + cb[u] * src2 : th[u];
+            qv = qv < th[u] ? qv : th[u];
+            if (!ov[u]) {
+              I[u] = I[u] * x[u] + qv;
+              j0[u] = j1[u]; a0[u] = a1[u]; S0[u] = S1[u];
+            }
+          }
+          steps += nv;
+          if (any) {
+            // compact the refined channels over the warp, refine them one per lane
+            int pos[kPass];
+            int cnt = 0;
+#pragma unroll
+            for (int u = 0; u < kPass; u++) {
+              const unsigned m = __ballot_sync(0xffffffffu, ov[u]);
+              pos[u] = cnt + __popc(m & lanemask_lt());
+              if (ov[u]) {
+                SW.I[pos[u]] = I[u]; SW.j0[pos[u]] = j0[u]; SW.a0[pos[u]] = a0[u]; SW.S0[pos[u]] = S0[u];
+                SW.w[pos[u]] = w[u]; SW.l[pos[u]] = (unsigned char)lsl[u];
+              }
+              cnt += __popc(m);
+            }
+            __syncwarp();
+            const T vl0 = S.vl[n], dsf = S.ds[n + 1], ids = S.ids[n + 1], hw3 = S.hw3[n + 1];
+            const T lgv = S.lg[n + 1], ilg = S.ilg[n + 1], idvs = S.idvs[n + 1], dvsg = S.dvs[n + 1];
+            for (int p = lane; p < cnt; p += 32) {
+              const T wp = SW.w[p];
+              const int lp = SW.l[p];
+              const T s_c = sizeof(T) == 8 ? dsf * (wp - vl0) / dvsg : dsf * (wp - vl0) * idvs;
+              const SlotOutT<T> o = slot_sub<T>(wp, S.lv[lp][n], S.lv[lp][n + 1], vl0, vl1, rl, dsf, ids, s_c - hw3,
+                                                lgv, ilg, SW.I[p], SW.j0[p], SW.a0[p], SW.S0[p]);
+              SW.I[p] = o.I; SW.j0[p] = o.j0; SW.a0[p] = o.a0; SW.S0[p] = o.S0;
+              steps += o.steps - 1;
+            }
+            __syncwarp();
+#pragma unroll
+            for (int u = 0; u < kPass; u++) {
+              if (ov[u]) { I[u] = SW.I[pos[u]]; j0[u] = SW.j0[pos[u]]; a0[u] = SW.a0[pos[u]]; S0[u] = SW.S0[pos[u]]; }
+            }
+            __syncwarp();
+          }
         } else {
-          const T vl0 = S.vl[n], dsf = S.ds[n + 1], dvs = S.dvs[n + 1], ids = S.ids[n + 1];
-          if (La >= 0) {
-            const SlotOutT<T> o = slot_slow<T>(init, sub, wa, S.lv[la][n], v1a, vl0, vl1, rl, hds, q, dsf, dvs, ids,
-                                               Ia, j0a, a0a, S0a);
-            Ia = o.I; j0a = o.j0; a0a = o.a0; S0a = o.S0; steps += o.steps;
-          }
-          if (Lb >= 0) {
-            const SlotOutT<T> o = slot_slow<T>(init, sub, wb, S.lv[lb][n], v1b, vl0, vl1, rl, hds, q, dsf, dvs, ids,
-                                               Ib, j0b, a0b, S0b);
-            Ib = o.I; j0b = o.j0; a0b = o.a0; S0b = o.S0; steps += o.steps;
+          const bool init = true, sub = fl & kFlagSub;
+          const T vl0 = S.vl[n], q = S.q[n + 1], dsf = S.ds[n + 1], dvs = S.dvs[n + 1], ids = S.ids[n + 1];
+#pragma unroll
+          for (int u = 0; u < kPass; u++) {
+            if (Ls[u] < 0) continue;
+            const SlotOutT<T> o = slot_slow<T>(init, sub, w[u], S.lv[Ls[u]][n], S.lv[Ls[u]][n + 1], vl0, vl1, rl, hds,
+                                               q, dsf, dvs, ids, I[u], j0[u], a0[u], S0[u]);
+            I[u] = o.I; j0[u] = o.j0; a0[u] = o.a0; S0[u] = o.S0; steps += o.steps;
           }
         }
       }
-      SS.I[ja][lane] = Ia; SS.j0[ja][lane] = j0a; SS.a0[ja][lane] = a0a; SS.S0[ja][lane] = S0a;
-      if (hb) { SS.I[jb][lane] = Ib; SS.j0[jb][lane] = j0b; SS.a0[jb][lane] = a0b; SS.S0[jb][lane] = S0b; }
+#pragma unroll
+      for (int u = 0; u < kPass; u++) {
+        const int j = kPass * pq + u;
+        if (j < C) { SS.I[j][lane] = I[u]; SS.j0[j][lane] = j0[u]; SS.a0[j][lane] = a0[u]; SS.S0[j][lane] = S0[u]; }
+      }
     }
     __syncwarp();
   }
@@ -501,10 +662,13 @@ __global__ void __launch_bounds__(128) k_walk(WalkParams<T> P) {
   const int capp = (cap + 7) & ~7;
   WarpStage<T>* stages = reinterpret_cast<WarpStage<T>*>(smem_raw);
   SlotState<T, C>* sstates = reinterpret_cast<SlotState<T, C>*>(smem_raw + sizeof(WarpStage<T>) * nw);
-  unsigned short* lists =
-      reinterpret_cast<unsigned short*>(smem_raw + (sizeof(WarpStage<T>) + sizeof(SlotState<T, C>)) * nw);
+  SubWork<T>* subw =
+      reinterpret_cast<SubWork<T>*>(smem_raw + (sizeof(WarpStage<T>) + sizeof(SlotState<T, C>)) * nw);
+  unsigned short* lists = reinterpret_cast<unsigned short*>(
+      smem_raw + (sizeof(WarpStage<T>) + sizeof(SlotState<T, C>) + sizeof(SubWork<T>)) * nw);
   WarpStage<T>& S = stages[wib];
   SlotState<T, C>& SS = sstates[wib];
+  SubWork<T>& SW = subw[wib];
   unsigned short* list = lists + (size_t)wib * capp;
   unsigned long long st_steps = 0, st_int = 0, st_nodes = 0;
   const NodeBuf<T>& nb = P.nb;
@@ -583,7 +747,7 @@ __global__ void __launch_bounds__(128) k_walk(WalkParams<T> P) {
     // 3. formal solution of the selected pairs, in tiles of 32*C
     for (int tb = 0; tb < nint; tb += 32 * C) {
       const int nt = min(32 * C, nint - tb);
-      st_steps += walk_ray<T, C>(P, S, SS, ray, K, l0, gl, list + tb, nt, lane);
+      st_steps += walk_ray<T, C>(P, S, SS, SW, ray, K, l0, gl, list + tb, nt, lane);
       for (int j = 0; j < C; j++) {
         const int idx = j * 32 + lane;
         if (idx < nt) {
@@ -627,7 +791,7 @@ __global__ void __launch_bounds__(128) k_walk(WalkParams<T> P) {
       __syncwarp();
       for (int tb = 0; tb < n2; tb += 32 * C) {
         const int nt = min(32 * C, n2 - tb);
-        st_steps += walk_ray<T, C>(P, S, SS, ray, K, l0, gl, list + tb, nt, lane);
+        st_steps += walk_ray<T, C>(P, S, SS, SW, ray, K, l0, gl, list + tb, nt, lane);
         for (int j = 0; j < C; j++) {
           const int idx = j * 32 + lane;
           if (idx < nt) img[list[tb + idx] & (kMaxChannels - 1)] = SS.I[j][lane];
@@ -779,7 +943,7 @@ template <typename T, int C>
 static cudaError_t launch_walk_c(const WalkParams<T>& P, int nsm, cudaStream_t s) {
   const int warps = 4, threads = warps * 32;
   const int capp = (kGroup * P.nfr + 7) & ~7;
-  const size_t smem = (sizeof(WarpStage<T>) + sizeof(SlotState<T, C>)) * warps +
+  const size_t smem = (sizeof(WarpStage<T>) + sizeof(SlotState<T, C>) + sizeof(SubWork<T>)) * warps +
                       sizeof(unsigned short) * (size_t)capp * warps;
   cudaError_t e = cudaFuncSetAttribute(k_walk<T, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
