@@ -61,6 +61,7 @@ struct WalkParams {
   NodeBuf<T> nb;
   int nth, ncell;
   int nlines, nfr, nitems;
+  int gsize;                 // lines per work item (<= 8), groups balanced over the launch
   const T* tab;              // [nlines][ncell][4] = {j-factor, alpha-factor, dust j, dust alpha}
   const T* nsum;             // [nlines][ncell] N_up + N_low (window threshold)
   const T* wch;              // [nlines][nfr] channel velocity in passband units

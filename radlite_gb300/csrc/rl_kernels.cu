@@ -673,14 +673,13 @@ __global__ void __launch_bounds__(128) k_walk(WalkParams<T> P) {
   unsigned long long st_steps = 0, st_int = 0, st_nodes = 0;
   const NodeBuf<T>& nb = P.nb;
   const int nl = P.nlines;
-  const int ngroups = (nl + kGroup - 1) / kGroup;
   for (;;) {
     int item = 0;
     if (lane == 0) item = atomicAdd(P.work, 1);
     item = __shfl_sync(0xffffffffu, item, 0);
     if (item >= P.nitems) break;
     const int g = item / nb.nrays, ray = item - g * nb.nrays;
-    const int l0 = g * kGroup, gl = min(kGroup, nl - l0);
+    const int l0 = g * P.gsize, gl = min(P.gsize, nl - l0);
     const int K = nb.nnodes[ray];
     if (nb.status[ray] != 0 || K < 1) {
       if (lane == 0) atomicCAS(P.err, 0, 100 + nb.status[ray]);
@@ -821,7 +820,6 @@ __global__ void __launch_bounds__(128) k_walk(WalkParams<T> P) {
     atomicAdd(&P.counters[1], st_int);
     atomicAdd(&P.counters[2], st_nodes);
   }
-  (void)ngroups;
 }
 
 // ------------------------------------------------------------------------------------
