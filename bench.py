@@ -180,6 +180,14 @@ def load_traffic():
         return {}
 
 
+def load_measured():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh)
+    except (OSError, ValueError):
+        return {}
+
+
 def ours(args):
     import numpy as np
     import radlite_gb300 as rl
@@ -232,6 +240,8 @@ def ours(args):
     achieved = (steps_fs * (BUDGET_MUFU if bound_mufu else BUDGET_FP32)) / wk
     peak = peaks["ex2_per_s"] if bound_mufu else peaks["ffma_per_s"]
     traffic = load_traffic().get("k_walk_dram_bytes_per_launch")
+    hbm_peak = load_measured().get("hbm_gbs")
+    traffic_gbs = traffic / (wk / len(INCLS)) / 1e9 if traffic else None
     # e2e: through the C ABI from host arrays, wall clock, copies included
     e2e_t, h2d, d2h = [], 0, 0
     for i in range(max(1, min(args.steps, 3))):
@@ -278,7 +288,10 @@ def ours(args):
                             "peak": peak / 1e12, "unit": "Tops/s", "frac": achieved / peak, "traffic": traffic,
                             "kernel": "k_walk<float>", "walk_ms_per_step": wk * 1e3,
                             "budget_per_step": {"fp32": BUDGET_FP32, "mufu": BUDGET_MUFU},
-                            "peaks_measured": peaks},
+                            "peaks_measured": peaks,
+                            "hbm_side": {"traffic_gb_per_s": traffic_gbs, "peak_gb_per_s": hbm_peak,
+                                         "frac_of_measured": (traffic_gbs / hbm_peak
+                                                              if traffic_gbs and hbm_peak else None)}},
                "cpu_baseline": cpu,
                "clocks": clk.summary(),
                "gpu_launches": args.steps * len(INCLS) * 4}
