@@ -125,6 +125,25 @@ int rl_debug_trajectory(rl_model* model, int iray, int cap, double* s, double* r
    whole device. Roofline denominators; no counterpart in the reference. */
 int rl_measure_peaks(rl_ctx* ctx, double* ffma_per_s, double* ex2_per_s);
 
+/* Circular image -> F_nu at `distance_pc` parsec, with no device allocation. No
+   counterpart in the reference: it serves callers that own all device memory (their
+   own pool or arena) and cannot let a library call cudaMalloc. Every pointer is a
+   device pointer of the calling thread's current device; `stream` is a cudaStream_t
+   (NULL = the default stream); the call only enqueues work on it.
+     image  [nlines][nrays][nfr], float (RL_FP32) or double (RL_FP64), ray 0 the
+            central beam, then rings from the inside out, azimuth fastest
+     ri     [nrr+2] ring edges (ri[1] the central-beam radius), scale [nlines] a factor
+            per line, flux [nlines][nfr] output; nrays must be 1 + nrr*nphi.
+   The ring sums live in a fixed 8 MiB array in the library's device image (2^20
+   doubles, held by every GPU that loads the library until exit); (nrr+1)*nfr above
+   2^20 is rejected with RL_ERR_ARG. Nothing in it has to start at zero. Calls that
+   overlap on one device (other streams or threads) share that array and race: order
+   them on one stream. The first call on a device looks the array up, which loads the
+   module: make it before any stream capture. Errors: rl_last_error(NULL, ...). */
+int rl_image_to_spectrum_noalloc(void* stream, int precision, const void* image, int nlines, int nrays, int nphi,
+                                 int nrr, int nfr, const double* ri, const double* scale, double distance_pc,
+                                 double* flux);
+
 #ifdef __cplusplus
 }
 #endif

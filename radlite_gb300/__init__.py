@@ -70,7 +70,8 @@ class ModelArrays(C.Structure):
 
 EXPORTS = ["rl_create", "rl_destroy", "rl_last_error", "rl_load_dir", "rl_load_arrays", "rl_model_free",
            "rl_model_get_info", "rl_set_camera", "rl_set_precision", "rl_line_spectrum", "rl_spectra",
-           "rl_line_image", "rl_run_dir", "rl_debug_trajectory", "rl_measure_peaks"]
+           "rl_line_image", "rl_run_dir", "rl_debug_trajectory", "rl_measure_peaks",
+           "rl_image_to_spectrum_noalloc"]
 
 _lib = None
 
@@ -98,6 +99,8 @@ def lib():
         L.rl_run_dir.argtypes = [C.c_char_p, C.c_int, C.POINTER(Stats)]
         L.rl_debug_trajectory.argtypes = [vp, C.c_int, C.c_int, _D, _D, _D, _D, _D, _I, _I, _I]
         L.rl_measure_peaks.argtypes = [vp, _D, _D]
+        L.rl_image_to_spectrum_noalloc.argtypes = [vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                                   vp, vp, C.c_double, vp]
         _lib = L
     return _lib
 
@@ -273,6 +276,21 @@ def run_dir(path: str, device: int = 0) -> dict:
     if rc < 0:
         raise RLError(_err())
     return st.as_dict()
+
+
+def image_to_spectrum_noalloc(image_ptr: int, nlines: int, nrays: int, nphi: int, nrr: int, nfr: int,
+                              ri_ptr: int, scale_ptr: int, flux_ptr: int, precision: int = 0,
+                              stream: int = 0, distance_pc: float = 1.0) -> None:
+    """rl_image_to_spectrum_noalloc: reduce a device-resident circular image to F_nu.
+
+    For callers that own every device buffer and cannot let the library allocate. All
+    pointers are device addresses on the current device. The call only enqueues work on
+    `stream` (a cudaStream_t value, 0 = default stream). The ring sums use a fixed 8 MiB
+    array inside the library, so calls that overlap on one device race with each other."""
+    rc = lib().rl_image_to_spectrum_noalloc(stream or None, precision, image_ptr, nlines, nrays, nphi, nrr, nfr,
+                                            ri_ptr, scale_ptr, distance_pc, flux_ptr)
+    if rc < 0:
+        raise RLError(_err())
 
 
 def read_spectrum_file(path: str):

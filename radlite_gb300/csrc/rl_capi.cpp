@@ -79,6 +79,11 @@ struct rl_model {
   DevBuf dtab, dnsum, dwch, dvelo, dstar, dlc, dimg, dring, dflux, dscale, dcnt, dwork, derr;
 };
 
+namespace rl {
+// Error text for entry points that take no context (read back with rl_last_error(NULL, ...)).
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace rl
+
 static int set_err(rl_ctx* c, int code, const std::string& msg) {
   g_last_error = msg;
   if (c) c->err = msg;
