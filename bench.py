@@ -263,6 +263,10 @@ def ours(args):
         m.set_precision(0)
         sel = f64 > 1e-3 * f64.max()
         rel = float(np.max(np.abs(f32[sel] - f64[sel]) / np.abs(f64[sel])))
+    m.free()
+    batched = None
+    if rank == 0 and args.batch_models > 0:
+        batched = batched_case(ctx, args.batch_models, 2)
     out = None
     if rank == 0:
         cpu = None
@@ -292,13 +296,74 @@ def ours(args):
                             "hbm_side": {"traffic_gb_per_s": traffic_gbs, "peak_gb_per_s": hbm_peak,
                                          "frac_of_measured": (traffic_gbs / hbm_peak
                                                               if traffic_gbs and hbm_peak else None)}},
+               "batched": batched,
                "cpu_baseline": cpu,
                "clocks": clk.summary(),
                "gpu_launches": args.steps * len(INCLS) * 4}
         print(json.dumps(out), flush=True)
-    m.free()
     ctx.close()
     return 0
+
+
+def batched_case(ctx, n_models, steps, tune_stride=32):
+    """Plain per-model launches against one batched, graph-replayed launch sequence on the
+    uneven multi-model workload (synth.batch_configs): same spectra, spectra/s of each."""
+    import numpy as np
+    import radlite_gb300 as rl
+    from radlite_gb300 import synth
+    cfgs = synth.batch_configs(n_models)
+    cams = [camera(c, c.incl_deg) for c in cfgs]
+    nspec = sum(c.nlines for c in cfgs)
+    # plain: one model at a time, as a driver loop over model directories would run it
+    plain, t_cold, t_warm, rc_total = [], 0.0, 0.0, 0
+    for c, cam in zip(cfgs, cams):
+        m = ctx.load_arrays(synth.model_arrays(c), cam)
+        t0 = time.perf_counter()
+        m.spectra(c.ilinestart, c.nlines)                    # geometry, line tables, walk, reduction
+        t1 = time.perf_counter()
+        f, st = m.spectra(c.ilinestart, c.nlines, stats=True)   # geometry and tables cached
+        t2 = time.perf_counter()
+        t_cold += t1 - t0
+        t_warm += t2 - t1
+        rc_total += st["ray_channels"]
+        plain.append(f)
+        m.free()
+    # batched: all jobs resident, one geometry + walk + reduction per memory wave, graph replay
+    models = [ctx.load_arrays(synth.model_arrays(c), cam) for c, cam in zip(cfgs, cams)]
+    b = rl.Batch(ctx)
+    for c, m in zip(cfgs, models):
+        b.add(m, c.ilinestart, c.nlines)
+    t0 = time.perf_counter()
+    tune = b.autotune(sample_stride=tune_stride)
+    t_setup = time.perf_counter() - t0
+    b.run()                                                  # graph capture + first replay
+    times, walls = [], []
+    for _ in range(max(1, steps)):
+        t0 = time.perf_counter()
+        out, st = b.run(stats=True)
+        walls.append(time.perf_counter() - t0)
+        times.append(st["total_ms"] * 1e-3)
+    rel = 0.0
+    for got, ref in zip(out, plain):
+        for k in range(ref.shape[0]):
+            sel = ref[k] > 1e-3 * ref[k].max()
+            if sel.any():
+                rel = max(rel, float(np.max(np.abs(got[k][sel] - ref[k][sel]) / np.abs(ref[k][sel]))))
+    t_b = statistics.median(times)
+    res = {"workload": f"{n_models} uneven disks (nr 64-512, ntheta 32-256, 1-50 lines, 32-256 channels, "
+                       f"incl 5-85 deg, {cfgs[0].nphi} azimuths)",
+           "spectra": nspec, "ray_channels": rc_total,
+           "plain": {"s_cold": t_cold, "s_warm": t_warm, "spectra_per_s_warm": nspec / t_warm,
+                     "spectra_per_s_cold": nspec / t_cold, "ray_channels_per_s_warm": rc_total / t_warm},
+           "batched": {"s": t_b, "wall_s": statistics.median(walls), "spectra_per_s": nspec / t_b,
+                       "ray_channels_per_s": rc_total / t_b, "tiles": tune, "tune_s": t_setup,
+                       "waves": b.waves(), "graph": True},
+           "speedup_vs_plain_warm": t_warm / t_b, "speedup_vs_plain_cold": t_cold / t_b,
+           "max_rel_diff_batched_vs_plain": rel}
+    b.close()
+    for m in models:
+        m.free()
+    return res
 
 
 def profile_case(args):
@@ -328,7 +393,16 @@ def main():
     ap.add_argument("--cpu-stride", type=int, default=16)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-verify", action="store_true")
+    ap.add_argument("--batch-models", type=int, default=256,
+                    help="models of the uneven batched comparison (0 skips it)")
+    ap.add_argument("--only-batch", action="store_true", help="run only the batched comparison")
     args = ap.parse_args()
+    if args.only_batch:
+        import radlite_gb300 as rl
+        ctx = rl.Context(0)
+        print(json.dumps(batched_case(ctx, args.batch_models, args.steps)), flush=True)
+        ctx.close()
+        return 0
     if args.warmup < 3:
         args.warmup = 3
     if args.profile:

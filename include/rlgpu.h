@@ -125,6 +125,43 @@ int rl_debug_trajectory(rl_model* model, int iray, int cap, double* s, double* r
    whole device. Roofline denominators; no counterpart in the reference. */
 int rl_measure_peaks(rl_ctx* ctx, double* ffma_per_s, double* ex2_per_s);
 
+/* ---- Batched rendering: many (model, camera, line range) jobs in one launch sequence.
+   Replaces the drivers' one-process-per-model loop (pyradlite radlite.py:592-595, IDL
+   line_run.pro:173) and the per-line calc_line_spectrum loop (main.F:1043-1049) with one
+   geometry launch, one persistent walk fed from a device work queue and one reduction per
+   memory wave, captured once in a CUDA graph and replayed. A job snapshots its model's
+   camera at the first run; models must outlive the batch and keep their grid. */
+typedef struct rl_batch rl_batch;
+int rl_batch_create(rl_ctx* ctx, int precision, rl_batch** batch);
+int rl_batch_destroy(rl_batch* batch);
+/* Adds lines iline0 .. iline0+nlines-1 of `model` at its current camera; returns the job
+   index (>= 0). */
+int rl_batch_add(rl_batch* batch, rl_model* model, int iline0, int nlines);
+/* Device bytes per memory wave (node records, images, ring sums); 0 = 70% of free memory. */
+int rl_batch_set_memory(rl_batch* batch, double bytes);
+/* Tile shape of the walk: lines per work item (1..8) and channel slots per lane (1, 2, 4, 8;
+   a tile is 32 x slots (line, channel) pairs). */
+int rl_batch_set_tiles(rl_batch* batch, int lines_per_item, int channel_slots);
+int rl_batch_get_tiles(rl_batch* batch, int* lines_per_item, int* channel_slots);
+/* Times every tile shape on every sample_stride-th work item of the first wave and keeps the
+   fastest; returns it and the sampled walk time. No counterpart in the reference. */
+int rl_batch_autotune(rl_batch* batch, int sample_stride, int* lines_per_item, int* channel_slots,
+                      double* sample_ms);
+/* 1 (default): capture the launch sequence in a CUDA graph at the first run, replay after. */
+int rl_batch_use_graph(rl_batch* batch, int enable);
+/* Number of flux values (sum over jobs of nlines x nfr) and the layout of one job in them. */
+int rl_batch_flux_size(rl_batch* batch, long long* n);
+int rl_batch_job_info(rl_batch* batch, int job, long long* flux_offset, int* nlines, int* nfr);
+/* Renders every job; flux_out receives each job's [nlines][nfr] F_nu at 1 pc in job order. */
+int rl_batch_run(rl_batch* batch, double* flux_out, rl_stats* stats);
+/* Memory waves of the last build. */
+int rl_batch_waves(rl_batch* batch, int* nwaves);
+/* The executable's work for every directory listed in `manifest` (one per line, '#'
+   comments), rendered as one FP32 batch: each directory gets its linespectrum_<mol>.dat
+   and radlite.success. Replaces the drivers' one-process-per-directory loop
+   (radlite.py:592-595). */
+int rl_run_manifest(const char* manifest, int device, rl_stats* stats);
+
 /* Circular image -> F_nu at `distance_pc` parsec, with no device allocation. No
    counterpart in the reference: it serves callers that own all device memory (their
    own pool or arena) and cannot let a library call cudaMalloc. Every pointer is a

@@ -71,6 +71,9 @@ class ModelArrays(C.Structure):
 EXPORTS = ["rl_create", "rl_destroy", "rl_last_error", "rl_load_dir", "rl_load_arrays", "rl_model_free",
            "rl_model_get_info", "rl_set_camera", "rl_set_precision", "rl_line_spectrum", "rl_spectra",
            "rl_line_image", "rl_run_dir", "rl_debug_trajectory", "rl_measure_peaks",
+           "rl_batch_create", "rl_batch_destroy", "rl_batch_add", "rl_batch_set_memory", "rl_batch_set_tiles",
+           "rl_batch_get_tiles", "rl_batch_autotune", "rl_batch_use_graph", "rl_batch_flux_size",
+           "rl_batch_job_info", "rl_batch_run", "rl_batch_waves", "rl_run_manifest",
            "rl_image_to_spectrum_noalloc"]
 
 _lib = None
@@ -99,6 +102,19 @@ def lib():
         L.rl_run_dir.argtypes = [C.c_char_p, C.c_int, C.POINTER(Stats)]
         L.rl_debug_trajectory.argtypes = [vp, C.c_int, C.c_int, _D, _D, _D, _D, _D, _I, _I, _I]
         L.rl_measure_peaks.argtypes = [vp, _D, _D]
+        L.rl_batch_create.argtypes = [vp, C.c_int, C.POINTER(vp)]
+        L.rl_batch_destroy.argtypes = [vp]
+        L.rl_batch_add.argtypes = [vp, vp, C.c_int, C.c_int]
+        L.rl_batch_set_memory.argtypes = [vp, C.c_double]
+        L.rl_batch_set_tiles.argtypes = [vp, C.c_int, C.c_int]
+        L.rl_batch_get_tiles.argtypes = [vp, _I, _I]
+        L.rl_batch_autotune.argtypes = [vp, C.c_int, _I, _I, _D]
+        L.rl_batch_use_graph.argtypes = [vp, C.c_int]
+        L.rl_batch_flux_size.argtypes = [vp, C.POINTER(C.c_longlong)]
+        L.rl_batch_job_info.argtypes = [vp, C.c_int, C.POINTER(C.c_longlong), _I, _I]
+        L.rl_batch_run.argtypes = [vp, _D, C.POINTER(Stats)]
+        L.rl_batch_waves.argtypes = [vp, _I]
+        L.rl_run_manifest.argtypes = [C.c_char_p, C.c_int, C.POINTER(Stats)]
         L.rl_image_to_spectrum_noalloc.argtypes = [vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                                    vp, vp, C.c_double, vp]
         _lib = L
@@ -262,6 +278,74 @@ class Model:
         return res
 
 
+class Batch:
+    """Many (model, camera, line range) jobs rendered by one launch sequence (rl_batch).
+
+    Replaces a driver loop over model directories: every job's inputs stay on the device,
+    the geometry, walk and reduction of all jobs run as one launch each per memory wave,
+    and the sequence is replayed from a CUDA graph."""
+
+    def __init__(self, ctx: Context, precision: int = 0):
+        self.ctx = ctx
+        self.h = C.c_void_p()
+        self.models = []
+        _check(lib().rl_batch_create(ctx.h, precision, C.byref(self.h)), ctx.h)
+
+    def close(self):
+        if self.h:
+            lib().rl_batch_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add(self, model: "Model", iline0: int, nlines: int) -> int:
+        """Queue lines iline0 .. iline0+nlines-1 of `model` at its current camera."""
+        self.models.append(model)   # the batch reads the model's device grid
+        return _check(lib().rl_batch_add(self.h, model.h, iline0, nlines), self.ctx.h)
+
+    def set_memory(self, nbytes: float):
+        _check(lib().rl_batch_set_memory(self.h, float(nbytes)), self.ctx.h)
+
+    def set_tiles(self, lines_per_item: int, channel_slots: int):
+        _check(lib().rl_batch_set_tiles(self.h, lines_per_item, channel_slots), self.ctx.h)
+
+    def tiles(self) -> tuple:
+        g, c = C.c_int(), C.c_int()
+        _check(lib().rl_batch_get_tiles(self.h, C.byref(g), C.byref(c)), self.ctx.h)
+        return g.value, c.value
+
+    def autotune(self, sample_stride: int = 16) -> dict:
+        g, c, ms = C.c_int(), C.c_int(), C.c_double()
+        _check(lib().rl_batch_autotune(self.h, sample_stride, C.byref(g), C.byref(c), C.byref(ms)), self.ctx.h)
+        return {"lines_per_item": g.value, "channel_slots": c.value, "sample_ms": ms.value}
+
+    def use_graph(self, enable: bool):
+        _check(lib().rl_batch_use_graph(self.h, int(bool(enable))), self.ctx.h)
+
+    def waves(self) -> int:
+        n = C.c_int()
+        _check(lib().rl_batch_waves(self.h, C.byref(n)), self.ctx.h)
+        return n.value
+
+    def run(self, stats: bool = False):
+        """Spectra of every job: a list of [nlines, nfr] arrays in job order."""
+        n = C.c_longlong()
+        _check(lib().rl_batch_flux_size(self.h, C.byref(n)), self.ctx.h)
+        flux = np.zeros(n.value)
+        st = Stats()
+        _check(lib().rl_batch_run(self.h, _dp(flux), C.byref(st)), self.ctx.h)
+        out = []
+        for j in range(len(self.models)):
+            off, nl, nfr = C.c_longlong(), C.c_int(), C.c_int()
+            _check(lib().rl_batch_job_info(self.h, j, C.byref(off), C.byref(nl), C.byref(nfr)), self.ctx.h)
+            out.append(flux[off.value:off.value + nl.value * nfr.value].reshape(nl.value, nfr.value))
+        return (out, st.as_dict()) if stats else out
+
+
 def load_dir_host(path: str) -> "Model":
     """Parse a model directory without a device (host-side checks of the input files)."""
     h = C.c_void_p()
@@ -291,6 +375,15 @@ def image_to_spectrum_noalloc(image_ptr: int, nlines: int, nrays: int, nphi: int
                                             ri_ptr, scale_ptr, distance_pc, flux_ptr)
     if rc < 0:
         raise RLError(_err())
+
+
+def run_manifest(path: str, device: int = 0) -> dict:
+    """Render every model directory listed in the manifest file `path` as one batch."""
+    st = Stats()
+    rc = lib().rl_run_manifest(os.fsencode(path), device, C.byref(st))
+    if rc < 0:
+        raise RLError(_err())
+    return st.as_dict()
 
 
 def read_spectrum_file(path: str):

@@ -15,96 +15,30 @@
 #include "rl_device.h"
 #include "rl_geometry.cuh"
 #include "rl_host.h"
-
-namespace rl {
-template <typename T>
-cudaError_t launch_geometry(const GeoParams& p, const NodeBuf<T>& nb, int ray0, int nray, TrajDebug* dbg,
-                            cudaStream_t s);
-template <typename T>
-cudaError_t launch_walk(const WalkParams<T>& P, int cpl, int nsm, cudaStream_t s);
-template <typename T>
-cudaError_t launch_reduce(const ReduceParams& p, const T* img, double* ring, double* flux, cudaStream_t s);
-cudaError_t measure_peaks(int nsm, cudaStream_t st, double* ffma_per_s, double* ex2_per_s);
-}  // namespace rl
+#include "rl_internal.h"
 
 using namespace rl;
-static constexpr int kWalkGroup = 8;   // lines per walk work item (k_walk's kGroup)
 
-namespace {
 thread_local std::string g_last_error;
-
-struct DevBuf {
-  void* p = nullptr;
-  size_t n = 0;
-  ~DevBuf() { if (p) cudaFree(p); }
-  cudaError_t ensure(size_t bytes) {
-    if (bytes <= n && p) return cudaSuccess;
-    if (p) { cudaFree(p); p = nullptr; n = 0; }
-    cudaError_t e = cudaMalloc(&p, bytes ? bytes : 16);
-    if (e == cudaSuccess) n = bytes;
-    return e;
-  }
-  template <typename T> T* as() const { return static_cast<T*>(p); }
-};
-}  // namespace
-
-struct rl_ctx {
-  int device = 0, nsm = 0;
-  cudaStream_t stream = nullptr;
-  cudaEvent_t ev[6] = {};
-  std::string err;
-};
-
-struct rl_model {
-  rl_ctx* ctx = nullptr;
-  Model m;
-  int precision = RL_FP32;
-  // camera request
-  double incl_rad = 0.0;
-  int nphi = 0, dbdr = 1, nrext = 0;
-  // device copies of the grid and cell fields (uploaded once)
-  bool grid_ready = false;
-  DevBuf dR, dTH, dtan2, dvel, dlw;
-  // camera geometry cache
-  bool geo_ready = false;
-  int geo_prec = -1;
-  Camera cam;
-  DevBuf dx0, dz0, dri;
-  DevBuf nb_nn, nb_st, nb_ds, nb_dvf, nb_vl, nb_dvs, nb_lw, nb_wr, nb_wt, nb_c00, nb_misc;
-  int kmax = 0;
-  // per-line tables of the last line range (reused while the range and precision match)
-  int tab_line0 = -1, tab_nl = 0, tab_prec = -1;
-  std::vector<double> tab_scale;
-  // per-call buffers
-  DevBuf dtab, dnsum, dwch, dvelo, dstar, dlc, dimg, dring, dflux, dscale, dcnt, dwork, derr;
-};
+thread_local unsigned long long g_h2d = 0, g_d2h = 0;   // per call, reset by the entry points
 
 namespace rl {
 // Error text for entry points that take no context (read back with rl_last_error(NULL, ...)).
 void set_last_error(const std::string& msg) { g_last_error = msg; }
-}  // namespace rl
-
-static int set_err(rl_ctx* c, int code, const std::string& msg) {
+int set_err(rl_ctx* c, int code, const std::string& msg) {
   g_last_error = msg;
   if (c) c->err = msg;
   return code;
 }
-#define CUDA_TRY(call)                                                                      \
-  do {                                                                                      \
-    cudaError_t e_ = (call);                                                                \
-    if (e_ != cudaSuccess)                                                                  \
-      return set_err(ctx, RL_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
-  } while (0)
-
-static thread_local unsigned long long g_h2d = 0, g_d2h = 0;   // per call, reset by the entry points
-static cudaError_t h2d(void* dst, const void* src, size_t n, cudaStream_t s) {
+cudaError_t h2d(void* dst, const void* src, size_t n, cudaStream_t s) {
   g_h2d += n;
   return cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, s);
 }
-static cudaError_t d2h(void* dst, const void* src, size_t n, cudaStream_t s) {
+cudaError_t d2h(void* dst, const void* src, size_t n, cudaStream_t s) {
   g_d2h += n;
   return cudaMemcpyAsync(dst, src, n, cudaMemcpyDeviceToHost, s);
 }
+}  // namespace rl
 
 static void camera_defaults(rl_model* md) {
   md->incl_rad = md->m.incl_rad;
@@ -113,7 +47,7 @@ static void camera_defaults(rl_model* md) {
   md->nrext = md->m.nrext;
 }
 
-static int upload_grid(rl_model* md) {
+int rl::upload_grid(rl_model* md) {
   rl_ctx* ctx = md->ctx;
   if (md->grid_ready) return 0;
   const Model& m = md->m;
@@ -136,33 +70,39 @@ static int upload_grid(rl_model* md) {
 }
 
 template <typename T>
-static NodeBuf<T> node_view(rl_model* md) {
-  NodeBuf<T> nb;
-  nb.nrays = md->cam.nrays;
-  nb.kmax = md->kmax;
-  nb.nnodes = md->nb_nn.as<int>();
-  nb.status = md->nb_st.as<int>();
-  nb.ds = md->nb_ds.as<T>();
-  nb.dvf = md->nb_dvf.as<float>();
-  nb.vl = md->nb_vl.as<T>();
-  nb.dvseg = md->nb_dvs.as<T>();
-  nb.lw = md->nb_lw.as<T>();
-  nb.wr = md->nb_wr.as<T>();
-  nb.wt = md->nb_wt.as<T>();
-  nb.c00 = md->nb_c00.as<int>();
-  nb.misc = md->nb_misc.as<unsigned>();
-  return nb;
+int rl::build_line_tables(const Model& m, int iline0, int nl, LineTables<T>& out, std::string& err) {
+  const int ncell = m.ncell(), nfr = m.nfr;
+  const bool scaled = std::is_same<T, float>::value;
+  out.nl = nl; out.ncell = ncell; out.nfr = nfr;
+  out.tab.assign((size_t)nl * ncell * 4, (T)0); out.nsum.assign((size_t)nl * ncell, (T)0);
+  out.wch.assign((size_t)nl * nfr, (T)0); out.star.assign((size_t)nl * nfr, (T)0);
+  out.velo.assign((size_t)nl * nfr, 0.0); out.scale.assign(nl, 1.0); out.lc.assign(nl, LineConst<T>{});
+  for (int l = 0; l < nl; l++) {
+    LinePrep lp;
+    if (prepare_line(m, iline0 + l, scaled, lp, err)) return RL_ERR_ARG;
+    // cell-major, line-minor: the corners of one node for consecutive lines are contiguous.
+    // The line factors carry the profile normalisation (phi = cphi / lwav * e^{-u^2}).
+    for (int c = 0; c < ncell; c++) {
+      out.tab[((size_t)c * nl + l) * 4 + 0] = (T)(lp.tab[4 * (size_t)c + 0] * lp.cphi);
+      out.tab[((size_t)c * nl + l) * 4 + 1] = (T)(lp.tab[4 * (size_t)c + 1] * lp.cphi);
+      out.tab[((size_t)c * nl + l) * 4 + 2] = (T)lp.tab[4 * (size_t)c + 2];
+      out.tab[((size_t)c * nl + l) * 4 + 3] = (T)lp.tab[4 * (size_t)c + 3];
+      out.nsum[(size_t)c * nl + l] = (T)lp.nsum[c];
+    }
+    for (int k = 0; k < nfr; k++) {
+      out.wch[(size_t)l * nfr + k] = (T)lp.wch[k];
+      out.star[(size_t)l * nfr + k] = (T)lp.star[k];
+      out.velo[(size_t)l * nfr + k] = lp.velo[k];
+    }
+    out.lc[l].cphi = (T)lp.cphi;
+    out.lc[l].istart = (T)lp.istart;
+    out.lc[l].scale = lp.scale;
+    out.scale[l] = lp.scale;
+  }
+  return 0;
 }
-
-static GeoParams geo_params(rl_model* md) {
-  GeoParams p;
-  const Model& m = md->m;
-  p.nr = m.nr; p.nth = m.nth; p.ny = m.ny; p.rstar = m.rstar; p.theta0 = md->cam.theta0;
-  p.R = md->dR.as<double>(); p.TH = md->dTH.as<double>(); p.tan2 = md->dtan2.as<double>();
-  p.vel = md->dvel.as<double>(); p.lw = md->dlw.as<double>();
-  p.x0 = md->dx0.as<double>(); p.z0 = md->dz0.as<double>();
-  return p;
-}
+template int rl::build_line_tables<float>(const Model&, int, int, LineTables<float>&, std::string&);
+template int rl::build_line_tables<double>(const Model&, int, int, LineTables<double>&, std::string&);
 
 template <typename T>
 static int build_geometry(rl_model* md, rl_stats* st) {
@@ -224,38 +164,17 @@ static int run_lines(rl_model* md, int iline0, int nl, double* flux_out, double*
   const int ncell = m.ncell(), nfr = m.nfr;
   // per-line tables (built on the host in FP64, kept on the device between calls)
   const bool cached = md->tab_line0 == iline0 && md->tab_nl == nl && md->tab_prec == md->precision;
-  std::vector<T> tab, nsum, wch, star;
-  std::vector<double> velo, scale = md->tab_scale;
-  std::vector<LineConst<T>> lc;
-  const bool scaled = std::is_same<T, float>::value;
+  LineTables<T> lt;
+  std::vector<double> scale = md->tab_scale;
   if (!cached) {
-    tab.resize((size_t)nl * ncell * 4); nsum.resize((size_t)nl * ncell); wch.resize((size_t)nl * nfr);
-    star.resize((size_t)nl * nfr); velo.resize((size_t)nl * nfr); scale.assign(nl, 1.0); lc.resize(nl);
     md->tab_line0 = -1;
-  }
-  for (int l = 0; l < nl && !cached; l++) {
-    LinePrep lp;
     std::string err;
-    if (prepare_line(m, iline0 + l, scaled, lp, err)) return set_err(ctx, RL_ERR_ARG, err);
-    // cell-major, line-minor: the corners of one node for consecutive lines are contiguous.
-    // The line factors carry the profile normalisation (phi = cphi / lwav * e^{-u^2}).
-    for (int c = 0; c < ncell; c++) {
-      tab[((size_t)c * nl + l) * 4 + 0] = (T)(lp.tab[4 * (size_t)c + 0] * lp.cphi);
-      tab[((size_t)c * nl + l) * 4 + 1] = (T)(lp.tab[4 * (size_t)c + 1] * lp.cphi);
-      tab[((size_t)c * nl + l) * 4 + 2] = (T)lp.tab[4 * (size_t)c + 2];
-      tab[((size_t)c * nl + l) * 4 + 3] = (T)lp.tab[4 * (size_t)c + 3];
-      nsum[(size_t)c * nl + l] = (T)lp.nsum[c];
-    }
-    for (int k = 0; k < nfr; k++) {
-      wch[(size_t)l * nfr + k] = (T)lp.wch[k];
-      star[(size_t)l * nfr + k] = (T)lp.star[k];
-      velo[(size_t)l * nfr + k] = lp.velo[k];
-    }
-    lc[l].cphi = (T)lp.cphi;
-    lc[l].istart = (T)lp.istart;
-    lc[l].scale = lp.scale;
-    scale[l] = lp.scale;
+    if (build_line_tables<T>(m, iline0, nl, lt, err)) return set_err(ctx, RL_ERR_ARG, err);
+    scale = lt.scale;
   }
+  const std::vector<T>&tab = lt.tab, &nsum = lt.nsum, &wch = lt.wch, &star = lt.star;
+  const std::vector<double>& velo = lt.velo;
+  const std::vector<LineConst<T>>& lc = lt.lc;
   const size_t nimg = (size_t)nl * cam.nrays * nfr;
   if (!cached) {
     CUDA_TRY(md->dtab.ensure(sizeof(T) * tab.size()));

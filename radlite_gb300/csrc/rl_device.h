@@ -84,4 +84,44 @@ struct ReduceParams {
   const double* scale;       // [nlines]
 };
 
+// ---- many jobs (model, camera, line range) in one launch sequence ----
+template <typename T>
+struct GeoJob {
+  GeoParams geo;
+  NodeBuf<T> nb;
+};
+
+template <typename T>
+struct WalkJobs {
+  const WalkParams<T>* jobs;  // [njobs] (device)
+  const int* item_prefix;     // [njobs+1] first item of each job
+  int njobs, total;           // total = item_prefix[njobs]
+  int stride;                 // 1, or > 1 to walk every stride-th item only (tuning samples)
+  int max_nfr;                // largest channel count of the jobs (shared-memory list size)
+  int* work;                  // queue counter
+  unsigned long long* counters;
+};
+
+template <typename T>
+struct RedJob {
+  ReduceParams p;
+  const T* img;
+  double* ring;
+  double* flux;
+};
+
+template <typename T>
+struct JobLaunch {
+  int njobs, nsm, cpl;
+  const GeoJob<T>* geo;      // [njobs] (device); nrays_total = 0 skips the geometry
+  const int* ray_prefix;
+  int nrays_total;
+  WalkJobs<T> walk;
+  bool reduce;
+  const RedJob<T>* red;      // [njobs] (device)
+  const int* ring_prefix;    // [njobs+1] (line, ring) pairs
+  const int* line_prefix;    // [njobs+1] lines
+  int nring_blocks, nline_blocks;
+};
+
 }  // namespace rl

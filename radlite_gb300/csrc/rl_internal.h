@@ -1,0 +1,144 @@
+// rl_internal.h -- library-internal state behind the opaque C handles, shared by the
+// single-model entry points (rl_capi.cpp) and the multi-job batch (rl_batch.cpp).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/rlgpu.h"
+#include "rl_device.h"
+#include "rl_host.h"
+
+namespace rl {
+template <typename T>
+cudaError_t launch_geometry(const GeoParams& p, const NodeBuf<T>& nb, int ray0, int nray, TrajDebug* dbg,
+                            cudaStream_t s);
+template <typename T>
+cudaError_t launch_walk(const WalkParams<T>& P, int cpl, int nsm, cudaStream_t s);
+template <typename T>
+cudaError_t launch_reduce(const ReduceParams& p, const T* img, double* ring, double* flux, cudaStream_t s);
+template <typename T>
+cudaError_t launch_jobs(const JobLaunch<T>& L, cudaStream_t s);
+cudaError_t measure_peaks(int nsm, cudaStream_t st, double* ffma_per_s, double* ex2_per_s);
+
+constexpr int kWalkGroup = 8;   // lines per walk work item at most (k_walk's kGroup)
+
+// Owned device allocation that only grows.
+struct DevBuf {
+  void* p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  DevBuf(DevBuf&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+  DevBuf& operator=(DevBuf&& o) noexcept {
+    if (this != &o) {
+      if (p) cudaFree(p);
+      p = o.p; n = o.n; o.p = nullptr; o.n = 0;
+    }
+    return *this;
+  }
+  ~DevBuf() { if (p) cudaFree(p); }
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= n && p) return cudaSuccess;
+    if (p) { cudaFree(p); p = nullptr; n = 0; }
+    cudaError_t e = cudaMalloc(&p, bytes ? bytes : 16);
+    if (e == cudaSuccess) n = bytes;
+    return e;
+  }
+  template <typename T> T* as() const { return static_cast<T*>(p); }
+};
+
+// Per-line device tables of a line range, built on the host in FP64 (prepare_line).
+template <typename T>
+struct LineTables {
+  int nl = 0, ncell = 0, nfr = 0;
+  std::vector<T> tab;        // [ncell][nl][4]: j-factor*cphi, alpha-factor*cphi, dust j, dust alpha
+  std::vector<T> nsum;       // [ncell][nl]
+  std::vector<T> wch, star;  // [nl][nfr]
+  std::vector<double> velo;  // [nl][nfr]
+  std::vector<LineConst<T>> lc;
+  std::vector<double> scale; // [nl]
+};
+template <typename T>
+int build_line_tables(const Model& m, int iline0, int nl, LineTables<T>& out, std::string& err);
+}  // namespace rl
+
+struct rl_ctx {
+  int device = 0, nsm = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[6] = {};
+  std::string err;
+};
+
+struct rl_model {
+  rl_ctx* ctx = nullptr;
+  rl::Model m;
+  int precision = RL_FP32;
+  // camera request
+  double incl_rad = 0.0;
+  int nphi = 0, dbdr = 1, nrext = 0;
+  // device copies of the grid and cell fields (uploaded once)
+  bool grid_ready = false;
+  rl::DevBuf dR, dTH, dtan2, dvel, dlw;
+  // camera geometry cache
+  bool geo_ready = false;
+  int geo_prec = -1;
+  rl::Camera cam;
+  rl::DevBuf dx0, dz0, dri;
+  rl::DevBuf nb_nn, nb_st, nb_ds, nb_dvf, nb_vl, nb_dvs, nb_lw, nb_wr, nb_wt, nb_c00, nb_misc;
+  int kmax = 0;
+  // per-line tables of the last line range (reused while the range and precision match)
+  int tab_line0 = -1, tab_nl = 0, tab_prec = -1;
+  std::vector<double> tab_scale;
+  // per-call buffers
+  rl::DevBuf dtab, dnsum, dwch, dvelo, dstar, dlc, dimg, dring, dflux, dscale, dcnt, dwork, derr;
+};
+
+extern thread_local std::string g_last_error;
+extern thread_local unsigned long long g_h2d, g_d2h;   // bytes copied by the current call
+
+namespace rl {
+void set_last_error(const std::string& msg);
+int set_err(rl_ctx* c, int code, const std::string& msg);
+cudaError_t h2d(void* dst, const void* src, size_t n, cudaStream_t s);
+cudaError_t d2h(void* dst, const void* src, size_t n, cudaStream_t s);
+int upload_grid(rl_model* md);
+
+inline GeoParams geo_params(const rl_model* md) {
+  GeoParams p;
+  const Model& m = md->m;
+  p.nr = m.nr; p.nth = m.nth; p.ny = m.ny; p.rstar = m.rstar; p.theta0 = md->cam.theta0;
+  p.R = md->dR.as<double>(); p.TH = md->dTH.as<double>(); p.tan2 = md->dtan2.as<double>();
+  p.vel = md->dvel.as<double>(); p.lw = md->dlw.as<double>();
+  p.x0 = md->dx0.as<double>(); p.z0 = md->dz0.as<double>();
+  return p;
+}
+
+template <typename T>
+inline NodeBuf<T> node_view(const rl_model* md) {
+  NodeBuf<T> nb;
+  nb.nrays = md->cam.nrays;
+  nb.kmax = md->kmax;
+  nb.nnodes = md->nb_nn.as<int>();
+  nb.status = md->nb_st.as<int>();
+  nb.ds = md->nb_ds.as<T>();
+  nb.dvf = md->nb_dvf.as<float>();
+  nb.vl = md->nb_vl.as<T>();
+  nb.dvseg = md->nb_dvs.as<T>();
+  nb.lw = md->nb_lw.as<T>();
+  nb.wr = md->nb_wr.as<T>();
+  nb.wt = md->nb_wt.as<T>();
+  nb.c00 = md->nb_c00.as<int>();
+  nb.misc = md->nb_misc.as<unsigned>();
+  return nb;
+}
+}  // namespace rl
+
+#define CUDA_TRY(call)                                                                          \
+  do {                                                                                          \
+    cudaError_t e_ = (call);                                                                    \
+    if (e_ != cudaSuccess)                                                                      \
+      return rl::set_err(ctx, RL_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)

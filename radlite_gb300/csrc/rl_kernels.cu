@@ -95,10 +95,7 @@ struct NodeEmitter {
 };
 
 template <typename T>
-__global__ void __launch_bounds__(128) k_geometry(GeoParams p, NodeBuf<T> nb, int ray0, int nray, TrajDebug* dbg) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nray) return;
-  const int ray = ray0 + i;
+__device__ __forceinline__ void geometry_ray(const GeoParams& p, NodeBuf<T>& nb, int ray, TrajDebug* dbg) {
   rlg::Grid g;
   g.R = p.R; g.TH = p.TH; g.tan2 = p.tan2; g.nr = p.nr; g.nth = p.nth; g.ny = p.ny; g.rstar = p.rstar;
   NodeEmitter<T> em;
@@ -108,6 +105,36 @@ __global__ void __launch_bounds__(128) k_geometry(GeoParams p, NodeBuf<T> nb, in
   if (em.status != 0) st = em.status;
   nb.nnodes[ray] = em.k;
   nb.status[ray] = st;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_geometry(GeoParams p, NodeBuf<T> nb, int ray0, int nray, TrajDebug* dbg) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nray) return;
+  geometry_ray<T>(p, nb, ray0 + i, dbg);
+}
+
+// index j with prefix[j] <= x < prefix[j+1] (prefix ascending, prefix[0] = 0)
+__device__ __forceinline__ int find_job(const int* __restrict__ prefix, int njobs, int x) {
+  int lo = 0, hi = njobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(&prefix[mid]) <= x) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Geometry of many cameras in one launch: thread i traces ray i of the concatenated
+// ray list; ray_prefix[j] is the first ray of job j.
+template <typename T>
+__global__ void __launch_bounds__(128) k_geometry_jobs(const GeoJob<T>* __restrict__ jobs, const int* __restrict__ ray_prefix,
+                                                       int njobs, int total) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= total) return;
+  const int j = find_job(ray_prefix, njobs, i);
+  GeoParams p = jobs[j].geo;
+  NodeBuf<T> nb = jobs[j].nb;
+  geometry_ray<T>(p, nb, i - ray_prefix[j], nullptr);
 }
 
 // ------------------------------------------------------------------------------------
@@ -654,181 +681,231 @@ __device__ long long walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState
   return steps;
 }
 
+struct WalkCounters { unsigned long long steps = 0, integ = 0, nodes = 0; };
+
+// One work item: line group g of ray `ray`, item = g * nrays + ray.
+template <typename T, int C>
+__device__ __forceinline__ void walk_item(const WalkParams<T>& P, int item, WarpStage<T>& S, SlotState<T, C>& SS,
+                                          SubWork<T>& SW, unsigned short* list, int lane, WalkCounters& wc) {
+  const NodeBuf<T>& nb = P.nb;
+  const int nl = P.nlines;
+  const int g = item / nb.nrays, ray = item - g * nb.nrays;
+  const int l0 = g * P.gsize, gl = min(P.gsize, nl - l0);
+  const int K = nb.nnodes[ray];
+  if (nb.status[ray] != 0 || K < 1) {
+    if (lane == 0) atomicCAS(P.err, 0, 100 + nb.status[ray]);
+    return;
+  }
+  const size_t row = (size_t)ray * nb.kmax;
+  // 1. velocity window of the ray per line (telescope.F:4265-4270): node projected
+  //    velocities where N_up + N_low exceeds 1e-3, nodes 0 .. K-2
+  float mn[kGroup], mx[kGroup];
+#pragma unroll
+  for (int l = 0; l < kGroup; l++) { mn[l] = 1.0f; mx[l] = -1.0f; }
+  __syncwarp();
+  if (ray != 0) {
+    for (int k = lane; k < K - 1; k += 32) {
+      const size_t o = row + k;
+      const T wr = nb.wr[o], wt = nb.wt[o];
+      const Corners c = corners(nb.c00[o], nb.misc[o], P.nth);
+      const float d = nb.dvf[o];
+#pragma unroll
+      for (int l = 0; l < kGroup; l++) {
+        if (l < gl && interp_1(P.nsum, c, nl, l0 + l, wr, wt) > (T)1.0e-3) {
+          mn[l] = fminf(mn[l], d); mx[l] = fmaxf(mx[l], d);
+        }
+      }
+    }
+#pragma unroll
+    for (int l = 0; l < kGroup; l++) {
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        mn[l] = fminf(mn[l], __shfl_xor_sync(0xffffffffu, mn[l], off));
+        mx[l] = fmaxf(mx[l], __shfl_xor_sync(0xffffffffu, mx[l], off));
+      }
+    }
+  }
+  if (lane == 0) {
+#pragma unroll
+    for (int l = 0; l < kGroup; l++) { S.mn[l] = mn[l]; S.mx[l] = mx[l]; }
+  }
+  __syncwarp();
+  // 2. (line, channel) pairs to integrate: channel 1, the in-window channels and the
+  //    channel that supplies the continuum of the others (telescope.F:541-613)
+  int nint = 0;
+  for (int l = 0; l < gl; l++) {
+    int cc = -1;
+    const double* velo = P.velo + (size_t)(l0 + l) * P.nfr;
+    const double lo = (double)S.mn[l] - 2.0 * P.aksmax_c, hi = (double)S.mx[l] + 2.0 * P.aksmax_c;
+    if (ray != 0 && !(velo[0] <= hi && velo[0] >= lo)) cc = 0;
+    for (int cb = 0; cb < P.nfr; cb += 32) {
+      const int c = cb + lane;
+      const bool valid = c < P.nfr;
+      const bool in = valid && (ray == 0 || (velo[c] <= hi && velo[c] >= lo));
+      if (cc < 0 && ray != 0) {
+        const unsigned outm = __ballot_sync(0xffffffffu, valid && !in && c >= 1);
+        if (outm) cc = cb + __ffs(outm) - 1;
+      }
+      const bool take = valid && (c == 0 || in || c == cc);
+      const unsigned m = __ballot_sync(0xffffffffu, take);
+      if (take) list[nint + __popc(m & lanemask_lt())] = (unsigned short)((l << kChBits) | c);
+      nint += __popc(m);
+    }
+    if (lane == 0) S.cont_ch[l] = cc;
+  }
+  __syncwarp();
+  // 3. formal solution of the selected pairs, in tiles of 32*C
+  for (int tb = 0; tb < nint; tb += 32 * C) {
+    const int nt = min(32 * C, nint - tb);
+    wc.steps += walk_ray<T, C>(P, S, SS, SW, ray, K, l0, gl, list + tb, nt, lane);
+    for (int j = 0; j < C; j++) {
+      const int idx = j * 32 + lane;
+      if (idx < nt) {
+        const unsigned e = list[tb + idx];
+        const int l = (int)(e >> kChBits), c = (int)(e & (kMaxChannels - 1));
+        const T Iv = SS.I[j][lane];
+        P.img[((size_t)(l0 + l) * nb.nrays + ray) * P.nfr + c] = Iv;
+        if (c == S.cont_ch[l]) S.contv[l] = Iv;
+      }
+    }
+  }
+  wc.integ += nint;
+  wc.nodes += (unsigned long long)nint * K;
+  __syncwarp();
+  // 4. continuum copy for the other channels of each line
+  for (int l = 0; l < gl; l++) {
+    const int cc = S.cont_ch[l];
+    if (cc < 0) continue;
+    const double* velo = P.velo + (size_t)(l0 + l) * P.nfr;
+    const double lo = (double)S.mn[l] - 2.0 * P.aksmax_c, hi = (double)S.mx[l] + 2.0 * P.aksmax_c;
+    T* img = P.img + ((size_t)(l0 + l) * nb.nrays + ray) * P.nfr;
+    const T contv = S.contv[l];
+    if (contv != (T)0) {
+      for (int c = lane; c < P.nfr; c += 32) {
+        const bool in = velo[c] <= hi && velo[c] >= lo;
+        if (!(c == 0 || in || c == cc)) img[c] = contv;
+      }
+      continue;
+    }
+    // a zero continuum is recomputed channel by channel in the reference: integrate
+    // every other out-of-window channel, then apply its sequential copy rule
+    int n2 = 0;
+    for (int cb = 0; cb < P.nfr; cb += 32) {
+      const int c = cb + lane;
+      const bool valid = c < P.nfr;
+      const bool take = valid && !(c == 0 || (velo[c] <= hi && velo[c] >= lo) || c == cc);
+      const unsigned m = __ballot_sync(0xffffffffu, take);
+      if (take) list[n2 + __popc(m & lanemask_lt())] = (unsigned short)((l << kChBits) | c);
+      n2 += __popc(m);
+    }
+    __syncwarp();
+    for (int tb = 0; tb < n2; tb += 32 * C) {
+      const int nt = min(32 * C, n2 - tb);
+      wc.steps += walk_ray<T, C>(P, S, SS, SW, ray, K, l0, gl, list + tb, nt, lane);
+      for (int j = 0; j < C; j++) {
+        const int idx = j * 32 + lane;
+        if (idx < nt) img[list[tb + idx] & (kMaxChannels - 1)] = SS.I[j][lane];
+      }
+    }
+    wc.integ += n2;
+    wc.nodes += (unsigned long long)n2 * K;
+    __syncwarp();
+    if (lane == 0) {
+      T cur = 0;
+      bool have = false;
+      for (int c = 0; c < P.nfr; c++) {
+        const bool in = velo[c] <= hi && velo[c] >= lo;
+        if (c != cc && (c == 0 || in)) continue;
+        if (have) img[c] = cur;
+        else if (img[c] != (T)0) { cur = img[c]; have = true; }
+      }
+    }
+    __syncwarp();
+  }
+  __syncwarp();
+}
+
+// Per-warp shared-memory regions of the walk; `listcap` (pairs) is kGroup x the largest
+// channel count of the launch.
+template <typename T, int C>
+struct WarpSmem {
+  WarpStage<T>* S; SlotState<T, C>* SS; SubWork<T>* SW; unsigned short* list;
+  __device__ WarpSmem(unsigned char* raw, int nw, int wib, int listcap) {
+    const int capp = (listcap + 7) & ~7;
+    S = reinterpret_cast<WarpStage<T>*>(raw) + wib;
+    SS = reinterpret_cast<SlotState<T, C>*>(raw + sizeof(WarpStage<T>) * nw) + wib;
+    SW = reinterpret_cast<SubWork<T>*>(raw + (sizeof(WarpStage<T>) + sizeof(SlotState<T, C>)) * nw) + wib;
+    list = reinterpret_cast<unsigned short*>(
+               raw + (sizeof(WarpStage<T>) + sizeof(SlotState<T, C>) + sizeof(SubWork<T>)) * nw) +
+           (size_t)wib * capp;
+  }
+};
+
+__device__ __forceinline__ void flush_counters(WalkCounters wc, unsigned long long* counters, int lane) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) wc.steps += __shfl_xor_sync(0xffffffffu, wc.steps, off);
+  if (lane == 0) {
+    atomicAdd(&counters[0], wc.steps);
+    atomicAdd(&counters[1], wc.integ);
+    atomicAdd(&counters[2], wc.nodes);
+  }
+}
+
 template <typename T, int C>
 __global__ void __launch_bounds__(128) k_walk(WalkParams<T> P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  const int cap = kGroup * P.nfr;
-  const int capp = (cap + 7) & ~7;
-  WarpStage<T>* stages = reinterpret_cast<WarpStage<T>*>(smem_raw);
-  SlotState<T, C>* sstates = reinterpret_cast<SlotState<T, C>*>(smem_raw + sizeof(WarpStage<T>) * nw);
-  SubWork<T>* subw =
-      reinterpret_cast<SubWork<T>*>(smem_raw + (sizeof(WarpStage<T>) + sizeof(SlotState<T, C>)) * nw);
-  unsigned short* lists = reinterpret_cast<unsigned short*>(
-      smem_raw + (sizeof(WarpStage<T>) + sizeof(SlotState<T, C>) + sizeof(SubWork<T>)) * nw);
-  WarpStage<T>& S = stages[wib];
-  SlotState<T, C>& SS = sstates[wib];
-  SubWork<T>& SW = subw[wib];
-  unsigned short* list = lists + (size_t)wib * capp;
-  unsigned long long st_steps = 0, st_int = 0, st_nodes = 0;
-  const NodeBuf<T>& nb = P.nb;
-  const int nl = P.nlines;
+  WarpSmem<T, C> W(smem_raw, nw, wib, kGroup * P.nfr);
+  WalkCounters wc;
   for (;;) {
     int item = 0;
     if (lane == 0) item = atomicAdd(P.work, 1);
     item = __shfl_sync(0xffffffffu, item, 0);
     if (item >= P.nitems) break;
-    const int g = item / nb.nrays, ray = item - g * nb.nrays;
-    const int l0 = g * P.gsize, gl = min(P.gsize, nl - l0);
-    const int K = nb.nnodes[ray];
-    if (nb.status[ray] != 0 || K < 1) {
-      if (lane == 0) atomicCAS(P.err, 0, 100 + nb.status[ray]);
-      continue;
-    }
-    const size_t row = (size_t)ray * nb.kmax;
-    // 1. velocity window of the ray per line (telescope.F:4265-4270): node projected
-    //    velocities where N_up + N_low exceeds 1e-3, nodes 0 .. K-2
-    float mn[kGroup], mx[kGroup];
-#pragma unroll
-    for (int l = 0; l < kGroup; l++) { mn[l] = 1.0f; mx[l] = -1.0f; }
-    __syncwarp();
-    if (ray != 0) {
-      for (int k = lane; k < K - 1; k += 32) {
-        const size_t o = row + k;
-        const T wr = nb.wr[o], wt = nb.wt[o];
-        const Corners c = corners(nb.c00[o], nb.misc[o], P.nth);
-        const float d = nb.dvf[o];
-#pragma unroll
-        for (int l = 0; l < kGroup; l++) {
-          if (l < gl && interp_1(P.nsum, c, nl, l0 + l, wr, wt) > (T)1.0e-3) {
-            mn[l] = fminf(mn[l], d); mx[l] = fmaxf(mx[l], d);
-          }
-        }
-      }
-#pragma unroll
-      for (int l = 0; l < kGroup; l++) {
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-          mn[l] = fminf(mn[l], __shfl_xor_sync(0xffffffffu, mn[l], off));
-          mx[l] = fmaxf(mx[l], __shfl_xor_sync(0xffffffffu, mx[l], off));
-        }
-      }
-    }
-    if (lane == 0) {
-#pragma unroll
-      for (int l = 0; l < kGroup; l++) { S.mn[l] = mn[l]; S.mx[l] = mx[l]; }
-    }
-    __syncwarp();
-    // 2. (line, channel) pairs to integrate: channel 1, the in-window channels and the
-    //    channel that supplies the continuum of the others (telescope.F:541-613)
-    int nint = 0;
-    for (int l = 0; l < gl; l++) {
-      int cc = -1;
-      const double* velo = P.velo + (size_t)(l0 + l) * P.nfr;
-      const double lo = (double)S.mn[l] - 2.0 * P.aksmax_c, hi = (double)S.mx[l] + 2.0 * P.aksmax_c;
-      if (ray != 0 && !(velo[0] <= hi && velo[0] >= lo)) cc = 0;
-      for (int cb = 0; cb < P.nfr; cb += 32) {
-        const int c = cb + lane;
-        const bool valid = c < P.nfr;
-        const bool in = valid && (ray == 0 || (velo[c] <= hi && velo[c] >= lo));
-        if (cc < 0 && ray != 0) {
-          const unsigned outm = __ballot_sync(0xffffffffu, valid && !in && c >= 1);
-          if (outm) cc = cb + __ffs(outm) - 1;
-        }
-        const bool take = valid && (c == 0 || in || c == cc);
-        const unsigned m = __ballot_sync(0xffffffffu, take);
-        if (take) list[nint + __popc(m & lanemask_lt())] = (unsigned short)((l << kChBits) | c);
-        nint += __popc(m);
-      }
-      if (lane == 0) S.cont_ch[l] = cc;
-    }
-    __syncwarp();
-    // 3. formal solution of the selected pairs, in tiles of 32*C
-    for (int tb = 0; tb < nint; tb += 32 * C) {
-      const int nt = min(32 * C, nint - tb);
-      st_steps += walk_ray<T, C>(P, S, SS, SW, ray, K, l0, gl, list + tb, nt, lane);
-      for (int j = 0; j < C; j++) {
-        const int idx = j * 32 + lane;
-        if (idx < nt) {
-          const unsigned e = list[tb + idx];
-          const int l = (int)(e >> kChBits), c = (int)(e & (kMaxChannels - 1));
-          const T Iv = SS.I[j][lane];
-          P.img[((size_t)(l0 + l) * nb.nrays + ray) * P.nfr + c] = Iv;
-          if (c == S.cont_ch[l]) S.contv[l] = Iv;
-        }
-      }
-    }
-    st_int += nint;
-    st_nodes += (unsigned long long)nint * K;
-    __syncwarp();
-    // 4. continuum copy for the other channels of each line
-    for (int l = 0; l < gl; l++) {
-      const int cc = S.cont_ch[l];
-      if (cc < 0) continue;
-      const double* velo = P.velo + (size_t)(l0 + l) * P.nfr;
-      const double lo = (double)S.mn[l] - 2.0 * P.aksmax_c, hi = (double)S.mx[l] + 2.0 * P.aksmax_c;
-      T* img = P.img + ((size_t)(l0 + l) * nb.nrays + ray) * P.nfr;
-      const T contv = S.contv[l];
-      if (contv != (T)0) {
-        for (int c = lane; c < P.nfr; c += 32) {
-          const bool in = velo[c] <= hi && velo[c] >= lo;
-          if (!(c == 0 || in || c == cc)) img[c] = contv;
-        }
-        continue;
-      }
-      // a zero continuum is recomputed channel by channel in the reference: integrate
-      // every other out-of-window channel, then apply its sequential copy rule
-      int n2 = 0;
-      for (int cb = 0; cb < P.nfr; cb += 32) {
-        const int c = cb + lane;
-        const bool valid = c < P.nfr;
-        const bool take = valid && !(c == 0 || (velo[c] <= hi && velo[c] >= lo) || c == cc);
-        const unsigned m = __ballot_sync(0xffffffffu, take);
-        if (take) list[n2 + __popc(m & lanemask_lt())] = (unsigned short)((l << kChBits) | c);
-        n2 += __popc(m);
-      }
-      __syncwarp();
-      for (int tb = 0; tb < n2; tb += 32 * C) {
-        const int nt = min(32 * C, n2 - tb);
-        st_steps += walk_ray<T, C>(P, S, SS, SW, ray, K, l0, gl, list + tb, nt, lane);
-        for (int j = 0; j < C; j++) {
-          const int idx = j * 32 + lane;
-          if (idx < nt) img[list[tb + idx] & (kMaxChannels - 1)] = SS.I[j][lane];
-        }
-      }
-      st_int += n2;
-      st_nodes += (unsigned long long)n2 * K;
-      __syncwarp();
-      if (lane == 0) {
-        T cur = 0;
-        bool have = false;
-        for (int c = 0; c < P.nfr; c++) {
-          const bool in = velo[c] <= hi && velo[c] >= lo;
-          if (c != cc && (c == 0 || in)) continue;
-          if (have) img[c] = cur;
-          else if (img[c] != (T)0) { cur = img[c]; have = true; }
-        }
-      }
-      __syncwarp();
-    }
-    __syncwarp();
+    walk_item<T, C>(P, item, *W.S, *W.SS, *W.SW, W.list, lane, wc);
   }
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) st_steps += __shfl_xor_sync(0xffffffffu, st_steps, off);
-  if (lane == 0) {
-    atomicAdd(&P.counters[0], st_steps);
-    atomicAdd(&P.counters[1], st_int);
-    atomicAdd(&P.counters[2], st_nodes);
+  flush_counters(wc, P.counters, lane);
+}
+
+// Walk of many jobs (model, camera, line range) from one device queue: queue entry i
+// is item i * stride of the concatenated item list (stride > 1 samples it for tuning);
+// item_prefix[j] is the first item of job j. Each warp keeps the parameters of its
+// current job in shared memory.
+template <typename T, int C>
+__global__ void __launch_bounds__(128) k_walk_jobs(WalkJobs<T> B) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ WalkParams<T> jp[4];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  WarpSmem<T, C> W(smem_raw, nw, wib, kGroup * B.max_nfr);
+  WalkCounters wc;
+  int cur = -1;
+  const int nq = (B.total + B.stride - 1) / B.stride;
+  for (;;) {
+    int q = 0;
+    if (lane == 0) q = atomicAdd(B.work, 1);
+    q = __shfl_sync(0xffffffffu, q, 0);
+    if (q >= nq) break;
+    const int item = q * B.stride;
+    const int j = find_job(B.item_prefix, B.njobs, item);
+    if (j != cur) {
+      __syncwarp();
+      const int* src = reinterpret_cast<const int*>(B.jobs + j);
+      int* dst = reinterpret_cast<int*>(&jp[wib]);
+      for (int w = lane; w < (int)(sizeof(WalkParams<T>) / 4); w += 32) dst[w] = __ldg(src + w);
+      __syncwarp();
+      cur = j;
+    }
+    walk_item<T, C>(jp[wib], item - __ldg(&B.item_prefix[j]), *W.S, *W.SS, *W.SW, W.list, lane, wc);
   }
+  flush_counters(wc, B.counters, lane);
 }
 
 // ------------------------------------------------------------------------------------
 // image -> spectrum (telescope.F:1346-1435), deterministic FP64
 // ------------------------------------------------------------------------------------
 template <typename T>
-__global__ void k_ring_sum(ReduceParams p, const T* __restrict__ img, double* __restrict__ ring) {
-  const int ir = blockIdx.x + 1;        // ring 1..nrr
-  const int line = blockIdx.y;
+__device__ __forceinline__ void ring_sum_one(const ReduceParams& p, const T* __restrict__ img, double* __restrict__ ring,
+                                             int line, int ir) {
   for (int k = threadIdx.x; k < p.nfr; k += blockDim.x) {
     double d = 0.0;
     const T* base = img + ((size_t)line * p.nrays + 1 + (size_t)(ir - 1) * p.nphi) * p.nfr + k;
@@ -838,11 +915,9 @@ __global__ void k_ring_sum(ReduceParams p, const T* __restrict__ img, double* __
 }
 
 template <typename T>
-__global__ void k_spectrum(ReduceParams p, const T* __restrict__ img, const double* __restrict__ ring,
-                           double* __restrict__ flux) {
-  const int line = blockIdx.y;
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= p.nfr) return;
+__device__ __forceinline__ void spectrum_one(const ReduceParams& p, const T* __restrict__ img,
+                                             const double* __restrict__ ring, double* __restrict__ flux, int line,
+                                             int k) {
   const double pi = 3.14159265359;
   double slum = 0.0;
   double surf = pi * (p.ri[1] * p.ri[1]);
@@ -855,6 +930,38 @@ __global__ void k_spectrum(ReduceParams p, const T* __restrict__ img, const doub
     slum = slum + d;
   }
   flux[(size_t)line * p.nfr + k] = p.scale[line] * slum / p.dist2;
+}
+
+template <typename T>
+__global__ void k_ring_sum(ReduceParams p, const T* __restrict__ img, double* __restrict__ ring) {
+  ring_sum_one<T>(p, img, ring, blockIdx.y, blockIdx.x + 1);   // ring 1..nrr of line blockIdx.y
+}
+
+template <typename T>
+__global__ void k_spectrum(ReduceParams p, const T* __restrict__ img, const double* __restrict__ ring,
+                           double* __restrict__ flux) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= p.nfr) return;
+  spectrum_one<T>(p, img, ring, flux, blockIdx.y, k);
+}
+
+// Reduction of many jobs: block b of k_ring_sum_jobs is (line, ring) pair b of the
+// concatenation (ring_prefix[j] = first pair of job j, nlines x nrr pairs per job);
+// block b of k_spectrum_jobs is line b (line_prefix[j] = first line of job j).
+template <typename T>
+__global__ void k_ring_sum_jobs(const RedJob<T>* __restrict__ jobs, const int* __restrict__ ring_prefix, int njobs) {
+  const int j = find_job(ring_prefix, njobs, blockIdx.x);
+  const RedJob<T>& J = jobs[j];
+  const int b = blockIdx.x - ring_prefix[j];
+  ring_sum_one<T>(J.p, J.img, J.ring, b / J.p.nrr, b % J.p.nrr + 1);
+}
+
+template <typename T>
+__global__ void k_spectrum_jobs(const RedJob<T>* __restrict__ jobs, const int* __restrict__ line_prefix, int njobs) {
+  const int j = find_job(line_prefix, njobs, blockIdx.x);
+  const RedJob<T>& J = jobs[j];
+  const int line = blockIdx.x - line_prefix[j];
+  for (int k = threadIdx.x; k < J.p.nfr; k += blockDim.x) spectrum_one<T>(J.p, J.img, J.ring, J.flux, line, k);
 }
 
 // ------------------------------------------------------------------------------------
@@ -959,6 +1066,27 @@ static cudaError_t launch_walk_c(const WalkParams<T>& P, int nsm, cudaStream_t s
   return cudaGetLastError();
 }
 
+template <typename T, int C>
+static cudaError_t launch_walk_jobs_c(const WalkJobs<T>& B, int nsm, cudaStream_t s) {
+  const int warps = 4, threads = warps * 32;
+  const int capp = (kGroup * B.max_nfr + 7) & ~7;
+  const size_t smem = (sizeof(WarpStage<T>) + sizeof(SlotState<T, C>) + sizeof(SubWork<T>)) * warps +
+                      sizeof(unsigned short) * (size_t)capp * warps;
+  cudaError_t e = cudaFuncSetAttribute(k_walk_jobs<T, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_walk_jobs<T, C>, threads, smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  long long blocks = (long long)nsm * per_sm;
+  const long long nq = ((long long)B.total + B.stride - 1) / B.stride;
+  const long long need = (nq + warps - 1) / warps;
+  if (blocks > need) blocks = need;
+  if (blocks < 1) blocks = 1;
+  k_walk_jobs<T, C><<<(unsigned)blocks, threads, smem, s>>>(B);
+  return cudaGetLastError();
+}
+
 template <typename T>
 cudaError_t launch_walk(const WalkParams<T>& P, int cpl, int nsm, cudaStream_t s) {
   switch (cpl) {
@@ -980,11 +1108,36 @@ cudaError_t launch_reduce(const ReduceParams& p, const T* img, double* ring, dou
   return cudaGetLastError();
 }
 
+template <typename T>
+cudaError_t launch_jobs(const JobLaunch<T>& L, cudaStream_t s) {
+  if (L.nrays_total > 0) {
+    k_geometry_jobs<T><<<(L.nrays_total + 127) / 128, 128, 0, s>>>(L.geo, L.ray_prefix, L.njobs, L.nrays_total);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  cudaError_t e = cudaMemsetAsync(L.walk.work, 0, sizeof(int), s);
+  if (e != cudaSuccess) return e;
+  switch (L.cpl) {
+    case 1: e = launch_walk_jobs_c<T, 1>(L.walk, L.nsm, s); break;
+    case 2: e = launch_walk_jobs_c<T, 2>(L.walk, L.nsm, s); break;
+    case 4: e = launch_walk_jobs_c<T, 4>(L.walk, L.nsm, s); break;
+    default: e = launch_walk_jobs_c<T, 8>(L.walk, L.nsm, s); break;
+  }
+  if (e != cudaSuccess || !L.reduce) return e;
+  k_ring_sum_jobs<T><<<L.nring_blocks, 256, 0, s>>>(L.red, L.ring_prefix, L.njobs);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_spectrum_jobs<T><<<L.nline_blocks, 128, 0, s>>>(L.red, L.line_prefix, L.njobs);
+  return cudaGetLastError();
+}
+
 template cudaError_t launch_geometry<float>(const GeoParams&, const NodeBuf<float>&, int, int, TrajDebug*, cudaStream_t);
 template cudaError_t launch_geometry<double>(const GeoParams&, const NodeBuf<double>&, int, int, TrajDebug*, cudaStream_t);
 template cudaError_t launch_walk<float>(const WalkParams<float>&, int, int, cudaStream_t);
 template cudaError_t launch_walk<double>(const WalkParams<double>&, int, int, cudaStream_t);
 template cudaError_t launch_reduce<float>(const ReduceParams&, const float*, double*, double*, cudaStream_t);
 template cudaError_t launch_reduce<double>(const ReduceParams&, const double*, double*, double*, cudaStream_t);
+template cudaError_t launch_jobs<float>(const JobLaunch<float>&, cudaStream_t);
+template cudaError_t launch_jobs<double>(const JobLaunch<double>&, cudaStream_t);
 
 }  // namespace rl

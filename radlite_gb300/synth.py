@@ -119,6 +119,31 @@ def config_by_name(name: str, **over) -> DiskConfig:
     return DiskConfig(**d)
 
 
+def batch_configs(n: int = 256, seed: int = 2, nphi: int = 16) -> list:
+    """The uneven multi-model workload: n seeded disks with nr ~ U[64,512], ntheta ~
+    U[32,256], surface-density index ~ U[-1.5,-0.5], temperature index ~ U[-0.7,-0.3],
+    stellar mass ~ U[0.3,2.5] Msun, inclination ~ U[5,85] deg, 1-50 lines of the
+    ro-vibrational band (P and R branches, J = 1..25) and 32-256 channels. Channel counts
+    come from (vmax, dv) pairs that satisfy the passband rule nfr = INT(2 vmax/dv + 1).
+    Image radii follow the grid: dbdr 2 plus nr/4 extra inner rings, so there are
+    2(nr-1) + 10 + nr/4 rings of nphi azimuths."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        nr = int(rng.integers(64, 513))
+        nt = int(rng.integers(32, 257))
+        nch = int(rng.integers(32, 257))
+        nl = int(rng.integers(1, 51))
+        dv = 0.4
+        out.append(DiskConfig(
+            name=f"batch{i:03d}", nr=nr, nt=nt, sigma_pow=float(rng.uniform(-1.5, -0.5)),
+            t_pow=float(rng.uniform(-0.7, -0.3)), mstar=float(rng.uniform(0.3, 2.5)),
+            incl_deg=float(rng.uniform(5.0, 85.0)), molecule="band", band_nj=25, ilinestart=1,
+            nlines=nl, dv=dv, vmax=((nch - 1) + 0.05) * dv / 2.0, nphi=nphi, dbdr=2,
+            nrrextra=-max(8, nr // 4), seed=seed * 1000 + i))
+    return out
+
+
 # ----------------------------------------------------------------------------------------
 # physical model on the stored grid
 # ----------------------------------------------------------------------------------------
