@@ -366,6 +366,36 @@ def batched_case(ctx, n_models, steps, tune_stride=32):
     return res
 
 
+def adjoint_case(ctx, name="adjoint_disk", reps=3):
+    """Forward and forward+adjoint of the differentiable raytrace (per-cell ln T, ln X,
+    width) on one model, FP32; timed with the library's CUDA events."""
+    import numpy as np
+    import torch
+    import radlite_gb300 as rl
+    from radlite_gb300 import synth
+    cfg = synth.config_by_name(name)
+    m = ctx.load_arrays(synth.lte_arrays(cfg), camera(cfg, cfg.incl_deg))
+    lnT, lnX, b = (torch.tensor(a, dtype=torch.float64, device="cuda") for a in synth.cell_params(cfg))
+    d = rl.Diff(m, cfg.ilinestart, cfg.nlines, precision=0)
+    target = d.forward(lnT + 0.05, lnX, b)
+    fw, bw = [], []
+    for _ in range(reps + 1):
+        flux, st = d.forward(lnT, lnX, b, stats=True)
+        gflux = 2.0 * (flux - target) / target.abs().max() ** 2
+        _, sb = d.backward(gflux, stats=True)
+        fw.append(st["total_ms"])
+        bw.append(sb["total_ms"])
+    res = {"workload": f"{name}: {cfg.nr}x{cfg.nt} disk, {cfg.nlines} lines x {d.nfr} channels, {d.nrays} rays, "
+                       "gradients w.r.t. per-cell ln T, ln X, width",
+           "forward_ms": statistics.median(fw[1:]), "adjoint_ms": statistics.median(bw[1:]),
+           "spectra": cfg.nlines}
+    res["adjoint_over_forward"] = res["adjoint_ms"] / res["forward_ms"]
+    res["forward_adjoint_spectra_per_s"] = cfg.nlines / ((res["forward_ms"] + res["adjoint_ms"]) * 1e-3)
+    d.close()
+    m.free()
+    return res
+
+
 def profile_case(args):
     """One pass of a named workload (geometry, walk, reduction), for profiler captures."""
     import radlite_gb300 as rl
@@ -396,7 +426,14 @@ def main():
     ap.add_argument("--batch-models", type=int, default=256,
                     help="models of the uneven batched comparison (0 skips it)")
     ap.add_argument("--only-batch", action="store_true", help="run only the batched comparison")
+    ap.add_argument("--only-adjoint", action="store_true", help="run only the forward+adjoint timing")
     args = ap.parse_args()
+    if args.only_adjoint:
+        import radlite_gb300 as rl
+        ctx = rl.Context(0)
+        print(json.dumps(adjoint_case(ctx)), flush=True)
+        ctx.close()
+        return 0
     if args.only_batch:
         import radlite_gb300 as rl
         ctx = rl.Context(0)

@@ -162,6 +162,28 @@ int rl_batch_waves(rl_batch* batch, int* nwaves);
    (radlite.py:592-595). */
 int rl_run_manifest(const char* manifest, int device, rl_stats* stats);
 
+/* ---- Differentiable raytrace. No counterpart in the reference, whose level populations
+   come precomputed from the setup (LTE in pyradlite radlite.py:1106-1118). A rl_diff holds
+   one model's camera and lines iline0 .. iline0+nlines-1; the spectra become a function of
+   three per-cell parameters (cell index (ir-1)*nth + (it-1)): ln T (gas and dust
+   temperature; LTE populations with the partition sum over the molecule's levels), ln X
+   (molecular abundance) and the line width b [km/s] (turbulence.inp). Everything else stays
+   as loaded, including the largest width (velocity-window margin) and the FP32 intensity
+   scale. All array arguments are DEVICE pointers of the context's device (FP64); the calls
+   return after the work is done. */
+typedef struct rl_diff rl_diff;
+int rl_diff_create(rl_model* model, int iline0, int nlines, int precision, rl_diff** diff);
+int rl_diff_destroy(rl_diff* diff);
+int rl_diff_info(rl_diff* diff, int* ncell, int* nlines, int* nfr, int* nrays);
+/* flux [nlines][nfr]: F_nu at 1 pc for the parameters lnT, lnX, width [ncell]. */
+int rl_diff_forward(rl_diff* diff, const double* lnT, const double* lnX, const double* width, double* flux,
+                    rl_stats* stats);
+/* Gradient of a loss L at the last forward's parameters: given gflux = dL/dflux
+   [nlines][nfr], writes dL/dlnT, dL/dlnX, dL/dwidth [ncell] (adjoint walk with
+   checkpoints every 32 nodes per ray). */
+int rl_diff_backward(rl_diff* diff, const double* gflux, double* g_lnT, double* g_lnX, double* g_width,
+                     rl_stats* stats);
+
 /* Circular image -> F_nu at `distance_pc` parsec, with no device allocation. No
    counterpart in the reference: it serves callers that own all device memory (their
    own pool or arena) and cannot let a library call cudaMalloc. Every pointer is a

@@ -74,6 +74,7 @@ EXPORTS = ["rl_create", "rl_destroy", "rl_last_error", "rl_load_dir", "rl_load_a
            "rl_batch_create", "rl_batch_destroy", "rl_batch_add", "rl_batch_set_memory", "rl_batch_set_tiles",
            "rl_batch_get_tiles", "rl_batch_autotune", "rl_batch_use_graph", "rl_batch_flux_size",
            "rl_batch_job_info", "rl_batch_run", "rl_batch_waves", "rl_run_manifest",
+           "rl_diff_create", "rl_diff_destroy", "rl_diff_info", "rl_diff_forward", "rl_diff_backward",
            "rl_image_to_spectrum_noalloc"]
 
 _lib = None
@@ -115,6 +116,11 @@ def lib():
         L.rl_batch_run.argtypes = [vp, _D, C.POINTER(Stats)]
         L.rl_batch_waves.argtypes = [vp, _I]
         L.rl_run_manifest.argtypes = [C.c_char_p, C.c_int, C.POINTER(Stats)]
+        L.rl_diff_create.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.POINTER(vp)]
+        L.rl_diff_destroy.argtypes = [vp]
+        L.rl_diff_info.argtypes = [vp, _I, _I, _I, _I]
+        L.rl_diff_forward.argtypes = [vp, vp, vp, vp, vp, C.POINTER(Stats)]
+        L.rl_diff_backward.argtypes = [vp, vp, vp, vp, vp, C.POINTER(Stats)]
         L.rl_image_to_spectrum_noalloc.argtypes = [vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                                    vp, vp, C.c_double, vp]
         _lib = L
@@ -344,6 +350,99 @@ class Batch:
             _check(lib().rl_batch_job_info(self.h, j, C.byref(off), C.byref(nl), C.byref(nfr)), self.ctx.h)
             out.append(flux[off.value:off.value + nl.value * nfr.value].reshape(nl.value, nfr.value))
         return (out, st.as_dict()) if stats else out
+
+
+class Diff:
+    """Differentiable spectra of one model (rl_diff): F_nu[lines, channels] as a function of
+    per-cell ln T, ln X (abundance) and line width b [km/s], cells in the library order
+    (ir-1)*nth + (it-1). Arrays are float64 CUDA tensors (torch) on the context's device."""
+
+    def __init__(self, model: "Model", iline0: int, nlines: int, precision: int = RL_FP32):
+        self.model = model
+        self.h = C.c_void_p()
+        _check(lib().rl_diff_create(model.h, iline0, nlines, precision, C.byref(self.h)), model._ch)
+        nc, nl, nf, nr = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        _check(lib().rl_diff_info(self.h, C.byref(nc), C.byref(nl), C.byref(nf), C.byref(nr)))
+        self.ncell, self.nlines, self.nfr, self.nrays = nc.value, nl.value, nf.value, nr.value
+        self.version = 0
+
+    def close(self):
+        if self.h:
+            lib().rl_diff_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def _dev(t):
+        import torch
+        if not (t.is_cuda and t.dtype == torch.float64 and t.is_contiguous()):
+            raise RLError("Diff takes contiguous float64 CUDA tensors")
+        return t
+
+    def forward(self, lnT, lnX, width, stats: bool = False):
+        import torch
+        for t in (lnT, lnX, width):
+            self._dev(t)
+            if t.numel() != self.ncell:
+                raise RLError(f"expected {self.ncell} cells, got {t.numel()}")
+        flux = torch.empty((self.nlines, self.nfr), dtype=torch.float64, device=lnT.device)
+        torch.cuda.current_stream(lnT.device).synchronize()
+        st = Stats()
+        _check(lib().rl_diff_forward(self.h, lnT.data_ptr(), lnX.data_ptr(), width.data_ptr(), flux.data_ptr(),
+                                     C.byref(st)), self.model._ch)
+        self.version += 1
+        return (flux, st.as_dict()) if stats else flux
+
+    def backward(self, gflux, stats: bool = False):
+        import torch
+        gflux = self._dev(gflux.contiguous())
+        g = [torch.empty(self.ncell, dtype=torch.float64, device=gflux.device) for _ in range(3)]
+        torch.cuda.current_stream(gflux.device).synchronize()
+        st = Stats()
+        _check(lib().rl_diff_backward(self.h, gflux.data_ptr(), g[0].data_ptr(), g[1].data_ptr(), g[2].data_ptr(),
+                                      C.byref(st)), self.model._ch)
+        return (tuple(g), st.as_dict()) if stats else tuple(g)
+
+
+def _raytrace_function():
+    import torch
+
+    class RaytraceFunction(torch.autograd.Function):
+        """spectra = raytrace(ln T, ln X, width); backward by the adjoint walk."""
+
+        @staticmethod
+        def forward(ctx, lnT, lnX, width, diff):
+            flux = diff.forward(lnT.contiguous(), lnX.contiguous(), width.contiguous())
+            ctx.diff, ctx.version = diff, diff.version
+            ctx.save_for_backward(lnT, lnX, width)
+            return flux
+
+        @staticmethod
+        def backward(ctx, gflux):
+            diff = ctx.diff
+            if diff.version != ctx.version:       # another forward ran since: restore this point
+                lnT, lnX, width = ctx.saved_tensors
+                diff.forward(lnT.contiguous(), lnX.contiguous(), width.contiguous())
+            gT, gX, gb = diff.backward(gflux)
+            return gT, gX, gb, None
+
+    return RaytraceFunction
+
+
+_RF = None
+
+
+def raytrace(diff: Diff, lnT, lnX, width):
+    """Differentiable spectra [nlines, nfr] of `diff` (torch autograd through the adjoint)."""
+    global _RF
+    if _RF is None:
+        _RF = _raytrace_function()
+    return _RF.apply(lnT, lnX, width, diff)
 
 
 def load_dir_host(path: str) -> "Model":

@@ -124,4 +124,50 @@ struct JobLaunch {
   int nring_blocks, nline_blocks;
 };
 
+// ---- differentiable path: LTE line tables from per-cell parameters, adjoint walk ----
+struct LteLine {
+  int lu, ld;                 // 0-based upper and lower level of the line
+  double C1, C2, Bud, Bdu;    // j = C1 N_up phi, alpha = C2 (N_low Bdu - N_up Bud) phi
+  double nu;                  // line frequency (dust Planck function at the line centre)
+  double cphi, scale;         // profile normalisation; fixed intensity scale of the walk
+};
+
+template <typename T>
+struct LteParams {
+  int ncell, nlev, nl;
+  const double* lnT;          // [ncell] ln gas (= dust) temperature
+  const double* lnX;          // [ncell] ln molecular abundance
+  const double* rho_m;        // [ncell] rho / (umass m_p): molecules per unit abundance
+  const double* Ek;           // [nlev] level energies E hc/k [K]
+  const double* lng;          // [nlev] ln statistical weight
+  const LteLine* lines;       // [nl]
+  const double* dust;         // [ncell][nl][3]: sum rho_d kappa_abs(nu0), scattering source, extinction
+  double* lnQ;                // [ncell] ln partition sum (work)
+  double* Emean;              // [ncell] mean level energy / kT (work)
+  T* tab;                     // [ncell][nl][4] walk table
+  T* nsum;                    // [ncell][nl] N_up + N_low
+  double* dtab;               // [ncell][nl][5]: d tab[0..2] / d lnT, tab[0], tab[1] (FP64)
+};
+
+template <typename T>
+struct AdjParams {
+  WalkParams<T> W;            // the forward walk of this job (node records, tables, window data)
+  const double* gflux;        // [nl][nfr] dL/dF_nu (F_nu at 1 pc)
+  const double* ri;           // [nrr+2] ring edges
+  int nphi, nrr;
+  double* g_tab;              // [ncell][nl][4] dL/d(walk table), accumulated
+  double* g_b;                // [ncell] dL/d(cell line width), accumulated
+};
+
+template <typename T>
+struct AdjJobs {
+  const AdjParams<T>* jobs;   // [njobs] (device)
+  const int* item_prefix;     // [njobs+1]; a job has nlines x nrays items (line-major)
+  int njobs, total, max_nfr;
+  T* ckpt;                    // per-warp checkpoint scratch, ckpt_warp values each
+  long long ckpt_warp;
+  int* work;
+  unsigned long long* counters;   // [0] adjoint steps, [1] items whose continuum was zero
+};
+
 }  // namespace rl

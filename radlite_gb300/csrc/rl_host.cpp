@@ -133,22 +133,6 @@ double col(const std::string& line, size_t start, size_t width, int d) {
   return mant * std::pow(10.0, ex - d);
 }
 
-double bplanck(double temp, double nu) {   // setup.F:937-952
-  if (temp == 0.0) return 0.0;
-  return 1.47455e-47 * nu * nu * nu / (std::exp(4.7989e-11 * nu / temp) - 1.0) + 1.0e-290;
-}
-
-// bracketing by bisection: j with xx[j-1] < x <= xx[j] in 1-based terms
-int bracket(const std::vector<double>& xx, double x) {
-  const int n = (int)xx.size();
-  const bool asc = xx[n - 1] > xx[0];
-  int lo = 0, hi = n + 1;
-  while (hi - lo != 1) {
-    const int m = (hi + lo) / 2;
-    if ((x > xx[m - 1]) == asc) lo = m; else hi = m;
-  }
-  return lo;
-}
 
 void read_scalar(const std::string& dir, const std::string& name, const Model& m, std::vector<double>& out) {
   Records f(dir, name);
@@ -463,6 +447,23 @@ void read_star(const std::string& dir, Model& m) {
 }
 
 }  // namespace
+
+double bplanck(double temp, double nu) {   // setup.F:937-952
+  if (temp == 0.0) return 0.0;
+  return 1.47455e-47 * nu * nu * nu / (std::exp(4.7989e-11 * nu / temp) - 1.0) + 1.0e-290;
+}
+
+// bracketing by bisection: j with xx[j-1] < x <= xx[j] in 1-based terms
+int bracket(const std::vector<double>& xx, double x) {
+  const int n = (int)xx.size();
+  const bool asc = xx[n - 1] > xx[0];
+  int lo = 0, hi = n + 1;
+  while (hi - lo != 1) {
+    const int m = (hi + lo) / 2;
+    if ((x > xx[m - 1]) == asc) lo = m; else hi = m;
+  }
+  return lo;
+}
 
 void finish_model(Model& m) {
   m.aksmax = 0.0;

@@ -62,6 +62,8 @@ struct LinePrep {
 int load_dir(const std::string& dir, Model& m, std::string& err);
 int setup_camera(const Model& m, double incl_rad, int nphi, int dbdr, int nrext, Camera& cam, std::string& err);
 int prepare_line(const Model& m, int iline, bool scaled, LinePrep& lp, std::string& err);
+double bplanck(double temp, double nu);                     // setup.F:937-952
+int bracket(const std::vector<double>& xx, double x);      // 1-based j with xx[j-1] < x <= xx[j]
 void finish_model(Model& m);   // derived quantities (aksmax, passband channel count)
 int write_spectrum_file(const std::string& path, const Model& m, const Camera& cam,
                         const std::vector<int>& lines, const std::vector<double>& flux, std::string& err);

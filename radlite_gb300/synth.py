@@ -383,6 +383,32 @@ def model_arrays(cfg: DiskConfig) -> dict:
     return f
 
 
+def cell_order(a):
+    """[nt, nr] field -> the library's cell order (ir-1)*nth + (it-1)."""
+    return np.asarray(a).T.ravel()
+
+
+def cell_params(cfg: DiskConfig):
+    """Per-cell parameters of the differentiable raytrace: ln T, ln abundance, width [km/s]."""
+    f = make_fields(cfg)
+    return (np.log(cell_order(f["temp"])), np.log(cell_order(f["abund"])), cell_order(f["width"]))
+
+
+def lte_arrays(cfg: DiskConfig) -> dict:
+    """model_arrays() with the level populations recomputed in LTE from the energies as the
+    molecule file stores them (F12.4 cm^-1), i.e. the populations the differentiable
+    raytrace derives from the temperature."""
+    f = model_arrays(cfg)
+    E = np.round(f["E"], 4)
+    ex = -np.multiply.outer(E * HC_K, 1.0 / f["temp"])
+    lg = np.log(f["g"])[:, None, None]
+    m = (lg + ex).max(axis=0, keepdims=True)
+    w = np.exp(lg + ex - m)
+    f["pop"] = w / w.sum(axis=0, keepdims=True)
+    f["pop"][f["pop"] < 1e-99] = 0.0
+    return f
+
+
 if __name__ == "__main__":
     import argparse
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
