@@ -366,14 +366,14 @@ def batched_case(ctx, n_models, steps, tune_stride=32):
     return res
 
 
-def adjoint_case(ctx, name="adjoint_disk", reps=3):
+def adjoint_case(ctx, name="adjoint_disk", reps=3, **over):
     """Forward and forward+adjoint of the differentiable raytrace (per-cell ln T, ln X,
     width) on one model, FP32; timed with the library's CUDA events."""
     import numpy as np
     import torch
     import radlite_gb300 as rl
     from radlite_gb300 import synth
-    cfg = synth.config_by_name(name)
+    cfg = synth.config_by_name(name, **over)
     m = ctx.load_arrays(synth.lte_arrays(cfg), camera(cfg, cfg.incl_deg))
     lnT, lnX, b = (torch.tensor(a, dtype=torch.float64, device="cuda") for a in synth.cell_params(cfg))
     d = rl.Diff(m, cfg.ilinestart, cfg.nlines, precision=0)
@@ -427,11 +427,13 @@ def main():
                     help="models of the uneven batched comparison (0 skips it)")
     ap.add_argument("--only-batch", action="store_true", help="run only the batched comparison")
     ap.add_argument("--only-adjoint", action="store_true", help="run only the forward+adjoint timing")
+    ap.add_argument("--nphi", type=int, default=0, help="azimuths of the adjoint timing (0: the workload's)")
     args = ap.parse_args()
     if args.only_adjoint:
         import radlite_gb300 as rl
         ctx = rl.Context(0)
-        print(json.dumps(adjoint_case(ctx)), flush=True)
+        over = {"nphi": args.nphi} if args.nphi else {}
+        print(json.dumps(adjoint_case(ctx, **over)), flush=True)
         ctx.close()
         return 0
     if args.only_batch:

@@ -175,6 +175,10 @@ typedef struct rl_diff rl_diff;
 int rl_diff_create(rl_model* model, int iline0, int nlines, int precision, rl_diff** diff);
 int rl_diff_destroy(rl_diff* diff);
 int rl_diff_info(rl_diff* diff, int* ncell, int* nlines, int* nfr, int* nrays);
+/* Adjoint checkpoints along each ray: every 32 nodes (the chunk is walked again in the
+   reverse sweep; per-warp scratch of 32 values a chunk) or every node (1, the default:
+   each intensity is kept, 32 values a node per resident warp, about 0.1-0.4 GB). */
+int rl_diff_set_checkpoint(rl_diff* diff, int every);
 /* flux [nlines][nfr]: F_nu at 1 pc for the parameters lnT, lnX, width [ncell]. */
 int rl_diff_forward(rl_diff* diff, const double* lnT, const double* lnX, const double* width, double* flux,
                     rl_stats* stats);

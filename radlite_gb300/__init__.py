@@ -74,7 +74,8 @@ EXPORTS = ["rl_create", "rl_destroy", "rl_last_error", "rl_load_dir", "rl_load_a
            "rl_batch_create", "rl_batch_destroy", "rl_batch_add", "rl_batch_set_memory", "rl_batch_set_tiles",
            "rl_batch_get_tiles", "rl_batch_autotune", "rl_batch_use_graph", "rl_batch_flux_size",
            "rl_batch_job_info", "rl_batch_run", "rl_batch_waves", "rl_run_manifest",
-           "rl_diff_create", "rl_diff_destroy", "rl_diff_info", "rl_diff_forward", "rl_diff_backward",
+           "rl_diff_create", "rl_diff_destroy", "rl_diff_info", "rl_diff_set_checkpoint", "rl_diff_forward",
+           "rl_diff_backward",
            "rl_image_to_spectrum_noalloc"]
 
 _lib = None
@@ -119,6 +120,7 @@ def lib():
         L.rl_diff_create.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.POINTER(vp)]
         L.rl_diff_destroy.argtypes = [vp]
         L.rl_diff_info.argtypes = [vp, _I, _I, _I, _I]
+        L.rl_diff_set_checkpoint.argtypes = [vp, C.c_int]
         L.rl_diff_forward.argtypes = [vp, vp, vp, vp, vp, C.POINTER(Stats)]
         L.rl_diff_backward.argtypes = [vp, vp, vp, vp, vp, C.POINTER(Stats)]
         L.rl_image_to_spectrum_noalloc.argtypes = [vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
@@ -365,6 +367,10 @@ class Diff:
         _check(lib().rl_diff_info(self.h, C.byref(nc), C.byref(nl), C.byref(nf), C.byref(nr)))
         self.ncell, self.nlines, self.nfr, self.nrays = nc.value, nl.value, nf.value, nr.value
         self.version = 0
+
+    def set_checkpoint(self, every: int):
+        """Adjoint checkpoint interval along each ray: 1 (every node) or 32 nodes."""
+        _check(lib().rl_diff_set_checkpoint(self.h, every), self.model._ch)
 
     def close(self):
         if self.h:

@@ -15,9 +15,9 @@
 //        each segment in shared memory, SUBGRID sub-steps again in registers) and
 //        propagates dL/dI backwards through the linear-source step (transfer.F:1498-1571,
 //        line.F:4515-4848). Per node, the gradients with respect to the interpolated
-//        line values and the line width are summed over the warp and scattered to the
-//        cell corners with FP64 atomics.
-//   k_lte_backward dL/d(walk table) -> dL/d ln T, dL/d ln X per cell.
+//        line values and the line width are summed over the warp, folded with the
+//        tables' temperature and abundance derivatives and scattered to the cell corners
+//        as dL/d ln T, dL/d ln X, dL/d width with FP64 atomics.
 //
 // The recomputed forward uses the forward walk's own routines (rl_walk_common.cuh).
 // Discrete decisions (velocity window, SUBGRID switch, sub-step index range, the
@@ -95,22 +95,6 @@ __global__ void k_lte_lines(LteParams<R> P) {
   dt[4] = t1;
 }
 
-// dL/d ln T and dL/d ln X per cell from dL/d(walk table); dL/db passes through.
-__global__ void k_lte_backward(int ncell, int nl, const double* __restrict__ g_tab, const double* __restrict__ dtab,
-                               double* __restrict__ g_lnT, double* __restrict__ g_lnX) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= ncell) return;
-  double gT = 0.0, gX = 0.0;
-  for (int l = 0; l < nl; l++) {
-    const double* g = g_tab + ((size_t)c * nl + l) * 4;
-    const double* d = dtab + ((size_t)c * nl + l) * 5;
-    gT += g[0] * d[0] + g[1] * d[1] + g[2] * d[2];
-    gX += g[0] * d[3] + g[1] * d[4];
-  }
-  g_lnT[c] = gT;
-  g_lnX[c] = gX;
-}
-
 // Node line widths from cell widths, with the weights the geometry stored (the same
 // bilinear form as the geometry's own interpolation).
 template <typename T>
@@ -128,7 +112,7 @@ __global__ void k_node_lw(NodeBuf<T> nb, const double* __restrict__ b, int nth) 
 // ------------------------------------------------------------------------------------
 // adjoint walk
 // ------------------------------------------------------------------------------------
-constexpr int kAdjSlots = 2;     // slots per lane per tile: 64 (line, channel) pairs
+constexpr int kAdjSlots = 1;     // slots per lane per tile: 32 (line, channel) pairs
 
 template <typename T>
 struct AdjStage {
@@ -169,29 +153,41 @@ __device__ __forceinline__ void coeffs_d(T d, T x, T a, T b, T& dx, T& da, T& db
   }
 }
 
-// Gradient of one point value P = (j, a, S) built by point_state from the line values v
-// and the profile phi = rl e^{-u^2}, u = (w - vl) rl. Adds dL/d(jd, ad, jf, af) scaled by
-// wgt to acc, and returns dL/d rl and dL/d vl through the profile.
+// One evaluated point: the line values v at velocity vl with profile width rl, as
+// profile() and point_state() form them (phi = rl e^{-u^2}, u = (w - vl) rl;
+// j = jd + jf phi, a = ad + af phi, S = j / a if a > 0), plus what the gradient reuses.
 template <typename T>
-__device__ __forceinline__ void point_back(const LineVals<T>& v, T w, T vl, T rl, T gj, T ga, T gS, T wgt, T* acc,
-                                           T& g_rl, T& g_vl) {
-  const T u = (w - vl) * rl;
-  const T E = Math<T>::expneg(u * u);
-  const T phi = rl * E;
-  const T a = v.ad + v.af * phi;
-  if (a > (T)0) {
-    const T j = v.jd + v.jf * phi;
-    const T ra = Math<T>::rcp(a);
-    gj += gS * ra;
-    ga -= gS * (j * ra) * ra;
+struct PV { LineVals<T> v; T vl, u, E, phi, j, a, S, ra; };
+
+template <typename T>
+__device__ __forceinline__ PV<T> pv_eval(const LineVals<T>& v, T w, T vl, T rl) {
+  PV<T> p;
+  p.v = v; p.vl = vl;
+  p.u = (w - vl) * rl;
+  p.E = Math<T>::expneg(p.u * p.u);
+  p.phi = rl * p.E;
+  p.j = v.jd + v.jf * p.phi;
+  p.a = v.ad + v.af * p.phi;
+  p.ra = p.a > (T)0 ? Math<T>::rcp(p.a) : (T)0;
+  p.S = p.a > (T)0 ? p.j * p.ra : (T)0;
+  return p;
+}
+
+// Gradient through one evaluated point: dL/d(j, a, S) -> adds dL/d(jd, ad, jf, af) to acc
+// and dL/d rl, dL/d vl through the profile.
+template <typename T>
+__device__ __forceinline__ void point_back(const PV<T>& p, T rl, T gj, T ga, T gS, T* acc, T& g_rl, T& g_vl) {
+  if (p.a > (T)0) {
+    gj += gS * p.ra;
+    ga -= gS * p.S * p.ra;
   }
-  acc[0] += wgt * gj;
-  acc[1] += wgt * ga;
-  acc[2] += wgt * gj * phi;
-  acc[3] += wgt * ga * phi;
-  const T gphi = gj * v.jf + ga * v.af;
-  g_rl += gphi * E * ((T)1 - (T)2 * u * u);
-  g_vl += gphi * (T)2 * u * rl * rl * E;
+  acc[0] += gj;
+  acc[1] += ga;
+  acc[2] += gj * p.phi;
+  acc[3] += ga * p.phi;
+  const T gphi = gj * p.v.jf + ga * p.v.af;
+  g_rl += gphi * p.E * ((T)1 - (T)2 * p.u * p.u);
+  g_vl += gphi * (T)2 * p.u * rl * rl * p.E;
 }
 
 // One linear-source step backwards. In: the step's end values and the intensity before
@@ -233,9 +229,8 @@ __device__ __forceinline__ StepGrad<T> step_back(T Iprev, T& lam, T j0, T a0, T 
 // Point values (j, a, S) of line values v at velocity vl with profile width rl.
 template <typename T>
 __device__ __forceinline__ void point_vals(const LineVals<T>& v, T w, T vl, T rl, T& j, T& a, T& S) {
-  const T ph = profile(w, vl, rl, rl);
-  const Pt<T> p = {v.jd, v.ad, v.jf, v.af, vl};
-  point_state(p, ph, j, a, S);
+  const PV<T> p = pv_eval(v, w, vl, rl);
+  j = p.j; a = p.a; S = p.S;
 }
 
 template <typename T>
@@ -255,11 +250,18 @@ __device__ __forceinline__ LineVals<T> lerp_lv(const LineVals<T>& v0, const Line
 // acc1 (node g); returns dL/d rl of the segment; (cgj, cga) carry dL/d(j, a) of the end
 // point in, and of the incoming point state out when it was carried (no reset).
 template <typename T>
-__device__ __noinline__ T seg_back_slow(bool init, int kind, T w, LineVals<T> v0, LineVals<T> v1, T vl0, T vl1, T rl,
-                                         T rl0, T hds, T q, T dsf, T dvs, T ids, T idvs, T hw3s, T lgs, T ilgs, T Iin,
-                                         T& lam, T& cgj, T& cga, T* acc0, T* acc1) {
-  T j0, a0, S0;
-  point_vals(v0, w, vl0, init ? rl : rl0, j0, a0, S0);
+struct SlowOut {
+  T lam, cgj, cga, g_rl;
+  T acc0[4], acc1[4];
+};
+
+template <typename T>
+__device__ __noinline__ SlowOut<T> seg_back_slow(bool init, int kind, T w, LineVals<T> v0, LineVals<T> v1, T vl0,
+                                                  T vl1, T rl, T rl0, T hds, T q, T dsf, T dvs, T ids, T idvs, T hw3s,
+                                                  T lgs, T ilgs, T Iin, T lam, T cgj, T cga) {
+  T acc0[4] = {0, 0, 0, 0}, acc1[4] = {0, 0, 0, 0};
+  const PV<T> p0 = pv_eval(v0, w, vl0, init ? rl : rl0);   // incoming state
+  const T j0 = p0.j, a0 = p0.a, S0 = p0.S;
   int ia = 1, ib = 0;
   T sleft = 0, lg = 0, ilg = 0;
   if (kind == 1) {
@@ -328,32 +330,36 @@ __device__ __noinline__ T seg_back_slow(bool init, int kind, T w, LineVals<T> v0
   }
   T g_rl = 0;
   T gj_next = cgj, ga_next = cga, gS_next = 0, gs_next = 0;
+  // point m (the end of sub-step m), carried to the next iteration as its end point
+  PV<T> pe;
+  T e = (T)1;
+  {
+    const int i = ia + npt - 1;
+    if (i <= ib) {
+      e = ssub[npt - 1] * ids;
+      pe = pv_eval(lerp_lv(v0, v1, e), w, ((T)1 - e) * vl0 + e * vl1, rl);
+    } else {
+      pe = pv_eval(v1, w, vl1, rl);
+    }
+  }
   for (int m = npt - 1; m >= 0; m--) {
     const int i = ia + m;
     const bool interior = i <= ib;
     const T s = ssub[m];
     const T sp = m > 0 ? ssub[m - 1] : (T)0;
-    LineVals<T> pv = v1;
-    T pvl = vl1, e = (T)1;
-    if (interior) {
-      e = s * ids;
-      pv = lerp_lv(v0, v1, e);
-      pvl = ((T)1 - e) * vl0 + e * vl1;
-    }
-    T j1, a1, S1;
-    point_vals(pv, w, pvl, rl, j1, a1, S1);
-    T jp, ap, Sp;
+    PV<T> ps;
+    T es = (T)0;
     if (m > 0) {
-      const T eq = sp * ids;
-      point_vals(lerp_lv(v0, v1, eq), w, ((T)1 - eq) * vl0 + eq * vl1, rl, jp, ap, Sp);
+      es = sp * ids;
+      ps = pv_eval(lerp_lv(v0, v1, es), w, ((T)1 - es) * vl0 + es * vl1, rl);
     } else {
-      jp = j0; ap = a0; Sp = S0;
+      ps = p0;
     }
     const T h = halves ? (T)0.5 * (s - sp) : hds;
-    const StepGrad<T> g = step_back<T>(Isub[m], lam, jp, ap, Sp, j1, a1, S1, h);
-    T acc[5] = {0, 0, 0, 0, 0};
+    const StepGrad<T> g = step_back<T>(Isub[m], lam, ps.j, ps.a, ps.S, pe.j, pe.a, pe.S, h);
+    T acc[4] = {0, 0, 0, 0};
     T gv = 0;
-    point_back<T>(pv, w, pvl, rl, g.j1 + gj_next, g.a1 + ga_next, g.S1 + gS_next, (T)1, acc, g_rl, gv);
+    point_back<T>(pe, rl, g.j1 + gj_next, g.a1 + ga_next, g.S1 + gS_next, acc, g_rl, gv);
     if (interior) {
       for (int k = 0; k < 4; k++) { acc0[k] += ((T)1 - e) * acc[k]; acc1[k] += e * acc[k]; }
       T ge = gs_next + (T)0.5 * g.h;
@@ -366,21 +372,25 @@ __device__ __noinline__ T seg_back_slow(bool init, int kind, T w, LineVals<T> v0
     }
     gs_next = -(T)0.5 * g.h;
     gj_next = g.j0; ga_next = g.a0; gS_next = g.S0;
+    pe = ps;
+    e = es;
   }
   if (init) {
     T gv = 0;
-    point_back<T>(v0, w, vl0, rl, gj_next, ga_next, gS_next, (T)1, acc0, g_rl, gv);
+    point_back<T>(p0, rl, gj_next, ga_next, gS_next, acc0, g_rl, gv);
     cgj = 0; cga = 0;
   } else {
     T gj = gj_next, ga = ga_next;
-    if (a0 > (T)0) {
-      const T ra = Math<T>::rcp(a0);
-      gj += gS_next * ra;
-      ga -= gS_next * (j0 * ra) * ra;
+    if (p0.a > (T)0) {
+      gj += gS_next * p0.ra;
+      ga -= gS_next * p0.S * p0.ra;
     }
     cgj = gj; cga = ga;
   }
-  return g_rl;
+  SlowOut<T> o;
+  o.lam = lam; o.cgj = cgj; o.cga = cga; o.g_rl = g_rl;
+  for (int k = 0; k < 4; k++) { o.acc0[k] = acc0[k]; o.acc1[k] = acc1[k]; }
+  return o;
 }
 
 // Stage nodes kb-1 .. kb+31 of a ray for line l (entries 0..32), as walk_ray stages them.
@@ -471,6 +481,38 @@ __device__ __forceinline__ void seg_fwd(const AdjStage<T>& S, int n, T w, T& I, 
   }
 }
 
+// Sum five per-lane values over the warp with a reduce-scatter (9 shuffles instead of
+// 25): afterwards the lanes with (lane & 3) == 0 hold the total of value
+// ((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1).
+template <typename T>
+__device__ __forceinline__ T warp_sum5(const T* v, int lane) {
+  const bool b4 = lane & 16, b3 = lane & 8, b2 = lane & 4;
+  T a[4];
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const T hi = i + 4 < 5 ? v[i + 4] : (T)0;
+    const T send = b4 ? v[i] : hi;
+    const T keep = b4 ? hi : v[i];
+    a[i] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+  }
+  T c[2];
+#pragma unroll
+  for (int i = 0; i < 2; i++) {
+    const T send = b3 ? a[i] : a[i + 2];
+    const T keep = b3 ? a[i + 2] : a[i];
+    c[i] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+  }
+  T d;
+  {
+    const T send = b2 ? c[0] : c[1];
+    const T keep = b2 ? c[1] : c[0];
+    d = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+  }
+  d += __shfl_xor_sync(0xffffffffu, d, 2);
+  d += __shfl_xor_sync(0xffffffffu, d, 1);
+  return d;
+}
+
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll
@@ -479,30 +521,29 @@ __device__ __forceinline__ T warp_sum(T v) {
 }
 
 // Scatter the per-node gradients of staged entries t0..t1 to the cell corners.
+// Scatter the per-node gradients of staged entries t0..t1 to the cell corners, folded
+// into the cell parameters on the way: with the table derivatives dtab of each corner,
+// dL/d ln T += w (g_jf dtab0 + g_af dtab1 + g_jd dtab2), dL/d ln X += w (g_jf tab0 +
+// g_af tab1), dL/d width += w g_lw (the width enters through the node width only).
 template <typename T>
 __device__ __forceinline__ void adj_scatter(const AdjParams<T>& A, AdjStage<T>& S, int l, int t0, int t1, int lane) {
   for (int t = t0 + lane; t <= t1; t += 32) {
     const T* g = S.gacc[t];
-    if (g[0] == (T)0 && g[1] == (T)0 && g[2] == (T)0 && g[3] == (T)0 && g[4] == (T)0) continue;
+    if (g[0] == (T)0 && g[2] == (T)0 && g[3] == (T)0 && g[4] == (T)0) continue;
     const Corners c = corners(S.c00[t], S.misc[t], A.W.nth);
     const double wr = (double)S.wr[t], wt = (double)S.wt[t];
     const double ar = 1.0 - wr, at = 1.0 - wt;
     const int cs[4] = {c.c00, c.c01, c.c10, c.c11};
     const double ws[4] = {ar * at, ar * wt, wr * at, wr * wt};
-    const bool live[4] = {true, wt != 0.0, wr != 0.0, wr != 0.0 && wt != 0.0};
+    const double gjd = (double)g[0], gjf = (double)g[2], gaf = (double)g[3], glw = (double)g[4];
     for (int q = 0; q < 4; q++) {
-      if (!live[q] || ws[q] == 0.0) continue;
-      double* gt = A.g_tab + ((size_t)cs[q] * A.W.nlines + l) * 4;
-      // table order: {jf, af, jd, ad}; gacc order: {jd, ad, jf, af, lw}
-      if (g[2] != (T)0) atomicAdd(gt + 0, ws[q] * (double)g[2]);
-      if (g[3] != (T)0) atomicAdd(gt + 1, ws[q] * (double)g[3]);
-      if (g[0] != (T)0) atomicAdd(gt + 2, ws[q] * (double)g[0]);
-      if (g[1] != (T)0) atomicAdd(gt + 3, ws[q] * (double)g[1]);
-    }
-    if (g[4] != (T)0) {
-      // node width = bilinear form of all four corners (k_node_lw)
-      for (int q = 0; q < 4; q++)
-        if (ws[q] != 0.0) atomicAdd(A.g_b + cs[q], ws[q] * (double)g[4]);
+      if (ws[q] == 0.0) continue;
+      const double* d = A.dtab + ((size_t)cs[q] * A.W.nlines + l) * 5;
+      const double gT = gjf * __ldg(d + 0) + gaf * __ldg(d + 1) + gjd * __ldg(d + 2);
+      const double gX = gjf * __ldg(d + 3) + gaf * __ldg(d + 4);
+      if (gT != 0.0) atomicAdd(A.g_lnT + cs[q], ws[q] * gT);
+      if (gX != 0.0) atomicAdd(A.g_lnX + cs[q], ws[q] * gX);
+      if (glw != 0.0) atomicAdd(A.g_b + cs[q], ws[q] * glw);   // node width: bilinear in all corners
     }
   }
   __syncwarp();
@@ -510,7 +551,7 @@ __device__ __forceinline__ void adj_scatter(const AdjParams<T>& A, AdjStage<T>& 
 
 template <typename T>
 __device__ void adjoint_item(const AdjParams<T>& A, int item, AdjStage<T>& S, AdjSlots<T>& SL, unsigned short* list,
-                             T* ck, long long ckcap, int lane, unsigned long long& steps,
+                             T* ck, long long ckcap, int every, int lane, unsigned long long& steps,
                              unsigned long long& zero_cont) {
   const WalkParams<T>& P = A.W;
   const NodeBuf<T>& nb = P.nb;
@@ -590,7 +631,7 @@ __device__ void adjoint_item(const AdjParams<T>& A, int item, AdjStage<T>& S, Ad
   const T fstar = P.fstar;
   for (int tb = 0; tb < nint; tb += 32 * kAdjSlots) {
     const int nt = min(32 * kAdjSlots, nint - tb);
-    if ((long long)nchunk * 32 * kAdjSlots > ckcap) {   // the scratch is sized for kmax
+    if ((long long)nchunk * 32 * (every == 1 ? 32 : kAdjSlots) > ckcap) {   // the scratch is sized for kmax
       if (lane == 0) atomicCAS(P.err, 0, 90);
       return;
     }
@@ -608,8 +649,10 @@ __device__ void adjoint_item(const AdjParams<T>& A, int item, AdjStage<T>& S, Ad
     for (int cix = 0; cix < nchunk; cix++) {
       const int kb = cix * 32;
       adj_stage(P, S, row, kb, K, l, star_node, lane);
+      if (every != 1) {
 #pragma unroll
-      for (int u = 0; u < kAdjSlots; u++) ck[(size_t)cix * 32 * kAdjSlots + u * 32 + lane] = I[u];
+        for (int u = 0; u < kAdjSlots; u++) ck[(size_t)cix * 32 * kAdjSlots + u * 32 + lane] = I[u];
+      }
       const int nn = min(32, K - kb);
       const int n0 = kb == 0 ? 1 : 0;
       for (int n = n0; n < nn; n++) {
@@ -617,6 +660,7 @@ __device__ void adjoint_item(const AdjParams<T>& A, int item, AdjStage<T>& S, Ad
         for (int u = 0; u < kAdjSlots; u++) {
           if (ch[u] < 0) continue;
           if (kb + n == star_node) I[u] = ((T)1 - fstar) * I[u] + fstar * P.star[(size_t)l * P.nfr + ch[u]];
+          if (every == 1) ck[((size_t)cix * 32 + n) * 32 + lane] = I[u];   // intensity entering the segment
           seg_fwd<T>(S, n, w[u], I[u], j0[u], a0[u], S0[u], steps);
         }
       }
@@ -644,9 +688,10 @@ __device__ void adjoint_item(const AdjParams<T>& A, int item, AdjStage<T>& S, Ad
         for (int k = 0; k < 5; k++) S.gacc[t][k] = 0;
       const int nn = min(32, K - kb);
       const int n0 = kb == 0 ? 1 : 0;
-      // recompute the chunk from its checkpoint
+      // recompute the chunk from its checkpoint (interval 32), or read the stored
+      // intensities back (interval 1)
 #pragma unroll
-      for (int u = 0; u < kAdjSlots; u++) {
+      for (int u = 0; u < kAdjSlots && every != 1; u++) {
         T Iu = ck[(size_t)cix * 32 * kAdjSlots + u * 32 + lane];
         T sj = 0, sa = 0, sS = 0;
         if (ch[u] >= 0 && kb > 0) point_vals(S.lv[0], w[u], S.vl[0], S.rlw[0], sj, sa, sS);
@@ -672,7 +717,7 @@ __device__ void adjoint_item(const AdjParams<T>& A, int item, AdjStage<T>& S, Ad
 #pragma unroll
         for (int u = 0; u < kAdjSlots; u++) {
           if (ch[u] < 0) continue;
-          const T Ip = SL.Ibuf[n][u][lane];
+          const T Ip = every == 1 ? ck[((size_t)cix * 32 + n) * 32 + lane] : SL.Ibuf[n][u][lane];
           const bool init = (fl & kFlagInit) != 0;
           bool ov = false;
           T hw3 = S.hw3[n + 1], lgs = S.lg[n + 1], ilgs = S.ilg[n + 1];
@@ -683,27 +728,26 @@ __device__ void adjoint_item(const AdjParams<T>& A, int item, AdjStage<T>& S, Ad
           }
           if (init || ov) {
             // refined or resetting segment
-            T gj = cgj[u], ga = cga[u];
             const int kind = init ? ((fl & kFlagSub) ? 2 : 0) : 1;
-            const T grl = seg_back_slow<T>(init, kind, w[u], v0, v1, vl0, vl1, rl, rl0, hds, S.q[n + 1], S.ds[n + 1],
-                                           S.dvs[n + 1], S.ids[n + 1], S.idvs[n + 1], hw3, lgs, ilgs, Ip, lam[u], gj,
-                                           ga, acc0, acc1);
-            grl_seg += grl;
-            cgj[u] = gj; cga[u] = ga;
+            const SlowOut<T> o = seg_back_slow<T>(init, kind, w[u], v0, v1, vl0, vl1, rl, rl0, hds, S.q[n + 1],
+                                                  S.ds[n + 1], S.dvs[n + 1], S.ids[n + 1], S.idvs[n + 1], hw3, lgs,
+                                                  ilgs, Ip, lam[u], cgj[u], cga[u]);
+            grl_seg += o.g_rl;
+            lam[u] = o.lam; cgj[u] = o.cgj; cga[u] = o.cga;
+#pragma unroll
+            for (int k = 0; k < 4; k++) { acc0[k] += o.acc0[k]; acc1[k] += o.acc1[k]; }
           } else {
             // regular step
-            T j0p, a0p, S0p, j1, a1, S1;
-            point_vals(v0, w[u], vl0, rl0, j0p, a0p, S0p);
-            point_vals(v1, w[u], vl1, rl, j1, a1, S1);
-            const StepGrad<T> g = step_back<T>(Ip, lam[u], j0p, a0p, S0p, j1, a1, S1, hds);
+            const PV<T> q0 = pv_eval(v0, w[u], vl0, rl0);
+            const PV<T> q1 = pv_eval(v1, w[u], vl1, rl);
+            const StepGrad<T> g = step_back<T>(Ip, lam[u], q0.j, q0.a, q0.S, q1.j, q1.a, q1.S, hds);
             T gv = 0;
-            point_back<T>(v1, w[u], vl1, rl, g.j1 + cgj[u], g.a1 + cga[u], g.S1, (T)1, acc1, grl_seg, gv);
+            point_back<T>(q1, rl, g.j1 + cgj[u], g.a1 + cga[u], g.S1, acc1, grl_seg, gv);
             // carried start state: dL/dS folded into (j, a)
             T gj = g.j0, ga = g.a0;
-            if (a0p > (T)0) {
-              const T ra = Math<T>::rcp(a0p);
-              gj += g.S0 * ra;
-              ga -= g.S0 * (j0p * ra) * ra;
+            if (q0.a > (T)0) {
+              gj += g.S0 * q0.ra;
+              ga -= g.S0 * q0.S * q0.ra;
             }
             cgj[u] = gj; cga[u] = ga;
           }
@@ -715,19 +759,22 @@ __device__ void adjoint_item(const AdjParams<T>& A, int item, AdjStage<T>& S, Ad
         acc0[4] += glw;
         acc1[4] += glw;
         // node kb+n is complete for this chunk: sum over the warp
+        {
+          const T s = warp_sum5(acc1, lane);
+          const int idx = ((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1);
+          if ((lane & 3) == 0 && idx < 5) S.gacc[n + 1][idx] += s;
+        }
 #pragma unroll
         for (int k = 0; k < 5; k++) {
-          const T s = warp_sum(acc1[k]);
-          if (lane == 0) S.gacc[n + 1][k] += s;
           acc1[k] = acc0[k];
           acc0[k] = 0;
         }
       }
       // what is left belongs to node kb+n0-1 (entry n0)
-#pragma unroll
-      for (int k = 0; k < 5; k++) {
-        const T s = warp_sum(acc1[k]);
-        if (lane == 0) S.gacc[n0][k] += s;
+      {
+        const T s = warp_sum5(acc1, lane);
+        const int idx = ((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1);
+        if ((lane & 3) == 0 && idx < 5) S.gacc[n0][idx] += s;
       }
       __syncwarp();
       adj_scatter<T>(A, S, l, kb == 0 ? 1 : 0, nn, lane);
@@ -763,8 +810,8 @@ __global__ void __launch_bounds__(128) k_adjoint_jobs(AdjJobs<T> B) {
       __syncwarp();
       cur = j;
     }
-    adjoint_item<T>(jp[wib], item - __ldg(&B.item_prefix[j]), stages[wib], slots[wib], list, ck, B.ckpt_warp, lane,
-                    steps, zc);
+    adjoint_item<T>(jp[wib], item - __ldg(&B.item_prefix[j]), stages[wib], slots[wib], list, ck, B.ckpt_warp, B.every,
+                    lane, steps, zc);
   }
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
@@ -801,12 +848,6 @@ cudaError_t launch_node_lw(const NodeBuf<T>& nb, const double* b, int nth, cudaS
   return cudaGetLastError();
 }
 
-cudaError_t launch_lte_backward(int ncell, int nl, const double* g_tab, const double* dtab, double* g_lnT,
-                                double* g_lnX, cudaStream_t s) {
-  k_lte_backward<<<(ncell + 127) / 128, 128, 0, s>>>(ncell, nl, g_tab, dtab, g_lnT, g_lnX);
-  return cudaGetLastError();
-}
-
 template <typename T>
 size_t adjoint_smem(int max_nfr) {
   const int warps = 4;
@@ -828,8 +869,8 @@ cudaError_t adjoint_grid(int nsm, int max_nfr, int* blocks) {
 }
 
 template <typename T>
-long long adjoint_ckpt_per_warp(int kmax) {
-  return (long long)((kmax + 31) / 32) * 32 * kAdjSlots;
+long long adjoint_ckpt_per_warp(int kmax, int every) {
+  return (long long)((kmax + 31) / 32) * 32 * (every == 1 ? 32 : kAdjSlots);
 }
 
 template <typename T>
@@ -847,8 +888,8 @@ template cudaError_t launch_node_lw<float>(const NodeBuf<float>&, const double*,
 template cudaError_t launch_node_lw<double>(const NodeBuf<double>&, const double*, int, cudaStream_t);
 template cudaError_t adjoint_grid<float>(int, int, int*);
 template cudaError_t adjoint_grid<double>(int, int, int*);
-template long long adjoint_ckpt_per_warp<float>(int);
-template long long adjoint_ckpt_per_warp<double>(int);
+template long long adjoint_ckpt_per_warp<float>(int, int);
+template long long adjoint_ckpt_per_warp<double>(int, int);
 template cudaError_t launch_adjoint<float>(const AdjJobs<float>&, int, cudaStream_t);
 template cudaError_t launch_adjoint<double>(const AdjJobs<double>&, int, cudaStream_t);
 

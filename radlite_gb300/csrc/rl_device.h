@@ -155,7 +155,9 @@ struct AdjParams {
   const double* gflux;        // [nl][nfr] dL/dF_nu (F_nu at 1 pc)
   const double* ri;           // [nrr+2] ring edges
   int nphi, nrr;
-  double* g_tab;              // [ncell][nl][4] dL/d(walk table), accumulated
+  const double* dtab;         // [ncell][nl][5] table derivatives of the LTE tables (LteParams::dtab)
+  double* g_lnT;              // [ncell] dL/d ln T, accumulated
+  double* g_lnX;              // [ncell] dL/d ln X, accumulated
   double* g_b;                // [ncell] dL/d(cell line width), accumulated
 };
 
@@ -166,6 +168,7 @@ struct AdjJobs {
   int njobs, total, max_nfr;
   T* ckpt;                    // per-warp checkpoint scratch, ckpt_warp values each
   long long ckpt_warp;
+  int every;                  // checkpoint interval in nodes: 1 (keep every intensity) or 32
   int* work;
   unsigned long long* counters;   // [0] adjoint steps, [1] items whose continuum was zero
 };

@@ -3,8 +3,8 @@
 //
 // Forward:  LTE tables on the device (k_lte_cells / k_lte_lines), node widths from the
 //           cell widths (k_node_lw), then the forward walk and reduction of the plain path.
-// Backward: the adjoint walk (k_adjoint_jobs) gives dL/d(walk table) and dL/d(width);
-//           k_lte_backward maps the tables to dL/d ln T and dL/d ln X.
+// Backward: the adjoint walk (k_adjoint_jobs) accumulates dL/d ln T, dL/d ln X and
+//           dL/d width per cell directly, through the tables' derivatives.
 // The reference has no differentiable path; its inputs are the level populations the
 // setup writes (pyradlite radlite.py:1106-1118 computes them in LTE, which is what the
 // table kernel does). What stays fixed from the loaded model: grid, velocities, densities,
@@ -29,12 +29,10 @@ template <typename T>
 cudaError_t launch_lte(const LteParams<T>& P, cudaStream_t s);
 template <typename T>
 cudaError_t launch_node_lw(const NodeBuf<T>& nb, const double* b, int nth, cudaStream_t s);
-cudaError_t launch_lte_backward(int ncell, int nl, const double* g_tab, const double* dtab, double* g_lnT,
-                                double* g_lnX, cudaStream_t s);
 template <typename T>
 cudaError_t adjoint_grid(int nsm, int max_nfr, int* blocks);
 template <typename T>
-long long adjoint_ckpt_per_warp(int kmax);
+long long adjoint_ckpt_per_warp(int kmax, int every);
 template <typename T>
 cudaError_t launch_adjoint(const AdjJobs<T>& B, int blocks, cudaStream_t s);
 }  // namespace rl
@@ -56,8 +54,9 @@ struct rl_diff {
   DevBuf tab, nsum, dtab, width;
   DevBuf img, ring, flux, cnt, work, err;
   // adjoint
-  DevBuf g_tab, g_b, ckpt, ajob, aprefix, acnt, awork;
+  DevBuf ckpt, ajob, aprefix, acnt, awork;
   bool have_forward = false;
+  int every = 1;   // adjoint checkpoint interval (nodes)
 };
 
 namespace {
@@ -211,8 +210,6 @@ int create(rl_diff* d) {
   CUDA_TRY(d->cnt.ensure(sizeof(unsigned long long) * 4));
   CUDA_TRY(d->work.ensure(sizeof(int)));
   CUDA_TRY(d->err.ensure(sizeof(int)));
-  CUDA_TRY(d->g_tab.ensure(sizeof(double) * (size_t)ncell * nl * 4));
-  CUDA_TRY(d->g_b.ensure(sizeof(double) * ncell));
   CUDA_TRY(d->acnt.ensure(sizeof(unsigned long long) * 4));
   CUDA_TRY(d->awork.ensure(sizeof(int)));
   CUDA_TRY(d->ajob.ensure(sizeof(AdjParams<T>)));
@@ -233,7 +230,7 @@ int create(rl_diff* d) {
   const int need = (d->gsize * d->nfr + 31) / 32;
   d->cpl = need <= 1 ? 1 : need <= 2 ? 2 : need <= 4 ? 4 : 8;
   CUDA_TRY(adjoint_grid<T>(ctx->nsm, d->nfr, &d->adj_blocks));
-  const long long per = adjoint_ckpt_per_warp<T>(d->kmax);
+  const long long per = adjoint_ckpt_per_warp<T>(d->kmax, d->every);
   CUDA_TRY(d->ckpt.ensure(sizeof(T) * (size_t)per * d->adj_blocks * 4));
   const int pre[2] = {0, nl * cam.nrays};
   CUDA_TRY(h2d(d->aprefix.p, pre, sizeof(pre), s));
@@ -298,26 +295,26 @@ int backward(rl_diff* d, const double* gflux, double* g_lnT, double* g_lnX, doub
   A.gflux = gflux;
   A.ri = d->ri.as<double>();
   A.nphi = d->cam.nphi; A.nrr = d->cam.nrr;
-  A.g_tab = d->g_tab.as<double>();
-  A.g_b = d->g_b.as<double>();
+  A.dtab = d->dtab.as<double>();
+  A.g_lnT = g_lnT; A.g_lnX = g_lnX; A.g_b = g_width;
   AdjJobs<T> B;
   B.jobs = d->ajob.as<AdjParams<T>>();
   B.item_prefix = d->aprefix.as<int>();
   B.njobs = 1; B.total = d->nl * d->cam.nrays; B.max_nfr = d->nfr;
   B.ckpt = d->ckpt.as<T>();
-  B.ckpt_warp = adjoint_ckpt_per_warp<T>(d->kmax);
+  B.ckpt_warp = adjoint_ckpt_per_warp<T>(d->kmax, d->every);
+  B.every = d->every;
   B.work = d->awork.as<int>();
   B.counters = d->acnt.as<unsigned long long>();
   CUDA_TRY(h2d(d->ajob.p, &A, sizeof A, s));
-  CUDA_TRY(cudaMemsetAsync(d->g_tab.p, 0, sizeof(double) * (size_t)d->ncell * d->nl * 4, s));
-  CUDA_TRY(cudaMemsetAsync(d->g_b.p, 0, sizeof(double) * d->ncell, s));
+  CUDA_TRY(cudaMemsetAsync(g_lnT, 0, sizeof(double) * d->ncell, s));
+  CUDA_TRY(cudaMemsetAsync(g_lnX, 0, sizeof(double) * d->ncell, s));
+  CUDA_TRY(cudaMemsetAsync(g_width, 0, sizeof(double) * d->ncell, s));
   CUDA_TRY(cudaMemsetAsync(d->acnt.p, 0, sizeof(unsigned long long) * 4, s));
   CUDA_TRY(cudaMemsetAsync(d->err.p, 0, sizeof(int), s));
   CUDA_TRY(cudaEventRecord(ctx->ev[0], s));
   CUDA_TRY(launch_adjoint<T>(B, d->adj_blocks, s));
   CUDA_TRY(cudaEventRecord(ctx->ev[1], s));
-  CUDA_TRY(launch_lte_backward(d->ncell, d->nl, d->g_tab.as<double>(), d->dtab.as<double>(), g_lnT, g_lnX, s));
-  CUDA_TRY(cudaMemcpyAsync(g_width, d->g_b.p, sizeof(double) * d->ncell, cudaMemcpyDeviceToDevice, s));
   CUDA_TRY(cudaEventRecord(ctx->ev[2], s));
   unsigned long long cnt[4] = {0, 0, 0, 0};
   int kerr = 0;
@@ -363,6 +360,19 @@ int rl_diff_destroy(rl_diff* d) {
   if (!d) return 0;
   if (d->ctx) cudaSetDevice(d->ctx->device);
   delete d;
+  return 0;
+}
+
+int rl_diff_set_checkpoint(rl_diff* d, int every) {
+  if (!d) return set_err(nullptr, RL_ERR_ARG, "rl_diff_set_checkpoint: null handle");
+  rl_ctx* ctx = d->ctx;
+  if (every != 1 && every != 32) return set_err(ctx, RL_ERR_ARG, "rl_diff_set_checkpoint: interval 1 or 32");
+  CUDA_TRY(cudaSetDevice(ctx->device));
+  d->every = every;
+  const long long per = d->precision == RL_FP64 ? adjoint_ckpt_per_warp<double>(d->kmax, every)
+                                                : adjoint_ckpt_per_warp<float>(d->kmax, every);
+  const size_t el = d->precision == RL_FP64 ? sizeof(double) : sizeof(float);
+  CUDA_TRY(d->ckpt.ensure(el * (size_t)per * d->adj_blocks * 4));
   return 0;
 }
 

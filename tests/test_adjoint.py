@@ -132,6 +132,21 @@ def test_fp32_adjoint_tracks_fp64(gpu_lib, ctx):
     m.free()
 
 
+def test_checkpoint_intervals_agree(gpu_lib, ctx):
+    cfg, m, lnT, lnX, b = _setup(gpu_lib, ctx)
+    out = []
+    for every in (1, 32):
+        d = gpu_lib.Diff(m, cfg.ilinestart, cfg.nlines, precision=1)
+        d.set_checkpoint(every)
+        target = d.forward(lnT + 0.05, lnX, b * 0.9)
+        flux = d.forward(lnT, lnX, b)
+        out.append([g.cpu().numpy() for g in d.backward(2.0 * (flux - target))])
+        d.close()
+    for a, r in zip(*out):
+        np.testing.assert_allclose(a, r, rtol=1e-12, atol=1e-12 * np.abs(r).max())
+    m.free()
+
+
 def test_autograd_function(gpu_lib, ctx):
     import torch
     cfg, m, lnT, lnX, b = _setup(gpu_lib, ctx)
