@@ -396,6 +396,24 @@ def adjoint_case(ctx, name="adjoint_disk", reps=3, **over):
     return res
 
 
+def fit_case(ctx, n_models=64, steps=5, plain_models=8):
+    """The batched forward+adjoint fitting step on n uneven models (radlite_gb300.fit)
+    against plain per-model forward + central finite differences in the four parameters,
+    timed on `plain_models` of the same models."""
+    from radlite_gb300 import fit
+    cfgs = fit.fit_configs(n_models)
+    res = fit.run_fit(ctx, cfgs, steps=steps)
+    plain = fit.plain_fd_step_seconds(ctx, cfgs[:plain_models])
+    per_spec = plain["seconds"] / plain["spectra"]
+    out = {"workload": f"{n_models} uneven disks (nr 100-400, ntheta 50-200), 20 lines x 200 channels, "
+                       f"{cfgs[0].nphi} azimuths, 4 parameters each",
+           "batched_forward_adjoint": res,
+           "plain_forward_fd": {"models_timed": plain_models, "seconds_per_gradient_spectrum": per_spec,
+                                "spectra_per_s": 1.0 / per_spec}}
+    out["speedup_vs_plain_fd"] = res["forward_adjoint_spectra_per_s"] * per_spec
+    return out
+
+
 def profile_case(args):
     """One pass of a named workload (geometry, walk, reduction), for profiler captures."""
     import radlite_gb300 as rl
@@ -428,7 +446,15 @@ def main():
     ap.add_argument("--only-batch", action="store_true", help="run only the batched comparison")
     ap.add_argument("--only-adjoint", action="store_true", help="run only the forward+adjoint timing")
     ap.add_argument("--nphi", type=int, default=0, help="azimuths of the adjoint timing (0: the workload's)")
+    ap.add_argument("--only-fit", action="store_true", help="run only the batched fitting-step comparison")
+    ap.add_argument("--fit-models", type=int, default=64)
     args = ap.parse_args()
+    if args.only_fit:
+        import radlite_gb300 as rl
+        ctx = rl.Context(0)
+        print(json.dumps(fit_case(ctx, args.fit_models, args.steps)), flush=True)
+        ctx.close()
+        return 0
     if args.only_adjoint:
         import radlite_gb300 as rl
         ctx = rl.Context(0)

@@ -188,6 +188,26 @@ int rl_diff_forward(rl_diff* diff, const double* lnT, const double* lnX, const d
 int rl_diff_backward(rl_diff* diff, const double* gflux, double* g_lnT, double* g_lnX, double* g_width,
                      rl_stats* stats);
 
+/* Many differentiable models rendered together: one forward launch sequence (LTE tables
+   and node widths per model, then one persistent walk over all models' items from a device
+   queue and one reduction) and one persistent adjoint launch, each captured once in a CUDA
+   graph and replayed. The batch owns concatenated device buffers (FP64): parameters
+   ln T, ln X, width [sum of ncell], spectra and their gradient [sum of nlines x nfr],
+   parameter gradients [sum of ncell]; rl_diff_batch_layout gives a model's offsets.
+   Fill the parameters (and gflux before a backward) in place, then call forward/backward;
+   the calls return after the work is done. All models share one precision. */
+typedef struct rl_diff_batch rl_diff_batch;
+int rl_diff_batch_create(rl_ctx* ctx, rl_diff_batch** batch);
+int rl_diff_batch_destroy(rl_diff_batch* batch);
+int rl_diff_batch_add(rl_diff_batch* batch, rl_diff* diff);   /* returns the model index */
+int rl_diff_batch_use_graph(rl_diff_batch* batch, int enable);
+int rl_diff_batch_buffers(rl_diff_batch* batch, double** lnT, double** lnX, double** width, double** flux,
+                          double** gflux, double** g_lnT, double** g_lnX, double** g_width, long long* ncell,
+                          long long* nflux);
+int rl_diff_batch_layout(rl_diff_batch* batch, int model, long long* cell_offset, long long* flux_offset);
+int rl_diff_batch_forward(rl_diff_batch* batch, rl_stats* stats);
+int rl_diff_batch_backward(rl_diff_batch* batch, rl_stats* stats);
+
 /* Circular image -> F_nu at `distance_pc` parsec, with no device allocation. No
    counterpart in the reference: it serves callers that own all device memory (their
    own pool or arena) and cannot let a library call cudaMalloc. Every pointer is a

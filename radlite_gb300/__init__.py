@@ -75,7 +75,9 @@ EXPORTS = ["rl_create", "rl_destroy", "rl_last_error", "rl_load_dir", "rl_load_a
            "rl_batch_get_tiles", "rl_batch_autotune", "rl_batch_use_graph", "rl_batch_flux_size",
            "rl_batch_job_info", "rl_batch_run", "rl_batch_waves", "rl_run_manifest",
            "rl_diff_create", "rl_diff_destroy", "rl_diff_info", "rl_diff_set_checkpoint", "rl_diff_forward",
-           "rl_diff_backward",
+           "rl_diff_backward", "rl_diff_batch_create", "rl_diff_batch_destroy", "rl_diff_batch_add",
+           "rl_diff_batch_use_graph", "rl_diff_batch_buffers", "rl_diff_batch_layout", "rl_diff_batch_forward",
+           "rl_diff_batch_backward",
            "rl_image_to_spectrum_noalloc"]
 
 _lib = None
@@ -121,6 +123,14 @@ def lib():
         L.rl_diff_destroy.argtypes = [vp]
         L.rl_diff_info.argtypes = [vp, _I, _I, _I, _I]
         L.rl_diff_set_checkpoint.argtypes = [vp, C.c_int]
+        L.rl_diff_batch_create.argtypes = [vp, C.POINTER(vp)]
+        L.rl_diff_batch_destroy.argtypes = [vp]
+        L.rl_diff_batch_add.argtypes = [vp, vp]
+        L.rl_diff_batch_use_graph.argtypes = [vp, C.c_int]
+        L.rl_diff_batch_buffers.argtypes = [vp] + [C.POINTER(vp)] * 8 + [C.POINTER(C.c_longlong)] * 2
+        L.rl_diff_batch_layout.argtypes = [vp, C.c_int, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
+        L.rl_diff_batch_forward.argtypes = [vp, C.POINTER(Stats)]
+        L.rl_diff_batch_backward.argtypes = [vp, C.POINTER(Stats)]
         L.rl_diff_forward.argtypes = [vp, vp, vp, vp, vp, C.POINTER(Stats)]
         L.rl_diff_backward.argtypes = [vp, vp, vp, vp, vp, C.POINTER(Stats)]
         L.rl_image_to_spectrum_noalloc.argtypes = [vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
@@ -413,6 +423,87 @@ class Diff:
         _check(lib().rl_diff_backward(self.h, gflux.data_ptr(), g[0].data_ptr(), g[1].data_ptr(), g[2].data_ptr(),
                                       C.byref(st)), self.model._ch)
         return (tuple(g), st.as_dict()) if stats else tuple(g)
+
+
+class _DevArray:
+    """A float64 device buffer owned by the library, exposed through
+    __cuda_array_interface__ so that torch.as_tensor wraps it without a copy."""
+
+    def __init__(self, ptr: int, n: int):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": "<f8", "data": (ptr, False), "version": 3,
+                                         "strides": None}
+
+
+class DiffBatch:
+    """Many Diff models rendered by one forward and one adjoint launch sequence, each
+    replayed from a CUDA graph (rl_diff_batch). The parameter, spectrum and gradient
+    buffers belong to the batch; `tensors()` returns torch views of them per model."""
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+        self.h = C.c_void_p()
+        self.diffs = []
+        _check(lib().rl_diff_batch_create(ctx.h, C.byref(self.h)), ctx.h)
+        self._views = None
+
+    def close(self):
+        if self.h:
+            lib().rl_diff_batch_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add(self, diff: Diff) -> int:
+        self.diffs.append(diff)
+        self._views = None
+        return _check(lib().rl_diff_batch_add(self.h, diff.h), self.ctx.h)
+
+    def use_graph(self, enable: bool):
+        _check(lib().rl_diff_batch_use_graph(self.h, int(bool(enable))), self.ctx.h)
+
+    def tensors(self) -> dict:
+        """torch views of the batch buffers: whole arrays ('lnT', ..., 'g_width') and per-model
+        slices ('models': [{'lnT', 'lnX', 'width', 'flux' [nl, nfr], 'gflux', 'g_lnT', ...}])."""
+        import torch
+        if self._views is not None:
+            return self._views
+        ptr = [C.c_void_p() for _ in range(8)]
+        nc, nf = C.c_longlong(), C.c_longlong()
+        _check(lib().rl_diff_batch_buffers(self.h, *(C.byref(p) for p in ptr), C.byref(nc), C.byref(nf)),
+               self.ctx.h)
+        names = ("lnT", "lnX", "width", "flux", "gflux", "g_lnT", "g_lnX", "g_width")
+        sizes = (nc.value, nc.value, nc.value, nf.value, nf.value, nc.value, nc.value, nc.value)
+        whole = {k: torch.as_tensor(_DevArray(p.value, n), device="cuda") for k, p, n in zip(names, ptr, sizes)}
+        models = []
+        for j, d in enumerate(self.diffs):
+            co, fo = C.c_longlong(), C.c_longlong()
+            _check(lib().rl_diff_batch_layout(self.h, j, C.byref(co), C.byref(fo)), self.ctx.h)
+            c0, f0 = co.value, fo.value
+            v = {k: whole[k][c0:c0 + d.ncell] for k in ("lnT", "lnX", "width", "g_lnT", "g_lnX", "g_width")}
+            for k in ("flux", "gflux"):
+                v[k] = whole[k][f0:f0 + d.nlines * d.nfr].view(d.nlines, d.nfr)
+            models.append(v)
+        whole["models"] = models
+        self._views = whole
+        return whole
+
+    def forward(self, stats: bool = False):
+        import torch
+        torch.cuda.current_stream().synchronize()
+        st = Stats()
+        _check(lib().rl_diff_batch_forward(self.h, C.byref(st)), self.ctx.h)
+        return st.as_dict() if stats else None
+
+    def backward(self, stats: bool = False):
+        import torch
+        torch.cuda.current_stream().synchronize()
+        st = Stats()
+        _check(lib().rl_diff_batch_backward(self.h, C.byref(st)), self.ctx.h)
+        return st.as_dict() if stats else None
 
 
 def _raytrace_function():

@@ -177,7 +177,9 @@ __device__ __forceinline__ PV<T> pv_eval(const LineVals<T>& v, T w, T vl, T rl) 
 // and dL/d rl, dL/d vl through the profile.
 template <typename T>
 __device__ __forceinline__ void point_back(const PV<T>& p, T rl, T gj, T ga, T gS, T* acc, T& g_rl, T& g_vl) {
-  if (p.a > (T)0) {
+  // S = j/a enters only where a step used it: gS == 0 elsewhere, and there the FP32
+  // reciprocal of a flushed opacity (inf) must not meet it (0 * inf)
+  if (p.a > (T)0 && gS != (T)0) {
     gj += gS * p.ra;
     ga -= gS * p.S * p.ra;
   }
@@ -381,7 +383,7 @@ __device__ __noinline__ SlowOut<T> seg_back_slow(bool init, int kind, T w, LineV
     cgj = 0; cga = 0;
   } else {
     T gj = gj_next, ga = ga_next;
-    if (p0.a > (T)0) {
+    if (p0.a > (T)0 && gS_next != (T)0) {
       gj += gS_next * p0.ra;
       ga -= gS_next * p0.S * p0.ra;
     }
@@ -745,7 +747,7 @@ __device__ void adjoint_item(const AdjParams<T>& A, int item, AdjStage<T>& S, Ad
             point_back<T>(q1, rl, g.j1 + cgj[u], g.a1 + cga[u], g.S1, acc1, grl_seg, gv);
             // carried start state: dL/dS folded into (j, a)
             T gj = g.j0, ga = g.a0;
-            if (q0.a > (T)0) {
+            if (q0.a > (T)0 && g.S0 != (T)0) {
               gj += g.S0 * q0.ra;
               ga -= g.S0 * q0.S * q0.ra;
             }

@@ -239,9 +239,7 @@ int create(rl_diff* d) {
 }
 
 template <typename T>
-int forward(rl_diff* d, const double* lnT, const double* lnX, const double* width, double* flux, rl_stats* st) {
-  rl_ctx* ctx = d->ctx;
-  cudaStream_t s = ctx->stream;
+LteParams<T> lte_params(const rl_diff* d, const double* lnT, const double* lnX) {
   const Model& m = d->md->m;
   LteParams<T> L;
   L.ncell = d->ncell; L.nlev = m.nlev; L.nl = d->nl;
@@ -249,6 +247,23 @@ int forward(rl_diff* d, const double* lnT, const double* lnX, const double* widt
   L.lines = d->lines.as<LteLine>(); L.dust = d->dust.as<double>();
   L.lnQ = d->lnQ.as<double>(); L.Emean = d->Emean.as<double>();
   L.tab = d->tab.as<T>(); L.nsum = d->nsum.as<T>(); L.dtab = d->dtab.as<double>();
+  return L;
+}
+
+template <typename T>
+ReduceParams reduce_params(const rl_diff* d) {
+  ReduceParams rp;
+  rp.nrays = d->cam.nrays; rp.nfr = d->nfr; rp.nphi = d->cam.nphi; rp.nrr = d->cam.nrr; rp.nlines = d->nl;
+  rp.ri = d->ri.as<double>(); rp.dist2 = 3.08572e18 * 3.08572e18; rp.scale = d->dscale.as<double>();
+  return rp;
+}
+
+template <typename T>
+int forward(rl_diff* d, const double* lnT, const double* lnX, const double* width, double* flux, rl_stats* st) {
+  rl_ctx* ctx = d->ctx;
+  cudaStream_t s = ctx->stream;
+  const Model& m = d->md->m;
+  const LteParams<T> L = lte_params<T>(d, lnT, lnX);
   CUDA_TRY(cudaEventRecord(ctx->ev[0], s));
   CUDA_TRY(launch_lte<T>(L, s));
   CUDA_TRY(cudaMemcpyAsync(d->width.p, width, sizeof(double) * d->ncell, cudaMemcpyDeviceToDevice, s));
@@ -260,10 +275,7 @@ int forward(rl_diff* d, const double* lnT, const double* lnX, const double* widt
   const WalkParams<T> P = walk_params<T>(d);
   CUDA_TRY(launch_walk<T>(P, d->cpl, ctx->nsm, s));
   CUDA_TRY(cudaEventRecord(ctx->ev[2], s));
-  ReduceParams rp;
-  rp.nrays = d->cam.nrays; rp.nfr = d->nfr; rp.nphi = d->cam.nphi; rp.nrr = d->cam.nrr; rp.nlines = d->nl;
-  rp.ri = d->ri.as<double>(); rp.dist2 = 3.08572e18 * 3.08572e18; rp.scale = d->dscale.as<double>();
-  CUDA_TRY(launch_reduce<T>(rp, d->img.as<T>(), d->ring.as<double>(), flux, s));
+  CUDA_TRY(launch_reduce<T>(reduce_params<T>(d), d->img.as<T>(), d->ring.as<double>(), flux, s));
   CUDA_TRY(cudaEventRecord(ctx->ev[3], s));
   unsigned long long cnt[4] = {0, 0, 0, 0};
   int kerr = 0;
@@ -336,7 +348,320 @@ int backward(rl_diff* d, const double* gflux, double* g_lnT, double* g_lnX, doub
 
 }  // namespace
 
+// ---- many differentiable models in one launch sequence per direction ----
+struct rl_diff_batch {
+  rl_ctx* ctx = nullptr;
+  int precision = -1;
+  std::vector<rl_diff*> jobs;
+  std::vector<size_t> cell_off, flux_off;
+  size_t ncell = 0, nflux = 0;
+  int max_nfr = 0, max_kmax = 0, adj_blocks = 0, every = 1;
+  bool built = false, use_graph = true;
+  DevBuf lnT, lnX, width, flux, gflux, g_lnT, g_lnX, g_width;
+  DevBuf walkjobs, redjobs, adjjobs, item_prefix, ring_prefix, line_prefix, adj_prefix, cnt, work, err, acnt, awork, ckpt;
+  JobLaunch<float> Lf{};
+  JobLaunch<double> Ld{};
+  AdjJobs<float> Af{};
+  AdjJobs<double> Ad{};
+  unsigned long long* cnt_h = nullptr;
+  int* err_h = nullptr;
+  cudaGraph_t g[2] = {nullptr, nullptr};
+  cudaGraphExec_t x[2] = {nullptr, nullptr};
+  void drop_graphs() {
+    for (int i = 0; i < 2; i++) {
+      if (x[i]) cudaGraphExecDestroy(x[i]);
+      if (g[i]) cudaGraphDestroy(g[i]);
+      x[i] = nullptr; g[i] = nullptr;
+    }
+  }
+  ~rl_diff_batch() {
+    if (ctx) cudaSetDevice(ctx->device);
+    drop_graphs();
+    if (cnt_h) cudaFreeHost(cnt_h);
+    if (err_h) cudaFreeHost(err_h);
+  }
+};
+
+namespace {
+
+template <typename T> JobLaunch<T>& launch_of(rl_diff_batch* b);
+template <> JobLaunch<float>& launch_of<float>(rl_diff_batch* b) { return b->Lf; }
+template <> JobLaunch<double>& launch_of<double>(rl_diff_batch* b) { return b->Ld; }
+template <typename T> AdjJobs<T>& adj_of(rl_diff_batch* b);
+template <> AdjJobs<float>& adj_of<float>(rl_diff_batch* b) { return b->Af; }
+template <> AdjJobs<double>& adj_of<double>(rl_diff_batch* b) { return b->Ad; }
+
+template <typename T>
+int batch_build(rl_diff_batch* b) {
+  rl_ctx* ctx = b->ctx;
+  cudaStream_t s = ctx->stream;
+  const int nj = (int)b->jobs.size();
+  if (nj == 0) return set_err(ctx, RL_ERR_STATE, "rl_diff_batch: no models");
+  b->cell_off.assign(nj, 0);
+  b->flux_off.assign(nj, 0);
+  b->ncell = 0; b->nflux = 0; b->max_nfr = 0; b->max_kmax = 0;
+  for (int j = 0; j < nj; j++) {
+    const rl_diff* d = b->jobs[j];
+    b->cell_off[j] = b->ncell;
+    b->flux_off[j] = b->nflux;
+    b->ncell += d->ncell;
+    b->nflux += (size_t)d->nl * d->nfr;
+    b->max_nfr = std::max(b->max_nfr, d->nfr);
+    b->max_kmax = std::max(b->max_kmax, d->kmax);
+  }
+  CUDA_TRY(b->lnT.ensure(sizeof(double) * b->ncell));
+  CUDA_TRY(b->lnX.ensure(sizeof(double) * b->ncell));
+  CUDA_TRY(b->width.ensure(sizeof(double) * b->ncell));
+  CUDA_TRY(b->g_lnT.ensure(sizeof(double) * b->ncell));
+  CUDA_TRY(b->g_lnX.ensure(sizeof(double) * b->ncell));
+  CUDA_TRY(b->g_width.ensure(sizeof(double) * b->ncell));
+  CUDA_TRY(b->flux.ensure(sizeof(double) * b->nflux));
+  CUDA_TRY(b->gflux.ensure(sizeof(double) * b->nflux));
+  CUDA_TRY(b->cnt.ensure(sizeof(unsigned long long) * 4));
+  CUDA_TRY(b->acnt.ensure(sizeof(unsigned long long) * 4));
+  CUDA_TRY(b->work.ensure(sizeof(int)));
+  CUDA_TRY(b->awork.ensure(sizeof(int)));
+  CUDA_TRY(b->err.ensure(sizeof(int)));
+  if (!b->cnt_h) CUDA_TRY(cudaMallocHost((void**)&b->cnt_h, sizeof(unsigned long long) * 8));
+  if (!b->err_h) CUDA_TRY(cudaMallocHost((void**)&b->err_h, sizeof(int) * 2));
+  std::vector<WalkParams<T>> walk(nj);
+  std::vector<RedJob<T>> red(nj);
+  std::vector<AdjParams<T>> adj(nj);
+  std::vector<int> itemp(nj + 1, 0), ringp(nj + 1, 0), linep(nj + 1, 0), adjp(nj + 1, 0);
+  for (int j = 0; j < nj; j++) {
+    const rl_diff* d = b->jobs[j];
+    WalkParams<T> w = walk_params<T>(d);
+    w.counters = b->cnt.as<unsigned long long>();
+    w.work = b->work.as<int>();
+    w.err = b->err.as<int>();
+    walk[j] = w;
+    red[j].p = reduce_params<T>(d);
+    red[j].img = d->img.as<T>();
+    red[j].ring = d->ring.as<double>();
+    red[j].flux = b->flux.as<double>() + b->flux_off[j];
+    AdjParams<T>& A = adj[j];
+    A.W = w;
+    A.gflux = b->gflux.as<double>() + b->flux_off[j];
+    A.ri = d->ri.as<double>();
+    A.nphi = d->cam.nphi; A.nrr = d->cam.nrr;
+    A.dtab = d->dtab.as<double>();
+    A.g_lnT = b->g_lnT.as<double>() + b->cell_off[j];
+    A.g_lnX = b->g_lnX.as<double>() + b->cell_off[j];
+    A.g_b = b->g_width.as<double>() + b->cell_off[j];
+    itemp[j + 1] = itemp[j] + w.nitems;
+    ringp[j + 1] = ringp[j] + d->nl * d->cam.nrr;
+    linep[j + 1] = linep[j] + d->nl;
+    adjp[j + 1] = adjp[j] + d->nl * d->cam.nrays;
+  }
+  CUDA_TRY(b->walkjobs.ensure(sizeof(WalkParams<T>) * nj));
+  CUDA_TRY(b->redjobs.ensure(sizeof(RedJob<T>) * nj));
+  CUDA_TRY(b->adjjobs.ensure(sizeof(AdjParams<T>) * nj));
+  CUDA_TRY(b->item_prefix.ensure(sizeof(int) * (nj + 1)));
+  CUDA_TRY(b->ring_prefix.ensure(sizeof(int) * (nj + 1)));
+  CUDA_TRY(b->line_prefix.ensure(sizeof(int) * (nj + 1)));
+  CUDA_TRY(b->adj_prefix.ensure(sizeof(int) * (nj + 1)));
+  CUDA_TRY(h2d(b->walkjobs.p, walk.data(), sizeof(WalkParams<T>) * nj, s));
+  CUDA_TRY(h2d(b->redjobs.p, red.data(), sizeof(RedJob<T>) * nj, s));
+  CUDA_TRY(h2d(b->adjjobs.p, adj.data(), sizeof(AdjParams<T>) * nj, s));
+  CUDA_TRY(h2d(b->item_prefix.p, itemp.data(), sizeof(int) * (nj + 1), s));
+  CUDA_TRY(h2d(b->ring_prefix.p, ringp.data(), sizeof(int) * (nj + 1), s));
+  CUDA_TRY(h2d(b->line_prefix.p, linep.data(), sizeof(int) * (nj + 1), s));
+  CUDA_TRY(h2d(b->adj_prefix.p, adjp.data(), sizeof(int) * (nj + 1), s));
+  CUDA_TRY(adjoint_grid<T>(ctx->nsm, b->max_nfr, &b->adj_blocks));
+  const long long per = adjoint_ckpt_per_warp<T>(b->max_kmax, b->every);
+  CUDA_TRY(b->ckpt.ensure(sizeof(T) * (size_t)per * b->adj_blocks * 4));
+  JobLaunch<T>& L = launch_of<T>(b);
+  L = JobLaunch<T>{};
+  L.njobs = nj; L.nsm = ctx->nsm; L.cpl = 8;
+  L.geo = nullptr; L.ray_prefix = nullptr; L.nrays_total = 0;
+  L.walk.jobs = b->walkjobs.as<WalkParams<T>>(); L.walk.item_prefix = b->item_prefix.as<int>();
+  L.walk.njobs = nj; L.walk.total = itemp[nj]; L.walk.stride = 1; L.walk.max_nfr = b->max_nfr;
+  L.walk.work = b->work.as<int>(); L.walk.counters = b->cnt.as<unsigned long long>();
+  L.reduce = true;
+  L.red = b->redjobs.as<RedJob<T>>(); L.ring_prefix = b->ring_prefix.as<int>(); L.line_prefix = b->line_prefix.as<int>();
+  L.nring_blocks = ringp[nj]; L.nline_blocks = linep[nj];
+  AdjJobs<T>& A = adj_of<T>(b);
+  A.jobs = b->adjjobs.as<AdjParams<T>>(); A.item_prefix = b->adj_prefix.as<int>();
+  A.njobs = nj; A.total = adjp[nj]; A.max_nfr = b->max_nfr;
+  A.ckpt = b->ckpt.as<T>(); A.ckpt_warp = per; A.every = b->every;
+  A.work = b->awork.as<int>(); A.counters = b->acnt.as<unsigned long long>();
+  CUDA_TRY(cudaStreamSynchronize(s));
+  b->drop_graphs();
+  b->built = true;
+  return 0;
+}
+
+template <typename T>
+cudaError_t batch_enqueue(rl_diff_batch* b, int dir, cudaStream_t s) {
+  cudaError_t e = cudaSuccess;
+  if (dir == 0) {
+    for (size_t j = 0; j < b->jobs.size() && e == cudaSuccess; j++) {
+      rl_diff* d = b->jobs[j];
+      e = launch_lte<T>(lte_params<T>(d, b->lnT.as<double>() + b->cell_off[j], b->lnX.as<double>() + b->cell_off[j]), s);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d->width.p, b->width.as<double>() + b->cell_off[j], sizeof(double) * d->ncell,
+                            cudaMemcpyDeviceToDevice, s);
+      if (e == cudaSuccess) e = launch_node_lw<T>(nodes<T>(d), d->width.as<double>(), d->md->m.nth, s);
+    }
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->cnt.p, 0, sizeof(unsigned long long) * 4, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->err.p, 0, sizeof(int), s);
+    if (e == cudaSuccess) e = launch_jobs<T>(launch_of<T>(b), s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b->cnt_h, b->cnt.p, sizeof(unsigned long long) * 4, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b->err_h, b->err.p, sizeof(int), cudaMemcpyDeviceToHost, s);
+  } else {
+    e = cudaMemsetAsync(b->g_lnT.p, 0, sizeof(double) * b->ncell, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->g_lnX.p, 0, sizeof(double) * b->ncell, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->g_width.p, 0, sizeof(double) * b->ncell, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->acnt.p, 0, sizeof(unsigned long long) * 4, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->err.p, 0, sizeof(int), s);
+    if (e == cudaSuccess) e = launch_adjoint<T>(adj_of<T>(b), b->adj_blocks, s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(b->cnt_h + 4, b->acnt.p, sizeof(unsigned long long) * 4, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b->err_h + 1, b->err.p, sizeof(int), cudaMemcpyDeviceToHost, s);
+  }
+  return e;
+}
+
+template <typename T>
+int batch_run(rl_diff_batch* b, int dir, rl_stats* st) {
+  rl_ctx* ctx = b->ctx;
+  cudaStream_t s = ctx->stream;
+  if (!b->built) {
+    int rc = batch_build<T>(b);
+    if (rc) return rc;
+  }
+  CUDA_TRY(cudaEventRecord(ctx->ev[0], s));
+  if (b->use_graph) {
+    if (!b->x[dir]) {
+      cudaGraph_t g = nullptr;
+      CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+      const cudaError_t e = batch_enqueue<T>(b, dir, s);
+      const cudaError_t e2 = cudaStreamEndCapture(s, &g);
+      if (e != cudaSuccess || e2 != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return set_err(ctx, RL_ERR_CUDA, std::string("rl_diff_batch: graph capture: ") +
+                                              cudaGetErrorString(e != cudaSuccess ? e : e2));
+      }
+      b->g[dir] = g;
+      CUDA_TRY(cudaGraphInstantiate(&b->x[dir], g, 0));
+    }
+    CUDA_TRY(cudaGraphLaunch(b->x[dir], s));
+  } else {
+    CUDA_TRY(batch_enqueue<T>(b, dir, s));
+  }
+  CUDA_TRY(cudaEventRecord(ctx->ev[1], s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  const int kerr = b->err_h[dir];
+  if (kerr != 0) return set_err(ctx, RL_ERR_GEOMETRY, std::string(dir ? "adjoint" : "walk") + ": error code " +
+                                                     std::to_string(kerr));
+  if (dir == 0) for (rl_diff* d : b->jobs) d->have_forward = true;
+  if (st) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
+    st->total_ms += ms;
+    st->walk_ms += ms;
+    const unsigned long long* c = b->cnt_h + 4 * dir;
+    st->steps += c[0];
+    st->integrated += c[1];
+    if (dir == 0) {
+      st->node_visits += c[2];
+      for (rl_diff* d : b->jobs) {
+        st->ray_channels += (unsigned long long)d->cam.nrays * d->nfr * d->nl;
+        st->nlines += d->nl;
+      }
+    }
+  }
+  return 0;
+}
+
+}  // namespace
+
 extern "C" {
+
+int rl_diff_batch_create(rl_ctx* ctx, rl_diff_batch** out) {
+  if (!ctx || !out) return set_err(ctx, RL_ERR_ARG, "rl_diff_batch_create: null argument");
+  *out = nullptr;
+  std::unique_ptr<rl_diff_batch> b(new rl_diff_batch);
+  b->ctx = ctx;
+  *out = b.release();
+  return 0;
+}
+
+int rl_diff_batch_destroy(rl_diff_batch* b) {
+  delete b;
+  return 0;
+}
+
+int rl_diff_batch_add(rl_diff_batch* b, rl_diff* d) {
+  if (!b || !d) return set_err(b ? b->ctx : nullptr, RL_ERR_ARG, "rl_diff_batch_add: null argument");
+  rl_ctx* ctx = b->ctx;
+  if (d->ctx != ctx) return set_err(ctx, RL_ERR_ARG, "rl_diff_batch_add: model of another context");
+  if (b->precision >= 0 && d->precision != b->precision)
+    return set_err(ctx, RL_ERR_ARG, "rl_diff_batch_add: all models of a batch have one precision");
+  b->precision = d->precision;
+  b->jobs.push_back(d);
+  b->built = false;
+  b->drop_graphs();
+  return (int)b->jobs.size() - 1;
+}
+
+int rl_diff_batch_use_graph(rl_diff_batch* b, int enable) {
+  if (!b) return set_err(nullptr, RL_ERR_ARG, "rl_diff_batch_use_graph: null batch");
+  b->use_graph = enable != 0;
+  return 0;
+}
+
+int rl_diff_batch_buffers(rl_diff_batch* b, double** lnT, double** lnX, double** width, double** flux, double** gflux,
+                          double** g_lnT, double** g_lnX, double** g_width, long long* ncell, long long* nflux) {
+  if (!b) return set_err(nullptr, RL_ERR_ARG, "rl_diff_batch_buffers: null batch");
+  rl_ctx* ctx = b->ctx;
+  CUDA_TRY(cudaSetDevice(ctx->device));
+  if (!b->built) {
+    const int rc = b->precision == RL_FP64 ? batch_build<double>(b) : batch_build<float>(b);
+    if (rc) return rc;
+  }
+  if (lnT) *lnT = b->lnT.as<double>();
+  if (lnX) *lnX = b->lnX.as<double>();
+  if (width) *width = b->width.as<double>();
+  if (flux) *flux = b->flux.as<double>();
+  if (gflux) *gflux = b->gflux.as<double>();
+  if (g_lnT) *g_lnT = b->g_lnT.as<double>();
+  if (g_lnX) *g_lnX = b->g_lnX.as<double>();
+  if (g_width) *g_width = b->g_width.as<double>();
+  if (ncell) *ncell = (long long)b->ncell;
+  if (nflux) *nflux = (long long)b->nflux;
+  return 0;
+}
+
+int rl_diff_batch_layout(rl_diff_batch* b, int job, long long* cell_offset, long long* flux_offset) {
+  if (!b || job < 0 || job >= (int)b->jobs.size())
+    return set_err(b ? b->ctx : nullptr, RL_ERR_ARG, "rl_diff_batch_layout: bad job");
+  if (!b->built) {
+    const int rc = rl_diff_batch_buffers(b, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                                         nullptr, nullptr);
+    if (rc) return rc;
+  }
+  if (cell_offset) *cell_offset = (long long)b->cell_off[job];
+  if (flux_offset) *flux_offset = (long long)b->flux_off[job];
+  return 0;
+}
+
+int rl_diff_batch_forward(rl_diff_batch* b, rl_stats* st) {
+  if (!b) return set_err(nullptr, RL_ERR_ARG, "rl_diff_batch_forward: null batch");
+  rl_ctx* ctx = b->ctx;
+  CUDA_TRY(cudaSetDevice(ctx->device));
+  if (st) std::memset(st, 0, sizeof *st);
+  return b->precision == RL_FP64 ? batch_run<double>(b, 0, st) : batch_run<float>(b, 0, st);
+}
+
+int rl_diff_batch_backward(rl_diff_batch* b, rl_stats* st) {
+  if (!b) return set_err(nullptr, RL_ERR_ARG, "rl_diff_batch_backward: null batch");
+  rl_ctx* ctx = b->ctx;
+  CUDA_TRY(cudaSetDevice(ctx->device));
+  if (st) std::memset(st, 0, sizeof *st);
+  return b->precision == RL_FP64 ? batch_run<double>(b, 1, st) : batch_run<float>(b, 1, st);
+}
+
 
 int rl_diff_create(rl_model* md, int iline0, int nlines, int precision, rl_diff** out) {
   if (!md || !out) return set_err(nullptr, RL_ERR_ARG, "rl_diff_create: null argument");
