@@ -13,6 +13,15 @@ inclinations 20 and 60 degrees: 40 spectra, 2.048e9 ray-channels. Synthetic inpu
   --impl reference   the reference algorithm on the host cores: the FP64 C restatement of
           RADLite's Fortran raytrace (the Fortran itself does not compile here), one
           process per core, on a bounded sample of the same workload.
+
+The same JSON line carries the other halves of the metric (plain vs batched+adjoint):
+  batched  256 uneven models rendered by one graph-replayed launch sequence against the
+           same models one per-model call at a time (spectra/s of each, same spectra)
+  adjoint  forward and adjoint times of the differentiable raytrace on the 200x100 disk
+           (10 lines x 128 channels, 600x128 rays; per-cell ln T, ln X, width gradients)
+  fit      the batched forward+adjoint fitting step on 64 uneven models (20 lines x 200
+           channels, 4 disk-law parameters each) against plain per-model forward + central
+           finite differences (9 forwards per gradient)
 """
 from __future__ import annotations
 
@@ -264,9 +273,12 @@ def ours(args):
         sel = f64 > 1e-3 * f64.max()
         rel = float(np.max(np.abs(f32[sel] - f64[sel]) / np.abs(f64[sel])))
     m.free()
-    batched = None
+    batched = adjoint = fitting = None
     if rank == 0 and args.batch_models > 0:
         batched = batched_case(ctx, args.batch_models, 2)
+    if rank == 0 and not args.no_diff:
+        adjoint = adjoint_case(ctx)
+        fitting = fit_case(ctx, args.fit_models, 3)
     out = None
     if rank == 0:
         cpu = None
@@ -297,6 +309,8 @@ def ours(args):
                                          "frac_of_measured": (traffic_gbs / hbm_peak
                                                               if traffic_gbs and hbm_peak else None)}},
                "batched": batched,
+               "adjoint": adjoint,
+               "fit": fitting,
                "cpu_baseline": cpu,
                "clocks": clk.summary(),
                "gpu_launches": args.steps * len(INCLS) * 4}
@@ -448,6 +462,7 @@ def main():
     ap.add_argument("--nphi", type=int, default=0, help="azimuths of the adjoint timing (0: the workload's)")
     ap.add_argument("--only-fit", action="store_true", help="run only the batched fitting-step comparison")
     ap.add_argument("--fit-models", type=int, default=64)
+    ap.add_argument("--no-diff", action="store_true", help="skip the adjoint and fitting measurements")
     args = ap.parse_args()
     if args.only_fit:
         import radlite_gb300 as rl
