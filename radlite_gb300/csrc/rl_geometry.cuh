@@ -94,13 +94,14 @@ struct TAcc { const Grid* g; RL_HD double operator()(int j) const { return Tg(*g
 
 struct Ray {
   double x0, z0, costh0, sinth0, costh02, sinth02, pitheta0, bimpact;
+  double bnew, znew;                    // direction(): impact distance and offset in the ray plane
   int iy0, isnr, isdblnr, caseA, iup;   // theta crossings
   int ir_min, ir_amount, ith_amount;    // r crossings
 };
 
 // One emitted node of the trajectory.
 struct Node {
-  double s, r, th, mu, sinphi, cosphi;
+  double s, r, th, mu, sinmu, sinphi, cosphi;   // sinmu = sqrt(1 - mu^2)
   int icr, ir, it;
 };
 
@@ -118,6 +119,8 @@ RL_HD int init_ray(const Grid& g, double x0, double z0, double theta0, Ray& y) {
   y.pitheta0 = 0.5 * kPi - theta0;
   y.costh0 = cos(theta0); y.sinth0 = sin(theta0);
   y.costh02 = y.costh0 * y.costh0; y.sinth02 = y.sinth0 * y.sinth0;
+  y.znew = z0 * y.sinth02;
+  y.bnew = sqrt(x0 * x0 + z0 * z0 * y.sinth02);
   // theta=const cones with two crossings: contiguous suffix iy0..nth of the stored half
   int first = 0, count = 0;
   for (int iy = 1; iy <= g.nth; iy++) {
@@ -309,15 +312,19 @@ RL_HD int make_extra(const Grid& g, const Ray& y, Extra& E, int& ixg, int& iyg) 
   return kGeoOk;
 }
 
-// Local photon direction at a node (telescope.F:3687-3718), returned as mu, sin(phi),
-// cos(phi); sin/cos follow from phi = asin(p) (x0<0) or pi - asin(p) directly.
-RL_HD void direction(const Ray& y, double s, double& mu, double& sinphi, double& cosphi) {
-  const double znew = y.z0 * y.sinth02;
-  const double bnew = sqrt(y.x0 * y.x0 + y.z0 * y.z0 * y.sinth02);
+// Local photon direction at a node (telescope.F:3687-3718), returned as mu, sqrt(1-mu^2),
+// sin(phi), cos(phi); sin/cos follow from phi = asin(p) (x0<0) or pi - asin(p) directly.
+// bnew (per ray) and the radius sqrt(bnew^2 + snew^2) give mu and sqrt(1 - mu^2) with one
+// square root and one reciprocal.
+RL_HD void direction(const Ray& y, double s, double& mu, double& sinmu, double& sinphi, double& cosphi) {
+  const double bnew = y.bnew, znew = y.znew;
   const double snew = s + y.z0 * y.costh0;
-  mu = snew / sqrt(bnew * bnew + snew * snew);
+  const double rr2 = bnew * bnew + snew * snew;
+  const double irad = 1.0 / sqrt(rr2);
+  mu = fmin(1.0, fmax(-1.0, snew * irad));   // the reciprocal may round |mu| past 1 on the axis
+  sinmu = bnew * irad;
   const double q = znew + snew * y.costh0;
-  const double dummy = bnew * sqrt(bnew * bnew + snew * snew - q * q);
+  const double dummy = bnew * sqrt(rr2 - q * q);
   const double sp = (dummy > 0.0) ? (bnew * bnew * y.costh0 - znew * snew) / dummy : 1.0e1 * kTelEps;
   sinphi = sp;
   const double c = sqrt(1.0 - sp * sp);
@@ -364,7 +371,7 @@ RL_HD int trace(const Grid& g, double x0, double z0, double theta0, Emit& emit) 
       if (E.r[ie] <= rmaxt && E.r[ie] >= rmint && (E.s[ie] - sprev) > kTelEps * E.r[ie] &&
           E.s[ie] >= sbeg && E.s[ie] <= send) {
         nd.icr = 3; nd.r = E.r[ie]; nd.th = E.th[ie]; nd.ir = E.ir[ie]; nd.it = E.it[ie]; nd.s = E.s[ie];
-        direction(y, nd.s, nd.mu, nd.sinphi, nd.cosphi);
+        direction(y, nd.s, nd.mu, nd.sinmu, nd.sinphi, nd.cosphi);
         sprev = nd.s;
         if (!emit(nd)) return kGeoOverflow;
       }
@@ -376,7 +383,7 @@ RL_HD int trace(const Grid& g, double x0, double z0, double theta0, Emit& emit) 
         if (thr < Rg(g, 1)) nd.ir = 0;
         else if (thr > Rg(g, g.nr)) nd.ir = g.nr;
         else { ixg = hunt(racc, g.nr, thr, ixg); nd.ir = ixg; }
-        direction(y, nd.s, nd.mu, nd.sinphi, nd.cosphi);
+        direction(y, nd.s, nd.mu, nd.sinmu, nd.sinphi, nd.cosphi);
         sprev = nd.s;
         if (!emit(nd)) return kGeoOverflow;
       }
@@ -386,7 +393,7 @@ RL_HD int trace(const Grid& g, double x0, double z0, double theta0, Emit& emit) 
       if (rr <= rmaxr && rr >= rminr && (rs - sprev) > kTelEps * rr && rs >= sbeg && rs <= send) {
         nd.icr = 1; nd.r = rr; nd.th = theta_at(y, rs); nd.ir = rix; nd.s = rs;
         iyg = hunt(tacc, g.ny, nd.th, iyg); nd.it = iyg;
-        direction(y, nd.s, nd.mu, nd.sinphi, nd.cosphi);
+        direction(y, nd.s, nd.mu, nd.sinmu, nd.sinphi, nd.cosphi);
         sprev = nd.s;
         if (!emit(nd)) return kGeoOverflow;
       }

@@ -64,7 +64,7 @@ struct NodeEmitter {
              dr * ((1.0 - dt) * p->vel[3 * c10 + i] + dt * p->vel[3 * c11 + i]);
     const double lwv = (1.0 - dr) * ((1.0 - dt) * p->lw[c00] + dt * p->lw[c01]) +
                        dr * ((1.0 - dt) * p->lw[c10] + dt * p->lw[c11]);
-    const double dvmu = 3.335668e-11 * (n.mu * v[0] + sqrt(1.0 - n.mu * n.mu) * (v[1] * n.sinphi + v[2] * n.cosphi));
+    const double dvmu = 3.335668e-11 * (n.mu * v[0] + n.sinmu * (v[1] * n.sinphi + v[2] * n.cosphi));
     const double kv = 1.0 / 3.33567e-6;
     unsigned flags = 0;
     double ds = 0.0;
