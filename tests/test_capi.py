@@ -56,3 +56,23 @@ def test_malformed_inputs_rejected(gpu_lib, tmp_path, fname, mutate, msg):
     open(p, "w").write(new)
     with pytest.raises(gpu_lib.RLError, match=msg):
         gpu_lib.load_dir_host(d)
+
+
+def test_batch_and_diff_entry_points_check_arguments(gpu_lib):
+    """The batched and differentiable entry points reject null handles on the host,
+    before any device work (no GPU needed)."""
+    import ctypes as C
+    L = gpu_lib.lib()
+    out = C.c_void_p()
+    assert L.rl_batch_create(None, 0, C.byref(out)) == -1
+    assert L.rl_batch_run(None, None, None) == -1
+    assert L.rl_batch_add(None, None, 1, 1) == -1
+    assert L.rl_batch_set_tiles(None, 1, 2) == -1
+    assert L.rl_diff_create(None, 1, 1, 0, C.byref(out)) == -1
+    assert L.rl_diff_forward(None, None, None, None, None, None) == -1
+    assert L.rl_diff_backward(None, None, None, None, None, None) == -1
+    assert L.rl_diff_set_checkpoint(None, 1) == -1
+    assert L.rl_diff_batch_create(None, C.byref(out)) == -1
+    assert L.rl_diff_batch_forward(None, None) == -1
+    assert L.rl_run_manifest(None, 0, None) == -1
+    assert "null" in gpu_lib._err()
