@@ -71,7 +71,7 @@ struct rl_batch {
   bool geo_valid = false;        // node records of a single-wave batch are in the arena
   Plan<float> pf;
   Plan<double> pd;
-  DevBuf arena, flux, counters, work, err;
+  DevBuf arena, flux, counters, work, err, list;
   double* flux_h = nullptr;
   unsigned long long* cnt_h = nullptr;
   int* err_h = nullptr;
@@ -224,6 +224,7 @@ int write_descriptors(rl_batch* b) {
       w.counters = b->counters.as<unsigned long long>();
       w.work = b->work.as<int>();
       w.err = b->err.as<int>();
+      w.list = b->list.as<unsigned short>();
       RedJob<T>& r = red[q];
       r.p.nrays = cam.nrays; r.p.nfr = J.nfr; r.p.nphi = cam.nphi; r.p.nrr = cam.nrr; r.p.nlines = J.nl;
       r.p.ri = J.ri.as<double>(); r.p.dist2 = 3.08572e18 * 3.08572e18; r.p.scale = J.scale.as<double>();
@@ -253,6 +254,7 @@ int write_descriptors(rl_batch* b) {
     L.walk.jobs = static_cast<WalkParams<T>*>(W.dwalk.p); L.walk.item_prefix = static_cast<int*>(W.ditem.p);
     L.walk.njobs = nj; L.walk.total = itemp[nj]; L.walk.stride = 1; L.walk.max_nfr = max_nfr;
     L.walk.work = b->work.as<int>(); L.walk.counters = b->counters.as<unsigned long long>();
+    L.walk.list = b->list.as<unsigned short>();
     L.reduce = true;
     L.red = static_cast<RedJob<T>*>(W.dred.p); L.ring_prefix = static_cast<int*>(W.dring.p); L.line_prefix = static_cast<int*>(W.dline.p);
     L.nring_blocks = ringp[nj]; L.nline_blocks = linep[nj];
@@ -302,6 +304,11 @@ int build(rl_batch* b) {
   CUDA_TRY(b->counters.ensure(sizeof(unsigned long long) * 4));
   CUDA_TRY(b->work.ensure(sizeof(int)));
   CUDA_TRY(b->err.ensure(sizeof(int)));
+  {
+    int max_nfr = 0;
+    for (auto& J : b->jobs) max_nfr = std::max(max_nfr, J->nfr);
+    CUDA_TRY(b->list.ensure(sizeof(unsigned short) * walk_list_elems(ctx->nsm, max_nfr)));
+  }
   if (b->flux_h) { cudaFreeHost(b->flux_h); b->flux_h = nullptr; }
   CUDA_TRY(cudaMallocHost((void**)&b->flux_h, sizeof(double) * b->nflux));
   if (!b->cnt_h) CUDA_TRY(cudaMallocHost((void**)&b->cnt_h, sizeof(unsigned long long) * 4));

@@ -191,6 +191,7 @@ static int run_lines(rl_model* md, int iline0, int nl, double* flux_out, double*
   CUDA_TRY(md->dcnt.ensure(sizeof(unsigned long long) * 4));
   CUDA_TRY(md->dwork.ensure(sizeof(int)));
   CUDA_TRY(md->derr.ensure(sizeof(int)));
+  CUDA_TRY(md->dlist.ensure(sizeof(unsigned short) * walk_list_elems(ctx->nsm, nfr)));
   CUDA_TRY(cudaEventRecord(ctx->ev[0], s));
   if (!cached) {
     CUDA_TRY(h2d(md->dtab.p, tab.data(), sizeof(T) * tab.size(), s));
@@ -223,6 +224,7 @@ static int run_lines(rl_model* md, int iline0, int nl, double* flux_out, double*
   P.counters = md->dcnt.as<unsigned long long>();
   P.work = md->dwork.as<int>();
   P.err = md->derr.as<int>();
+  P.list = md->dlist.as<unsigned short>();
   if (cam.ri[1] < m.rstar) return set_err(ctx, RL_ERR_ARG, "central beam smaller than the star");
   // slots per lane: enough for every (line, channel) pair of a line group in one tile
   const int need = (P.gsize * nfr + 31) / 32;

@@ -5,6 +5,14 @@
 
 namespace rl {
 
+// Walk launch shape: 4-warp blocks, at most this many per SM (sizes the list scratch).
+constexpr int kWalkBlocksPerSm = 4;
+constexpr int kWalkWarps = 4;
+// Elements of the walk's list scratch for nsm SMs and up to nfr channels per line.
+inline size_t walk_list_elems(int nsm, int nfr) {
+  return (size_t)nsm * kWalkBlocksPerSm * kWalkWarps * (size_t)((8 * nfr + 7) & ~7);
+}
+
 // Per-node flag bits in NodeBuf::misc (bits 0-15: theta-corner offset + 32768,
 // bits 16-17: radial-corner offset + 1).
 constexpr unsigned kFlagHole = 1u << 20;   // segment ending here lies in the central hole
@@ -75,6 +83,7 @@ struct WalkParams {
   unsigned long long* counters;   // [0] steps, [1] integrated channels, [2] node visits
   int* work;                 // dynamic work counter
   int* err;                  // first error code
+  unsigned short* list;      // per-warp (line, channel) list rows: blocks x 4 warps x ((8 nfr + 7) & ~7)
 };
 
 struct ReduceParams {
@@ -97,9 +106,10 @@ struct WalkJobs {
   const int* item_prefix;     // [njobs+1] first item of each job
   int njobs, total;           // total = item_prefix[njobs]
   int stride;                 // 1, or > 1 to walk every stride-th item only (tuning samples)
-  int max_nfr;                // largest channel count of the jobs (shared-memory list size)
+  int max_nfr;                // largest channel count of the jobs (list row size)
   int* work;                  // queue counter
   unsigned long long* counters;
+  unsigned short* list;       // per-warp list rows, as WalkParams::list with max_nfr
 };
 
 template <typename T>

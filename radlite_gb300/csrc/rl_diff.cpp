@@ -52,7 +52,7 @@ struct rl_diff {
   DevBuf Ek, lng, lines, dust, rho_m, lnQ, Emean, wch, velo, star, lc, dscale;
   // tables of the last forward
   DevBuf tab, nsum, dtab, width;
-  DevBuf img, ring, flux, cnt, work, err;
+  DevBuf img, ring, flux, cnt, work, err, list;
   // adjoint
   DevBuf ckpt, ajob, aprefix, acnt, awork;
   bool have_forward = false;
@@ -91,6 +91,7 @@ WalkParams<T> walk_params(const rl_diff* d) {
   P.counters = d->cnt.as<unsigned long long>();
   P.work = d->work.as<int>();
   P.err = d->err.as<int>();
+  P.list = d->list.as<unsigned short>();
   return P;
 }
 
@@ -210,6 +211,7 @@ int create(rl_diff* d) {
   CUDA_TRY(d->cnt.ensure(sizeof(unsigned long long) * 4));
   CUDA_TRY(d->work.ensure(sizeof(int)));
   CUDA_TRY(d->err.ensure(sizeof(int)));
+  CUDA_TRY(d->list.ensure(sizeof(unsigned short) * walk_list_elems(ctx->nsm, d->nfr)));
   CUDA_TRY(d->acnt.ensure(sizeof(unsigned long long) * 4));
   CUDA_TRY(d->awork.ensure(sizeof(int)));
   CUDA_TRY(d->ajob.ensure(sizeof(AdjParams<T>)));
@@ -358,7 +360,8 @@ struct rl_diff_batch {
   int max_nfr = 0, max_kmax = 0, adj_blocks = 0, every = 1;
   bool built = false, use_graph = true;
   DevBuf lnT, lnX, width, flux, gflux, g_lnT, g_lnX, g_width;
-  DevBuf walkjobs, redjobs, adjjobs, item_prefix, ring_prefix, line_prefix, adj_prefix, cnt, work, err, acnt, awork, ckpt;
+  DevBuf walkjobs, redjobs, adjjobs, item_prefix, ring_prefix, line_prefix, adj_prefix, cnt, work, err, acnt, awork, ckpt,
+      list;
   JobLaunch<float> Lf{};
   JobLaunch<double> Ld{};
   AdjJobs<float> Af{};
@@ -422,6 +425,7 @@ int batch_build(rl_diff_batch* b) {
   CUDA_TRY(b->work.ensure(sizeof(int)));
   CUDA_TRY(b->awork.ensure(sizeof(int)));
   CUDA_TRY(b->err.ensure(sizeof(int)));
+  CUDA_TRY(b->list.ensure(sizeof(unsigned short) * walk_list_elems(ctx->nsm, b->max_nfr)));
   if (!b->cnt_h) CUDA_TRY(cudaMallocHost((void**)&b->cnt_h, sizeof(unsigned long long) * 8));
   if (!b->err_h) CUDA_TRY(cudaMallocHost((void**)&b->err_h, sizeof(int) * 2));
   std::vector<WalkParams<T>> walk(nj);
@@ -434,6 +438,7 @@ int batch_build(rl_diff_batch* b) {
     w.counters = b->cnt.as<unsigned long long>();
     w.work = b->work.as<int>();
     w.err = b->err.as<int>();
+    w.list = b->list.as<unsigned short>();
     walk[j] = w;
     red[j].p = reduce_params<T>(d);
     red[j].img = d->img.as<T>();
@@ -477,6 +482,7 @@ int batch_build(rl_diff_batch* b) {
   L.walk.jobs = b->walkjobs.as<WalkParams<T>>(); L.walk.item_prefix = b->item_prefix.as<int>();
   L.walk.njobs = nj; L.walk.total = itemp[nj]; L.walk.stride = 1; L.walk.max_nfr = b->max_nfr;
   L.walk.work = b->work.as<int>(); L.walk.counters = b->cnt.as<unsigned long long>();
+  L.walk.list = b->list.as<unsigned short>();
   L.reduce = true;
   L.red = b->redjobs.as<RedJob<T>>(); L.ring_prefix = b->ring_prefix.as<int>(); L.line_prefix = b->line_prefix.as<int>();
   L.nring_blocks = ringp[nj]; L.nline_blocks = linep[nj];

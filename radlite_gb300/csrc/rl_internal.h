@@ -93,7 +93,7 @@ struct rl_model {
   int tab_line0 = -1, tab_nl = 0, tab_prec = -1;
   std::vector<double> tab_scale;
   // per-call buffers
-  rl::DevBuf dtab, dnsum, dwch, dvelo, dstar, dlc, dimg, dring, dflux, dscale, dcnt, dwork, derr;
+  rl::DevBuf dtab, dnsum, dwch, dvelo, dstar, dlc, dimg, dring, dflux, dscale, dcnt, dwork, derr, dlist;
 };
 
 extern thread_local std::string g_last_error;

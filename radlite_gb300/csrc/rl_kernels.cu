@@ -500,19 +500,28 @@ __device__ __forceinline__ void walk_item(const WalkParams<T>& P, int item, Warp
   __syncwarp();
 }
 
-// Per-warp shared-memory regions of the walk; `listcap` (pairs) is kGroup x the largest
-// channel count of the launch.
+// Per-warp regions of the walk: stage, slot state and SUBGRID work in shared memory;
+// the (line, channel) list of the item in a per-warp global scratch row (L1-cached) when
+// kListInSmem is false, which leaves room for four 4-warp blocks per SM. `listcap`
+// (pairs) is kGroup x the largest channel count of the launch.
+constexpr bool kListInSmem = false;
+// FP32: four blocks per SM (at most 128 registers); FP64 (the parity path) keeps its registers.
+template <typename T> struct WalkMinBlocks { static constexpr int value = sizeof(T) == 4 ? kWalkBlocksPerSm : 1; };
+
 template <typename T, int C>
 struct WarpSmem {
   WarpStage<T>* S; SlotState<T, C>* SS; SubWork<T>* SW; unsigned short* list;
-  __device__ WarpSmem(unsigned char* raw, int nw, int wib, int listcap) {
+  __device__ WarpSmem(unsigned char* raw, int nw, int wib, int listcap, unsigned short* gscratch) {
     const int capp = (listcap + 7) & ~7;
     S = reinterpret_cast<WarpStage<T>*>(raw) + wib;
     SS = reinterpret_cast<SlotState<T, C>*>(raw + sizeof(WarpStage<T>) * nw) + wib;
     SW = reinterpret_cast<SubWork<T>*>(raw + (sizeof(WarpStage<T>) + sizeof(SlotState<T, C>)) * nw) + wib;
-    list = reinterpret_cast<unsigned short*>(
-               raw + (sizeof(WarpStage<T>) + sizeof(SlotState<T, C>) + sizeof(SubWork<T>)) * nw) +
-           (size_t)wib * capp;
+    if (kListInSmem)
+      list = reinterpret_cast<unsigned short*>(
+                 raw + (sizeof(WarpStage<T>) + sizeof(SlotState<T, C>) + sizeof(SubWork<T>)) * nw) +
+             (size_t)wib * capp;
+    else
+      list = gscratch + ((size_t)blockIdx.x * nw + wib) * capp;
   }
 };
 
@@ -527,10 +536,10 @@ __device__ __forceinline__ void flush_counters(WalkCounters wc, unsigned long lo
 }
 
 template <typename T, int C>
-__global__ void __launch_bounds__(128) k_walk(WalkParams<T> P) {
+__global__ void __launch_bounds__(128, WalkMinBlocks<T>::value) k_walk(WalkParams<T> P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  WarpSmem<T, C> W(smem_raw, nw, wib, kGroup * P.nfr);
+  WarpSmem<T, C> W(smem_raw, nw, wib, kGroup * P.nfr, P.list);
   WalkCounters wc;
   for (;;) {
     int item = 0;
@@ -547,11 +556,11 @@ __global__ void __launch_bounds__(128) k_walk(WalkParams<T> P) {
 // item_prefix[j] is the first item of job j. Each warp keeps the parameters of its
 // current job in shared memory.
 template <typename T, int C>
-__global__ void __launch_bounds__(128) k_walk_jobs(WalkJobs<T> B) {
+__global__ void __launch_bounds__(128, WalkMinBlocks<T>::value) k_walk_jobs(WalkJobs<T> B) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ WalkParams<T> jp[4];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  WarpSmem<T, C> W(smem_raw, nw, wib, kGroup * B.max_nfr);
+  WarpSmem<T, C> W(smem_raw, nw, wib, kGroup * B.max_nfr, B.list);
   WalkCounters wc;
   int cur = -1;
   const int nq = (B.total + B.stride - 1) / B.stride;
@@ -726,13 +735,14 @@ static cudaError_t launch_walk_c(const WalkParams<T>& P, int nsm, cudaStream_t s
   const int warps = 4, threads = warps * 32;
   const int capp = (kGroup * P.nfr + 7) & ~7;
   const size_t smem = (sizeof(WarpStage<T>) + sizeof(SlotState<T, C>) + sizeof(SubWork<T>)) * warps +
-                      sizeof(unsigned short) * (size_t)capp * warps;
+                      (kListInSmem ? sizeof(unsigned short) * (size_t)capp * warps : 0);
   cudaError_t e = cudaFuncSetAttribute(k_walk<T, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_walk<T, C>, threads, smem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
+  if (per_sm > kWalkBlocksPerSm) per_sm = kWalkBlocksPerSm;   // the list scratch holds this many
   long long blocks = (long long)nsm * per_sm;
   const long long need = ((long long)P.nitems + warps - 1) / warps;
   if (blocks > need) blocks = need;
@@ -746,13 +756,14 @@ static cudaError_t launch_walk_jobs_c(const WalkJobs<T>& B, int nsm, cudaStream_
   const int warps = 4, threads = warps * 32;
   const int capp = (kGroup * B.max_nfr + 7) & ~7;
   const size_t smem = (sizeof(WarpStage<T>) + sizeof(SlotState<T, C>) + sizeof(SubWork<T>)) * warps +
-                      sizeof(unsigned short) * (size_t)capp * warps;
+                      (kListInSmem ? sizeof(unsigned short) * (size_t)capp * warps : 0);
   cudaError_t e = cudaFuncSetAttribute(k_walk_jobs<T, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_walk_jobs<T, C>, threads, smem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
+  if (per_sm > kWalkBlocksPerSm) per_sm = kWalkBlocksPerSm;
   long long blocks = (long long)nsm * per_sm;
   const long long nq = ((long long)B.total + B.stride - 1) / B.stride;
   const long long need = (nq + warps - 1) / warps;

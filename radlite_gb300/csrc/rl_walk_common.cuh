@@ -153,7 +153,7 @@ struct SubWork {
 template <typename T, int C>
 struct SlotState {
   T I[C][32], j0[C][32], a0[C][32], S0[C][32], w[C][32];
-  int ll[C][32];
+  signed char ll[C][32];   // line of the slot within the group, -1 = empty
 };
 
 __device__ __forceinline__ unsigned lanemask_lt() {
