@@ -52,6 +52,8 @@ struct GeoParams {
   const double* tan2;   // [nth+1]
   const double* vel;    // [ncell*3]
   const double* lw;     // [ncell]
+  const float* velf;    // [ncell*3] FP32 copies for the FP32 build's node values
+  const float* lwf;     // [ncell]
   const double* x0;     // [nrays]
   const double* z0;     // [nrays]
 };

@@ -95,6 +95,7 @@ struct TAcc { const Grid* g; RL_HD double operator()(int j) const { return Tg(*g
 struct Ray {
   double x0, z0, costh0, sinth0, costh02, sinth02, pitheta0, bimpact;
   double bnew, znew;                    // direction(): impact distance and offset in the ray plane
+  float bnew_f, znew_f, costh0_f;       // FP32 copies for direction_f
   int iy0, isnr, isdblnr, caseA, iup;   // theta crossings
   int ir_min, ir_amount, ith_amount;    // r crossings
 };
@@ -102,6 +103,7 @@ struct Ray {
 // One emitted node of the trajectory.
 struct Node {
   double s, r, th, mu, sinmu, sinphi, cosphi;   // sinmu = sqrt(1 - mu^2)
+  float mu_f, sinmu_f, sinphi_f, cosphi_f;      // the same from direction_f (FP32 node values)
   int icr, ir, it;
 };
 
@@ -121,6 +123,7 @@ RL_HD int init_ray(const Grid& g, double x0, double z0, double theta0, Ray& y) {
   y.costh02 = y.costh0 * y.costh0; y.sinth02 = y.sinth0 * y.sinth0;
   y.znew = z0 * y.sinth02;
   y.bnew = sqrt(x0 * x0 + z0 * z0 * y.sinth02);
+  y.bnew_f = (float)y.bnew; y.znew_f = (float)y.znew; y.costh0_f = (float)y.costh0;
   // theta=const cones with two crossings: contiguous suffix iy0..nth of the stored half
   int first = 0, count = 0;
   for (int iy = 1; iy <= g.nth; iy++) {
@@ -331,6 +334,43 @@ RL_HD void direction(const Ray& y, double s, double& mu, double& sinmu, double& 
   cosphi = (y.x0 < 0.0) ? c : -c;
 }
 
+// direction() in FP32 from the FP64 position along the ray: the FP32 build stores the
+// projected velocity in FP32, so its direction needs no more.
+// Every operation is spelled out (no contraction left to the compiler), so that all
+// kernels that inline it produce the same bits.
+#ifdef __CUDA_ARCH__
+#define RL_FMA(a, b, c) __fmaf_rn(a, b, c)
+#define RL_MUL(a, b) __fmul_rn(a, b)
+#define RL_ADD(a, b) __fadd_rn(a, b)
+#define RL_SUB(a, b) __fsub_rn(a, b)
+#else
+#define RL_FMA(a, b, c) fmaf(a, b, c)
+#define RL_MUL(a, b) ((a) * (b))
+#define RL_ADD(a, b) ((a) + (b))
+#define RL_SUB(a, b) ((a) - (b))
+#endif
+RL_HD void direction_f(const Ray& y, double s, float& mu, float& sinmu, float& sinphi, float& cosphi) {
+  const float snew = (float)(s + y.z0 * y.costh0);
+  const float bnew = y.bnew_f, znew = y.znew_f;
+  const float rr2 = RL_FMA(snew, snew, RL_MUL(bnew, bnew));
+  const float irad = 1.0f / sqrtf(rr2);
+  mu = fminf(1.0f, fmaxf(-1.0f, RL_MUL(snew, irad)));
+  sinmu = RL_MUL(bnew, irad);
+  const float q = RL_FMA(snew, y.costh0_f, znew);
+  const float dummy = RL_MUL(bnew, sqrtf(fmaxf(RL_FMA(-q, q, rr2), 0.0f)));
+  const float num = RL_FMA(RL_MUL(bnew, bnew), y.costh0_f, -RL_MUL(znew, snew));
+  const float sp = (dummy > 0.0f) ? num / dummy : (float)(1.0e1 * kTelEps);
+  sinphi = sp;
+  const float c = sqrtf(fmaxf(RL_FMA(-sp, sp, 1.0f), 0.0f));
+  cosphi = (y.x0 < 0.0) ? c : -c;
+}
+
+template <bool kFp32>
+RL_HD void set_direction(const Ray& y, Node& nd) {
+  if (kFp32) direction_f(y, nd.s, nd.mu_f, nd.sinmu_f, nd.sinphi_f, nd.cosphi_f);
+  else direction(y, nd.s, nd.mu, nd.sinmu, nd.sinphi, nd.cosphi);
+}
+
 // Walk the merged node sequence, calling emit(const Node&) for each accepted node.
 // Returns a GeoStatus; emit returns false to stop (buffer full).
 template <class Emit>
@@ -371,7 +411,7 @@ RL_HD int trace(const Grid& g, double x0, double z0, double theta0, Emit& emit) 
       if (E.r[ie] <= rmaxt && E.r[ie] >= rmint && (E.s[ie] - sprev) > kTelEps * E.r[ie] &&
           E.s[ie] >= sbeg && E.s[ie] <= send) {
         nd.icr = 3; nd.r = E.r[ie]; nd.th = E.th[ie]; nd.ir = E.ir[ie]; nd.it = E.it[ie]; nd.s = E.s[ie];
-        direction(y, nd.s, nd.mu, nd.sinmu, nd.sinphi, nd.cosphi);
+        set_direction<Emit::kFp32Direction>(y, nd);
         sprev = nd.s;
         if (!emit(nd)) return kGeoOverflow;
       }
@@ -383,7 +423,7 @@ RL_HD int trace(const Grid& g, double x0, double z0, double theta0, Emit& emit) 
         if (thr < Rg(g, 1)) nd.ir = 0;
         else if (thr > Rg(g, g.nr)) nd.ir = g.nr;
         else { ixg = hunt(racc, g.nr, thr, ixg); nd.ir = ixg; }
-        direction(y, nd.s, nd.mu, nd.sinmu, nd.sinphi, nd.cosphi);
+        set_direction<Emit::kFp32Direction>(y, nd);
         sprev = nd.s;
         if (!emit(nd)) return kGeoOverflow;
       }
@@ -393,7 +433,7 @@ RL_HD int trace(const Grid& g, double x0, double z0, double theta0, Emit& emit) 
       if (rr <= rmaxr && rr >= rminr && (rs - sprev) > kTelEps * rr && rs >= sbeg && rs <= send) {
         nd.icr = 1; nd.r = rr; nd.th = theta_at(y, rs); nd.ir = rix; nd.s = rs;
         iyg = hunt(tacc, g.ny, nd.th, iyg); nd.it = iyg;
-        direction(y, nd.s, nd.mu, nd.sinmu, nd.sinphi, nd.cosphi);
+        set_direction<Emit::kFp32Direction>(y, nd);
         sprev = nd.s;
         if (!emit(nd)) return kGeoOverflow;
       }

@@ -32,6 +32,10 @@ __device__ __forceinline__ int ridx_dev(int it, int ny) {
 
 template <typename T>
 struct NodeEmitter {
+  // The FP32 build stores every node value in FP32, so it forms the direction, the
+  // projected velocity, the interpolation weights and the width in FP32 from the FP64
+  // positions and cell differences; the FP64 build does all of it in FP64.
+  static constexpr bool kFp32Direction = sizeof(T) == 4;
   const GeoParams* p;
   const rlg::Grid* g;
   NodeBuf<T>* nb;
@@ -40,9 +44,11 @@ struct NodeEmitter {
   int k, status;
   int ir_prev, icr_prev;
   double s_prev, dvmu_prev;
+  float dvmu_prev_f;
 
   __device__ bool operator()(const rlg::Node& n) {
     if (k >= nb->kmax) return false;
+    if constexpr (sizeof(T) == 4) return emit_fp32(n);
     const int nr = p->nr, nth = p->nth, ny = p->ny;
     const double R0 = rlg::Rg(*g, n.ir), R1 = rlg::Rg(*g, n.ir + 1);
     const double T0 = rlg::Tg(*g, n.it), T1 = rlg::Tg(*g, n.it + 1);
@@ -93,6 +99,57 @@ struct NodeEmitter {
     k++;
     return true;
   }
+
+  __device__ bool emit_fp32(const rlg::Node& n) {
+    const int nr = p->nr, nth = p->nth, ny = p->ny;
+    const double R0 = rlg::Rg(*g, n.ir), R1 = rlg::Rg(*g, n.ir + 1);
+    const double T0 = rlg::Tg(*g, n.it), T1 = rlg::Tg(*g, n.it + 1);
+    const float dr = (float)(n.r - R0) / (float)(R1 - R0);
+    const float dt = (float)(n.th - T0) / (float)(T1 - T0);
+    if (!(dr >= 0.0f && dr <= 1.0f) || !(dt >= 0.0f && dt <= 1.0f)) { status = rlg::kGeoRange; return false; }
+    if (k == 0 && n.ir == 0) { status = rlg::kGeoStarStart; return false; }
+    int r1;
+    if (dr > 0.0f) { r1 = n.ir + 1; if (r1 > nr) r1 = nr; } else { r1 = n.ir - 1; if (r1 < 1) r1 = 1; }
+    const int t0 = ridx_dev(n.it, ny);
+    const int t1 = ridx_dev(dt > 0.0f ? n.it + 1 : n.it - 1, ny);
+    const int c00 = (n.ir - 1) * nth + (t0 - 1);
+    const int dto = t1 - t0, dro = r1 - n.ir;
+    const int c01 = c00 + dto, c10 = c00 + dro * nth, c11 = c10 + dto;
+    const float ar = RL_SUB(1.0f, dr), at = RL_SUB(1.0f, dt);
+    // bilinear form with every rounding fixed (RL_FMA/RL_MUL), identical in every kernel
+    auto bil = [&](float f00, float f01, float f10, float f11) {
+      return RL_FMA(dr, RL_FMA(dt, f11, RL_MUL(at, f10)), RL_MUL(ar, RL_FMA(dt, f01, RL_MUL(at, f00))));
+    };
+    float v[3];
+    for (int i = 0; i < 3; i++)
+      v[i] = bil(p->velf[3 * c00 + i], p->velf[3 * c01 + i], p->velf[3 * c10 + i], p->velf[3 * c11 + i]);
+    const float lwv = bil(p->lwf[c00], p->lwf[c01], p->lwf[c10], p->lwf[c11]);
+    const float tang = RL_FMA(v[1], n.sinphi_f, RL_MUL(v[2], n.cosphi_f));
+    const float dvmu = RL_MUL(3.335668e-11f, RL_FMA(n.mu_f, v[0], RL_MUL(n.sinmu_f, tang)));
+    const float kv = (float)(1.0 / 3.33567e-6);
+    unsigned flags = 0;
+    double ds = 0.0;
+    if (k > 0) {
+      ds = n.s - s_prev;
+      const bool hole = (n.ir == 1 && ir_prev == 1 && n.icr == 1 && icr_prev == 1) ||
+                        (n.ir == 1 && ir_prev == 0 && n.icr == 1 && icr_prev == 1);
+      if (hole) { flags |= kFlagHole; ds = 0.0; }
+    }
+    if (n.ir <= 1) flags |= kFlagIr1;
+    const size_t o = row + k;
+    nb->ds[o] = (T)ds;
+    nb->dvf[o] = dvmu;
+    nb->vl[o] = (T)RL_MUL(dvmu, kv);
+    nb->dvseg[o] = (T)(k > 0 ? RL_MUL(RL_SUB(dvmu, dvmu_prev_f), kv) : 0.0f);
+    nb->lw[o] = (T)lwv;
+    nb->wr[o] = (T)dr;
+    nb->wt[o] = (T)dt;
+    nb->c00[o] = c00;
+    nb->misc[o] = (unsigned)(dto + 32768) | ((unsigned)(dro + 1) << 16) | ((unsigned)n.icr << kIcrShift) | flags;
+    s_prev = n.s; dvmu_prev_f = dvmu; ir_prev = n.ir; icr_prev = n.icr;
+    k++;
+    return true;
+  }
 };
 
 template <typename T>
@@ -102,6 +159,7 @@ __device__ __forceinline__ void geometry_ray(const GeoParams& p, NodeBuf<T>& nb,
   NodeEmitter<T> em;
   em.p = &p; em.g = &g; em.nb = &nb; em.dbg = dbg; em.row = (size_t)ray * nb.kmax;
   em.k = 0; em.status = 0; em.ir_prev = -1; em.icr_prev = -1; em.s_prev = 0.0; em.dvmu_prev = 0.0;
+  em.dvmu_prev_f = 0.0f;
   int st = rlg::trace(g, p.x0[ray], p.z0[ray], p.theta0, em);
   if (em.status != 0) st = em.status;
   nb.nnodes[ray] = em.k;

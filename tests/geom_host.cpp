@@ -6,6 +6,7 @@
 
 namespace {
 struct Collect {
+  static constexpr bool kFp32Direction = false;
   int cap, n;
   double *s, *r, *th, *mu;
   int *icr, *ir, *it;
