@@ -111,8 +111,28 @@ int rl_spectra(rl_model* model, int iline0, int nlines, double* flux_out, rl_sta
    rings from the inside out, azimuth fastest), as imcir_int. */
 int rl_line_image(rl_model* model, int iline, double* image_out, rl_stats* stats);
 
-/* The RADlite executable's work in `dir`: read the inputs, render the lines requested by
-   linespectrum.inp, write linespectrum_<mol>.dat and radlite.success. */
+/* ---- Position-velocity cube (linespectrum.inp command 2): the rectangular image of
+   setup_rays_rectang / make_freq_image_rectang / calc_write_line_posvel
+   (telescope.F:1828-2475). The request is read from a command-2 linespectrum.inp by
+   rl_load_dir, or set here; the camera inclination is the model's (rl_set_camera). */
+typedef struct rl_posvel_spec {
+  int nx, ny;                  /* pixels, both even (imr_nx, imr_ny) */
+  double szimx, szimy;         /* full image size [cm] as in the file (size specifier 1) */
+  double phioff;               /* image rotation [rad] */
+  double xoff, yoff;           /* image offsets [cm] */
+  int addstar;                 /* > 0: add the unresolved star to the four central pixels */
+} rl_posvel_spec;
+int rl_set_posvel(rl_model* model, const rl_posvel_spec* spec);
+int rl_get_posvel(rl_model* model, rl_posvel_spec* spec);
+/* Lines iline0 .. iline0+nlines-1: I_out and tau_out (either may be NULL) receive
+   [nlines][nfr][ny][nx] intensity [erg/s/cm^2/Hz/ster] and line-of-sight optical depth,
+   as imrec_int and imrec_tau (per channel, iy outer, ix inner: the file's order). */
+int rl_posvel(rl_model* model, int iline0, int nlines, double* I_out, double* tau_out, rl_stats* stats);
+
+/* The RADlite executable's work in `dir`: read the inputs and render the lines requested
+   by linespectrum.inp (starting at line 1, main.F:204). Command 0 writes
+   linespectrum_<mol>.dat (main.F:1034-1049), command 2 one lineposvel_<mol>_<iline>.dat
+   per line (main.F:1061-1074); both then write radlite.success. */
 int rl_run_dir(const char* dir, int device, rl_stats* stats);
 
 /* Node list of one ray as the geometry kernel produces it (inspection and tests):

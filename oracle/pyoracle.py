@@ -36,9 +36,13 @@ def lib():
         L.rlo_info.argtypes = [vp, _I, _D]
         L.rlo_rays.argtypes = [vp, _D, _D, _D, _D]
         L.rlo_trajectory.argtypes = [vp, C.c_int, C.c_int, _D, _D, _D, _D, _D, _I, _I, _I]
+        L.rlo_ray_spectrum.argtypes = [vp, C.c_int, C.c_double, C.c_double, _D, _D]
         L.rlo_line_image.argtypes = [vp, C.c_int, C.c_int, C.c_int, _D, C.POINTER(C.c_ubyte), C.POINTER(C.c_longlong)]
         L.rlo_image_to_spectrum.argtypes = [vp, _D, _D]
         L.rlo_line_spectrum.argtypes = [vp, C.c_int, _D, _D, C.POINTER(C.c_longlong)]
+        L.rlo_pv_request.argtypes = [vp, _I, _D]
+        L.rlo_pv_rays.argtypes = [vp, C.c_int, C.c_int] + [C.c_double] * 5 + [C.c_int, _D, _D, _D, _I, _D]
+        L.rlo_posvel.argtypes = [vp, C.c_int, C.c_int, C.c_int] + [C.c_double] * 5 + [C.c_int, _D, _D]
         L.rlo_run_dir.argtypes = [C.c_char_p]
         _lib = L
     return _lib
@@ -63,6 +67,12 @@ class Oracle:
         (self.nr, self.nth, self.nlines_spec, self.ilinestart, self.nfr, self.nrays, self.nphi, self.nrr,
          self.nlines_mol, self.nlev) = (int(x) for x in iv)
         self.incl_rad, self.vmax, self.rstar, self.aksmax, self.theta0 = (float(x) for x in dv)
+        pi = np.zeros(4, dtype=np.int32)
+        pd = np.zeros(5)
+        lib().rlo_pv_request(self.h, pi.ctypes.data_as(_I), _dp(pd))
+        self.command = int(pi[0])
+        self.pv = dict(nx=int(pi[1]), ny=int(pi[2]), szimx=float(pd[0]), szimy=float(pd[1]), phioff=float(pd[2]),
+                       xoff=float(pd[3]), yoff=float(pd[4]), addstar=int(pi[3]))
 
     def __del__(self):
         if getattr(self, "h", None):
@@ -97,6 +107,37 @@ class Oracle:
         if rc != 0:
             raise OracleError(lib().rlo_last_error().decode())
         return img, mask, {"steps": int(cnt[0]), "integrated": int(cnt[1]), "node_visits": int(cnt[2])}
+
+    def ray_spectrum(self, iline: int, x0: float, z0: float):
+        """I and the line-of-sight optical depth of every channel along one ray (x0, z0):
+        one pixel of the rectangular (position-velocity) image."""
+        I, tau = np.zeros(self.nfr), np.zeros(self.nfr)
+        rc = lib().rlo_ray_spectrum(self.h, iline, float(x0), float(z0), _dp(I), _dp(tau))
+        if rc != 0:
+            raise OracleError(lib().rlo_last_error().decode())
+        return I, tau
+
+    def pv_rays(self, nx, ny, szimx, szimy, phioff=0.0, xoff=0.0, yoff=0.0, addstar=0):
+        """Pixel rays of the rectangular camera: x0, z0, b [nx*ny] (ix outer, iy inner) and
+        (starunres, spx, spy, srat, theta0)."""
+        n = nx * ny
+        x0, z0, b = np.zeros(n), np.zeros(n), np.zeros(n)
+        iv = np.zeros(1, dtype=np.int32)
+        dv = np.zeros(4)
+        rc = lib().rlo_pv_rays(self.h, nx, ny, szimx, szimy, phioff, xoff, yoff, addstar, _dp(x0), _dp(z0), _dp(b),
+                               iv.ctypes.data_as(_I), _dp(dv))
+        if rc != 0:
+            raise OracleError(lib().rlo_last_error().decode())
+        return x0, z0, b, (int(iv[0]), *(float(v) for v in dv))
+
+    def posvel(self, iline, nx, ny, szimx, szimy, phioff=0.0, xoff=0.0, yoff=0.0, addstar=0):
+        """Intensity and optical-depth cube [nfr, ny, nx] of one line."""
+        I = np.zeros((self.nfr, ny, nx))
+        tau = np.zeros((self.nfr, ny, nx))
+        rc = lib().rlo_posvel(self.h, iline, nx, ny, szimx, szimy, phioff, xoff, yoff, addstar, _dp(I), _dp(tau))
+        if rc != 0:
+            raise OracleError(lib().rlo_last_error().decode())
+        return I, tau
 
     def image_to_spectrum(self, img):
         flux = np.zeros(self.nfr)

@@ -218,6 +218,8 @@ struct rlo_model {
     /* camera & passband */
     double incl_rad; int nphi, dbdr, nrext;
     double vmax, dv, radvelo; int nlspec, ilstart, style, nfr;
+    int command;                                   /* 0 spectrum, 2 position-velocity cube */
+    int pv_nx, pv_ny, pv_addstar; double pv_szx, pv_szy, pv_phioff, pv_xoff, pv_yoff;
     char molname[96], molfile[200];
     double aksmax;
     /* rays */
@@ -475,7 +477,15 @@ static int read_model(const char* dir, rlo_model* m) {
         size_t nlen = (size_t)(d - s); memcpy(m->molname, s, nlen); m->molname[nlen] = 0;
         if (rd_i(&f, &cmd) || rd_d(&f, &dist) || rd_d(&f, &inc) || rd_d(&f, &m->radvelo) ||
             rd_i(&f, &m->nlspec) || rd_i(&f, &m->ilstart)) return -1;
-        if (cmd != 0) return fail("linespectrum.inp: only the line-spectrum command (0) is supported");
+        if (cmd != 0 && cmd != 2) return fail("linespectrum.inp: command %d not supported", cmd);
+        m->command = cmd;
+        if (cmd == 2) {   /* telescope.F:190-218 */
+            int sizespec;
+            if (rd_i(&f, &m->pv_nx) || rd_i(&f, &m->pv_ny) || rd_i(&f, &sizespec) || rd_d(&f, &m->pv_szx) ||
+                rd_d(&f, &m->pv_szy) || rd_d(&f, &m->pv_phioff) || rd_d(&f, &m->pv_xoff) || rd_d(&f, &m->pv_yoff) ||
+                rd_i(&f, &m->pv_addstar)) return -1;
+            if (sizespec != 1) return fail("linespectrum.inp: size specifier %d not supported", sizespec);
+        }
         m->incl_rad = inc * 0.0174532925199;
         fr_close(&f);
     }
@@ -518,6 +528,7 @@ static int read_model(const char* dir, rlo_model* m) {
             if (m->lfreq[i] == 0.0) return fail("moldata: zero line frequency");
         }
         if (m->ilstart < 1 || m->ilstart + m->nlspec - 1 > m->nlin) return fail("linespectrum.inp: non-existing line requested");
+        m->ilstart = 1;   /* main.F:204: the run starts at line 1 whatever the file asked */
     }
     /* line.inp per-line blocks are consumed by the reference but only feed unused options */
     /* level populations (line.F:811-950) */
@@ -933,6 +944,7 @@ typedef struct {
     double* dnu;   /* [1..nfr] */
     double* star;  /* [1..nfr] */
     long long steps;
+    double tau;        /* char_tau: running optical depth of the current (ray, channel), line.F:4598 */
 } linectx;
 
 static int node_values(const linectx* L, int icr, int ir, int it, double dr, double dt, double mu, double phi,
@@ -1025,6 +1037,7 @@ static void integrate_el(linectx* L, int inu, double* I, double ds, double sd0, 
     double alpl1 = 5.27296241956e-28 * L->lfreq * phi1 * (nd1 * L->Bdu - nu1 * L->Bud);
     double src0 = sd0 + st->srcl0, src1 = sd1 + srcl1, alp0 = ad0 + st->alpl0, alp1 = ad1 + alpl1;
     *I = qdr_src_2(*I, src0, alp0, src1, alp1, ds);
+    L->tau = L->tau + 0.5 * (alp0 + alp1) * ds;
     st->phiprof0 = phi1; st->srcl0 = srcl1; st->alpl0 = alpl1; st->init = 0;
     L->steps++;
 }
@@ -1143,6 +1156,14 @@ int rlo_load_dir(const char* dir, rlo_model** out) {
     *out = m; return 0;
 }
 
+/* command and rectangular-image request of linespectrum.inp: iv = command, nx, ny, addstar;
+   dv = szx, szy, phioff, xoff, yoff */
+int rlo_pv_request(const rlo_model* m, int* iv, double* dv) {
+    iv[0] = m->command; iv[1] = m->pv_nx; iv[2] = m->pv_ny; iv[3] = m->pv_addstar;
+    dv[0] = m->pv_szx; dv[1] = m->pv_szy; dv[2] = m->pv_phioff; dv[3] = m->pv_xoff; dv[4] = m->pv_yoff;
+    return 0;
+}
+
 int rlo_info(const rlo_model* m, int* info, double* dinfo) {
     info[0] = m->nr; info[1] = m->nth; info[2] = m->nlspec; info[3] = m->ilstart; info[4] = m->nfr;
     info[5] = m->nrays; info[6] = m->nphi; info[7] = m->nrr; info[8] = m->nlin; info[9] = m->nlev;
@@ -1225,6 +1246,107 @@ int rlo_line_image(rlo_model* m, int iline, int ray_begin, int ray_end, double* 
     return rc;
 }
 
+/* Every channel of one ray (x0, z0) at the camera's inclination, without the NONREDUNDANT
+   window and without central-star mixing: one pixel of the rectangular image
+   (make_freq_image_rectang, telescope.F:2061-2150; charintline with rbeam 0). I and the
+   line-of-sight optical depth char_tau per channel. */
+int rlo_ray_spectrum(rlo_model* m, int iline, double x0, double z0, double* I_out, double* tau_out) {
+    if (iline < 1 || iline > m->nlin) return fail("line index out of range");
+    linectx L; line_ctx(m, iline, &L);
+    traj_t T; memset(&T, 0, sizeof T);
+    int rc = trajectory(m, x0, z0, m->theta0, &T);
+    for (int k = 1; k <= m->nfr && !rc; k++) {
+        float minv = 1.0f, maxv = -1.0f;
+        L.tau = 0.0;
+        rc = charint(&L, &T, k, 0.0, &minv, &maxv, &I_out[k - 1]);
+        if (tau_out) tau_out[k - 1] = L.tau;
+    }
+    traj_free(&T);
+    free(L.dnu); free(L.star);
+    return rc;
+}
+
+/* Rectangular camera (setup_rays_rectang, telescope.F:2229-2475) of the request
+   (nx, ny, szx, szy, phioff, xoff, yoff, addstar): pixel rays in the reference's order
+   (ix outer, iy inner), x0/z0/b of [nx*ny]. info[0] = 1 when the unresolved star is added;
+   dinfo: spx, spy, srat, theta0. */
+int rlo_pv_rays(const rlo_model* m, int nx, int ny, double szx, double szy, double phioff, double xoff, double yoff,
+                int addstar, double* x0, double* z0, double* b, int* info, double* dinfo) {
+    if (nx < 2 || ny < 2 || nx % 2 || ny % 2) return fail("rectangular image: nx, ny must be even");
+    double spx = (szx * 0.5) / (nx * 0.5), spy = (szy * 0.5) / (ny * 0.5);
+    if (!(spx > 0.0) || !(spy > 0.0)) return fail("rectangular image: pixel size must be positive");
+    if (addstar > 0 && (xoff != 0.0 || yoff != 0.0)) return fail("rectangular image: star needs zero offsets");
+    double anginf = m->incl_rad;
+    if (anginf < 1.0e-1) anginf = (double)0.1f;
+    double theta0 = anginf + 1.0e-4, sinth0 = sin(theta0);
+    int ir = 0;
+    for (int ix = 1; ix <= nx; ix++) {
+        for (int iy = 1; iy <= ny; iy++) {
+            double x_c = (ix - nx / 2 - 0.5) * spx - xoff;
+            double y_c = (iy - ny / 2 - 0.5) * spy - yoff;
+            double r_c = sqrt(x_c * x_c + y_c * y_c);
+            if (x_c == 0.0) x_c = x_c + 0.001 * spx;
+            double p_c = atan(y_c / x_c) - phioff;
+            if (x_c < 0.0) p_c = p_c + 3.14159265359;
+            while (p_c < 0.0) p_c = p_c + 6.28318530718;
+            while (p_c >= 6.28318530718) p_c = p_c - 6.28318530718;
+            double zh0 = -sin(p_c) / sinth0;
+            double dum = 1.0 - zh0 * zh0 * sinth0 * sinth0 + 1e-4;
+            double xh0 = cos(p_c) > 0.0 ? sqrt(dum) : -sqrt(dum);
+            x0[ir] = r_c * xh0; z0[ir] = r_c * zh0; b[ir] = r_c;
+            ir++;
+        }
+    }
+    info[0] = addstar > 0 && spx * spx + spy * spy > m->rstar * m->rstar;
+    dinfo[0] = spx; dinfo[1] = spy;
+    dinfo[2] = (3.14159265 * (m->rstar * m->rstar)) / (4.0 * spx * spy);
+    dinfo[3] = theta0;
+    return 0;
+}
+
+/* The position-velocity cube of one line (make_freq_image_rectang, telescope.F:2061-2206):
+   I and tau of [nfr][ny][nx] (per channel, iy outer, ix inner). */
+int rlo_posvel(rlo_model* m, int iline, int nx, int ny, double szx, double szy, double phioff, double xoff,
+               double yoff, int addstar, double* I, double* tau) {
+    if (iline < 1 || iline > m->nlin) return fail("line index out of range");
+    int npix = nx * ny, info[1]; double dinfo[4];
+    double* x0 = (double*)malloc(sizeof(double) * (size_t)npix * 3);
+    if (!x0) return fail("out of memory");
+    double *z0 = x0 + npix, *b = z0 + npix;
+    int rc = rlo_pv_rays(m, nx, ny, szx, szy, phioff, xoff, yoff, addstar, x0, z0, b, info, dinfo);
+    double theta_saved = m->theta0;
+    m->theta0 = dinfo[3];
+    double rmax = RG(m, m->nr);
+    int nfr = m->nfr;
+    double *Ir = (double*)malloc(sizeof(double) * nfr * 2), *tr = Ir + nfr;
+    for (int ix = 1; ix <= nx && !rc; ix++) {
+        for (int iy = 1; iy <= ny && !rc; iy++) {
+            int r = (ix - 1) * ny + (iy - 1);
+            if (b[r] < 0.999 * rmax) rc = rlo_ray_spectrum(m, iline, x0[r], z0[r], Ir, tr);
+            else for (int k = 0; k < nfr; k++) { Ir[k] = 0.0; tr[k] = 0.0; }
+            for (int k = 0; k < nfr; k++) {
+                size_t o = ((size_t)k * ny + (iy - 1)) * nx + (ix - 1);
+                I[o] = Ir[k]; tau[o] = tr[k];
+            }
+        }
+    }
+    if (!rc && info[0]) {   /* the unresolved star over the four central pixels */
+        double srat = dinfo[2], srat1 = 1.0 - srat;
+        rc = rlo_ray_spectrum(m, iline, 0.0, 0.0, Ir, tr);
+        for (int k = 0; k < nfr && !rc; k++) {
+            double dummy = Ir[k] * srat;
+            for (int dx = 0; dx < 2; dx++)
+                for (int dy = 0; dy < 2; dy++) {
+                    size_t o = ((size_t)k * ny + (ny / 2 - 1 + dy)) * nx + (nx / 2 - 1 + dx);
+                    I[o] = dummy + srat1 * I[o];
+                }
+        }
+    }
+    m->theta0 = theta_saved;
+    free(Ir); free(x0);
+    return rc;
+}
+
 /* image -> F_nu at 1 pc (telescope.F:1320-1437). image covers all rays. */
 int rlo_image_to_spectrum(const rlo_model* m, const double* image, double* flux) {
     int nfr = m->nfr, nphi = m->nphi;
@@ -1291,6 +1413,7 @@ int rlo_run_dir(const char* dir) {
     rlo_model* m;
     if (rlo_load_dir(dir, &m)) return -1;
     if (m->style != 1) { rlo_free(m); return fail("only output style 1 (F_nu) is supported without a beam"); }
+    if (m->command != 0) { rlo_free(m); return fail("the oracle's run writes line spectra (command 0) only"); }
     char path[1024]; snprintf(path, sizeof path, "%s/linespectrum_%s.dat", dir, m->molname);
     FILE* fp = fopen(path, "w");
     if (!fp) { rlo_free(m); return fail("cannot write %s", path); }

@@ -12,10 +12,16 @@ int rlo_info(const rlo_model* m, int* info, double* dinfo);
 int rlo_rays(const rlo_model* m, double* x0, double* z0, double* rays_r, double* ri);
 int rlo_trajectory(const rlo_model* m, int iray, int maxn, double* s, double* r, double* th, double* mu,
                    double* phi, int* icr, int* ir, int* it);
+int rlo_ray_spectrum(rlo_model* m, int iline, double x0, double z0, double* I_out, double* tau_out);
 int rlo_line_image(rlo_model* m, int iline, int ray_begin, int ray_end, double* image, unsigned char* mask,
                    long long* counts);
 int rlo_image_to_spectrum(const rlo_model* m, const double* image, double* flux);
 int rlo_line_spectrum(rlo_model* m, int iline, double* flux, double* velo_kms, long long* counts);
+int rlo_pv_request(const rlo_model* m, int* iv, double* dv);
+int rlo_pv_rays(const rlo_model* m, int nx, int ny, double szx, double szy, double phioff, double xoff, double yoff,
+                int addstar, double* x0, double* z0, double* b, int* info, double* dinfo);
+int rlo_posvel(rlo_model* m, int iline, int nx, int ny, double szx, double szy, double phioff, double xoff,
+               double yoff, int addstar, double* I, double* tau);
 int rlo_run_dir(const char* dir);
 #ifdef __cplusplus
 }

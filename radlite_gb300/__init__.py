@@ -68,6 +68,14 @@ class ModelArrays(C.Structure):
                 ("molname", C.c_char_p)]
 
 
+class PosvelSpec(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("szimx", C.c_double), ("szimy", C.c_double),
+                ("phioff", C.c_double), ("xoff", C.c_double), ("yoff", C.c_double), ("addstar", C.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 EXPORTS = ["rl_create", "rl_destroy", "rl_last_error", "rl_load_dir", "rl_load_arrays", "rl_model_free",
            "rl_model_get_info", "rl_set_camera", "rl_set_precision", "rl_line_spectrum", "rl_spectra",
            "rl_line_image", "rl_run_dir", "rl_debug_trajectory", "rl_measure_peaks",
@@ -78,7 +86,7 @@ EXPORTS = ["rl_create", "rl_destroy", "rl_last_error", "rl_load_dir", "rl_load_a
            "rl_diff_backward", "rl_diff_batch_create", "rl_diff_batch_destroy", "rl_diff_batch_add",
            "rl_diff_batch_use_graph", "rl_diff_batch_buffers", "rl_diff_batch_layout", "rl_diff_batch_forward",
            "rl_diff_batch_backward",
-           "rl_image_to_spectrum_noalloc"]
+           "rl_image_to_spectrum_noalloc", "rl_set_posvel", "rl_get_posvel", "rl_posvel"]
 
 _lib = None
 
@@ -104,6 +112,9 @@ def lib():
         L.rl_spectra.argtypes = [vp, C.c_int, C.c_int, _D, C.POINTER(Stats)]
         L.rl_line_image.argtypes = [vp, C.c_int, _D, C.POINTER(Stats)]
         L.rl_run_dir.argtypes = [C.c_char_p, C.c_int, C.POINTER(Stats)]
+        L.rl_set_posvel.argtypes = [vp, C.POINTER(PosvelSpec)]
+        L.rl_get_posvel.argtypes = [vp, C.POINTER(PosvelSpec)]
+        L.rl_posvel.argtypes = [vp, C.c_int, C.c_int, _D, _D, C.POINTER(Stats)]
         L.rl_debug_trajectory.argtypes = [vp, C.c_int, C.c_int, _D, _D, _D, _D, _D, _I, _I, _I]
         L.rl_measure_peaks.argtypes = [vp, _D, _D]
         L.rl_batch_create.argtypes = [vp, C.c_int, C.POINTER(vp)]
@@ -284,6 +295,28 @@ class Model:
         st = Stats()
         _check(lib().rl_line_image(self.h, iline, _dp(img), C.byref(st)), self._ch)
         return img
+
+    def set_posvel(self, nx: int, ny: int, szimx: float, szimy: float, phioff: float = 0.0, xoff: float = 0.0,
+                   yoff: float = 0.0, addstar: int = 1):
+        """The rectangular image of linespectrum.inp command 2: nx x ny pixels (even) over a
+        full image size szimx x szimy [cm], rotation phioff [rad], offsets [cm]."""
+        sp = PosvelSpec(nx, ny, szimx, szimy, phioff, xoff, yoff, addstar)
+        _check(lib().rl_set_posvel(self.h, C.byref(sp)), self._ch)
+
+    def posvel_spec(self) -> dict:
+        sp = PosvelSpec()
+        _check(lib().rl_get_posvel(self.h, C.byref(sp)), self._ch)
+        return sp.as_dict()
+
+    def posvel(self, iline0: int, nlines: int = 1, stats: bool = False):
+        """Intensity and optical-depth cubes [nlines, nfr, ny, nx] of the position-velocity
+        image (imrec_int, imrec_tau)."""
+        sp = self.posvel_spec()
+        shape = (nlines, self.info()["nfr"], sp["ny"], sp["nx"])
+        I, tau = np.zeros(shape), np.zeros(shape)
+        st = Stats()
+        _check(lib().rl_posvel(self.h, iline0, nlines, _dp(I), _dp(tau), C.byref(st)), self._ch)
+        return (I, tau, st.as_dict()) if stats else (I, tau)
 
     def trajectory(self, iray: int, cap: int = 8192) -> dict:
         out = {k: np.zeros(cap) for k in ("s", "r", "theta", "mu", "dvmu")}
@@ -580,6 +613,46 @@ def run_manifest(path: str, device: int = 0) -> dict:
     if rc < 0:
         raise RLError(_err())
     return st.as_dict()
+
+
+def _fnum(txt: str) -> float:
+    """A Fortran E/ES field (the 'E' is dropped for three-digit exponents)."""
+    t = txt.strip()
+    if "E" not in t and "e" not in t:
+        for i in range(len(t) - 1, 0, -1):
+            if t[i] in "+-" and t[i - 1].isdigit():
+                t = t[:i] + "E" + t[i:]
+                break
+    return float(t)
+
+
+def read_posvel_file(path: str) -> dict:
+    """Parse lineposvel_<mol>_<iline>.dat (the reference's position-velocity layout,
+    telescope.F:1965-2016): header fields, velocities [nfr], and the per-channel images of
+    3.25465503368e36 I / nu0^2 ("temp") and optical depth ("tau"), each [nfr, ny, nx]."""
+    with open(path) as fh:
+        L = fh.read().split("\n")
+    h = {"version": int(L[1]), "molname": L[2].strip(), "molfile": L[3].strip()}
+    h["distance_pc"], h["radvelo"], h["incl_deg"] = _fnum(L[4][0:12]), _fnum(L[4][12:24]), float(L[4][24:31])
+    h["up"], h["low"] = int(L[5][0:5]), int(L[5][5:10])
+    h["freq"] = _fnum(L[6])
+    nfr = h["nfr"] = int(L[7])
+    g = L[8]
+    nx, ny = int(g[0:5]), int(g[5:10])
+    h.update(nx=nx, ny=ny, spx=_fnum(g[10:22]), spy=_fnum(g[22:34]), phioff=float(g[34:41]), xoff=_fnum(g[41:53]),
+             yoff=_fnum(g[53:65]))
+    i = 10
+    h["velo"] = np.array([_fnum(L[i + k]) for k in range(nfr)])
+    i += nfr + 1
+    temp = np.zeros((nfr, ny, nx))
+    tau = np.zeros((nfr, ny, nx))
+    for k in range(nfr):
+        rows = L[i:i + nx * ny]
+        temp[k] = np.array([_fnum(r[0:12]) for r in rows]).reshape(ny, nx)
+        tau[k] = np.array([_fnum(r[13:25]) for r in rows]).reshape(ny, nx)
+        i += nx * ny + 1
+    h["temp"], h["tau"] = temp, tau
+    return h
 
 
 def read_spectrum_file(path: str):

@@ -13,7 +13,7 @@ OUT = os.path.join(HERE, "_lib")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-lineinfo"]
 SOURCES = ["rl_kernels.cu", "rl_adjoint.cu", "rl_host.cpp", "rl_capi.cpp", "rl_batch.cpp", "rl_diff.cpp",
-           "rl_noalloc.cu"]
+           "rl_noalloc.cu", "rl_posvel.cu"]
 
 
 def nvcc() -> str:

@@ -584,6 +584,11 @@ int rl_run_manifest(const char* manifest, int device, rl_stats* st) {
     rc = rl_load_dir(ctx, dirs[i].c_str(), &models[i]);
     if (rc) { set_err(ctx, rc, dirs[i] + ": " + ctx->err); break; }
     const Model& m = models[i]->m;
+    if (m.command != 0) {
+      rc = set_err(ctx, RL_ERR_ARG, dirs[i] + ": a batch renders line spectra (command 0); run position-velocity "
+                                              "directories one by one");
+      break;
+    }
     const int job = rl_batch_add(b, models[i], m.ilstart, m.nlspec);
     if (job < 0) rc = job;
   }

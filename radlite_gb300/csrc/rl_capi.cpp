@@ -318,6 +318,7 @@ int rl_load_dir(rl_ctx* ctx, const char* dir, rl_model** out) {
   std::string err;
   if (load_dir(dir, md->m, err)) return set_err(ctx, RL_ERR_IO, err);
   camera_defaults(md.get());
+  md->pvspec = md->m.pv;
   *out = md.release();
   return 0;
 }
@@ -493,7 +494,36 @@ int rl_run_dir(const char* dir, int device, rl_stats* st) {
   if (rc) return rc;
   rl_model* md = nullptr;
   rc = rl_load_dir(ctx, dir, &md);
-  if (rc == 0) {
+  if (rc == 0 && md->m.command == 2) {
+    // one lineposvel file per line (main.F:1061-1074); lines in chunks of at most 2 GB of
+    // cube per array
+    const Model& m = md->m;
+    if (st) std::memset(st, 0, sizeof *st);
+    PVCamera pc;
+    std::string err;
+    if (setup_pv_camera(m, md->pvspec, md->incl_rad, pc, err)) rc = set_err(ctx, RL_ERR_ARG, err);
+    const size_t per_line = (size_t)m.nfr * pc.nx * pc.ny;
+    const int chunk = rc ? 1 : (int)std::max<size_t>(1, std::min<size_t>(m.nlspec, (size_t)(2u << 30) / (8 * per_line + 1)));
+    std::vector<double> I, tau;
+    for (int l0 = 0; l0 < m.nlspec && rc == 0; l0 += chunk) {
+      const int nl = std::min(chunk, m.nlspec - l0);
+      I.resize(per_line * nl);
+      tau.resize(per_line * nl);
+      rc = dispatch_posvel(md, m.ilstart + l0, nl, I.data(), tau.data(), st);
+      for (int l = 0; l < nl && rc == 0; l++) {
+        const int iline = m.ilstart + l0 + l;
+        const std::string name = posvel_file_name(m, iline);
+        if (name.empty()) { rc = set_err(ctx, RL_ERR_ARG, "position-velocity file names stop at line 99"); break; }
+        if (write_posvel_file(std::string(dir) + "/" + name, m, pc, md->pvspec, iline, &I[per_line * l],
+                              &tau[per_line * l], err))
+          rc = set_err(ctx, RL_ERR_IO, err);
+      }
+    }
+    if (rc == 0) {
+      FILE* fp = std::fopen((std::string(dir) + "/radlite.success").c_str(), "w");
+      if (fp) { std::fprintf(fp, " 1\n"); std::fclose(fp); }
+    }
+  } else if (rc == 0) {
     const Model& m = md->m;
     std::vector<double> flux((size_t)m.nlspec * m.nfr);
     if (st) std::memset(st, 0, sizeof *st);

@@ -82,6 +82,8 @@ struct WalkParams {
   T kq;                      // 3.33567e-6 * 2.99792458e5
   T fstar;                   // (R*/ri(1))^2 for the central beam
   T* img;                    // [nlines][nrays][nfr]
+  T* tau = nullptr;          // position-velocity walk only: [nlines][nrays][nfr] char_tau
+  T* tauc = nullptr;         //   and its compensation term (same layout)
   unsigned long long* counters;   // [0] steps, [1] integrated channels, [2] node visits
   int* work;                 // dynamic work counter
   int* err;                  // first error code

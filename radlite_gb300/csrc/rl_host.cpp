@@ -344,12 +344,28 @@ void read_linespectrum(const std::string& dir, Model& m) {
   m.molfile = mf.substr(0, p + 4);
   m.molname = mf.substr(0, p);
   const int cmd = f.i();
-  if (cmd != 0) fail("linespectrum.inp: only the line spectrum command (0) is supported");
+  if (cmd == 1) fail("linespectrum.inp: command 1 is not implemented in the reference either");
+  if (cmd != 0 && cmd != 2) fail("linespectrum.inp: command " + std::to_string(cmd) + " unknown");
+  m.command = cmd;
   f.d();   // distance: the spectrum is computed at 1 pc (main.F:206,213)
   m.incl_rad = f.d() * 0.0174532925199;
   m.radvelo = f.d();
   m.nlspec = f.i();
   m.ilstart = f.i();
+  if (cmd == 2) {   // position-velocity cube (telescope.F:190-218)
+    PVSpec& pv = m.pv;
+    pv.nx = f.i();
+    pv.ny = f.i();
+    const int sizespec = f.i();
+    pv.szimx = f.d();
+    pv.szimy = f.d();
+    pv.phioff = f.d();
+    pv.xoff = f.d();
+    pv.yoff = f.d();
+    pv.addstar = f.i();
+    if (sizespec == 0) fail("linespectrum.inp: image size in arcsec is not implemented in the reference either");
+    if (sizespec != 1) fail("linespectrum.inp: size specifier " + std::to_string(sizespec) + " unknown");
+  }
 }
 
 void read_molecule(const std::string& dir, Model& m) {
@@ -389,6 +405,9 @@ void read_molecule(const std::string& dir, Model& m) {
   }
   if (m.ilstart < 1 || m.ilstart + m.nlspec - 1 > nlin || m.nlspec < 1)
     fail("linespectrum.inp: spectrum of a non-existing line requested");
+  // the run then starts at line 1 whatever the file asked (main.F:204); the check above
+  // still uses the requested start (telescope.F:292-299)
+  m.ilstart = 1;
 }
 
 void read_levelpop(const std::string& dir, Model& m) {
@@ -572,6 +591,61 @@ int setup_camera(const Model& m, double incl, int nphi, int dbdr, int nrext, Cam
   return 0;
 }
 
+int setup_pv_camera(const Model& m, const PVSpec& spec, double incl, PVCamera& cam, std::string& err) {
+  const int nx = spec.nx, ny = spec.ny;
+  if (nx < 2 || ny < 2 || nx % 2 || ny % 2) { err = "position-velocity image: nx and ny must be even and positive"; return -1; }
+  if ((long long)nx * ny > 64LL * 1024 * 1024) { err = "position-velocity image: more than 2^26 pixels"; return -1; }
+  // pixel size: the file gives the full image size, halved and divided by half the pixel
+  // count (telescope.F:197-200)
+  const double hx = spec.szimx * 0.5, hy = spec.szimy * 0.5;
+  cam.spx = hx / (nx * 0.5);
+  cam.spy = hy / (ny * 0.5);
+  if (!(cam.spx > 0.0) || !(cam.spy > 0.0)) { err = "position-velocity image: pixel size must be positive"; return -1; }
+  if (spec.addstar > 0 && (spec.xoff != 0.0 || spec.yoff != 0.0)) {
+    err = "position-velocity image: the unresolved star can only be added to a star-centred image (offsets 0)";
+    return -1;
+  }
+  if (incl < 1.0e-1) incl = (double)0.1f;   // (telescope.F:2289-2300, no absolute value here)
+  cam.incl_rad = incl;
+  cam.theta0 = incl + 1.0e-4;
+  cam.nx = nx; cam.ny = ny;
+  const double sinth0 = std::sin(cam.theta0);
+  const int nxh = nx / 2, nyh = ny / 2;
+  const int npix = nx * ny;
+  cam.nrays = npix + (spec.addstar > 0 ? 1 : 0);
+  cam.x0.assign(cam.nrays, 0.0);
+  cam.z0.assign(cam.nrays, 0.0);
+  cam.b.assign(npix, 0.0);
+  int ir = 0;
+  for (int ix = 1; ix <= nx; ix++) {
+    for (int iy = 1; iy <= ny; iy++) {
+      double xc = (ix - nxh - 0.5) * cam.spx - spec.xoff;
+      const double yc = (iy - nyh - 0.5) * cam.spy - spec.yoff;
+      const double rc = std::sqrt(xc * xc + yc * yc);
+      if (xc == 0.0) xc = xc + 0.001 * cam.spx;
+      double pc = std::atan(yc / xc) - spec.phioff;
+      if (xc < 0.0) pc = pc + 3.14159265359;
+      while (pc < 0.0) pc = pc + 6.28318530718;
+      while (pc >= 6.28318530718) pc = pc - 6.28318530718;
+      const double zh = -std::sin(pc) / sinth0;
+      double dum = 1.0 - zh * zh * sinth0 * sinth0;
+      dum = dum + 1.0e-4;
+      if (dum < 0.0) { err = "position-velocity image: negative discriminant in the ray setup"; return -1; }
+      const double xh = std::cos(pc) > 0.0 ? std::sqrt(dum) : -std::sqrt(dum);
+      cam.x0[ir] = rc * xh;
+      cam.z0[ir] = rc * zh;
+      cam.b[ir] = rc;
+      ir++;
+    }
+  }
+  // central ray (x0 = z0 = 0) for the unresolved star, used when the pixels are larger
+  // than the star (telescope.F:2404-2441)
+  cam.starunres = spec.addstar > 0 && cam.spx * cam.spx + cam.spy * cam.spy > m.rstar * m.rstar;
+  cam.srat = (3.14159265 * (m.rstar * m.rstar)) / (4.0 * cam.spx * cam.spy);
+  cam.rmax = m.R[m.nr + 1];
+  return 0;
+}
+
 int prepare_line(const Model& m, int iline, bool scaled, LinePrep& lp, std::string& err) {
   if (iline < 1 || iline > (int)m.lfreq.size()) { err = "line index out of range"; return -1; }
   const int il = iline - 1, ncell = m.ncell(), nfr = m.nfr;
@@ -690,6 +764,65 @@ static std::string fmt_e(double v, int w, int d) {
   std::string body = std::string(neg ? "-" : "") + (lead0 ? "0" : "") + "." + dig + expo;
   if ((int)body.size() > w) return std::string(w, '*');
   return std::string(w - body.size(), ' ') + body;
+}
+
+// gfortran ESw.d output: d.dddE+ee (the E dropped for three-digit exponents)
+static std::string fmt_es(double v, int w, int d) {
+  const bool neg = v < 0 || (v == 0.0 && std::signbit(v));
+  const double a = std::fabs(v);
+  char tmp[64];
+  std::snprintf(tmp, sizeof tmp, "%.*e", d, a);
+  std::string mant(tmp, std::strchr(tmp, 'e'));
+  int ex = std::atoi(std::strchr(tmp, 'e') + 1);
+  if (a == 0.0) ex = 0;
+  char expo[16];
+  if (std::abs(ex) <= 99) std::snprintf(expo, sizeof expo, "E%c%02d", ex < 0 ? '-' : '+', std::abs(ex));
+  else std::snprintf(expo, sizeof expo, "%c%03d", ex < 0 ? '-' : '+', std::abs(ex));
+  std::string body = std::string(neg ? "-" : "") + mant + expo;
+  if ((int)body.size() > w) return std::string(w, '*');
+  return std::string(w - body.size(), ' ') + body;
+}
+
+std::string posvel_file_name(const Model& m, int iline) {
+  if (iline < 1 || iline > 99) return std::string();
+  return "lineposvel_" + m.molname + "_" + std::to_string(iline) + ".dat";
+}
+
+int write_posvel_file(const std::string& path, const Model& m, const PVCamera& cam, const PVSpec& spec, int iline,
+                      const double* I, const double* tau, std::string& err) {
+  FILE* fp = std::fopen(path.c_str(), "w");
+  if (!fp) { err = "cannot write " + path; return -1; }
+  const int il = iline - 1;
+  const double lf = m.lfreq[il], nu0 = std::fabs(lf);
+  const double passb = 3.33567e-6 * nu0 * m.vmax, dnu = 2.0 * passb / (m.nfr - 1.0);
+  // header (telescope.F:1965-1984); the distance is 1 pc (main.F:206)
+  std::fprintf(fp, "\n%2d\n%-80s\n%-80s\n", 1, m.molname.c_str(), ("./" + m.molfile).c_str());
+  std::fprintf(fp, "%s%s%7.3f\n", fmt_es(1.0, 12, 4).c_str(), fmt_es(m.radvelo, 12, 4).c_str(),
+               m.incl_rad * 57.2957795132);
+  std::fprintf(fp, "%5d%5d\n%s\n%5d\n", m.lup[il], m.ldn[il], fmt_es(lf, 12, 4).c_str(), m.nfr);
+  std::fprintf(fp, "%5d%5d%s%s%7.3f%s%s\n  \n", cam.nx, cam.ny, fmt_es(cam.spx, 12, 4).c_str(),
+               fmt_es(cam.spy, 12, 4).c_str(), spec.phioff, fmt_es(spec.xoff, 12, 4).c_str(),
+               fmt_es(spec.yoff, 12, 4).c_str());
+  for (int k = 0; k < m.nfr; k++) {   // velocities (telescope.F:1989-1995)
+    const double fq = nu0 + (-passb + k * dnu);
+    const double velo = -2.99792458e5 * (fq - lf) / lf + m.radvelo;
+    std::fprintf(fp, "%s \n", fmt_e(velo, 10, 3).c_str());
+  }
+  std::fprintf(fp, "  \n");
+  // per channel, iy outer and ix inner: brightness temperature-like 3.25465503368e36 I / nu0^2
+  // and the line-of-sight optical depth (telescope.F:2006-2016)
+  const size_t npix = (size_t)cam.nx * cam.ny;
+  for (int k = 0; k < m.nfr; k++) {
+    const double* Ik = I + (size_t)k * npix;
+    const double* tk = tau + (size_t)k * npix;
+    for (size_t p = 0; p < npix; p++) {
+      const double temp = (3.25465503368e36 / (lf * lf)) * Ik[p];
+      std::fprintf(fp, "%s %s \n", fmt_es(temp, 12, 5).c_str(), fmt_es(tk[p], 12, 5).c_str());
+    }
+    std::fprintf(fp, "  \n");
+  }
+  std::fclose(fp);
+  return 0;
 }
 
 int write_spectrum_file(const std::string& path, const Model& m, const Camera& cam, const std::vector<int>& lines,

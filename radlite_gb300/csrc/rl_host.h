@@ -5,6 +5,14 @@
 
 namespace rl {
 
+// The rectangular image request of linespectrum.inp command 2 (telescope.F:190-218).
+struct PVSpec {
+  int nx = 0, ny = 0;
+  double szimx = 0.0, szimy = 0.0;   // full image size [cm]
+  double phioff = 0.0, xoff = 0.0, yoff = 0.0;
+  int addstar = 0;
+};
+
 // Everything the line raytrace reads from the reference's input files.
 struct Model {
   // spatial grid: R(ix) = R[ix+1] (ix=-1..nr+2), TH(iy) = TH[iy+1] (iy=-1..ny+2)
@@ -37,6 +45,8 @@ struct Model {
   int nphi = 0, dbdr = 1, nrext = 0;
   double vmax = 0.0, dv = 0.0, radvelo = 0.0;
   int nlspec = 0, ilstart = 1, style = 1, nfr = 0;
+  int command = 0;                          // 0: line spectrum, 2: position-velocity cube
+  PVSpec pv;
   double aksmax = 0.0;
   int ncell() const { return nr * nth; }
 };
@@ -51,6 +61,18 @@ struct Camera {
   std::vector<double> ri;       // [nrr+2] ring edges
 };
 
+// The rectangular camera (setup_rays_rectang, telescope.F:2229-2475): pixel rays in the
+// reference's order (ix outer, iy inner), then the central ray when the star is added.
+struct PVCamera {
+  int nx = 0, ny = 0, nrays = 0;
+  double spx = 0.0, spy = 0.0, incl_rad = 0.0, theta0 = 0.0;
+  int starunres = 0;            // add the unresolved star to the four central pixels
+  double srat = 0.0;            // pi R*^2 / (4 spx spy)
+  double rmax = 0.0;            // outer grid radius: pixels with b >= 0.999 rmax are empty
+  std::vector<double> x0, z0;   // [nrays]
+  std::vector<double> b;        // [nx*ny] impact parameter
+};
+
 // Per-line constants and cell tables (line.F:427-545, 1708-1823, 3502-3677, 3797-3845).
 struct LinePrep {
   double lfreq = 0.0, nu0 = 0.0, Bud = 0.0, Bdu = 0.0, scale = 1.0, istart = 0.0, cphi = 0.0;
@@ -61,10 +83,16 @@ struct LinePrep {
 
 int load_dir(const std::string& dir, Model& m, std::string& err);
 int setup_camera(const Model& m, double incl_rad, int nphi, int dbdr, int nrext, Camera& cam, std::string& err);
+int setup_pv_camera(const Model& m, const PVSpec& spec, double incl_rad, PVCamera& cam, std::string& err);
 int prepare_line(const Model& m, int iline, bool scaled, LinePrep& lp, std::string& err);
 double bplanck(double temp, double nu);                     // setup.F:937-952
 int bracket(const std::vector<double>& xx, double x);      // 1-based j with xx[j-1] < x <= xx[j]
 void finish_model(Model& m);   // derived quantities (aksmax, passband channel count)
+// lineposvel_<molecule>_<iline>.dat (telescope.F:1940-1961; empty for iline > 99)
+std::string posvel_file_name(const Model& m, int iline);
+// I and tau: [nfr][ny][nx] intensity and optical depth of line iline (1-based)
+int write_posvel_file(const std::string& path, const Model& m, const PVCamera& cam, const PVSpec& spec, int iline,
+                      const double* I, const double* tau, std::string& err);
 int write_spectrum_file(const std::string& path, const Model& m, const Camera& cam,
                         const std::vector<int>& lines, const std::vector<double>& flux, std::string& err);
 

@@ -63,6 +63,42 @@ struct LineTables {
 };
 template <typename T>
 int build_line_tables(const Model& m, int iline0, int nl, LineTables<T>& out, std::string& err);
+
+// Node records of a ray set (NodeBuf's arrays), grown on demand.
+struct NodeStore {
+  DevBuf nn, st, ds, dvf, vl, dvs, lw, wr, wt, c00, misc;
+  template <typename T>
+  cudaError_t ensure(size_t nrays, int kmax) {
+    const size_t n = nrays * (size_t)kmax;
+    cudaError_t e;
+    if ((e = nn.ensure(sizeof(int) * nrays)) != cudaSuccess) return e;
+    if ((e = st.ensure(sizeof(int) * nrays)) != cudaSuccess) return e;
+    if ((e = ds.ensure(sizeof(T) * n)) != cudaSuccess) return e;
+    if ((e = dvf.ensure(sizeof(float) * n)) != cudaSuccess) return e;
+    if ((e = vl.ensure(sizeof(T) * n)) != cudaSuccess) return e;
+    if ((e = dvs.ensure(sizeof(T) * n)) != cudaSuccess) return e;
+    if ((e = lw.ensure(sizeof(T) * n)) != cudaSuccess) return e;
+    if ((e = wr.ensure(sizeof(T) * n)) != cudaSuccess) return e;
+    if ((e = wt.ensure(sizeof(T) * n)) != cudaSuccess) return e;
+    if ((e = c00.ensure(sizeof(int) * n)) != cudaSuccess) return e;
+    return misc.ensure(sizeof(unsigned) * n);
+  }
+  template <typename T>
+  NodeBuf<T> view(int nrays, int kmax) const {
+    NodeBuf<T> nb;
+    nb.nrays = nrays; nb.kmax = kmax;
+    nb.nnodes = nn.as<int>(); nb.status = st.as<int>();
+    nb.ds = ds.as<T>(); nb.dvf = dvf.as<float>(); nb.vl = vl.as<T>(); nb.dvseg = dvs.as<T>();
+    nb.lw = lw.as<T>(); nb.wr = wr.as<T>(); nb.wt = wt.as<T>(); nb.c00 = c00.as<int>(); nb.misc = misc.as<unsigned>();
+    return nb;
+  }
+};
+
+// Device buffers of the position-velocity cube (rl_posvel.cu).
+struct PVBuffers {
+  DevBuf x0, z0, pix, scale, img, tau, tauc, I, tauo;
+  NodeStore nodes;
+};
 }  // namespace rl
 
 struct rl_ctx {
@@ -92,6 +128,9 @@ struct rl_model {
   // per-line tables of the last line range (reused while the range and precision match)
   int tab_line0 = -1, tab_nl = 0, tab_prec = -1;
   std::vector<double> tab_scale;
+  // position-velocity cube: the image request and its buffers
+  rl::PVSpec pvspec;
+  rl::PVBuffers pv;
   // per-call buffers
   rl::DevBuf dtab, dnsum, dwch, dvelo, dstar, dlc, dimg, dring, dflux, dscale, dcnt, dwork, derr, dlist;
 };
@@ -105,6 +144,8 @@ int set_err(rl_ctx* c, int code, const std::string& msg);
 cudaError_t h2d(void* dst, const void* src, size_t n, cudaStream_t s);
 cudaError_t d2h(void* dst, const void* src, size_t n, cudaStream_t s);
 int upload_grid(rl_model* md);
+// the position-velocity cube of lines iline0.. into [nl][nfr][ny][nx] (rl_posvel.cu)
+int dispatch_posvel(rl_model* md, int iline0, int nl, double* I, double* tau, rl_stats* st);
 
 inline GeoParams geo_params(const rl_model* md) {
   GeoParams p;

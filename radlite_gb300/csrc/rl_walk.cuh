@@ -1,0 +1,462 @@
+// rl_walk.cuh -- the formal-solution walk of one (line group, ray) work item, shared by
+// the circular-image kernels (rl_kernels.cu) and the position-velocity cube (rl_posvel.cu).
+//
+// PV = false: the circular image of calc_line_spectrum (telescope.F:339-631): the central
+//   beam (ray 0) integrates every channel and mixes in the star; every other ray integrates
+//   channel 1, its NONREDUNDANT velocity window and one continuum channel.
+// PV = true: a pixel of the rectangular image (make_freq_image_rectang,
+//   telescope.F:2061-2150): every channel of every ray, no star mixing (charintline with
+//   rbeam 0), and the line-of-sight optical depth char_tau per channel.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "rl_device.h"
+#include "rl_walk_common.cuh"
+
+namespace rl {
+
+// Formal solution of the (line, channel) pairs list[0..nt) of lines l0.. of one ray.
+// The per-line tables carry the profile normalisation 0.56419583546/(3.33567e-6 nu0), so
+// the profile of every slot is rlw * exp(-u^2) with the node's shared 1/linewidth.
+// Work order: per 32-node chunk, per pair of slots (two independent channels per lane),
+// all nodes of the chunk; the slot state lives in shared memory between pairs.
+// compensated summation s += x (Kahan), c carries the lost low-order part
+template <typename T>
+__device__ __forceinline__ void kahan_add(T& s, T& c, T x) {
+  const T y = x - c;
+  const T t = s + y;
+  c = (t - s) - y;
+  s = t;
+}
+
+// PV: also the optical depth of every slot, Kahan-compensated in P.tau / P.tauc (the slot's
+// image position), and no star mixing.
+template <typename T, int C, bool PV = false>
+__device__ long long walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<T, C>& SS, SubWork<T>& SW, int ray,
+                              int K, int l0, int gl, const unsigned short* list, int nt, int lane) {
+  const NodeBuf<T>& nb = P.nb;
+  const size_t row = (size_t)ray * nb.kmax;
+  const int nl = P.nlines;
+  const int nslot = (nt + 31) >> 5;
+  const int npass = (nslot + kPass - 1) / kPass;
+  for (int j = 0; j < kPass * npass && j < C; j++) {
+    const int idx = j * 32 + lane;
+    int L = -1;
+    T w = 0, I = 0;
+    if (idx < nt) {
+      const unsigned e = list[idx];
+      L = (int)(e >> kChBits);
+      w = P.wch[(size_t)(l0 + L) * P.nfr + (e & (kMaxChannels - 1))];
+      I = P.lc[l0 + L].istart;
+      if constexpr (PV) {
+        const size_t a = ((size_t)(l0 + L) * nb.nrays + ray) * P.nfr + (e & (kMaxChannels - 1));
+        P.tau[a] = 0; P.tauc[a] = 0;
+      }
+    }
+    SS.ll[j][lane] = L; SS.w[j][lane] = w; SS.I[j][lane] = I;
+    SS.j0[j][lane] = 0; SS.a0[j][lane] = 0; SS.S0[j][lane] = 0;
+  }
+  // central beam: the node where the ray first reaches the innermost cell mixes in the
+  // star (telescope.F:4166-4191)
+  int star_node = -1;
+  if (!PV && ray == 0) {
+    for (int kb = 0; kb < K && star_node < 0; kb += 32) {
+      const int k = kb + lane;
+      const bool f = k >= 1 && k < K && (nb.misc[row + k] & kFlagIr1);
+      const unsigned m = __ballot_sync(0xffffffffu, f);
+      if (m) star_node = kb + __ffs(m) - 1;
+    }
+  }
+  long long steps = 0;
+  T lw_last = 0;
+  for (int kb = 0; kb < K; kb += 32) {
+    if (kb > 0) {   // carry the last node of the previous chunk into entry 0
+      if (lane == 0) {
+        S.vl[0] = S.vl[32]; S.hds[0] = S.hds[32]; S.ds[0] = S.ds[32]; S.rlw[0] = S.rlw[32];
+        S.q[0] = S.q[32]; S.ids[0] = S.ids[32]; S.dvs[0] = S.dvs[32]; S.flags[0] = S.flags[32];
+        S.idvs[0] = S.idvs[32]; S.hw3[0] = S.hw3[32]; S.lg[0] = S.lg[32]; S.ilg[0] = S.ilg[32];
+      }
+      if (lane < gl) S.lv[lane][0] = S.lv[lane][32];
+      __syncwarp();
+    }
+    const int k = kb + lane;
+    T vl = 0, ds = 0, dvs = 0, lwk = 0;
+    unsigned misc = 0;
+    if (k < K) {
+      const size_t o = row + k;
+      const T wr = nb.wr[o], wt = nb.wt[o];
+      misc = nb.misc[o];
+      const Corners c = corners(nb.c00[o], misc, P.nth);
+      for (int l = 0; l < gl; l++) S.lv[l][lane + 1] = interp_lv(P.tab, c, nl, l0 + l, wr, wt);
+      vl = nb.vl[o]; ds = nb.ds[o]; dvs = nb.dvseg[o]; lwk = nb.lw[o];
+    }
+    T lwp = __shfl_up_sync(0xffffffffu, lwk, 1);
+    if (lane == 0) lwp = lw_last;
+    lw_last = __shfl_sync(0xffffffffu, lwk, 31);
+    const T lwav = (T)0.5 * (lwp + lwk);
+    const T rlw = lwav > (T)0 ? Math<T>::div((T)1, lwav) : (T)0;
+    S.vl[lane + 1] = vl; S.hds[lane + 1] = (T)0.5 * ds; S.ds[lane + 1] = ds; S.rlw[lane + 1] = rlw;
+    S.q[lane + 1] = (dvs < (T)0 ? -dvs : dvs) * P.kq * rlw;
+    S.ids[lane + 1] = ds > (T)0 ? Math<T>::div((T)1, ds) : (T)0;
+    S.dvs[lane + 1] = dvs;
+    {
+      // refined window half width 3 l = 3 ds/q and the spacing of its 31-point grid
+      const T qv = S.q[lane + 1];
+      const T dls = qv > (T)0 ? Math<T>::div(ds, qv) : (T)0;
+      S.idvs[lane + 1] = dvs != (T)0 ? Math<T>::div((T)1, dvs) : (T)0;
+      S.hw3[lane + 1] = (T)3 * dls;
+      S.lg[lane + 1] = (T)6 * dls / (T)30;
+      S.ilg[lane + 1] = dls > (T)0 ? Math<T>::div((T)30, (T)6 * dls) : (T)0;
+    }
+    {
+      unsigned f = misc;
+      if (k == 1 || (misc & kFlagHole) || k == star_node) f |= kFlagInit;
+      if ((T)6 * S.q[lane + 1] > (T)1) f |= kFlagSub;
+      S.flags[lane + 1] = f;
+    }
+    __syncwarp();
+    const int nn = min(32, K - kb);
+    const int n0 = kb == 0 ? 1 : 0;   // node 0 of the ray starts the walk
+    for (int pq = 0; pq < npass; pq++) {
+      T I[kPass], j0[kPass], a0[kPass], S0[kPass], w[kPass];
+      int Ls[kPass], lsl[kPass];
+      int nv = 0;
+#pragma unroll
+      for (int u = 0; u < kPass; u++) {
+        const int j = kPass * pq + u;
+        if (j < C) {
+          I[u] = SS.I[j][lane]; j0[u] = SS.j0[j][lane]; a0[u] = SS.a0[j][lane]; S0[u] = SS.S0[j][lane];
+          w[u] = SS.w[j][lane]; Ls[u] = SS.ll[j][lane];
+        } else {
+          I[u] = 0; j0[u] = 0; a0[u] = 0; S0[u] = 0; w[u] = 0; Ls[u] = -1;
+        }
+        lsl[u] = Ls[u] < 0 ? 0 : Ls[u];
+        nv += Ls[u] >= 0 ? 1 : 0;
+      }
+      T tau[kPass], tcp[kPass];
+      size_t ta[kPass];
+      if constexpr (PV) {
+#pragma unroll
+        for (int u = 0; u < kPass; u++) {
+          tau[u] = 0; tcp[u] = 0; ta[u] = 0;
+          if (Ls[u] >= 0) {
+            ta[u] = ((size_t)(l0 + Ls[u]) * nb.nrays + ray) * P.nfr +
+                    (list[(kPass * pq + u) * 32 + lane] & (kMaxChannels - 1));
+            tau[u] = P.tau[ta[u]]; tcp[u] = P.tauc[ta[u]];
+          }
+        }
+      }
+      for (int n = n0; n < nn; n++) {
+        const int g = kb + n;
+        const unsigned fl = S.flags[n + 1];
+        if (g == star_node) {
+#pragma unroll
+          for (int u = 0; u < kPass; u++)
+            if (Ls[u] >= 0)
+              I[u] = ((T)1 - P.fstar) * I[u] +
+                     P.fstar * P.star[(size_t)(l0 + Ls[u]) * P.nfr + (list[(kPass * pq + u) * 32 + lane] & (kMaxChannels - 1))];
+        }
+        const T vl1 = S.vl[n + 1], rl = S.rlw[n + 1], hds = S.hds[n + 1];
+        if (!(fl & kFlagInit)) {
+          // SUBGRID window test of the reference (line.F:4733-4742): slots whose refined
+          // window [s_c - 3l, s_c + 3l] overlaps (0, ds) keep their state here and are
+          // refined below; all others take one formal-solution step
+          bool ov[kPass];
+          bool any = false;
+#pragma unroll
+          for (int u = 0; u < kPass; u++) ov[u] = false;
+          if (fl & kFlagSub) {
+            const T vl0 = S.vl[n], dsf = S.ds[n + 1], hw3 = S.hw3[n + 1];
+#pragma unroll
+            for (int u = 0; u < kPass; u++) {
+              const T s_c = sizeof(T) == 8 ? dsf * (w[u] - vl0) / S.dvs[n + 1] : dsf * (w[u] - vl0) * S.idvs[n + 1];
+              ov[u] = Ls[u] >= 0 && (s_c + hw3 > (T)0) && (s_c - hw3 < dsf);
+              any = any || ov[u];
+            }
+            any = __any_sync(0xffffffffu, any);
+          }
+          T j1[kPass], a1[kPass], S1[kPass], dt[kPass], th[kPass];
+          bool ser_all = true, dir_all = true;
+#pragma unroll
+          for (int u = 0; u < kPass; u++) {
+            const LineVals<T> v = S.lv[lsl[u]][n + 1];
+            const T ph = profile(w[u], vl1, rl, rl);
+            j1[u] = v.jd + v.jf * ph;
+            a1[u] = v.ad + v.af * ph;
+            S1[u] = a1[u] > (T)0 ? j1[u] * Math<T>::rcp(a1[u]) : (T)0;
+            dt[u] = (a0[u] + a1[u]) * hds;
+            th[u] = (j0[u] + j1[u]) * hds;
+            const bool ser = dt[u] < (T)0.25;
+            ser_all = ser_all && ser;
+            dir_all = dir_all && !ser;
+          }
+          ser_all = __all_sync(0xffffffffu, ser_all);
+          dir_all = __all_sync(0xffffffffu, dir_all);
+          T x[kPass], ca[kPass], cb[kPass];
+          if (ser_all) {
+#pragma unroll
+            for (int u = 0; u < kPass; u++) Math<T>::series(dt[u], x[u], ca[u], cb[u]);
+          } else if (dir_all) {
+#pragma unroll
+            for (int u = 0; u < kPass; u++) Math<T>::direct(dt[u], x[u], ca[u], cb[u]);
+          } else {
+#pragma unroll
+            for (int u = 0; u < kPass; u++) Math<T>::coeffs(dt[u], x[u], ca[u], cb[u]);
+          }
+#pragma unroll
+          for (int u = 0; u < kPass; u++) {
+            const T src1 = a0[u] > (T)0 ? S0[u] : S1[u];
+            const T src2 = a1[u] > (T)0 ? S1[u] : S0[u];
+            T qv = dt[u] > (T)1.0e-9f ? ca[u] * src1 + cb[u] * src2 : th[u];
+            qv = qv < th[u] ? qv : th[u];
+            if (!ov[u]) {
+              I[u] = I[u] * x[u] + qv;
+              j0[u] = j1[u]; a0[u] = a1[u]; S0[u] = S1[u];
+              if constexpr (PV) kahan_add(tau[u], tcp[u], dt[u]);
+            }
+          }
+          steps += nv;
+          if (any) {
+            // compact the refined channels over the warp, refine them one per lane
+            int pos[kPass];
+            int cnt = 0;
+#pragma unroll
+            for (int u = 0; u < kPass; u++) {
+              const unsigned m = __ballot_sync(0xffffffffu, ov[u]);
+              pos[u] = cnt + __popc(m & lanemask_lt());
+              if (ov[u]) {
+                SW.I[pos[u]] = I[u]; SW.j0[pos[u]] = j0[u]; SW.a0[pos[u]] = a0[u]; SW.S0[pos[u]] = S0[u];
+                SW.w[pos[u]] = w[u]; SW.l[pos[u]] = (unsigned char)lsl[u];
+              }
+              cnt += __popc(m);
+            }
+            __syncwarp();
+            const T vl0 = S.vl[n], dsf = S.ds[n + 1], ids = S.ids[n + 1], hw3 = S.hw3[n + 1];
+            const T lgv = S.lg[n + 1], ilg = S.ilg[n + 1], idvs = S.idvs[n + 1], dvsg = S.dvs[n + 1];
+            for (int p = lane; p < cnt; p += 32) {
+              const T wp = SW.w[p];
+              const int lp = SW.l[p];
+              const T s_c = sizeof(T) == 8 ? dsf * (wp - vl0) / dvsg : dsf * (wp - vl0) * idvs;
+              const SlotOutT<T, PV> o = slot_sub<T, PV>(wp, S.lv[lp][n], S.lv[lp][n + 1], vl0, vl1, rl, dsf, ids,
+                                                        s_c - hw3, lgv, ilg, SW.I[p], SW.j0[p], SW.a0[p], SW.S0[p]);
+              SW.I[p] = o.I; SW.j0[p] = o.j0; SW.a0[p] = o.a0; SW.S0[p] = o.S0;
+              if constexpr (PV) SW.w[p] = o.dtau;   // the owner keeps w in a register
+              steps += o.steps - 1;
+            }
+            __syncwarp();
+#pragma unroll
+            for (int u = 0; u < kPass; u++) {
+              if (ov[u]) {
+                I[u] = SW.I[pos[u]]; j0[u] = SW.j0[pos[u]]; a0[u] = SW.a0[pos[u]]; S0[u] = SW.S0[pos[u]];
+                if constexpr (PV) kahan_add(tau[u], tcp[u], SW.w[pos[u]]);
+              }
+            }
+            __syncwarp();
+          }
+        } else {
+          const bool init = true, sub = fl & kFlagSub;
+          const T vl0 = S.vl[n], q = S.q[n + 1], dsf = S.ds[n + 1], dvs = S.dvs[n + 1], ids = S.ids[n + 1];
+#pragma unroll
+          for (int u = 0; u < kPass; u++) {
+            if (Ls[u] < 0) continue;
+            const SlotOutT<T, PV> o = slot_slow<T, PV>(init, sub, w[u], S.lv[Ls[u]][n], S.lv[Ls[u]][n + 1], vl0, vl1,
+                                                       rl, hds, q, dsf, dvs, ids, I[u], j0[u], a0[u], S0[u]);
+            I[u] = o.I; j0[u] = o.j0; a0[u] = o.a0; S0[u] = o.S0; steps += o.steps;
+            if constexpr (PV) kahan_add(tau[u], tcp[u], o.dtau);
+          }
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kPass; u++) {
+        const int j = kPass * pq + u;
+        if (j < C) { SS.I[j][lane] = I[u]; SS.j0[j][lane] = j0[u]; SS.a0[j][lane] = a0[u]; SS.S0[j][lane] = S0[u]; }
+        if constexpr (PV) {
+          if (Ls[u] >= 0) { P.tau[ta[u]] = tau[u]; P.tauc[ta[u]] = tcp[u]; }
+        }
+      }
+    }
+    __syncwarp();
+  }
+  return steps;
+}
+
+struct WalkCounters { unsigned long long steps = 0, integ = 0, nodes = 0; };
+
+// One work item: line group g of ray `ray`, item = g * nrays + ray.
+template <typename T, int C, bool PV = false>
+__device__ __forceinline__ void walk_item(const WalkParams<T>& P, int item, WarpStage<T>& S, SlotState<T, C>& SS,
+                                          SubWork<T>& SW, unsigned short* list, int lane, WalkCounters& wc) {
+  const NodeBuf<T>& nb = P.nb;
+  const int nl = P.nlines;
+  const int g = item / nb.nrays, ray = item - g * nb.nrays;
+  const int l0 = g * P.gsize, gl = min(P.gsize, nl - l0);
+  const int K = nb.nnodes[ray];
+  if (nb.status[ray] != 0 || K < 1) {
+    if (lane == 0) atomicCAS(P.err, 0, 100 + nb.status[ray]);
+    return;
+  }
+  const size_t row = (size_t)ray * nb.kmax;
+  // 1. velocity window of the ray per line (telescope.F:4265-4270): node projected
+  //    velocities where N_up + N_low exceeds 1e-3, nodes 0 .. K-2
+  float mn[kGroup], mx[kGroup];
+#pragma unroll
+  for (int l = 0; l < kGroup; l++) { mn[l] = 1.0f; mx[l] = -1.0f; }
+  __syncwarp();
+  if (!PV && ray != 0) {
+    for (int k = lane; k < K - 1; k += 32) {
+      const size_t o = row + k;
+      const T wr = nb.wr[o], wt = nb.wt[o];
+      const Corners c = corners(nb.c00[o], nb.misc[o], P.nth);
+      const float d = nb.dvf[o];
+#pragma unroll
+      for (int l = 0; l < kGroup; l++) {
+        if (l < gl && interp_1(P.nsum, c, nl, l0 + l, wr, wt) > (T)1.0e-3) {
+          mn[l] = fminf(mn[l], d); mx[l] = fmaxf(mx[l], d);
+        }
+      }
+    }
+#pragma unroll
+    for (int l = 0; l < kGroup; l++) {
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        mn[l] = fminf(mn[l], __shfl_xor_sync(0xffffffffu, mn[l], off));
+        mx[l] = fmaxf(mx[l], __shfl_xor_sync(0xffffffffu, mx[l], off));
+      }
+    }
+  }
+  if (lane == 0) {
+#pragma unroll
+    for (int l = 0; l < kGroup; l++) { S.mn[l] = mn[l]; S.mx[l] = mx[l]; }
+  }
+  __syncwarp();
+  // 2. (line, channel) pairs to integrate: channel 1, the in-window channels and the
+  //    channel that supplies the continuum of the others (telescope.F:541-613)
+  int nint = 0;
+  for (int l = 0; l < gl; l++) {
+    int cc = -1;
+    const double* velo = P.velo + (size_t)(l0 + l) * P.nfr;
+    const double lo = (double)S.mn[l] - 2.0 * P.aksmax_c, hi = (double)S.mx[l] + 2.0 * P.aksmax_c;
+    if (!PV && ray != 0 && !(velo[0] <= hi && velo[0] >= lo)) cc = 0;
+    for (int cb = 0; cb < P.nfr; cb += 32) {
+      const int c = cb + lane;
+      const bool valid = c < P.nfr;
+      const bool in = valid && (PV || ray == 0 || (velo[c] <= hi && velo[c] >= lo));
+      if (!PV && cc < 0 && ray != 0) {
+        const unsigned outm = __ballot_sync(0xffffffffu, valid && !in && c >= 1);
+        if (outm) cc = cb + __ffs(outm) - 1;
+      }
+      const bool take = valid && (c == 0 || in || c == cc);
+      const unsigned m = __ballot_sync(0xffffffffu, take);
+      if (take) list[nint + __popc(m & lanemask_lt())] = (unsigned short)((l << kChBits) | c);
+      nint += __popc(m);
+    }
+    if (lane == 0) S.cont_ch[l] = cc;
+  }
+  __syncwarp();
+  // 3. formal solution of the selected pairs, in tiles of 32*C
+  for (int tb = 0; tb < nint; tb += 32 * C) {
+    const int nt = min(32 * C, nint - tb);
+    wc.steps += walk_ray<T, C, PV>(P, S, SS, SW, ray, K, l0, gl, list + tb, nt, lane);
+    for (int j = 0; j < C; j++) {
+      const int idx = j * 32 + lane;
+      if (idx < nt) {
+        const unsigned e = list[tb + idx];
+        const int l = (int)(e >> kChBits), c = (int)(e & (kMaxChannels - 1));
+        const T Iv = SS.I[j][lane];
+        P.img[((size_t)(l0 + l) * nb.nrays + ray) * P.nfr + c] = Iv;
+        if (c == S.cont_ch[l]) S.contv[l] = Iv;
+      }
+    }
+  }
+  wc.integ += nint;
+  wc.nodes += (unsigned long long)nint * K;
+  __syncwarp();
+  // 4. continuum copy for the other channels of each line
+  for (int l = 0; l < gl; l++) {
+    const int cc = S.cont_ch[l];
+    if (cc < 0) continue;
+    const double* velo = P.velo + (size_t)(l0 + l) * P.nfr;
+    const double lo = (double)S.mn[l] - 2.0 * P.aksmax_c, hi = (double)S.mx[l] + 2.0 * P.aksmax_c;
+    T* img = P.img + ((size_t)(l0 + l) * nb.nrays + ray) * P.nfr;
+    const T contv = S.contv[l];
+    if (contv != (T)0) {
+      for (int c = lane; c < P.nfr; c += 32) {
+        const bool in = velo[c] <= hi && velo[c] >= lo;
+        if (!(c == 0 || in || c == cc)) img[c] = contv;
+      }
+      continue;
+    }
+    // a zero continuum is recomputed channel by channel in the reference: integrate
+    // every other out-of-window channel, then apply its sequential copy rule
+    int n2 = 0;
+    for (int cb = 0; cb < P.nfr; cb += 32) {
+      const int c = cb + lane;
+      const bool valid = c < P.nfr;
+      const bool take = valid && !(c == 0 || (velo[c] <= hi && velo[c] >= lo) || c == cc);
+      const unsigned m = __ballot_sync(0xffffffffu, take);
+      if (take) list[n2 + __popc(m & lanemask_lt())] = (unsigned short)((l << kChBits) | c);
+      n2 += __popc(m);
+    }
+    __syncwarp();
+    for (int tb = 0; tb < n2; tb += 32 * C) {
+      const int nt = min(32 * C, n2 - tb);
+      wc.steps += walk_ray<T, C>(P, S, SS, SW, ray, K, l0, gl, list + tb, nt, lane);
+      for (int j = 0; j < C; j++) {
+        const int idx = j * 32 + lane;
+        if (idx < nt) img[list[tb + idx] & (kMaxChannels - 1)] = SS.I[j][lane];
+      }
+    }
+    wc.integ += n2;
+    wc.nodes += (unsigned long long)n2 * K;
+    __syncwarp();
+    if (lane == 0) {
+      T cur = 0;
+      bool have = false;
+      for (int c = 0; c < P.nfr; c++) {
+        const bool in = velo[c] <= hi && velo[c] >= lo;
+        if (c != cc && (c == 0 || in)) continue;
+        if (have) img[c] = cur;
+        else if (img[c] != (T)0) { cur = img[c]; have = true; }
+      }
+    }
+    __syncwarp();
+  }
+  __syncwarp();
+}
+
+// Per-warp regions of the walk: stage, slot state and SUBGRID work in shared memory;
+// the (line, channel) list of the item in a per-warp global scratch row (L1-cached) when
+// kListInSmem is false, which leaves room for four 4-warp blocks per SM. `listcap`
+// (pairs) is kGroup x the largest channel count of the launch.
+constexpr bool kListInSmem = false;
+// FP32: four blocks per SM (at most 128 registers); FP64 (the parity path) keeps its registers.
+template <typename T> struct WalkMinBlocks { static constexpr int value = sizeof(T) == 4 ? kWalkBlocksPerSm : 1; };
+
+template <typename T, int C>
+struct WarpSmem {
+  WarpStage<T>* S; SlotState<T, C>* SS; SubWork<T>* SW; unsigned short* list;
+  __device__ WarpSmem(unsigned char* raw, int nw, int wib, int listcap, unsigned short* gscratch) {
+    const int capp = (listcap + 7) & ~7;
+    S = reinterpret_cast<WarpStage<T>*>(raw) + wib;
+    SS = reinterpret_cast<SlotState<T, C>*>(raw + sizeof(WarpStage<T>) * nw) + wib;
+    SW = reinterpret_cast<SubWork<T>*>(raw + (sizeof(WarpStage<T>) + sizeof(SlotState<T, C>)) * nw) + wib;
+    if (kListInSmem)
+      list = reinterpret_cast<unsigned short*>(
+                 raw + (sizeof(WarpStage<T>) + sizeof(SlotState<T, C>) + sizeof(SubWork<T>)) * nw) +
+             (size_t)wib * capp;
+    else
+      list = gscratch + ((size_t)blockIdx.x * nw + wib) * capp;
+  }
+};
+
+__device__ __forceinline__ void flush_counters(WalkCounters wc, unsigned long long* counters, int lane) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) wc.steps += __shfl_xor_sync(0xffffffffu, wc.steps, off);
+  if (lane == 0) {
+    atomicAdd(&counters[0], wc.steps);
+    atomicAdd(&counters[1], wc.integ);
+    atomicAdd(&counters[2], wc.nodes);
+  }
+}
+
+}  // namespace rl

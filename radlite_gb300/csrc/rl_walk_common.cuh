@@ -94,9 +94,10 @@ __device__ __forceinline__ T profile(T w, T vl, T rlw, T nrm) {
 }
 
 // One application of the linear-source formal solution (qdr_src_2, transfer.F:1498-1571)
-// from point 0 (j0, a0, S0) to point 1 (j1, a1, S1) over half-length hds.
+// from point 0 (j0, a0, S0) to point 1 (j1, a1, S1) over half-length hds. Returns the
+// step's optical depth 0.5 (a0 + a1) ds, the increment of char_tau (line.F:4598).
 template <typename T>
-__device__ __forceinline__ void formal(T& I, T j0, T a0, T S0, T j1, T a1, T S1, T hds) {
+__device__ __forceinline__ T formal(T& I, T j0, T a0, T S0, T j1, T a1, T S1, T hds) {
   const T dtau = (a0 + a1) * hds;
   const T theo = (j0 + j1) * hds;
   T x, a, b;
@@ -106,6 +107,7 @@ __device__ __forceinline__ void formal(T& I, T j0, T a0, T S0, T j1, T a1, T S1,
   T q = dtau > (T)1.0e-9f ? a * src1 + b * src2 : theo;
   q = q < theo ? q : theo;
   I = I * x + q;
+  return dtau;
 }
 
 template <typename T>
@@ -219,14 +221,19 @@ __device__ __forceinline__ T interp_1(const T* __restrict__ v, const Corners& c,
 }
 
 template <typename T>
-struct SlotOutT { T I, j0, a0, S0; int steps; };
+struct SlotOutBase { T I, j0, a0, S0; int steps; };
+// TAU: the walk also accumulates the optical depth of the segment's steps
+template <typename T, bool TAU = false>
+struct SlotOutT : SlotOutBase<T> {};
+template <typename T>
+struct SlotOutT<T, true> : SlotOutBase<T> { T dtau; };
 
 // Segment with a state reset (first segment, central hole, star) or with SUBGRID
 // refinement (line.F:4703-4833): interior points i = ia..ib of the 31-point grid over
 // [s_c - 3 l, s_c + 3 l] strictly inside (0, ds), then the segment end. Kept out of line:
 // it is rare, and inlining it per slot overflows the instruction cache.
-template <typename T>
-__device__ __noinline__ SlotOutT<T> slot_slow(bool init, bool sub, T w, LineVals<T> v0, LineVals<T> v1, T vl0,
+template <typename T, bool TAU = false>
+__device__ __noinline__ SlotOutT<T, TAU> slot_slow(bool init, bool sub, T w, LineVals<T> v0, LineVals<T> v1, T vl0,
                                                T vl1, T rl, T hds, T q, T dsf, T dvs, T ids, T I, T j0, T a0, T S0) {
   const Pt<T> p0 = {v0.jd, v0.ad, v0.jf, v0.af, vl0};
   const Pt<T> p1 = {v1.jd, v1.ad, v1.jf, v1.af, vl1};
@@ -260,7 +267,7 @@ __device__ __noinline__ SlotOutT<T> slot_slow(bool init, bool sub, T w, LineVals
     }
   }
   int steps = 0;
-  T sp = 0;
+  T sp = 0, tau = 0;
   for (int i = ia; i <= ib + 1; i++) {
     T s;
     Pt<T> pq;
@@ -277,13 +284,15 @@ __device__ __noinline__ SlotOutT<T> slot_slow(bool init, bool sub, T w, LineVals
     T j1, a1, S1;
     point_state(pq, ph, j1, a1, S1);
     const T h = (ia <= ib) ? (T)0.5 * (s - sp) : hds;
-    formal(I, j0, a0, S0, j1, a1, S1, h);
+    const T dt = formal(I, j0, a0, S0, j1, a1, S1, h);
+    if constexpr (TAU) tau = tau + dt;
     j0 = j1; a0 = a1; S0 = S1;
     sp = s;
     steps++;
   }
-  SlotOutT<T> o;
+  SlotOutT<T, TAU> o;
   o.I = I; o.j0 = j0; o.a0 = a0; o.S0 = S0; o.steps = steps;
+  if constexpr (TAU) o.dtau = tau;
   return o;
 }
 
@@ -291,8 +300,8 @@ __device__ __noinline__ SlotOutT<T> slot_slow(bool init, bool sub, T w, LineVals
 // overlaps it: interior points ia..ib of the grid s_i = sleft + i*lg, i = 0..30, that lie
 // strictly inside (0, ds), then the segment end (line.F:4769-4821). Called for those
 // channels only.
-template <typename T>
-__device__ __noinline__ SlotOutT<T> slot_sub(T w, LineVals<T> v0, LineVals<T> v1, T vl0, T vl1, T rl, T dsf, T ids,
+template <typename T, bool TAU = false>
+__device__ __noinline__ SlotOutT<T, TAU> slot_sub(T w, LineVals<T> v0, LineVals<T> v1, T vl0, T vl1, T rl, T dsf, T ids,
                                               T sleft, T lg, T ilg, T I, T j0, T a0, T S0) {
   int ia = 0;
   if (!(sleft > (T)0)) {
@@ -309,7 +318,7 @@ __device__ __noinline__ SlotOutT<T> slot_sub(T w, LineVals<T> v0, LineVals<T> v1
     while (ib >= 0 && !(sleft + (T)ib * lg < dsf)) ib--;
   }
   int steps = 0;
-  T sp = 0;
+  T sp = 0, tau = 0;
   for (int i = ia; i <= ib + 1; i++) {
     T s;
     Pt<T> pq;
@@ -326,13 +335,15 @@ __device__ __noinline__ SlotOutT<T> slot_sub(T w, LineVals<T> v0, LineVals<T> v1
     const T ph = profile(w, pq.vl, rl, rl);
     T j1, a1, S1;
     point_state(pq, ph, j1, a1, S1);
-    formal(I, j0, a0, S0, j1, a1, S1, (T)0.5 * (s - sp));
+    const T dt = formal(I, j0, a0, S0, j1, a1, S1, (T)0.5 * (s - sp));
+    if constexpr (TAU) tau = tau + dt;
     j0 = j1; a0 = a1; S0 = S1;
     sp = s;
     steps++;
   }
-  SlotOutT<T> o;
+  SlotOutT<T, TAU> o;
   o.I = I; o.j0 = j0; o.a0 = a0; o.S0 = S0; o.steps = steps;
+  if constexpr (TAU) o.dtau = tau;
   return o;
 }
 

@@ -86,6 +86,16 @@ class DiskConfig:
     outer_bc: int = 0                 # 0 = black, 2 = CMB
     starpump: int = 1                 # 1 = read the stellar spectrum (central-ray star)
     nfreq_dust: int = 24
+    # linespectrum.inp command 2 (position-velocity cube): pixels, full image size [AU],
+    # rotation [rad], offsets [AU], unresolved-star flag
+    command: int = 0
+    pv_nx: int = 16
+    pv_ny: int = 12
+    pv_size_au: float = 0.0           # 0: the grid's outer diameter
+    pv_phioff: float = 0.0
+    pv_xoff_au: float = 0.0
+    pv_yoff_au: float = 0.0
+    pv_addstar: int = 1
 
     def to_dict(self):
         return asdict(self)
@@ -339,12 +349,18 @@ def write_model(cfg: DiskConfig, outdir: str) -> str:
                  f"{cfg.vmax:<8.3f}Width of line passband [km/s]\n"
                  f"{cfg.dv:<8.4f}Velocity sampling [km/s]\n" + "-" * 65 + "\n"
                  "2       Format number\nmoldata.dat\tMolecular data file\n"
-                 "0       Command (0=spectrum, 2=image[3-D P/V cube])\n"
+                 f"{cfg.command:<8d}Command (0=spectrum, 2=image[3-D P/V cube])\n"
                  "1.0     Distance in [pc]\n"
                  f"{cfg.incl_deg:<8.3f}Inclination [deg]\n"
                  "0.0     Radial velocity, rel. to local standard of rest [km/s]\n"
                  f"{cfg.nlines:<8d}Nr of lines to make spectrum/image\n"
                  f"{cfg.ilinestart:<8d}Starting line to make spectrum/image\n")
+        if cfg.command == 2:
+            size = (cfg.pv_size_au * AU) if cfg.pv_size_au > 0 else 2.0 * float(f["r"][-1])
+            fh.write(f"{cfg.pv_nx:<8d}Nr of x pixels\n{cfg.pv_ny:<8d}Nr of y pixels\n1       image size in cm?\n"
+                     f"{size:.10e} size x direction\n{size * cfg.pv_ny / cfg.pv_nx:.10e} size y direction\n"
+                     f"{cfg.pv_phioff:.10e} Phi offset?\n{cfg.pv_xoff_au * AU:.10e} x offset?\n"
+                     f"{cfg.pv_yoff_au * AU:.10e} y offset?\n{cfg.pv_addstar:<8d}add star?\n")
 
     with open(P("radlite.inp"), "w") as fh:
         sep = "=" * 40 + "\n"

@@ -41,7 +41,8 @@ def test_host_only_load_matches_files(gpu_lib, model_dir, oracle_lib):
     ("density.inp", lambda t: "3\t3\t1\n" + t.split("\n", 1)[1], "inconsistent"),
     ("levelpop.info", lambda t: "-3\nwrongname.dat\n0", "levelpop.info"),
     ("levelpop.info", lambda t: "-1\n", "cannot open"),
-    ("linespectrum.inp", lambda t: t.replace("0       Command", "2       Command"), "only the line spectrum"),
+    ("linespectrum.inp", lambda t: t.replace("0       Command", "1       Command"), "command 1"),
+    ("linespectrum.inp", lambda t: t.replace("0       Command", "2       Command"), "end of file"),
     ("radlite.inp", lambda t: t.replace("-551", "-500"), "setup type"),
     ("moldata.dat", lambda t: t.replace("    4    3", "    3    4"), "invalid levels"),
     ("velocity.inp", lambda t: t.replace("e+", "x+", 1), "not a number"),

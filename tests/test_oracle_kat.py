@@ -11,11 +11,14 @@ from radlite_gb300 import synth
 def test_keplerian_line_symmetric(oracle_lib, model_dir):
     """A Keplerian disk line is symmetric in velocity (azimuth phi <-> -phi)."""
     o = oracle_lib.Oracle(model_dir("tiny_line"))
-    flux, velo, cnt = o.line_spectrum(o.ilinestart)
-    assert np.all(np.isfinite(flux)) and flux.max() > 0
-    np.testing.assert_allclose(flux, flux[::-1], rtol=1e-6)
-    np.testing.assert_allclose(velo, -velo[::-1], atol=1e-9)
-    assert cnt["steps"] > cnt["integrated"] > 0
+    for iline in (1, 2, 3):
+        flux, velo, cnt = o.line_spectrum(iline)
+        assert np.all(np.isfinite(flux)) and flux.max() > 0
+        # to 1e-6 of the peak: the window and sub-step decisions are taken in FP32 / on
+        # discrete thresholds, which breaks the mirror symmetry in the far wings
+        np.testing.assert_allclose(flux, flux[::-1], rtol=0, atol=1e-6 * flux.max())
+        np.testing.assert_allclose(velo, -velo[::-1], atol=1e-9)
+        assert cnt["steps"] > cnt["integrated"] > 0
 
 
 def test_star_only_central_beam(oracle_lib, tmp_path):
@@ -23,7 +26,7 @@ def test_star_only_central_beam(oracle_lib, tmp_path):
     cfg = synth.config_by_name("tiny_line", abund=0.0, kappa_abs=0.0)
     d = synth.write_model(cfg, str(tmp_path / "m"))
     o = oracle_lib.Oracle(d)
-    flux, _, _ = o.line_spectrum(o.ilinestart)
+    flux, _, _ = o.line_spectrum(cfg.ilinestart)
     f = synth.make_fields(cfg)
     # moldata.dat stores energies with 4 decimals (F12.4): the line frequency follows them
     nu0 = synth.line_freqs(cfg, np.round(f["E"], 4), f["lines"])[cfg.ilinestart - 1]
@@ -41,9 +44,10 @@ def test_star_only_central_beam(oracle_lib, tmp_path):
 
 def test_dust_only_continuum_flat(oracle_lib, tmp_path):
     """Without line opacity every channel of every ray carries the same continuum."""
-    d = synth.write_model(synth.config_by_name("tiny_line", abund=0.0), str(tmp_path / "m"))
+    cfg = synth.config_by_name("tiny_line", abund=0.0)
+    d = synth.write_model(cfg, str(tmp_path / "m"))
     o = oracle_lib.Oracle(d)
-    img, mask, _ = o.line_image(o.ilinestart)
+    img, mask, _ = o.line_image(cfg.ilinestart)
     assert np.all(img > 0)
     # (the central beam, row 0, carries the frequency-dependent stellar intensity)
     np.testing.assert_allclose(img[1:], img[1:, :1].repeat(img.shape[1], 1), rtol=1e-12)
@@ -60,7 +64,7 @@ def test_optically_thick_saturates_to_planck(oracle_lib, tmp_path):
                                mstar=1e-12, nphi=8, vmax=3.0, dv=0.5, incl_deg=60.0)
     d = synth.write_model(cfg, str(tmp_path / "m"))
     o = oracle_lib.Oracle(d)
-    img, _, _ = o.line_image(o.ilinestart, 1 + 8 * 20, 1 + 8 * 40)
+    img, _, _ = o.line_image(cfg.ilinestart, 1 + 8 * 20, 1 + 8 * 40)
     f = synth.make_fields(cfg)
     nu0 = synth.line_freqs(cfg, np.round(f["E"], 4), f["lines"])[cfg.ilinestart - 1]
     B = 1.47455e-47 * nu0 ** 3 / math.expm1(4.7989e-11 * nu0 / T)
@@ -74,7 +78,7 @@ def test_thin_dust_trapezoid(oracle_lib, tmp_path):
     d = synth.write_model(cfg, str(tmp_path / "m"))
     o = oracle_lib.Oracle(d)
     ray = 1 + 8 * 20
-    img, _, _ = o.line_image(o.ilinestart, ray, ray + 1)
+    img, _, _ = o.line_image(cfg.ilinestart, ray, ray + 1)
     t = o.trajectory(ray)
     f = synth.make_fields(cfg)
     nu0 = synth.line_freqs(cfg, np.round(f["E"], 4), f["lines"])[cfg.ilinestart - 1]
