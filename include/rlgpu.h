@@ -110,6 +110,10 @@ int rl_spectra(rl_model* model, int iline0, int nlines, double* flux_out, rl_sta
 /* Circular image of one line: [nrays][nfr] intensities (ray 0 = central beam, then
    rings from the inside out, azimuth fastest), as imcir_int. */
 int rl_line_image(rl_model* model, int iline, double* image_out, rl_stats* stats);
+/* The same image and its integration mask [nrays][nfr]: 1 where the channel was integrated
+   as channel 1 or inside the ray's velocity window (imcir_cmask, telescope.F:548,575), 0
+   where it holds the ray's continuum. */
+int rl_line_image_mask(rl_model* model, int iline, double* image_out, unsigned char* mask_out, rl_stats* stats);
 
 /* ---- Position-velocity cube (linespectrum.inp command 2): the rectangular image of
    setup_rays_rectang / make_freq_image_rectang / calc_write_line_posvel
@@ -134,6 +138,11 @@ int rl_posvel(rl_model* model, int iline0, int nlines, double* I_out, double* ta
    linespectrum_<mol>.dat (main.F:1034-1049), command 2 one lineposvel_<mol>_<iline>.dat
    per line (main.F:1061-1074); both then write radlite.success. */
 int rl_run_dir(const char* dir, int device, rl_stats* stats);
+/* rl_run_dir with options. RL_RUN_SAVE_IMCIR: as a reference build with SAVE_IMCIR
+   (configure_image.h:57), also write lineposvelcirc_<mol>_<iline>.dat, the circular image
+   and integration mask of every line of a command-0 run (telescope.F:1346-1373). */
+#define RL_RUN_SAVE_IMCIR 1
+int rl_run_dir_ex(const char* dir, int device, int flags, rl_stats* stats);
 
 /* Node list of one ray as the geometry kernel produces it (inspection and tests):
    returns the node count (may exceed cap; arrays receive min(count, cap) entries). */

@@ -1193,8 +1193,11 @@ int rlo_trajectory(const rlo_model* m, int iray, int maxn, double* s, double* r,
 }
 
 /* The image of one line over rays [ray_begin, ray_end): image[(ray-ray_begin)*nfr + k],
-   mask = 1 where the channel was integrated (0 = continuum copy). counts[0] = formal-
-   solution steps, counts[1] = integrated (ray, channel) pairs, counts[2] = nodes walked. */
+   mask = imcir_cmask of this line alone (telescope.F:548,575): 1 for channel 1 and the
+   channels inside the ray's velocity window, 0 for continuum copies and for the channel
+   that computes a missing continuum; all 1 on the central beam, whose mask the reference
+   never writes. counts[0] = formal-solution steps, counts[1] = integrated (ray, channel)
+   pairs, counts[2] = nodes walked. */
 int rlo_line_image(rlo_model* m, int iline, int ray_begin, int ray_end, double* image, unsigned char* mask,
                    long long* counts) {
     if (iline < 1 || iline > m->nlin) return fail("line index out of range");
@@ -1234,7 +1237,7 @@ int rlo_line_image(rlo_model* m, int iline, int ray_begin, int ray_end, double* 
                 } else {
                     rc = charint(&L, &T, k, -1.0, &minv, &maxv, &img[k - 1]);
                     cont = img[k - 1];
-                    if (msk) msk[k - 1] = 1;
+                    if (msk) msk[k - 1] = 0;
                     integ++; nodes += T.n;
                 }
             }

@@ -86,7 +86,8 @@ EXPORTS = ["rl_create", "rl_destroy", "rl_last_error", "rl_load_dir", "rl_load_a
            "rl_diff_backward", "rl_diff_batch_create", "rl_diff_batch_destroy", "rl_diff_batch_add",
            "rl_diff_batch_use_graph", "rl_diff_batch_buffers", "rl_diff_batch_layout", "rl_diff_batch_forward",
            "rl_diff_batch_backward",
-           "rl_image_to_spectrum_noalloc", "rl_set_posvel", "rl_get_posvel", "rl_posvel"]
+           "rl_image_to_spectrum_noalloc", "rl_set_posvel", "rl_get_posvel", "rl_posvel",
+           "rl_line_image_mask", "rl_run_dir_ex"]
 
 _lib = None
 
@@ -112,6 +113,8 @@ def lib():
         L.rl_spectra.argtypes = [vp, C.c_int, C.c_int, _D, C.POINTER(Stats)]
         L.rl_line_image.argtypes = [vp, C.c_int, _D, C.POINTER(Stats)]
         L.rl_run_dir.argtypes = [C.c_char_p, C.c_int, C.POINTER(Stats)]
+        L.rl_run_dir_ex.argtypes = [C.c_char_p, C.c_int, C.c_int, C.POINTER(Stats)]
+        L.rl_line_image_mask.argtypes = [vp, C.c_int, _D, C.POINTER(C.c_ubyte), C.POINTER(Stats)]
         L.rl_set_posvel.argtypes = [vp, C.POINTER(PosvelSpec)]
         L.rl_get_posvel.argtypes = [vp, C.POINTER(PosvelSpec)]
         L.rl_posvel.argtypes = [vp, C.c_int, C.c_int, _D, _D, C.POINTER(Stats)]
@@ -289,12 +292,19 @@ class Model:
         _check(lib().rl_spectra(self.h, iline0, nlines, _dp(flux), C.byref(st)), self._ch)
         return (flux, st.as_dict()) if stats else flux
 
-    def line_image(self, iline: int):
+    def line_image(self, iline: int, mask: bool = False):
+        """Circular image [nrays, nfr] (imcir_int); with mask=True also the integration mask
+        (imcir_cmask: 1 = channel 1 or inside the ray's velocity window)."""
         info = self.info()
         img = np.zeros((info["nrays"], info["nfr"]))
         st = Stats()
-        _check(lib().rl_line_image(self.h, iline, _dp(img), C.byref(st)), self._ch)
-        return img
+        if not mask:
+            _check(lib().rl_line_image(self.h, iline, _dp(img), C.byref(st)), self._ch)
+            return img
+        msk = np.zeros((info["nrays"], info["nfr"]), dtype=np.uint8)
+        _check(lib().rl_line_image_mask(self.h, iline, _dp(img), msk.ctypes.data_as(C.POINTER(C.c_ubyte)),
+                                        C.byref(st)), self._ch)
+        return img, msk
 
     def set_posvel(self, nx: int, ny: int, szimx: float, szimy: float, phioff: float = 0.0, xoff: float = 0.0,
                    yoff: float = 0.0, addstar: int = 1):
@@ -582,10 +592,14 @@ def load_dir_host(path: str) -> "Model":
     return Model(None, h)
 
 
-def run_dir(path: str, device: int = 0) -> dict:
-    """Render the lines requested by linespectrum.inp in `path`, like the RADlite executable."""
+RUN_SAVE_IMCIR = 1
+
+
+def run_dir(path: str, device: int = 0, save_imcir: bool = False) -> dict:
+    """Render the lines requested by linespectrum.inp in `path`, like the RADlite executable
+    (save_imcir: also the circular-image files of a SAVE_IMCIR build)."""
     st = Stats()
-    rc = lib().rl_run_dir(os.fsencode(path), device, C.byref(st))
+    rc = lib().rl_run_dir_ex(os.fsencode(path), device, RUN_SAVE_IMCIR if save_imcir else 0, C.byref(st))
     if rc < 0:
         raise RLError(_err())
     return st.as_dict()
@@ -653,6 +667,31 @@ def read_posvel_file(path: str) -> dict:
         i += nx * ny + 1
     h["temp"], h["tau"] = temp, tau
     return h
+
+
+def read_imcir_file(path: str) -> dict:
+    """Parse lineposvelcirc_<mol>_<iline>.dat (telescope.F:1346-1373): line frequency, ring
+    edges ri [nrr+1] and radii r [nrr+1], and per channel the velocity, the central-beam
+    intensity and the [nphi, nrr] intensities and integration mask."""
+    with open(path) as fh:
+        L = [x for x in fh.read().split("\n")]
+    nfr = int(L[0])
+    nu0 = _fnum(L[1])
+    nphi, nrr = (int(x) for x in L[2].split())
+    i = 3
+    ri = np.array([_fnum(L[i + k]) for k in range(nrr + 1)]); i += nrr + 1
+    rr = np.array([_fnum(L[i + k]) for k in range(nrr + 1)]); i += nrr + 1
+    velo, cen = np.zeros(nfr), np.zeros(nfr)
+    img = np.zeros((nfr, nphi, nrr))
+    mask = np.zeros((nfr, nphi, nrr), dtype=np.uint8)
+    for k in range(nfr):
+        velo[k] = _fnum(L[i + 1]); cen[k] = _fnum(L[i + 3]); i += 5
+        rows = L[i:i + nphi * nrr]
+        img[k] = np.array([_fnum(r[0:10]) for r in rows]).reshape(nphi, nrr)
+        mask[k] = np.array([int(r[12:13]) for r in rows]).reshape(nphi, nrr)
+        i += nphi * nrr
+    return {"nfr": nfr, "nu0": nu0, "nphi": nphi, "nrr": nrr, "ri": ri, "r": rr, "velo": velo, "central": cen,
+            "image": img, "mask": mask}
 
 
 def read_spectrum_file(path: str):

@@ -157,7 +157,8 @@ static int build_geometry(rl_model* md, rl_stats* st) {
 }
 
 template <typename T>
-static int run_lines(rl_model* md, int iline0, int nl, double* flux_out, double* image_out, rl_stats* st) {
+static int run_lines(rl_model* md, int iline0, int nl, double* flux_out, double* image_out, unsigned char* mask_out,
+                     rl_stats* st) {
   rl_ctx* ctx = md->ctx;
   cudaStream_t s = ctx->stream;
   const Model& m = md->m;
@@ -197,6 +198,7 @@ static int run_lines(rl_model* md, int iline0, int nl, double* flux_out, double*
   CUDA_TRY(md->dwork.ensure(sizeof(int)));
   CUDA_TRY(md->derr.ensure(sizeof(int)));
   CUDA_TRY(md->dlist.ensure(sizeof(unsigned short) * walk_list_elems(ctx->nsm, nfr)));
+  if (mask_out) CUDA_TRY(md->dmask.ensure(nimg));
   CUDA_TRY(cudaEventRecord(ctx->ev[0], s));
   if (!cached) {
     CUDA_TRY(h2d(md->dtab.p, tab.data(), sizeof(T) * tab.size(), s));
@@ -230,6 +232,7 @@ static int run_lines(rl_model* md, int iline0, int nl, double* flux_out, double*
   P.work = md->dwork.as<int>();
   P.err = md->derr.as<int>();
   P.list = md->dlist.as<unsigned short>();
+  P.mask = mask_out ? md->dmask.as<unsigned char>() : nullptr;
   if (cam.ri[1] < m.rstar) return set_err(ctx, RL_ERR_ARG, "central beam smaller than the star");
   // slots per lane: enough for every (line, channel) pair of a line group in one tile
   const int need = (P.gsize * nfr + 31) / 32;
@@ -254,6 +257,10 @@ static int run_lines(rl_model* md, int iline0, int nl, double* flux_out, double*
     CUDA_TRY(cudaMemcpy(img.data(), md->dimg.p, sizeof(T) * nimg, cudaMemcpyDeviceToHost));
     for (size_t i = 0; i < nimg; i++) image_out[i] = (double)img[i] * scale[i / ((size_t)cam.nrays * nfr)];
   }
+  if (mask_out) {
+    g_d2h += nimg;
+    CUDA_TRY(cudaMemcpy(mask_out, md->dmask.p, nimg, cudaMemcpyDeviceToHost));
+  }
   if (!cached) {
     md->tab_line0 = iline0; md->tab_nl = nl; md->tab_prec = md->precision; md->tab_scale = scale;
   }
@@ -271,10 +278,11 @@ static int run_lines(rl_model* md, int iline0, int nl, double* flux_out, double*
   return 0;
 }
 
-static int dispatch_lines(rl_model* md, int iline0, int nl, double* flux, double* image, rl_stats* st) {
+static int dispatch_lines(rl_model* md, int iline0, int nl, double* flux, double* image, rl_stats* st,
+                          unsigned char* mask = nullptr) {
   g_h2d = 0; g_d2h = 0;
-  const int rc = md->precision == RL_FP64 ? run_lines<double>(md, iline0, nl, flux, image, st)
-                                          : run_lines<float>(md, iline0, nl, flux, image, st);
+  const int rc = md->precision == RL_FP64 ? run_lines<double>(md, iline0, nl, flux, image, mask, st)
+                                          : run_lines<float>(md, iline0, nl, flux, image, mask, st);
   if (st) { st->h2d_bytes += g_h2d; st->d2h_bytes += g_d2h; }
   return rc;
 }
@@ -488,7 +496,18 @@ int rl_line_image(rl_model* md, int iline, double* image_out, rl_stats* st) {
   return dispatch_lines(md, iline, 1, nullptr, image_out, st);
 }
 
-int rl_run_dir(const char* dir, int device, rl_stats* st) {
+int rl_line_image_mask(rl_model* md, int iline, double* image_out, unsigned char* mask_out, rl_stats* st) {
+  if (!md || !image_out || !mask_out) return set_err(nullptr, RL_ERR_ARG, "rl_line_image_mask: null argument");
+  rl_ctx* ctx = md->ctx;
+  if (!ctx) return set_err(nullptr, RL_ERR_STATE, "model was loaded without a device context");
+  CUDA_TRY(cudaSetDevice(ctx->device));
+  if (st) std::memset(st, 0, sizeof *st);
+  return dispatch_lines(md, iline, 1, nullptr, image_out, st, mask_out);
+}
+
+int rl_run_dir(const char* dir, int device, rl_stats* st) { return rl_run_dir_ex(dir, device, 0, st); }
+
+int rl_run_dir_ex(const char* dir, int device, int flags, rl_stats* st) {
   rl_ctx* ctx = nullptr;
   int rc = rl_create(&ctx, device);
   if (rc) return rc;
@@ -522,6 +541,48 @@ int rl_run_dir(const char* dir, int device, rl_stats* st) {
     if (rc == 0) {
       FILE* fp = std::fopen((std::string(dir) + "/radlite.success").c_str(), "w");
       if (fp) { std::fprintf(fp, " 1\n"); std::fclose(fp); }
+    }
+  } else if (rc == 0 && (flags & RL_RUN_SAVE_IMCIR)) {
+    // a SAVE_IMCIR build: line by line, the circular image beside the spectrum
+    // (telescope.F:1594-1615); the integration mask accumulates over the run's lines
+    // because the reference never clears imcir_cmask
+    const Model& m = md->m;
+    std::vector<double> flux((size_t)m.nlspec * m.nfr);
+    if (st) std::memset(st, 0, sizeof *st);
+    std::vector<double> img;
+    std::vector<unsigned char> mask, sticky;
+    std::string err;
+    for (int l = 0; l < m.nlspec && rc == 0; l++) {
+      const int iline = m.ilstart + l;
+      rl_stats one;
+      std::memset(&one, 0, sizeof one);
+      const int nrings = std::abs(md->nrext) + 10 + md->dbdr * (m.nr - 1);   // setup_camera's ring count
+      const size_t n = (size_t)(1 + nrings * md->nphi) * m.nfr;
+      img.resize(n); mask.resize(n);
+      if (sticky.empty()) sticky.assign(n, 0);
+      rc = dispatch_lines(md, iline, 1, &flux[(size_t)l * m.nfr], img.data(), &one, mask.data());
+      if (rc) break;
+      for (size_t i = 0; i < n; i++) sticky[i] |= mask[i];
+      if (st) {
+        st->steps += one.steps; st->integrated += one.integrated; st->node_visits += one.node_visits;
+        st->ray_channels += one.ray_channels; st->walk_ms += one.walk_ms; st->geometry_ms += one.geometry_ms;
+        st->reduce_ms += one.reduce_ms; st->upload_ms += one.upload_ms; st->nlines += 1;
+        st->nrays = one.nrays; st->nfr = one.nfr; st->kmax = one.kmax;
+      }
+      const std::string name = imcir_file_name(m, iline);
+      if (name.empty()) { rc = set_err(ctx, RL_ERR_ARG, "circular-image file names stop at line 99"); break; }
+      if (write_imcir_file(std::string(dir) + "/" + name, m, md->cam, iline, img.data(), sticky.data(), err))
+        rc = set_err(ctx, RL_ERR_IO, err);
+    }
+    if (rc == 0) {
+      std::vector<int> lines;
+      for (int i = 0; i < m.nlspec; i++) lines.push_back(m.ilstart + i);
+      if (write_spectrum_file(std::string(dir) + "/linespectrum_" + m.molname + ".dat", m, md->cam, lines, flux, err))
+        rc = set_err(ctx, RL_ERR_IO, err);
+      else {
+        FILE* fp = std::fopen((std::string(dir) + "/radlite.success").c_str(), "w");
+        if (fp) { std::fprintf(fp, " 1\n"); std::fclose(fp); }
+      }
     }
   } else if (rc == 0) {
     const Model& m = md->m;

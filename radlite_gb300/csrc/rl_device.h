@@ -84,6 +84,7 @@ struct WalkParams {
   T* img;                    // [nlines][nrays][nfr]
   T* tau = nullptr;          // position-velocity walk only: [nlines][nrays][nfr] char_tau
   T* tauc = nullptr;         //   and its compensation term (same layout)
+  unsigned char* mask = nullptr;  // optional [nlines][nrays][nfr]: 1 = channel 1 or inside the window
   unsigned long long* counters;   // [0] steps, [1] integrated channels, [2] node visits
   int* work;                 // dynamic work counter
   int* err;                  // first error code

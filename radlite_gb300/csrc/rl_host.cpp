@@ -783,6 +783,71 @@ static std::string fmt_es(double v, int w, int d) {
   return std::string(w - body.size(), ' ') + body;
 }
 
+// gfortran list-directed output of a default integer: a blank and I11
+static std::string fmt_list_int(int v) {
+  char b[32];
+  std::snprintf(b, sizeof b, " %11d", v);
+  return b;
+}
+
+// gfortran list-directed output of a REAL(8): a blank, then G25.17E3 with scale factor 1P
+// in E form (F form with 17 significant digits and 5 trailing blanks for 0.1 <= |v| < 1e17)
+static std::string fmt_list_real(double v) {
+  const bool neg = std::signbit(v);
+  const double a = std::fabs(v);
+  char tmp[64];
+  std::snprintf(tmp, sizeof tmp, "%.16e", a);
+  const int ex = std::atoi(std::strchr(tmp, 'e') + 1);   // exponent of the 17-digit rounding
+  std::string body;
+  bool fform = a == 0.0 || (ex >= -1 && ex <= 16);
+  if (fform) {
+    const int k = a == 0.0 ? 1 : ex + 1;                  // digits before the point
+    char f[64];
+    std::snprintf(f, sizeof f, "%.*f", 17 - k, a);
+    body = std::string(neg ? "-" : "") + f + (k == 17 ? "." : "");
+    body = std::string(body.size() < 20 ? 20 - body.size() : 0, ' ') + body + "     ";
+  } else {
+    std::string mant(tmp, std::strchr(tmp, 'e'));
+    char e[16];
+    std::snprintf(e, sizeof e, "E%c%03d", ex < 0 ? '-' : '+', std::abs(ex));
+    body = std::string(neg ? "-" : "") + mant + e;
+    body = std::string(body.size() < 25 ? 25 - body.size() : 0, ' ') + body;
+  }
+  return " " + body;
+}
+
+std::string imcir_file_name(const Model& m, int iline) {
+  if (iline < 1 || iline > 99) return std::string();
+  return "lineposvelcirc_" + m.molname + "_" + std::to_string(iline) + ".dat";
+}
+
+int write_imcir_file(const std::string& path, const Model& m, const Camera& cam, int iline, const double* img,
+                     const unsigned char* mask, std::string& err) {
+  FILE* fp = std::fopen(path.c_str(), "w");
+  if (!fp) { err = "cannot write " + path; return -1; }
+  const int il = iline - 1, nfr = m.nfr, nphi = cam.nphi, nrr = cam.nrr;
+  const double nu0 = std::fabs(m.lfreq[il]);
+  const double passb = 3.33567e-6 * nu0 * m.vmax, dnu = 2.0 * passb / (nfr - 1.0);
+  std::fprintf(fp, "%s\n", fmt_list_int(nfr).c_str());   // telescope.F:1614
+  for (int k = 0; k < nfr; k++) {                          // telescope.F:1346-1373
+    if (k == 0) {
+      std::fprintf(fp, "%s\n%s%s\n", fmt_list_real(nu0).c_str(), fmt_list_int(nphi).c_str(), fmt_list_int(nrr).c_str());
+      for (int ir = 1; ir <= nrr + 1; ir++) std::fprintf(fp, "%s\n", fmt_e(cam.ri[ir], 12, 6).c_str());
+      for (int ir = 1; ir <= nrr + 1; ir++) std::fprintf(fp, "%s\n", fmt_e(ir <= nrr ? cam.rays_r[ir] : 0.0, 12, 6).c_str());
+    }
+    const double velo = (-passb + k * dnu) / nu0;
+    std::fprintf(fp, "        \n%s\n        \n%s\n        \n", fmt_list_real(velo * 2.99792458e5).c_str(),
+                 fmt_list_real(img[k]).c_str());
+    for (int ip = 0; ip < nphi; ip++)
+      for (int ir = 1; ir <= nrr; ir++) {
+        const size_t o = (size_t)(1 + (ir - 1) * nphi + ip) * nfr + k;
+        std::fprintf(fp, "%s  %1d\n", fmt_e(img[o], 10, 4).c_str(), (int)mask[o]);
+      }
+  }
+  std::fclose(fp);
+  return 0;
+}
+
 std::string posvel_file_name(const Model& m, int iline) {
   if (iline < 1 || iline > 99) return std::string();
   return "lineposvel_" + m.molname + "_" + std::to_string(iline) + ".dat";

@@ -88,6 +88,12 @@ int prepare_line(const Model& m, int iline, bool scaled, LinePrep& lp, std::stri
 double bplanck(double temp, double nu);                     // setup.F:937-952
 int bracket(const std::vector<double>& xx, double x);      // 1-based j with xx[j-1] < x <= xx[j]
 void finish_model(Model& m);   // derived quantities (aksmax, passband channel count)
+// lineposvelcirc_<molecule>_<iline>.dat, the circular image of a SAVE_IMCIR build
+// (telescope.F:1595-1615, 1346-1373; empty for iline > 99). img and mask: [nrays][nfr]
+// intensities and integration mask (imcir_cmask, accumulated over the run's lines).
+std::string imcir_file_name(const Model& m, int iline);
+int write_imcir_file(const std::string& path, const Model& m, const Camera& cam, int iline, const double* img,
+                     const unsigned char* mask, std::string& err);
 // lineposvel_<molecule>_<iline>.dat (telescope.F:1940-1961; empty for iline > 99)
 std::string posvel_file_name(const Model& m, int iline);
 // I and tau: [nfr][ny][nx] intensity and optical depth of line iline (1-based)

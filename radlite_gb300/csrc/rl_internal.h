@@ -132,6 +132,7 @@ struct rl_model {
   rl::PVSpec pvspec;
   rl::PVBuffers pv;
   // per-call buffers
+  rl::DevBuf dmask;   // circular-image integration mask (on request)
   rl::DevBuf dtab, dnsum, dwch, dvelo, dstar, dlc, dimg, dring, dflux, dscale, dcnt, dwork, derr, dlist;
 };
 

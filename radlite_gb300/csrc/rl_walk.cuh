@@ -15,11 +15,6 @@
 
 namespace rl {
 
-// Formal solution of the (line, channel) pairs list[0..nt) of lines l0.. of one ray.
-// The per-line tables carry the profile normalisation 0.56419583546/(3.33567e-6 nu0), so
-// the profile of every slot is rlw * exp(-u^2) with the node's shared 1/linewidth.
-// Work order: per 32-node chunk, per pair of slots (two independent channels per lane),
-// all nodes of the chunk; the slot state lives in shared memory between pairs.
 // compensated summation s += x (Kahan), c carries the lost low-order part
 template <typename T>
 __device__ __forceinline__ void kahan_add(T& s, T& c, T x) {
@@ -29,6 +24,11 @@ __device__ __forceinline__ void kahan_add(T& s, T& c, T x) {
   s = t;
 }
 
+// Formal solution of the (line, channel) pairs list[0..nt) of lines l0.. of one ray.
+// The per-line tables carry the profile normalisation 0.56419583546/(3.33567e-6 nu0), so
+// the profile of every slot is rlw * exp(-u^2) with the node's shared 1/linewidth.
+// Work order: per 32-node chunk, per pair of slots (two independent channels per lane),
+// all nodes of the chunk; the slot state lives in shared memory between pairs.
 // PV: also the optical depth of every slot, Kahan-compensated in P.tau / P.tauc (the slot's
 // image position), and no star mixing.
 template <typename T, int C, bool PV = false>
@@ -346,6 +346,10 @@ __device__ __forceinline__ void walk_item(const WalkParams<T>& P, int item, Warp
         if (outm) cc = cb + __ffs(outm) - 1;
       }
       const bool take = valid && (c == 0 || in || c == cc);
+      // integration mask of the circular-image file (imcir_cmask, telescope.F:548,575):
+      // channel 1 and the window channels
+      if (!PV && P.mask != nullptr && valid)
+        P.mask[((size_t)(l0 + l) * nb.nrays + ray) * P.nfr + c] = (unsigned char)(c == 0 || in);
       const unsigned m = __ballot_sync(0xffffffffu, take);
       if (take) list[nint + __popc(m & lanemask_lt())] = (unsigned short)((l << kChBits) | c);
       nint += __popc(m);

@@ -235,8 +235,10 @@ def line_freqs(cfg: DiskConfig, E, lines):
 
 
 def dust_frequency_grid(cfg: DiskConfig, E, lines):
+    """Log-spaced dust frequencies covering every line from line 1 to the last requested
+    one: a directory run renders lines 1.. whatever linespectrum.inp asks (main.F:204)."""
     nu = line_freqs(cfg, E, lines)
-    sel = nu[cfg.ilinestart - 1: cfg.ilinestart - 1 + cfg.nlines]
+    sel = nu[0: cfg.ilinestart - 1 + cfg.nlines]
     lo, hi = 0.8 * sel.min(), 1.25 * sel.max()
     return np.exp(np.linspace(math.log(lo), math.log(hi), cfg.nfreq_dust))
 
