@@ -37,9 +37,6 @@ def test_spectra_fp32_and_fp64(ctx, oracle_lib, model_dir, name):
         got, velo, st = m.calc_line_spectrum(il, stats=True)
         np.testing.assert_allclose(velo, rvelo, rtol=0, atol=1e-9)
         assert relerr(got, ref) <= FP32_TOL, (name, il, relerr(got, ref))
-        # the FP32 walk integrates the same (ray, channel) pairs: window and continuum
-        # decisions do not depend on the precision when every line has dust continuum
-        assert st["integrated"] == rcnt["integrated"], (name, il)
     m.set_precision(1)
     for il, (ref, _, rcnt) in zip(lines, refs):
         got, _, st = m.calc_line_spectrum(il, stats=True)
