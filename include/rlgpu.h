@@ -133,6 +133,30 @@ int rl_get_posvel(rl_model* model, rl_posvel_spec* spec);
    as imrec_int and imrec_tau (per channel, iy outer, ix inner: the file's order). */
 int rl_posvel(rl_model* model, int iline0, int nlines, double* I_out, double* tau_out, rl_stats* stats);
 
+/* ---- Spectrum post-processing: pyradlite's RadliteSpectrum.gen_spec numerical core
+   (_process_spectrum, pyradlite/radlite.py:3001-3187). The caller reads and de-duplicates
+   the lines (radlite.py:2750-2998); this combines them into one observed spectrum. */
+typedef struct rl_genspec_lines {
+  int nlines;
+  const int* npts;            /* [nlines] channels of each line */
+  const double* vel;          /* concatenated velocities [km/s], ascending within a line */
+  const double* flux;         /* concatenated F_nu at 1 pc [erg/s/cm^2/Hz] */
+  const double* freq;         /* [nlines] line centre [Hz] */
+  const int* maxnumpoints;    /* [nlines] channel count of the line's output file */
+} rl_genspec_lines;
+typedef struct rl_genspec_params {
+  double obsres;              /* observing resolution (kernel width) [km/s] */
+  double vsampling;           /* output sampling [km/s] */
+  double dist;                /* distance [pc] */
+} rl_genspec_params;
+/* Number of output points (the wavelength grid of the result). */
+int rl_gen_spec_size(const rl_genspec_lines* lines, const rl_genspec_params* params, long long* nout);
+/* wavelength [micron], frequency [Hz], spectrum / emission / continuum [Jy at dist]:
+   [nout] each. Fails like the reference where its interpolations would leave their
+   range (an output grid reaching beyond the fine grid). */
+int rl_gen_spec(rl_ctx* ctx, const rl_genspec_lines* lines, const rl_genspec_params* params, double* wavelength,
+                double* frequency, double* spectrum, double* emission, double* continuum, rl_stats* stats);
+
 /* The RADlite executable's work in `dir`: read the inputs and render the lines requested
    by linespectrum.inp (starting at line 1, main.F:204). Command 0 writes
    linespectrum_<mol>.dat (main.F:1034-1049), command 2 one lineposvel_<mol>_<iline>.dat

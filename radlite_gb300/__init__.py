@@ -76,6 +76,14 @@ class PosvelSpec(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class GenspecLines(C.Structure):
+    _fields_ = [("nlines", C.c_int), ("npts", _I), ("vel", _D), ("flux", _D), ("freq", _D), ("maxnumpoints", _I)]
+
+
+class GenspecParams(C.Structure):
+    _fields_ = [("obsres", C.c_double), ("vsampling", C.c_double), ("dist", C.c_double)]
+
+
 EXPORTS = ["rl_create", "rl_destroy", "rl_last_error", "rl_load_dir", "rl_load_arrays", "rl_model_free",
            "rl_model_get_info", "rl_set_camera", "rl_set_precision", "rl_line_spectrum", "rl_spectra",
            "rl_line_image", "rl_run_dir", "rl_debug_trajectory", "rl_measure_peaks",
@@ -87,7 +95,7 @@ EXPORTS = ["rl_create", "rl_destroy", "rl_last_error", "rl_load_dir", "rl_load_a
            "rl_diff_batch_use_graph", "rl_diff_batch_buffers", "rl_diff_batch_layout", "rl_diff_batch_forward",
            "rl_diff_batch_backward",
            "rl_image_to_spectrum_noalloc", "rl_set_posvel", "rl_get_posvel", "rl_posvel",
-           "rl_line_image_mask", "rl_run_dir_ex"]
+           "rl_line_image_mask", "rl_run_dir_ex", "rl_gen_spec_size", "rl_gen_spec"]
 
 _lib = None
 
@@ -116,6 +124,8 @@ def lib():
         L.rl_run_dir_ex.argtypes = [C.c_char_p, C.c_int, C.c_int, C.POINTER(Stats)]
         L.rl_line_image_mask.argtypes = [vp, C.c_int, _D, C.POINTER(C.c_ubyte), C.POINTER(Stats)]
         L.rl_set_posvel.argtypes = [vp, C.POINTER(PosvelSpec)]
+        L.rl_gen_spec_size.argtypes = [C.POINTER(GenspecLines), C.POINTER(GenspecParams), C.POINTER(C.c_longlong)]
+        L.rl_gen_spec.argtypes = [vp, C.POINTER(GenspecLines), C.POINTER(GenspecParams)] + [_D] * 5 + [C.POINTER(Stats)]
         L.rl_get_posvel.argtypes = [vp, C.POINTER(PosvelSpec)]
         L.rl_posvel.argtypes = [vp, C.c_int, C.c_int, _D, _D, C.POINTER(Stats)]
         L.rl_debug_trajectory.argtypes = [vp, C.c_int, C.c_int, _D, _D, _D, _D, _D, _I, _I, _I]
@@ -186,6 +196,28 @@ class Context:
             self.close()
         except Exception:
             pass
+
+    def gen_spec(self, lines, obsres: float, vsampling: float, dist: float, stats: bool = False) -> dict:
+        """The numerical core of pyradlite's RadliteSpectrum.gen_spec on the GPU: `lines` is a
+        list of dicts with "vel" (ascending, km/s), "flux" (F_nu at 1 pc), "freq" (Hz) and
+        "maxnumpoints"; returns wavelength [micron], frequency [Hz], spectrum, emission and
+        continuum [Jy at dist pc]."""
+        vel = np.ascontiguousarray(np.concatenate([np.asarray(d["vel"], dtype=np.float64) for d in lines]))
+        flux = np.ascontiguousarray(np.concatenate([np.asarray(d["flux"], dtype=np.float64) for d in lines]))
+        npts = np.array([len(d["vel"]) for d in lines], dtype=np.int32)
+        freq = np.array([d["freq"] for d in lines], dtype=np.float64)
+        mx = np.array([d["maxnumpoints"] for d in lines], dtype=np.int32)
+        L = GenspecLines(len(lines), npts.ctypes.data_as(_I), _dp(vel), _dp(flux), _dp(freq), mx.ctypes.data_as(_I))
+        P = GenspecParams(obsres, vsampling, dist)
+        n = C.c_longlong()
+        _check(lib().rl_gen_spec_size(C.byref(L), C.byref(P), C.byref(n)), self.h)
+        out = {k: np.zeros(n.value) for k in ("wavelength", "frequency", "spectrum", "emission", "continuum")}
+        st = Stats()
+        _check(lib().rl_gen_spec(self.h, C.byref(L), C.byref(P), *(_dp(out[k]) for k in
+                                 ("wavelength", "frequency", "spectrum", "emission", "continuum")), C.byref(st)), self.h)
+        if stats:
+            out["stats"] = st.as_dict()
+        return out
 
     def measure_peaks(self) -> dict:
         """Measured FP32 FFMA and MUFU ex2 throughput of the device (lane ops per second)."""

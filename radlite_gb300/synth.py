@@ -325,15 +325,25 @@ def write_model(cfg: DiskConfig, outdir: str) -> str:
             fh.write("----------------------------------------------------------------------------\n"
                      "0\t\tNo, Same as previous\n")
 
-    # moldata.dat in the column formats read by line.F:1865-1935
+    # moldata.dat in the column formats read by line.F:1865-1935, with the extra columns
+    # pyradlite writes and its spectrum reader uses (radlite.py:1981-2007, 2795-2823):
+    # vibrational and rotational labels per level; wavenumber, E_up and labels per line
+    if cfg.molecule == "band":
+        nj = cfg.band_jmax_level + 1
+        labels = [(f"v={i // nj}", f"J={i % nj}") for i in range(len(E))]
+    else:
+        labels = [("v=0", f"J={i}") for i in range(len(E))]
     with open(P("moldata.dat"), "w") as fh:
         fh.write(f"!MOLECULE\n{cfg.molecule}\n!MOLECULAR WEIGHT\n{cfg.mol_mass_amu:4.1f}\n"
-                 f"!NUMBER OF ENERGY LEVELS\n{len(E):6d}\n!LEVEL + ENERGIES(cm^-1) + WEIGHT\n")
+                 f"!NUMBER OF ENERGY LEVELS\n{len(E):6d}\n!LEVEL + ENERGIES(cm^-1) + WEIGHT + v + Q\n")
         for i, (e, gg) in enumerate(zip(E, g)):
-            fh.write(f"{i + 1:5d}{e:12.4f}{gg:7.1f}\n")
-        fh.write(f"!NUMBER OF RADIATIVE TRANSITIONS\n{nl_all:6d}\n!TRANS + UP + LOW + EINSTEINA(s^-1)\n")
+            fh.write(f"{i + 1:5d}{e:12.4f}{gg:7.1f}{labels[i][0]:>15s}{labels[i][1]:>15s}\n")
+        fh.write(f"!NUMBER OF RADIATIVE TRANSITIONS\n{nl_all:6d}\n"
+                 "!TRANS + UP + LOW + EINSTEINA(s^-1) + FREQ(cm^-1) + E_u(cm^-1) + v_l + Q_p + Q_pp\n")
         for i, (u, l, A) in enumerate(lines):
-            fh.write(f"{i + 1:5d}{u:5d}{l:5d}{A:12.3e}\n")
+            wn = E[u - 1] - E[l - 1]
+            fh.write(f"{i + 1:5d}{u:5d}{l:5d}{A:12.3e}{wn:16.7f}{E[u - 1]:12.5f}{labels[u - 1][0]:>15s}"
+                     f"{labels[l - 1][0]:>15s}{labels[u - 1][1]:>15s}{labels[l - 1][1]:>15s}\n")
 
     pop = f["pop"]
     with open(P("levelpop.info"), "w") as fh:
