@@ -210,7 +210,7 @@ class Context:
         L = GenspecLines(len(lines), npts.ctypes.data_as(_I), _dp(vel), _dp(flux), _dp(freq), mx.ctypes.data_as(_I))
         P = GenspecParams(obsres, vsampling, dist)
         n = C.c_longlong()
-        _check(lib().rl_gen_spec_size(C.byref(L), C.byref(P), C.byref(n)), self.h)
+        _check(lib().rl_gen_spec_size(C.byref(L), C.byref(P), C.byref(n)))
         out = {k: np.zeros(n.value) for k in ("wavelength", "frequency", "spectrum", "emission", "continuum")}
         st = Stats()
         _check(lib().rl_gen_spec(self.h, C.byref(L), C.byref(P), *(_dp(out[k]) for k in

@@ -17,6 +17,7 @@
 // (telescope.F:1662-1804).
 #include "rl_host.h"
 
+#include <charconv>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -34,60 +35,87 @@ struct Fail {
 
 // Record-oriented reader with Fortran list-directed semantics: each read statement
 // starts on a new record, consumes tokens across records as needed and drops the
-// remainder of its last record.
+// remainder of its last record. Tokens are views into the file buffer and numbers are
+// parsed with from_chars (correctly rounded, like strtod), without allocations.
 class Records {
  public:
   Records(const std::string& dir, const std::string& name) : name_(name) {
     std::ifstream f(dir + "/" + name, std::ios::binary);
     if (!f) fail("cannot open " + dir + "/" + name);
-    std::stringstream ss;
-    ss << f.rdbuf();
-    buf_ = ss.str();
+    f.seekg(0, std::ios::end);
+    const std::streamoff n = f.tellg();
+    f.seekg(0, std::ios::beg);
+    buf_.resize(n > 0 ? (size_t)n : 0);
+    if (n > 0) f.read(&buf_[0], n);
   }
   struct FromText {};
   Records(FromText, std::string text, std::string name) : name_(std::move(name)), buf_(std::move(text)) {}
-  bool line(std::string& out) {
+  // next record as [b, e) without the line end; false at the end of the file
+  bool view(const char*& b, const char*& e) {
     if (pos_ >= buf_.size()) return false;
-    size_t e = buf_.find('\n', pos_);
-    if (e == std::string::npos) e = buf_.size();
-    out.assign(buf_, pos_, e - pos_);
-    if (!out.empty() && out.back() == '\r') out.pop_back();
-    pos_ = e + 1;
+    const char* base = buf_.data();
+    const void* nl = std::memchr(base + pos_, '\n', buf_.size() - pos_);
+    const size_t end = nl ? (size_t)((const char*)nl - base) : buf_.size();
+    b = base + pos_;
+    e = base + end;
+    if (e > b && e[-1] == '\r') e--;
+    pos_ = end + 1;
     return true;
   }
-  void list(size_t n, std::vector<std::string>& toks) {
+  bool line(std::string& out) {
+    const char *b, *e;
+    if (!view(b, e)) return false;
+    out.assign(b, e);
+    return true;
+  }
+  struct Tok { const char* p; size_t n; };
+  void list(size_t n, std::vector<Tok>& toks) {
     toks.clear();
-    std::string l;
+    const char *b, *e;
     while (toks.size() < n) {
-      if (!line(l)) fail(name_ + ": unexpected end of file");
-      size_t i = 0;
-      while (i < l.size() && toks.size() < n) {
-        while (i < l.size() && (l[i] == ' ' || l[i] == '\t' || l[i] == ',')) i++;
-        if (i >= l.size()) break;
-        size_t j = i;
-        while (j < l.size() && l[j] != ' ' && l[j] != '\t' && l[j] != ',') j++;
-        toks.emplace_back(l.substr(i, j - i));
+      if (!view(b, e)) fail(name_ + ": unexpected end of file");
+      const char* i = b;
+      while (i < e && toks.size() < n) {
+        while (i < e && (*i == ' ' || *i == '\t' || *i == ',')) i++;
+        if (i >= e) break;
+        const char* j = i;
+        while (j < e && *j != ' ' && *j != '\t' && *j != ',') j++;
+        toks.push_back(Tok{i, (size_t)(j - i)});
         i = j;
       }
     }
   }
-  double num(const std::string& t) {
-    std::string b = t;
-    for (char& c : b) if (c == 'd' || c == 'D') c = 'e';
-    char* e = nullptr;
-    double v = std::strtod(b.c_str(), &e);
-    if (e == b.c_str()) fail(name_ + ": not a number: '" + t + "'");
-    if (*e == '+' || *e == '-') {   // Fortran exponent without a letter, e.g. 1.0+05
-      char* e2 = nullptr;
-      const long ex = std::strtol(e, &e2, 10);
-      if (e2 != e + 1 && *e2 == 0) return v * std::pow(10.0, (double)ex);
+  double num(const Tok& t) {
+    char tmp[64];
+    const char* b = t.p;
+    const char* e = t.p + t.n;
+    // Fortran D exponents and a leading '+' go through a small copy
+    bool copy = t.n < sizeof tmp && (*b == '+' || std::memchr(b, 'd', t.n) || std::memchr(b, 'D', t.n));
+    if (copy) {
+      size_t k = 0;
+      for (const char* c = (*b == '+' ? b + 1 : b); c < e; c++) tmp[k++] = (*c == 'd' || *c == 'D') ? 'e' : *c;
+      b = tmp;
+      e = tmp + k;
     }
-    if (*e != 0) fail(name_ + ": not a number: '" + t + "'");
+    double v = 0.0;
+    const auto r = std::from_chars(b, e, v);
+    if (r.ec == std::errc::invalid_argument || r.ptr == b) fail(name_ + ": not a number: '" + std::string(t.p, t.n) + "'");
+    if (r.ec == std::errc::result_out_of_range) {   // overflow and underflow as strtod gives them
+      const std::string z(b, r.ptr);
+      v = std::strtod(z.c_str(), nullptr);
+    }
+    const char* q = r.ptr;
+    if (q < e && (*q == '+' || *q == '-')) {   // Fortran exponent without a letter, e.g. 1.0+05
+      long ex = 0;
+      const auto r2 = std::from_chars(q + 1, e, ex);
+      if (r2.ec == std::errc() && r2.ptr == e && r2.ptr != q + 1) return v * std::pow(10.0, (double)(*q == '-' ? -ex : ex));
+    }
+    if (q != e) fail(name_ + ": not a number: '" + std::string(t.p, t.n) + "'");
     return v;
   }
   double d() { list(1, t_); return num(t_[0]); }
   int i() { return (int)d(); }
-  std::string s() { list(1, t_); return t_[0]; }
+  std::string s() { list(1, t_); return std::string(t_[0].p, t_[0].n); }
   void dn(size_t n, double* out) {
     list(n, t_);
     for (size_t k = 0; k < n; k++) out[k] = num(t_[k]);
@@ -102,7 +130,7 @@ class Records {
  private:
   std::string name_, buf_;
   size_t pos_ = 0;
-  std::vector<std::string> t_;
+  std::vector<Tok> t_;
 };
 
 bool exists(const std::string& dir, const std::string& name) {
