@@ -94,6 +94,12 @@ int rl_last_error(rl_ctx* ctx, char* buf, size_t len);
 int rl_load_dir(rl_ctx* ctx, const char* dir, rl_model** model);
 int rl_load_arrays(rl_ctx* ctx, const rl_model_arrays* arrays, rl_model** model);
 int rl_model_free(rl_model* model);
+/* 64-bit hash of everything the model holds from its inputs (inspection and tests; no
+   reference counterpart). Input cache: with the environment variable RLGPU_INPUT_CACHE
+   naming a writable directory, rl_load_dir keeps each parsed directory there in binary,
+   keyed by its real path and the size and modification time of every input file the
+   parse opened or probed, and reads that binary while the files are unchanged. */
+int rl_model_checksum(rl_model* model, unsigned long long* checksum);
 int rl_model_get_info(rl_model* model, rl_model_info* info);
 
 /* Camera override (radlite.inp / linespectrum.inp values are the default). */

@@ -95,7 +95,8 @@ EXPORTS = ["rl_create", "rl_destroy", "rl_last_error", "rl_load_dir", "rl_load_a
            "rl_diff_batch_use_graph", "rl_diff_batch_buffers", "rl_diff_batch_layout", "rl_diff_batch_forward",
            "rl_diff_batch_backward",
            "rl_image_to_spectrum_noalloc", "rl_set_posvel", "rl_get_posvel", "rl_posvel",
-           "rl_line_image_mask", "rl_run_dir_ex", "rl_gen_spec_size", "rl_gen_spec"]
+           "rl_line_image_mask", "rl_run_dir_ex", "rl_gen_spec_size", "rl_gen_spec",
+           "rl_model_checksum"]
 
 _lib = None
 
@@ -115,6 +116,7 @@ def lib():
         L.rl_load_arrays.argtypes = [vp, C.POINTER(ModelArrays), C.POINTER(vp)]
         L.rl_model_free.argtypes = [vp]
         L.rl_model_get_info.argtypes = [vp, C.POINTER(ModelInfo)]
+        L.rl_model_checksum.argtypes = [vp, C.POINTER(C.c_ulonglong)]
         L.rl_set_camera.argtypes = [vp, C.c_double, C.c_int, C.c_int, C.c_int]
         L.rl_set_precision.argtypes = [vp, C.c_int]
         L.rl_line_spectrum.argtypes = [vp, C.c_int, _D, _D, C.POINTER(Stats)]
@@ -293,6 +295,12 @@ class Model:
             self.free()
         except Exception:
             pass
+
+    def checksum(self) -> int:
+        """Hash of everything the model holds from its inputs."""
+        v = C.c_ulonglong()
+        _check(lib().rl_model_checksum(self.h, C.byref(v)), self._ch)
+        return v.value
 
     def info(self) -> dict:
         i = ModelInfo()

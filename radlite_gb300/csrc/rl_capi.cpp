@@ -424,6 +424,12 @@ int rl_model_free(rl_model* md) {
   return 0;
 }
 
+int rl_model_checksum(rl_model* md, unsigned long long* out) {
+  if (!md || !out) return set_err(nullptr, RL_ERR_ARG, "rl_model_checksum: null argument");
+  *out = model_checksum(md->m);
+  return 0;
+}
+
 int rl_model_get_info(rl_model* md, rl_model_info* info) {
   if (!md || !info) return set_err(nullptr, RL_ERR_ARG, "rl_model_get_info: null argument");
   const Model& m = md->m;

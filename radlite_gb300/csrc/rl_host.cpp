@@ -17,6 +17,9 @@
 // (telescope.F:1662-1804).
 #include "rl_host.h"
 
+#include <sys/stat.h>
+#include <unistd.h>
+
 #include <charconv>
 #include <cmath>
 #include <cstdio>
@@ -33,6 +36,29 @@ struct Fail {
 };
 [[noreturn]] void fail(const std::string& m) { throw Fail{m}; }
 
+// Every input file a parse opens or probes, with its size and modification time: the key
+// of the binary input cache.
+struct InputStamp {
+  std::string name;
+  long long size = -1, mtime_ns = 0;   // size -1: absent
+};
+thread_local std::vector<InputStamp>* g_stamps = nullptr;
+
+InputStamp stat_input(const std::string& dir, const std::string& name) {
+  InputStamp s;
+  s.name = name;
+  struct stat st;
+  if (::stat((dir + "/" + name).c_str(), &st) == 0) {
+    s.size = (long long)st.st_size;
+    s.mtime_ns = (long long)st.st_mtim.tv_sec * 1000000000LL + (long long)st.st_mtim.tv_nsec;
+  }
+  return s;
+}
+
+void stamp(const std::string& dir, const std::string& name) {
+  if (g_stamps) g_stamps->push_back(stat_input(dir, name));
+}
+
 // Record-oriented reader with Fortran list-directed semantics: each read statement
 // starts on a new record, consumes tokens across records as needed and drops the
 // remainder of its last record. Tokens are views into the file buffer and numbers are
@@ -40,6 +66,7 @@ struct Fail {
 class Records {
  public:
   Records(const std::string& dir, const std::string& name) : name_(name) {
+    stamp(dir, name);
     std::ifstream f(dir + "/" + name, std::ios::binary);
     if (!f) fail("cannot open " + dir + "/" + name);
     f.seekg(0, std::ios::end);
@@ -134,6 +161,7 @@ class Records {
 };
 
 bool exists(const std::string& dir, const std::string& name) {
+  stamp(dir, name);
   std::ifstream f(dir + "/" + name);
   return (bool)f;
 }
@@ -519,7 +547,7 @@ void finish_model(Model& m) {
   m.vmax = 0.5 * (m.nfr - 1) * m.dv;
 }
 
-int load_dir(const std::string& dir, Model& m, std::string& err) {
+static int parse_dir(const std::string& dir, Model& m, std::string& err) {
   try {
     read_radlite_inp(dir, m);
     read_grid(dir, m);
@@ -551,6 +579,170 @@ int load_dir(const std::string& dir, Model& m, std::string& err) {
     return -1;
   }
   return 0;
+}
+
+namespace {
+
+// Every member of Model, in one order, for the cache writer, reader and checksum.
+template <typename V>
+void visit_model(Model& m, V& v) {
+  v(m.nr); v(m.nth); v(m.ny); v(m.R); v(m.TH); v(m.rho); v(m.abun); v(m.lw); v(m.vel);
+  v(m.nspec); v(m.nsize); v(m.drho); v(m.dtemp); v(m.ncont); v(m.cnu); v(m.kabs); v(m.ksca); v(m.scat);
+  v(m.nlev); v(m.pop); v(m.molname); v(m.molfile); v(m.Ecm); v(m.gdeg); v(m.lup); v(m.ldn); v(m.Aud); v(m.lfreq);
+  v(m.umass); v(m.rstar); v(m.starcont); v(m.starpump); v(m.outer_bc); v(m.line_dust); v(m.incl_rad); v(m.nphi);
+  v(m.dbdr); v(m.nrext); v(m.vmax); v(m.dv); v(m.radvelo); v(m.nlspec); v(m.ilstart); v(m.style); v(m.nfr);
+  v(m.command); v(m.pv.nx); v(m.pv.ny); v(m.pv.szimx); v(m.pv.szimy); v(m.pv.phioff); v(m.pv.xoff); v(m.pv.yoff);
+  v(m.pv.addstar); v(m.aksmax);
+}
+
+struct Writer {
+  std::string out;
+  void raw(const void* p, size_t n) { out.append(static_cast<const char*>(p), n); }
+  void operator()(int& x) { raw(&x, sizeof x); }
+  void operator()(long long& x) { raw(&x, sizeof x); }
+  void operator()(double& x) { raw(&x, sizeof x); }
+  void operator()(std::string& x) { long long n = (long long)x.size(); raw(&n, sizeof n); raw(x.data(), x.size()); }
+  template <typename T> void operator()(std::vector<T>& x) {
+    long long n = (long long)x.size();
+    raw(&n, sizeof n);
+    if (n) raw(x.data(), sizeof(T) * x.size());
+  }
+};
+
+struct Reader {
+  const char* p;
+  const char* e;
+  bool ok = true;
+  void raw(void* d, size_t n) {
+    if (!ok || (size_t)(e - p) < n) { ok = false; return; }
+    std::memcpy(d, p, n);
+    p += n;
+  }
+  long long count() {
+    long long n = 0;
+    raw(&n, sizeof n);
+    if (n < 0 || n > (long long)(e - p)) { ok = false; n = 0; }
+    return n;
+  }
+  void operator()(int& x) { raw(&x, sizeof x); }
+  void operator()(long long& x) { raw(&x, sizeof x); }
+  void operator()(double& x) { raw(&x, sizeof x); }
+  void operator()(std::string& x) { const long long n = count(); x.assign(ok ? p : "", ok ? (size_t)n : 0); if (ok) p += n; }
+  template <typename T> void operator()(std::vector<T>& x) {
+    const long long n = count();
+    if (!ok || (size_t)n * sizeof(T) > (size_t)(e - p)) { ok = false; return; }
+    x.resize((size_t)n);
+    raw(x.data(), sizeof(T) * (size_t)n);
+  }
+};
+
+// 64-bit FNV-1a over bytes (cache file names and the model checksum)
+struct Hasher {
+  unsigned long long h = 1469598103934665603ULL;
+  void raw(const void* p, size_t n) {
+    const unsigned char* b = static_cast<const unsigned char*>(p);
+    for (size_t i = 0; i < n; i++) { h ^= b[i]; h *= 1099511628211ULL; }
+  }
+  void operator()(int& x) { raw(&x, sizeof x); }
+  void operator()(double& x) { raw(&x, sizeof x); }
+  void operator()(std::string& x) { raw(x.data(), x.size()); raw("\0", 1); }
+  template <typename T> void operator()(std::vector<T>& x) {
+    const long long n = (long long)x.size();
+    raw(&n, sizeof n);
+    if (n) raw(x.data(), sizeof(T) * x.size());
+  }
+};
+
+constexpr char kCacheMagic[8] = {'R', 'L', 'G', 'P', 'U', 'I', 'N', '2'};
+
+std::string cache_path(const std::string& cache_dir, const std::string& key) {
+  Hasher h;
+  std::string k = key;
+  h(k);
+  char b[32];
+  std::snprintf(b, sizeof b, "%016llx.rlin", h.h);
+  return cache_dir + "/" + b;
+}
+
+std::string real_dir(const std::string& dir) {
+  char buf[4096];
+  return ::realpath(dir.c_str(), buf) ? std::string(buf) : dir;
+}
+
+// The cached model of `dir` if every input it was parsed from is unchanged.
+bool load_cached(const std::string& cache_dir, const std::string& dir, Model& m) {
+  const std::string key = real_dir(dir);
+  std::ifstream f(cache_path(cache_dir, key), std::ios::binary);
+  if (!f) return false;
+  f.seekg(0, std::ios::end);
+  const std::streamoff n = f.tellg();
+  f.seekg(0, std::ios::beg);
+  if (n <= 0) return false;
+  std::string buf((size_t)n, '\0');
+  if (!f.read(&buf[0], n)) return false;
+  if (buf.size() < sizeof kCacheMagic || std::memcmp(buf.data(), kCacheMagic, sizeof kCacheMagic) != 0) return false;
+  Reader r{buf.data() + sizeof kCacheMagic, buf.data() + buf.size()};
+  std::string kdir;
+  r(kdir);
+  if (!r.ok || kdir != key) return false;
+  long long ns = 0;
+  r(ns);
+  if (!r.ok || ns < 0 || ns > 4096) return false;
+  for (long long i = 0; i < ns; i++) {
+    InputStamp s;
+    r(s.name); r(s.size); r(s.mtime_ns);
+    if (!r.ok) return false;
+    const InputStamp now = stat_input(dir, s.name);
+    if (now.size != s.size || now.mtime_ns != s.mtime_ns) return false;
+  }
+  Model c;
+  visit_model(c, r);
+  if (!r.ok || r.p != r.e) return false;
+  m = std::move(c);
+  return true;
+}
+
+void save_cached(const std::string& cache_dir, const std::string& dir, Model& m, std::vector<InputStamp>& stamps) {
+  Writer w;
+  w.raw(kCacheMagic, sizeof kCacheMagic);
+  std::string key = real_dir(dir);
+  w(key);
+  long long ns = (long long)stamps.size();
+  w(ns);
+  for (auto& s : stamps) { w(s.name); w(s.size); w(s.mtime_ns); }
+  visit_model(m, w);
+  const std::string path = cache_path(cache_dir, key);
+  const std::string tmp = path + "." + std::to_string((long long)::getpid()) + ".tmp";
+  FILE* fp = std::fopen(tmp.c_str(), "wb");
+  if (!fp) return;   // the cache is an optimisation: a failure to write it is not an error
+  const bool ok = std::fwrite(w.out.data(), 1, w.out.size(), fp) == w.out.size();
+  if (std::fclose(fp) == 0 && ok) std::rename(tmp.c_str(), path.c_str());
+  else std::remove(tmp.c_str());
+}
+
+}  // namespace
+
+// Parse the input files of `dir`. With RLGPU_INPUT_CACHE set to a writable directory,
+// the parsed model is also kept there in binary, keyed by the directory's real path and
+// by the size and modification time of every input file the parse opened or probed; a
+// later load of an unchanged directory reads the binary instead of the text.
+int load_dir(const std::string& dir, Model& m, std::string& err) {
+  const char* cdir = std::getenv("RLGPU_INPUT_CACHE");
+  const bool cache = cdir && *cdir;
+  if (cache && load_cached(cdir, dir, m)) return 0;
+  std::vector<InputStamp> stamps;
+  g_stamps = cache ? &stamps : nullptr;
+  const int rc = parse_dir(dir, m, err);
+  g_stamps = nullptr;
+  if (rc == 0 && cache) save_cached(cdir, dir, m, stamps);
+  return rc;
+}
+
+unsigned long long model_checksum(const Model& m) {
+  Hasher h;
+  Model& mm = const_cast<Model&>(m);
+  visit_model(mm, h);
+  return h.h;
 }
 
 int setup_camera(const Model& m, double incl, int nphi, int dbdr, int nrext, Camera& cam, std::string& err) {

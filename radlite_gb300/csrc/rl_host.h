@@ -81,7 +81,10 @@ struct LinePrep {
   std::vector<double> nsum;                    // [ncell]
 };
 
+// Parse the input files of `dir` (or read their binary cache, see RLGPU_INPUT_CACHE).
 int load_dir(const std::string& dir, Model& m, std::string& err);
+// 64-bit hash over every member of the model (equal models, equal hashes)
+unsigned long long model_checksum(const Model& m);
 int setup_camera(const Model& m, double incl_rad, int nphi, int dbdr, int nrext, Camera& cam, std::string& err);
 int setup_pv_camera(const Model& m, const PVSpec& spec, double incl_rad, PVCamera& cam, std::string& err);
 int prepare_line(const Model& m, int iline, bool scaled, LinePrep& lp, std::string& err);
