@@ -282,12 +282,16 @@ def ours(args):
     out = None
     if rank == 0:
         cpu = None
-        if not args.no_cpu:
-            with tempfile.TemporaryDirectory() as tmp:
+        extras = {}
+        with tempfile.TemporaryDirectory() as tmp:
+            if not args.no_cpu:
                 s = cpu_sample(cfg, args.cpu_stride, os.cpu_count() or 1, tmp)
-            cpu = {"value": s["value"], "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
-                   "sample": f"band_large line {cfg.ilinestart}, incl {INCLS[0]:.0f} deg, every {args.cpu_stride}th "
-                             f"ray ({s['rays']} rays x {nfr} channels), FP64 C restatement, one process per core"}
+                cpu = {"value": s["value"], "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+                       "sample": f"band_large line {cfg.ilinestart}, incl {INCLS[0]:.0f} deg, every "
+                                 f"{args.cpu_stride}th ray ({s['rays']} rays x {nfr} channels), FP64 C restatement, "
+                                 f"one process per core"}
+            if not args.no_extras:
+                extras = extras_case(ctx, cfg, arr, tmp, with_cpu=not args.no_cpu)
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": ms, "wall_ms_per_step": wall * 1e3,
                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32 (fp64 geometry)",
@@ -311,12 +315,112 @@ def ours(args):
                "batched": batched,
                "adjoint": adjoint,
                "fit": fitting,
+               "posvel": extras.get("posvel"),
+               "genspec": extras.get("genspec"),
+               "input": extras.get("input"),
                "cpu_baseline": cpu,
                "clocks": clk.summary(),
                "gpu_launches": args.steps * len(INCLS) * 4}
         print(json.dumps(out), flush=True)
     ctx.close()
     return 0
+
+
+def extras_case(ctx, cfg, arr, tmp, with_cpu=True):
+    """The rows beside the raytrace: the position-velocity cube of the band_large disk, the
+    spectrum post-processing of a 2000-line band, and the input parsing of the band_large
+    directory (text and binary cache). Each with its CPU counterpart where it has one."""
+    import numpy as np
+    import radlite_gb300 as rl
+    from radlite_gb300 import synth
+    out = {}
+    # position-velocity cube: 256 x 256 pixels over the disk diameter, 4 lines x 200 channels
+    m = ctx.load_arrays(arr, camera(cfg, INCLS[0]))
+    size = 2.0 * float(arr["r"][-1])
+    npx, nl = 256, 4
+    m.set_posvel(npx, npx, size, size, addstar=1)
+    m.posvel(cfg.ilinestart, nl)
+    runs = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        _, _, st = m.posvel(cfg.ilinestart, nl, stats=True)
+        runs.append((time.perf_counter() - t0, st))
+    wall = statistics.median(r[0] for r in runs)
+    st = runs[-1][1]
+    dev_ms = st["geometry_ms"] + st["upload_ms"] + st["walk_ms"] + st["reduce_ms"]
+    pv = {"workload": f"band_large incl {INCLS[0]:.0f} deg, {npx}x{npx} pixels over the disk diameter, "
+                      f"lines {cfg.ilinestart}-{cfg.ilinestart + nl - 1} x 200 channels, intensity and optical depth",
+          "traced_rays": st["nrays"], "ray_channels": st["ray_channels"], "device_ms": dev_ms, "walk_ms": st["walk_ms"],
+          "geometry_ms": st["geometry_ms"], "ray_channels_per_s": st["ray_channels"] / (dev_ms * 1e-3),
+          "e2e_ray_channels_per_s": st["ray_channels"] / wall, "d2h_bytes": st["d2h_bytes"]}
+    m.free()
+    d = os.path.join(tmp, "band_large_i20")
+    if with_cpu:
+        from oracle import pyoracle
+        if not os.path.exists(os.path.join(d, "radlite.inp")):
+            synth.write_model(synth.config_by_name("band_large", incl_deg=INCLS[0]), d)
+        pyoracle.build()
+        o = pyoracle.Oracle(d)
+        x0, z0, b, _ = o.pv_rays(npx, npx, size, size, 0.0, 0.0, 0.0, 1)
+        inside = np.flatnonzero(b < 0.999 * float(arr["r"][-1]))
+        pick = inside[:: max(1, len(inside) // 16)][:16]
+        t0 = time.perf_counter()
+        for r in pick:
+            o.ray_spectrum(cfg.ilinestart, x0[r], z0[r])
+        cpu_s = time.perf_counter() - t0
+        pv["cpu_baseline"] = {"value": len(pick) * o.nfr / cpu_s, "unit": "ray-channels/s", "cores": 1, "kind": "port",
+                              "sample": f"{len(pick)} pixel rays x {o.nfr} channels of line {cfg.ilinestart}, FP64 C "
+                                        "restatement, one core"}
+        del o
+    out["posvel"] = pv
+    # spectrum post-processing of a 2000-line band (201 channels per line)
+    rng = np.random.default_rng(5)
+    lines = []
+    vel = np.linspace(-20.0, 20.0, 201)
+    for i in range(2000):
+        flux = (1 + 0.001 * vel) * rng.uniform(1e-20, 2e-20) + rng.uniform(0, 4e-20) * np.exp(-(vel / rng.uniform(2, 6)) ** 2)
+        lines.append({"vel": vel, "flux": flux, "freq": 2.99792458e10 * rng.uniform(2000.0, 2200.0), "maxnumpoints": 201})
+    ctx.gen_spec(lines, 3.0, 1.0, 140.0)
+    gs = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        o2 = ctx.gen_spec(lines, 3.0, 1.0, 140.0, stats=True)
+        gs.append((time.perf_counter() - t0, o2["stats"]))
+    g = {"workload": "2000 lines x 201 channels over 2000-2200 cm^-1, obsres 3 km/s, sampling 1 km/s",
+         "fine_points": gs[-1][1]["nrays"], "output_points": gs[-1][1]["nfr"],
+         "device_ms": gs[-1][1]["upload_ms"] + gs[-1][1]["walk_ms"], "e2e_ms": statistics.median(x[0] for x in gs) * 1e3}
+    if with_cpu:
+        from oracle import genspec_ref
+        t0 = time.perf_counter()
+        ref = genspec_ref.process(lines, 3.0, 1.0, 140.0)
+        g["cpu_baseline"] = {"value": (time.perf_counter() - t0) * 1e3, "unit": "ms", "cores": 1, "kind": "port",
+                             "sample": "the whole workload, numpy restatement of _process_spectrum"}
+        g["max_rel_diff_vs_cpu"] = float(np.max(np.abs(o2["spectrum"] - ref["spectrum"]) / np.abs(ref["spectrum"]).max()))
+    out["genspec"] = g
+    # input parsing of the band_large directory: text, then the binary cache
+    if not os.path.exists(os.path.join(d, "radlite.inp")):
+        synth.write_model(synth.config_by_name("band_large", incl_deg=INCLS[0]), d)
+    t0 = time.perf_counter()
+    rl.load_dir_host(d).free()
+    text_s = time.perf_counter() - t0
+    cache = os.path.join(tmp, "input_cache")
+    os.makedirs(cache, exist_ok=True)
+    old = os.environ.get("RLGPU_INPUT_CACHE")
+    os.environ["RLGPU_INPUT_CACHE"] = cache
+    rl.load_dir_host(d).free()
+    ts = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        rl.load_dir_host(d).free()
+        ts.append(time.perf_counter() - t0)
+    if old is None:
+        del os.environ["RLGPU_INPUT_CACHE"]
+    else:
+        os.environ["RLGPU_INPUT_CACHE"] = old
+    nbytes = sum(os.path.getsize(os.path.join(d, f)) for f in os.listdir(d))
+    out["input"] = {"workload": f"band_large input directory ({nbytes / 1e6:.0f} MB of text)",
+                    "text_parse_s": text_s, "cached_load_s": statistics.median(ts)}
+    return out
 
 
 def batched_case(ctx, n_models, steps, tune_stride=32):
@@ -463,6 +567,8 @@ def main():
     ap.add_argument("--only-fit", action="store_true", help="run only the batched fitting-step comparison")
     ap.add_argument("--fit-models", type=int, default=64)
     ap.add_argument("--no-diff", action="store_true", help="skip the adjoint and fitting measurements")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the position-velocity, gen_spec and input-parsing measurements")
     args = ap.parse_args()
     if args.only_fit:
         import radlite_gb300 as rl
