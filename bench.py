@@ -533,9 +533,38 @@ def fit_case(ctx, n_models=64, steps=5, plain_models=8):
 
 
 def profile_case(args):
-    """One pass of a named workload (geometry, walk, reduction), for profiler captures."""
+    """One pass of a named workload (geometry, walk, reduction), for profiler captures.
+    "posvel_disk": the 200x100 disk's 128x128-pixel position-velocity cube of 2 lines;
+    "genspec_band": gen_spec of 500 lines x 201 channels."""
+    import numpy as np
     import radlite_gb300 as rl
     from radlite_gb300 import synth
+    if args.workload == "genspec_band":
+        rng = np.random.default_rng(5)
+        vel = np.linspace(-20.0, 20.0, 201)
+        lines = [{"vel": vel, "flux": (1 + 0.001 * vel) * rng.uniform(1e-20, 2e-20)
+                  + rng.uniform(0, 4e-20) * np.exp(-(vel / rng.uniform(2, 6)) ** 2),
+                  "freq": 2.99792458e10 * rng.uniform(2000.0, 2050.0), "maxnumpoints": 201} for _ in range(500)]
+        ctx = rl.Context(0)
+        o = ctx.gen_spec(lines, 3.0, 1.0, 140.0, stats=True)
+        print(json.dumps({"workload": args.workload, "fine_points": o["stats"]["nrays"],
+                          "device_ms": o["stats"]["walk_ms"]}), flush=True)
+        ctx.close()
+        return 0
+    if args.workload == "posvel_disk":
+        cfg = synth.config_by_name("adjoint_disk")
+        arr = synth.model_arrays(cfg)
+        ctx = rl.Context(0)
+        m = ctx.load_arrays(arr, camera(cfg, cfg.incl_deg))
+        size = 2.0 * float(arr["r"][-1])
+        m.set_posvel(128, 128, size, size, addstar=1)
+        _, _, st = m.posvel(cfg.ilinestart, 2, stats=True)
+        print(json.dumps({"workload": args.workload, "steps": st["steps"], "walk_ms": st["walk_ms"],
+                          "geometry_ms": st["geometry_ms"], "nrays": st["nrays"], "ray_channels": st["ray_channels"]}),
+              flush=True)
+        m.free()
+        ctx.close()
+        return 0
     cfg = synth.config_by_name(args.workload)
     arr = synth.model_arrays(cfg)
     ctx = rl.Context(0)
