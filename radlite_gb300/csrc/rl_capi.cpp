@@ -514,6 +514,7 @@ int rl_line_image_mask(rl_model* md, int iline, double* image_out, unsigned char
 int rl_run_dir(const char* dir, int device, rl_stats* st) { return rl_run_dir_ex(dir, device, 0, st); }
 
 int rl_run_dir_ex(const char* dir, int device, int flags, rl_stats* st) {
+  if (flags & ~RL_RUN_SAVE_IMCIR) return set_err(nullptr, RL_ERR_ARG, "rl_run_dir_ex: unknown flags");
   rl_ctx* ctx = nullptr;
   int rc = rl_create(&ctx, device);
   if (rc) return rc;

@@ -77,3 +77,6 @@ def test_batch_and_diff_entry_points_check_arguments(gpu_lib):
     assert L.rl_diff_batch_forward(None, None) == -1
     assert L.rl_run_manifest(None, 0, None) == -1
     assert "null" in gpu_lib._err()
+    assert L.rl_run_dir_ex(b".", 0, 8, None) == -1 and "unknown flags" in gpu_lib._err()
+    assert L.rl_posvel(None, 1, 1, None, None, None) == -1
+    assert L.rl_gen_spec(None, None, None, None, None, None, None, None, None) == -1
