@@ -214,6 +214,9 @@ static int gs_host(const rl_genspec_lines* in, const rl_genspec_params* p, GsHos
   int imax = 0;
   for (int l = 0; l < nl; l++) {
     if (in->npts[l] < 2) { err = "gen_spec: a line needs at least 2 channels"; return -1; }
+    // the reference leaves lines of frequency 0 out of the grid range but still divides
+    // by their frequency (radlite.py:3045, 3097); such lines are rejected here
+    if (!(in->freq[l] > 0.0)) { err = "gen_spec: a line's frequency is not positive"; return -1; }
     for (int i = 1; i < in->npts[l]; i++)
       if (!(in->vel[off + i] > in->vel[off + i - 1])) { err = "gen_spec: velocities must ascend"; return -1; }
     // the continuum is evaluated at velocity 0 (interp1d's bounds check in the reference)
@@ -232,13 +235,11 @@ static int gs_host(const rl_genspec_lines* in, const rl_genspec_params* p, GsHos
   double mulo = 0, muhi = 0;
   bool any = false;
   for (int l = 0; l < nl; l++) {
-    if (in->freq[l] == 0.0) continue;
     const double mu = kCinMu / 1.0 / in->freq[l];
     if (!any || mu < mulo) mulo = mu;
     if (!any || mu > muhi) muhi = mu;
     any = true;
   }
-  if (!any) { err = "gen_spec: every line has frequency 0"; return -1; }
   h.mumin = mulo - (h.boxwidth * 1.0e9 * mulo / kCinMu);
   h.mumax = muhi + (h.boxwidth * 1.0e9 * muhi / kCinMu);
   const double g = 1 + (h.vres / 1.0 / kCinKm);
