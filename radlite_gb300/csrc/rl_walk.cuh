@@ -24,174 +24,6 @@ __device__ __forceinline__ void kahan_add(T& s, T& c, T x) {
   s = t;
 }
 
-// One pass of the walk over a 32-node chunk: NP slots per lane (slot indices jb..jb+NP-1),
-// NP independent chains interleaved. A tile's last pass with at most two valid slots runs
-// the NP = 2 instance, so that empty slots are not computed.
-template <typename T, int C, bool PV, int NP>
-__device__ __forceinline__ long long walk_pass(const WalkParams<T>& P, WarpStage<T>& S, SlotState<T, C>& SS,
-                                               SubWork<T>& SW, const unsigned short* list, int lane, int ray, int l0,
-                                               int kb, int nn, int n0, int star_node, int jb) {
-  const NodeBuf<T>& nb = P.nb;
-  long long steps = 0;
-  T I[NP], j0[NP], a0[NP], S0[NP], w[NP];
-  int Ls[NP], lsl[NP];
-  int nv = 0;
-#pragma unroll
-  for (int u = 0; u < NP; u++) {
-    const int j = jb + u;
-    if (j < C) {
-      I[u] = SS.I[j][lane]; j0[u] = SS.j0[j][lane]; a0[u] = SS.a0[j][lane]; S0[u] = SS.S0[j][lane];
-      w[u] = SS.w[j][lane]; Ls[u] = SS.ll[j][lane];
-    } else {
-      I[u] = 0; j0[u] = 0; a0[u] = 0; S0[u] = 0; w[u] = 0; Ls[u] = -1;
-    }
-    lsl[u] = Ls[u] < 0 ? 0 : Ls[u];
-    nv += Ls[u] >= 0 ? 1 : 0;
-  }
-  T tau[NP], tcp[NP];
-  size_t ta[NP];
-  if constexpr (PV) {
-#pragma unroll
-    for (int u = 0; u < NP; u++) {
-      tau[u] = 0; tcp[u] = 0; ta[u] = 0;
-      if (Ls[u] >= 0) {
-        ta[u] = ((size_t)(l0 + Ls[u]) * nb.nrays + ray) * P.nfr +
-                (list[(jb + u) * 32 + lane] & (kMaxChannels - 1));
-        tau[u] = P.tau[ta[u]]; tcp[u] = P.tauc[ta[u]];
-      }
-    }
-  }
-  for (int n = n0; n < nn; n++) {
-    const int g = kb + n;
-    const unsigned fl = S.flags[n + 1];
-    if (g == star_node) {
-#pragma unroll
-      for (int u = 0; u < NP; u++)
-        if (Ls[u] >= 0)
-          I[u] = ((T)1 - P.fstar) * I[u] +
-                 P.fstar * P.star[(size_t)(l0 + Ls[u]) * P.nfr + (list[(jb + u) * 32 + lane] & (kMaxChannels - 1))];
-    }
-    const T vl1 = S.vl[n + 1], rl = S.rlw[n + 1], hds = S.hds[n + 1];
-    if (!(fl & kFlagInit)) {
-      // SUBGRID window test of the reference (line.F:4733-4742): slots whose refined
-      // window [s_c - 3l, s_c + 3l] overlaps (0, ds) keep their state here and are
-      // refined below; all others take one formal-solution step
-      bool ov[NP];
-      bool any = false;
-#pragma unroll
-      for (int u = 0; u < NP; u++) ov[u] = false;
-      if (fl & kFlagSub) {
-        const T vl0 = S.vl[n], dsf = S.ds[n + 1], hw3 = S.hw3[n + 1];
-#pragma unroll
-        for (int u = 0; u < NP; u++) {
-          const T s_c = sizeof(T) == 8 ? dsf * (w[u] - vl0) / S.dvs[n + 1] : dsf * (w[u] - vl0) * S.idvs[n + 1];
-          ov[u] = Ls[u] >= 0 && (s_c + hw3 > (T)0) && (s_c - hw3 < dsf);
-          any = any || ov[u];
-        }
-        any = __any_sync(0xffffffffu, any);
-      }
-      T j1[NP], a1[NP], S1[NP], dt[NP], th[NP];
-      bool ser_all = true, dir_all = true;
-#pragma unroll
-      for (int u = 0; u < NP; u++) {
-        const LineVals<T> v = S.lv[lsl[u]][n + 1];
-        const T ph = profile(w[u], vl1, rl, rl);
-        j1[u] = v.jd + v.jf * ph;
-        a1[u] = v.ad + v.af * ph;
-        S1[u] = a1[u] > (T)0 ? j1[u] * Math<T>::rcp(a1[u]) : (T)0;
-        dt[u] = (a0[u] + a1[u]) * hds;
-        th[u] = (j0[u] + j1[u]) * hds;
-        const bool ser = dt[u] < (T)0.25;
-        ser_all = ser_all && ser;
-        dir_all = dir_all && !ser;
-      }
-      ser_all = __all_sync(0xffffffffu, ser_all);
-      dir_all = __all_sync(0xffffffffu, dir_all);
-      T x[NP], ca[NP], cb[NP];
-      if (ser_all) {
-#pragma unroll
-        for (int u = 0; u < NP; u++) Math<T>::series(dt[u], x[u], ca[u], cb[u]);
-      } else if (dir_all) {
-#pragma unroll
-        for (int u = 0; u < NP; u++) Math<T>::direct(dt[u], x[u], ca[u], cb[u]);
-      } else {
-#pragma unroll
-        for (int u = 0; u < NP; u++) Math<T>::coeffs(dt[u], x[u], ca[u], cb[u]);
-      }
-#pragma unroll
-      for (int u = 0; u < NP; u++) {
-        const T src1 = a0[u] > (T)0 ? S0[u] : S1[u];
-        const T src2 = a1[u] > (T)0 ? S1[u] : S0[u];
-        T qv = dt[u] > (T)1.0e-9f ? ca[u] * src1 + cb[u] * src2 : th[u];
-        qv = qv < th[u] ? qv : th[u];
-        if (!ov[u]) {
-          I[u] = I[u] * x[u] + qv;
-          j0[u] = j1[u]; a0[u] = a1[u]; S0[u] = S1[u];
-          if constexpr (PV) kahan_add(tau[u], tcp[u], dt[u]);
-        }
-      }
-      steps += nv;
-      if (any) {
-        // compact the refined channels over the warp, refine them one per lane
-        int pos[NP];
-        int cnt = 0;
-#pragma unroll
-        for (int u = 0; u < NP; u++) {
-          const unsigned m = __ballot_sync(0xffffffffu, ov[u]);
-          pos[u] = cnt + __popc(m & lanemask_lt());
-          if (ov[u]) {
-            SW.I[pos[u]] = I[u]; SW.j0[pos[u]] = j0[u]; SW.a0[pos[u]] = a0[u]; SW.S0[pos[u]] = S0[u];
-            SW.w[pos[u]] = w[u]; SW.l[pos[u]] = (unsigned char)lsl[u];
-          }
-          cnt += __popc(m);
-        }
-        __syncwarp();
-        const T vl0 = S.vl[n], dsf = S.ds[n + 1], ids = S.ids[n + 1], hw3 = S.hw3[n + 1];
-        const T lgv = S.lg[n + 1], ilg = S.ilg[n + 1], idvs = S.idvs[n + 1], dvsg = S.dvs[n + 1];
-        for (int p = lane; p < cnt; p += 32) {
-          const T wp = SW.w[p];
-          const int lp = SW.l[p];
-          const T s_c = sizeof(T) == 8 ? dsf * (wp - vl0) / dvsg : dsf * (wp - vl0) * idvs;
-          const SlotOutT<T, PV> o = slot_sub<T, PV>(wp, S.lv[lp][n], S.lv[lp][n + 1], vl0, vl1, rl, dsf, ids,
-                                                    s_c - hw3, lgv, ilg, SW.I[p], SW.j0[p], SW.a0[p], SW.S0[p]);
-          SW.I[p] = o.I; SW.j0[p] = o.j0; SW.a0[p] = o.a0; SW.S0[p] = o.S0;
-          if constexpr (PV) SW.w[p] = o.dtau;   // the owner keeps w in a register
-          steps += o.steps - 1;
-        }
-        __syncwarp();
-#pragma unroll
-        for (int u = 0; u < NP; u++) {
-          if (ov[u]) {
-            I[u] = SW.I[pos[u]]; j0[u] = SW.j0[pos[u]]; a0[u] = SW.a0[pos[u]]; S0[u] = SW.S0[pos[u]];
-            if constexpr (PV) kahan_add(tau[u], tcp[u], SW.w[pos[u]]);
-          }
-        }
-        __syncwarp();
-      }
-    } else {
-      const bool init = true, sub = fl & kFlagSub;
-      const T vl0 = S.vl[n], q = S.q[n + 1], dsf = S.ds[n + 1], dvs = S.dvs[n + 1], ids = S.ids[n + 1];
-#pragma unroll
-      for (int u = 0; u < NP; u++) {
-        if (Ls[u] < 0) continue;
-        const SlotOutT<T, PV> o = slot_slow<T, PV>(init, sub, w[u], S.lv[Ls[u]][n], S.lv[Ls[u]][n + 1], vl0, vl1,
-                                                   rl, hds, q, dsf, dvs, ids, I[u], j0[u], a0[u], S0[u]);
-        I[u] = o.I; j0[u] = o.j0; a0[u] = o.a0; S0[u] = o.S0; steps += o.steps;
-        if constexpr (PV) kahan_add(tau[u], tcp[u], o.dtau);
-      }
-    }
-  }
-#pragma unroll
-  for (int u = 0; u < NP; u++) {
-    const int j = jb + u;
-    if (j < C) { SS.I[j][lane] = I[u]; SS.j0[j][lane] = j0[u]; SS.a0[j][lane] = a0[u]; SS.S0[j][lane] = S0[u]; }
-    if constexpr (PV) {
-      if (Ls[u] >= 0) { P.tau[ta[u]] = tau[u]; P.tauc[ta[u]] = tcp[u]; }
-    }
-  }
-  return steps;
-}
-
 // Formal solution of the (line, channel) pairs list[0..nt) of lines l0.. of one ray.
 // The per-line tables carry the profile normalisation 0.56419583546/(3.33567e-6 nu0), so
 // the profile of every slot is rlw * exp(-u^2) with the node's shared 1/linewidth.
@@ -286,11 +118,162 @@ __device__ long long walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState
     const int nn = min(32, K - kb);
     const int n0 = kb == 0 ? 1 : 0;   // node 0 of the ray starts the walk
     for (int pq = 0; pq < npass; pq++) {
-      const int jb = kPass * pq;
-      if (nslot - jb <= 2)
-        steps += walk_pass<T, C, PV, 2>(P, S, SS, SW, list, lane, ray, l0, kb, nn, n0, star_node, jb);
-      else
-        steps += walk_pass<T, C, PV, kPass>(P, S, SS, SW, list, lane, ray, l0, kb, nn, n0, star_node, jb);
+      T I[kPass], j0[kPass], a0[kPass], S0[kPass], w[kPass];
+      int Ls[kPass], lsl[kPass];
+      int nv = 0;
+#pragma unroll
+      for (int u = 0; u < kPass; u++) {
+        const int j = kPass * pq + u;
+        if (j < C) {
+          I[u] = SS.I[j][lane]; j0[u] = SS.j0[j][lane]; a0[u] = SS.a0[j][lane]; S0[u] = SS.S0[j][lane];
+          w[u] = SS.w[j][lane]; Ls[u] = SS.ll[j][lane];
+        } else {
+          I[u] = 0; j0[u] = 0; a0[u] = 0; S0[u] = 0; w[u] = 0; Ls[u] = -1;
+        }
+        lsl[u] = Ls[u] < 0 ? 0 : Ls[u];
+        nv += Ls[u] >= 0 ? 1 : 0;
+      }
+      T tau[kPass], tcp[kPass];
+      size_t ta[kPass];
+      if constexpr (PV) {
+#pragma unroll
+        for (int u = 0; u < kPass; u++) {
+          tau[u] = 0; tcp[u] = 0; ta[u] = 0;
+          if (Ls[u] >= 0) {
+            ta[u] = ((size_t)(l0 + Ls[u]) * nb.nrays + ray) * P.nfr +
+                    (list[(kPass * pq + u) * 32 + lane] & (kMaxChannels - 1));
+            tau[u] = P.tau[ta[u]]; tcp[u] = P.tauc[ta[u]];
+          }
+        }
+      }
+      for (int n = n0; n < nn; n++) {
+        const int g = kb + n;
+        const unsigned fl = S.flags[n + 1];
+        if (g == star_node) {
+#pragma unroll
+          for (int u = 0; u < kPass; u++)
+            if (Ls[u] >= 0)
+              I[u] = ((T)1 - P.fstar) * I[u] +
+                     P.fstar * P.star[(size_t)(l0 + Ls[u]) * P.nfr + (list[(kPass * pq + u) * 32 + lane] & (kMaxChannels - 1))];
+        }
+        const T vl1 = S.vl[n + 1], rl = S.rlw[n + 1], hds = S.hds[n + 1];
+        if (!(fl & kFlagInit)) {
+          // SUBGRID window test of the reference (line.F:4733-4742): slots whose refined
+          // window [s_c - 3l, s_c + 3l] overlaps (0, ds) keep their state here and are
+          // refined below; all others take one formal-solution step
+          bool ov[kPass];
+          bool any = false;
+#pragma unroll
+          for (int u = 0; u < kPass; u++) ov[u] = false;
+          if (fl & kFlagSub) {
+            const T vl0 = S.vl[n], dsf = S.ds[n + 1], hw3 = S.hw3[n + 1];
+#pragma unroll
+            for (int u = 0; u < kPass; u++) {
+              const T s_c = sizeof(T) == 8 ? dsf * (w[u] - vl0) / S.dvs[n + 1] : dsf * (w[u] - vl0) * S.idvs[n + 1];
+              ov[u] = Ls[u] >= 0 && (s_c + hw3 > (T)0) && (s_c - hw3 < dsf);
+              any = any || ov[u];
+            }
+            any = __any_sync(0xffffffffu, any);
+          }
+          T j1[kPass], a1[kPass], S1[kPass], dt[kPass], th[kPass];
+          bool ser_all = true, dir_all = true;
+#pragma unroll
+          for (int u = 0; u < kPass; u++) {
+            const LineVals<T> v = S.lv[lsl[u]][n + 1];
+            const T ph = profile(w[u], vl1, rl, rl);
+            j1[u] = v.jd + v.jf * ph;
+            a1[u] = v.ad + v.af * ph;
+            S1[u] = a1[u] > (T)0 ? j1[u] * Math<T>::rcp(a1[u]) : (T)0;
+            dt[u] = (a0[u] + a1[u]) * hds;
+            th[u] = (j0[u] + j1[u]) * hds;
+            const bool ser = dt[u] < (T)0.25;
+            ser_all = ser_all && ser;
+            dir_all = dir_all && !ser;
+          }
+          ser_all = __all_sync(0xffffffffu, ser_all);
+          dir_all = __all_sync(0xffffffffu, dir_all);
+          T x[kPass], ca[kPass], cb[kPass];
+          if (ser_all) {
+#pragma unroll
+            for (int u = 0; u < kPass; u++) Math<T>::series(dt[u], x[u], ca[u], cb[u]);
+          } else if (dir_all) {
+#pragma unroll
+            for (int u = 0; u < kPass; u++) Math<T>::direct(dt[u], x[u], ca[u], cb[u]);
+          } else {
+#pragma unroll
+            for (int u = 0; u < kPass; u++) Math<T>::coeffs(dt[u], x[u], ca[u], cb[u]);
+          }
+#pragma unroll
+          for (int u = 0; u < kPass; u++) {
+            const T src1 = a0[u] > (T)0 ? S0[u] : S1[u];
+            const T src2 = a1[u] > (T)0 ? S1[u] : S0[u];
+            T qv = dt[u] > (T)1.0e-9f ? ca[u] * src1 + cb[u] * src2 : th[u];
+            qv = qv < th[u] ? qv : th[u];
+            if (!ov[u]) {
+              I[u] = I[u] * x[u] + qv;
+              j0[u] = j1[u]; a0[u] = a1[u]; S0[u] = S1[u];
+              if constexpr (PV) kahan_add(tau[u], tcp[u], dt[u]);
+            }
+          }
+          steps += nv;
+          if (any) {
+            // compact the refined channels over the warp, refine them one per lane
+            int pos[kPass];
+            int cnt = 0;
+#pragma unroll
+            for (int u = 0; u < kPass; u++) {
+              const unsigned m = __ballot_sync(0xffffffffu, ov[u]);
+              pos[u] = cnt + __popc(m & lanemask_lt());
+              if (ov[u]) {
+                SW.I[pos[u]] = I[u]; SW.j0[pos[u]] = j0[u]; SW.a0[pos[u]] = a0[u]; SW.S0[pos[u]] = S0[u];
+                SW.w[pos[u]] = w[u]; SW.l[pos[u]] = (unsigned char)lsl[u];
+              }
+              cnt += __popc(m);
+            }
+            __syncwarp();
+            const T vl0 = S.vl[n], dsf = S.ds[n + 1], ids = S.ids[n + 1], hw3 = S.hw3[n + 1];
+            const T lgv = S.lg[n + 1], ilg = S.ilg[n + 1], idvs = S.idvs[n + 1], dvsg = S.dvs[n + 1];
+            for (int p = lane; p < cnt; p += 32) {
+              const T wp = SW.w[p];
+              const int lp = SW.l[p];
+              const T s_c = sizeof(T) == 8 ? dsf * (wp - vl0) / dvsg : dsf * (wp - vl0) * idvs;
+              const SlotOutT<T, PV> o = slot_sub<T, PV>(wp, S.lv[lp][n], S.lv[lp][n + 1], vl0, vl1, rl, dsf, ids,
+                                                        s_c - hw3, lgv, ilg, SW.I[p], SW.j0[p], SW.a0[p], SW.S0[p]);
+              SW.I[p] = o.I; SW.j0[p] = o.j0; SW.a0[p] = o.a0; SW.S0[p] = o.S0;
+              if constexpr (PV) SW.w[p] = o.dtau;   // the owner keeps w in a register
+              steps += o.steps - 1;
+            }
+            __syncwarp();
+#pragma unroll
+            for (int u = 0; u < kPass; u++) {
+              if (ov[u]) {
+                I[u] = SW.I[pos[u]]; j0[u] = SW.j0[pos[u]]; a0[u] = SW.a0[pos[u]]; S0[u] = SW.S0[pos[u]];
+                if constexpr (PV) kahan_add(tau[u], tcp[u], SW.w[pos[u]]);
+              }
+            }
+            __syncwarp();
+          }
+        } else {
+          const bool init = true, sub = fl & kFlagSub;
+          const T vl0 = S.vl[n], q = S.q[n + 1], dsf = S.ds[n + 1], dvs = S.dvs[n + 1], ids = S.ids[n + 1];
+#pragma unroll
+          for (int u = 0; u < kPass; u++) {
+            if (Ls[u] < 0) continue;
+            const SlotOutT<T, PV> o = slot_slow<T, PV>(init, sub, w[u], S.lv[Ls[u]][n], S.lv[Ls[u]][n + 1], vl0, vl1,
+                                                       rl, hds, q, dsf, dvs, ids, I[u], j0[u], a0[u], S0[u]);
+            I[u] = o.I; j0[u] = o.j0; a0[u] = o.a0; S0[u] = o.S0; steps += o.steps;
+            if constexpr (PV) kahan_add(tau[u], tcp[u], o.dtau);
+          }
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kPass; u++) {
+        const int j = kPass * pq + u;
+        if (j < C) { SS.I[j][lane] = I[u]; SS.j0[j][lane] = j0[u]; SS.a0[j][lane] = a0[u]; SS.S0[j][lane] = S0[u]; }
+        if constexpr (PV) {
+          if (Ls[u] >= 0) { P.tau[ta[u]] = tau[u]; P.tauc[ta[u]] = tcp[u]; }
+        }
+      }
     }
     __syncwarp();
   }
