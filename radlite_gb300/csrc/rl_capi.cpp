@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
+#include <ctime>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -513,6 +515,30 @@ int rl_line_image_mask(rl_model* md, int iline, double* image_out, unsigned char
 
 int rl_run_dir(const char* dir, int device, rl_stats* st) { return rl_run_dir_ex(dir, device, 0, st); }
 
+// radlite.log: the start and finish stamps the reference appends around the telescope
+// step (write_logmessage_start/_end, main.F:983-985, 1093-1095, 1119-1520; the list of
+// compile-time switches and the transfer warnings of the reference are not reproduced).
+static void run_log(const std::string& dir, bool start) {
+  FILE* fp = std::fopen((dir + "/radlite.log").c_str(), "a");
+  if (!fp) return;
+  const auto now = std::chrono::system_clock::now();
+  const std::time_t t = std::chrono::system_clock::to_time_t(now);
+  const int ms = (int)(std::chrono::duration_cast<std::chrono::milliseconds>(now.time_since_epoch()).count() % 1000);
+  std::tm tmv;
+  localtime_r(&t, &tmv);
+  char d[32], h[32];
+  std::snprintf(d, sizeof d, "%02d-%02d-%04d", tmv.tm_mday, tmv.tm_mon + 1, tmv.tm_year + 1900);
+  std::snprintf(h, sizeof h, "%02d:%02d:%02d.%03d", tmv.tm_hour, tmv.tm_min, tmv.tm_sec, ms);
+  if (start)
+    std::fprintf(fp, "\n\n\n =========== RUN OF RADICAL ===========\n Action       : spectrum/image\n"
+                     " Starting Date: %s\n          Time: %s\n ......................................\n"
+                     "       COMPILATION OF CODE:            \n radlite_gb300 line raytrace (GB300, sm_103a)\n",
+                 d, h);
+  else
+    std::fprintf(fp, " ......................................\n Finished Date: %s\n          Time: %s\n", d, h);
+  std::fclose(fp);
+}
+
 int rl_run_dir_ex(const char* dir, int device, int flags, rl_stats* st) {
   if (flags & ~RL_RUN_SAVE_IMCIR) return set_err(nullptr, RL_ERR_ARG, "rl_run_dir_ex: unknown flags");
   rl_ctx* ctx = nullptr;
@@ -520,6 +546,7 @@ int rl_run_dir_ex(const char* dir, int device, int flags, rl_stats* st) {
   if (rc) return rc;
   rl_model* md = nullptr;
   rc = rl_load_dir(ctx, dir, &md);
+  if (rc == 0) run_log(dir, true);
   if (rc == 0 && md->m.command == 2) {
     // one lineposvel file per line (main.F:1061-1074); lines in chunks of at most 2 GB of
     // cube per array
@@ -608,6 +635,7 @@ int rl_run_dir_ex(const char* dir, int device, int flags, rl_stats* st) {
       }
     }
   }
+  if (rc == 0) run_log(dir, false);
   if (rc) g_last_error = ctx->err;
   rl_model_free(md);
   rl_destroy(ctx);

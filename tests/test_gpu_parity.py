@@ -118,9 +118,35 @@ def test_executable(gpu_lib, model_dir, tmp_path):
     r = subprocess.run([gpu_lib.EXE_PATH, d], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     assert os.path.exists(os.path.join(d, "linespectrum_moldata.dat"))
+    log = open(os.path.join(d, "radlite.log")).read()
+    assert "RUN OF RADICAL" in log and "Finished" in log
+    # a SAVE_IMCIR build's circular images beside the spectrum
+    r = subprocess.run([gpu_lib.EXE_PATH, "--save-imcir", d], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert os.path.exists(os.path.join(d, "lineposvelcirc_moldata_1.dat"))
+    assert open(os.path.join(d, "radlite.log")).read().count("RUN OF RADICAL") == 2
     os.remove(os.path.join(d, "density.inp"))
     r = subprocess.run([gpu_lib.EXE_PATH, d], capture_output=True, text=True)
     assert r.returncode == 13 and "density.inp" in r.stderr
+
+
+def test_executable_posvel_and_manifest(gpu_lib, tmp_path):
+    """linespectrum.inp command 2 through the executable; a manifest of such directories
+    is refused (a batch renders line spectra)."""
+    import subprocess
+    from radlite_gb300 import synth
+    d = synth.write_model(synth.config_by_name("tiny_line", command=2, pv_nx=6, pv_ny=4, nlines=2, ilinestart=1),
+                          str(tmp_path / "pv"))
+    r = subprocess.run([gpu_lib.EXE_PATH, d], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    for il in (1, 2):
+        f = gpu_lib.read_posvel_file(os.path.join(d, f"lineposvel_moldata_{il}.dat"))
+        assert f["temp"].shape == (f["nfr"], 4, 6) and f["temp"].max() > 0
+    assert not os.path.exists(os.path.join(d, "linespectrum_moldata.dat"))
+    man = tmp_path / "models.txt"
+    man.write_text(d + "\n")
+    r = subprocess.run([gpu_lib.EXE_PATH, "--manifest", str(man)], capture_output=True, text=True)
+    assert r.returncode == 13 and "command 0" in r.stderr
 
 
 def test_arrays_path_matches_files(ctx, model_dir):
