@@ -123,6 +123,11 @@ CASES = {
     "star": dict(),
     "rotated_offset": dict(pv_phioff=0.4, pv_xoff_au=0.3, pv_yoff_au=-0.2, pv_addstar=0, pv_nx=10, pv_ny=8),
     "resolved_star": dict(pv_size_au=0.0015, pv_nx=6, pv_ny=6, incl_deg=80.0),
+    # the rectangular camera raises every inclination below 0.1 rad to 0.1, negative
+    # ones included (telescope.F:2289-2300)
+    "low_incl": dict(incl_deg=3.0, pv_nx=6, pv_ny=6),
+    "negative_incl": dict(incl_deg=-30.0, pv_nx=6, pv_ny=6, pv_addstar=0),
+    "cmb_boundary": dict(outer_bc=2, pv_nx=8, pv_ny=4),
 }
 
 
