@@ -156,6 +156,22 @@ def test_gpu_cube_matches_oracle(gpu_lib, oracle_lib, ctx, tmp_path, case):
 
 
 @pytest.mark.gpu
+def test_gpu_cube_outside_the_grid(gpu_lib, oracle_lib, ctx, tmp_path):
+    """An image offset beyond the outer radius traces no ray: every pixel is empty
+    (telescope.F:2136-2146), in both precisions."""
+    cfg = pv_cfg(pv_xoff_au=1.0e4, pv_addstar=0, pv_nx=4, pv_ny=4)
+    d = synth.write_model(cfg, str(tmp_path / "m"))
+    I_ref, tau_ref = oracle_lib.Oracle(d).posvel(1, **oracle_lib.Oracle(d).pv)
+    assert not I_ref.any() and not tau_ref.any()
+    m = ctx.load_dir(d)
+    for prec in (0, 1):
+        m.set_precision(prec)
+        I, tau, st = m.posvel(1, 1, stats=True)
+        assert st["nrays"] == 0 and not I.any() and not tau.any()
+    m.free()
+
+
+@pytest.mark.gpu
 def test_run_dir_writes_posvel_files(gpu_lib, ctx, tmp_path):
     cfg = pv_cfg(ilinestart=2)
     d = synth.write_model(cfg, str(tmp_path / "m"))
