@@ -139,6 +139,21 @@ def cpu_sample(cfg, stride, procs, tmpdir):
     return {"ray_channels": n, "rays": len(rays), "compute_s": busy, "wall_s": wall, "value": n / busy}
 
 
+def cpu_model() -> str:
+    """The host CPU as lscpu names it (architecture and model)."""
+    import platform
+    name = ""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                name = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return f"{platform.machine()} {name}".strip()
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -172,7 +187,8 @@ def reference_arm(args):
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator in the reference file formats)",
             "config": {"workload": "band_large: 400x200 disk, 20 band lines x 200 channels, 1000x256 rays, "
                                    "incl 20+60 deg (bounded CPU sample)"},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": procs, "kind": "port", "sample": sample},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": procs, "cpu": cpu_model(), "kind": "port",
+                             "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "the reference Fortran cannot be compiled on this image (no Fortran compiler); timed is the "
                     "FP64 C restatement of its raytrace (oracle/), one process per host core"}
@@ -286,7 +302,7 @@ def ours(args):
         with tempfile.TemporaryDirectory() as tmp:
             if not args.no_cpu:
                 s = cpu_sample(cfg, args.cpu_stride, os.cpu_count() or 1, tmp)
-                cpu = {"value": s["value"], "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+                cpu = {"value": s["value"], "unit": UNIT, "cores": os.cpu_count() or 1, "cpu": cpu_model(), "kind": "port",
                        "sample": f"band_large line {cfg.ilinestart}, incl {INCLS[0]:.0f} deg, every "
                                  f"{args.cpu_stride}th ray ({s['rays']} rays x {nfr} channels), FP64 C restatement, "
                                  f"one process per core"}
