@@ -65,7 +65,7 @@ struct rl_batch {
   std::vector<std::unique_ptr<BatchJob>> jobs;
   size_t nflux = 0;
   double mem_budget = 0.0;       // bytes per wave; 0 = 70% of the free device memory
-  int gcap = kWalkGroup, cpl = 8;
+  int gcap = kItemLines, cpl = 4;
   bool use_graph = true;
   bool built = false;
   bool geo_valid = false;        // node records of a single-wave batch are in the arena
@@ -415,12 +415,12 @@ int autotune(rl_batch* b, int stride, int* gbest, int* cbest, double* best_ms) {
   }
   int maxnl = 1;
   for (int j : P.waves[0].jobs) maxnl = std::max(maxnl, b->jobs[j]->nl);
-  const int gc[] = {1, 2, 4, 8};
+  const int gc[] = {2, 8, 16, kItemLines};
   const int cc[] = {2, 4, 8};
   double best = 1e300;
   int bg = b->gcap, bc = b->cpl;
   for (int g : gc) {
-    if (g > maxnl && g != 1) continue;
+    if (g > maxnl && g != gc[0]) continue;
     for (int c : cc) {
       b->gcap = g; b->cpl = c;
       int rc = write_descriptors<T>(b);
@@ -494,9 +494,9 @@ int rl_batch_set_memory(rl_batch* b, double bytes) {
 
 int rl_batch_set_tiles(rl_batch* b, int lines_per_item, int channel_slots) {
   if (!b) return set_err(nullptr, RL_ERR_ARG, "rl_batch_set_tiles: null batch");
-  if (lines_per_item < 1 || lines_per_item > kWalkGroup ||
+  if (lines_per_item < 1 || lines_per_item > kItemLines ||
       (channel_slots != 1 && channel_slots != 2 && channel_slots != 4 && channel_slots != 8))
-    return set_err(b->ctx, RL_ERR_ARG, "rl_batch_set_tiles: lines_per_item 1..8, channel_slots 1, 2, 4 or 8");
+    return set_err(b->ctx, RL_ERR_ARG, "rl_batch_set_tiles: lines_per_item 1..32, channel_slots 1, 2, 4 or 8");
   b->gcap = lines_per_item;
   b->cpl = channel_slots;
   if (!b->built) return 0;

@@ -218,10 +218,10 @@ static int run_lines(rl_model* md, int iline0, int nl, double* flux_out, double*
   WalkParams<T> P;
   P.nb = node_view<T>(md);
   P.nth = m.nth; P.ncell = ncell; P.nlines = nl; P.nfr = nfr;
+  int cpl = 4;
   {
-    const int ng = (nl + kWalkGroup - 1) / kWalkGroup;   // balanced line groups per ray
-    P.gsize = (nl + ng - 1) / ng;
-    P.nitems = ng * cam.nrays;                           // (line group, ray) work items
+    walk_shape(nl, nfr, P.gsize, cpl);                   // balanced line groups per ray
+    P.nitems = ((nl + P.gsize - 1) / P.gsize) * cam.nrays;   // (line group, ray) work items
   }
   if (nfr >= 2048) return set_err(ctx, RL_ERR_ARG, "at most 2047 channels per line are supported");
   P.tab = md->dtab.as<T>(); P.nsum = md->dnsum.as<T>(); P.wch = md->dwch.as<T>(); P.velo = md->dvelo.as<double>();
@@ -236,9 +236,6 @@ static int run_lines(rl_model* md, int iline0, int nl, double* flux_out, double*
   P.list = md->dlist.as<unsigned short>();
   P.mask = mask_out ? md->dmask.as<unsigned char>() : nullptr;
   if (cam.ri[1] < m.rstar) return set_err(ctx, RL_ERR_ARG, "central beam smaller than the star");
-  // slots per lane: enough for every (line, channel) pair of a line group in one tile
-  const int need = (P.gsize * nfr + 31) / 32;
-  const int cpl = need <= 1 ? 1 : need <= 2 ? 2 : need <= 4 ? 4 : 8;
   CUDA_TRY(launch_walk<T>(P, cpl, ctx->nsm, s));
   CUDA_TRY(cudaEventRecord(ctx->ev[2], s));
   ReduceParams rp;

@@ -8,9 +8,13 @@ namespace rl {
 // Walk launch shape: 4-warp blocks, at most this many per SM (sizes the list scratch).
 constexpr int kWalkBlocksPerSm = 4;
 constexpr int kWalkWarps = 4;
+// Lines of one walk work item at most (the list packs a line index into 5 bits).
+constexpr int kItemLines = 32;
+// Elements of one warp's list row for up to nfr channels per line.
+inline size_t walk_list_row(int nfr) { return (size_t)((kItemLines * nfr + 7) & ~7); }
 // Elements of the walk's list scratch for nsm SMs and up to nfr channels per line.
 inline size_t walk_list_elems(int nsm, int nfr) {
-  return (size_t)nsm * kWalkBlocksPerSm * kWalkWarps * (size_t)((8 * nfr + 7) & ~7);
+  return (size_t)nsm * kWalkBlocksPerSm * kWalkWarps * walk_list_row(nfr);
 }
 
 // Per-node flag bits in NodeBuf::misc (bits 0-15: theta-corner offset + 32768,

@@ -227,10 +227,7 @@ int create(rl_diff* d) {
   CUDA_TRY(h2d(d->lc.p, lt.lc.data(), sizeof(LineConst<T>) * nl, s));
   CUDA_TRY(h2d(d->dscale.p, lt.scale.data(), sizeof(double) * nl, s));
   // walk shape as the plain path: balanced groups of up to 8 lines
-  const int ng = (nl + kWalkGroup - 1) / kWalkGroup;
-  d->gsize = (nl + ng - 1) / ng;
-  const int need = (d->gsize * d->nfr + 31) / 32;
-  d->cpl = need <= 1 ? 1 : need <= 2 ? 2 : need <= 4 ? 4 : 8;
+  walk_shape(nl, d->nfr, d->gsize, d->cpl);
   CUDA_TRY(adjoint_grid<T>(ctx->nsm, d->nfr, &d->adj_blocks));
   const long long per = adjoint_ckpt_per_warp<T>(d->kmax, d->every);
   CUDA_TRY(d->ckpt.ensure(sizeof(T) * (size_t)per * d->adj_blocks * 4));
@@ -477,7 +474,7 @@ int batch_build(rl_diff_batch* b) {
   CUDA_TRY(b->ckpt.ensure(sizeof(T) * (size_t)per * b->adj_blocks * 4));
   JobLaunch<T>& L = launch_of<T>(b);
   L = JobLaunch<T>{};
-  L.njobs = nj; L.nsm = ctx->nsm; L.cpl = 8;
+  L.njobs = nj; L.nsm = ctx->nsm; L.cpl = 4;
   L.geo = nullptr; L.ray_prefix = nullptr; L.nrays_total = 0;
   L.walk.jobs = b->walkjobs.as<WalkParams<T>>(); L.walk.item_prefix = b->item_prefix.as<int>();
   L.walk.njobs = nj; L.walk.total = itemp[nj]; L.walk.stride = 1; L.walk.max_nfr = b->max_nfr;

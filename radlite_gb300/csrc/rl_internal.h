@@ -22,7 +22,17 @@ template <typename T>
 cudaError_t launch_jobs(const JobLaunch<T>& L, cudaStream_t s);
 cudaError_t measure_peaks(int nsm, cudaStream_t st, double* ffma_per_s, double* ex2_per_s);
 
-constexpr int kWalkGroup = 8;   // lines per walk work item at most (k_walk's kGroup)
+constexpr int kWalkGroup = 8;   // lines of one walk tile at most (k_walk's kGroup)
+
+// Work-item shape of a line range: balanced items of at most kItemLines lines (their
+// channels are packed into tiles of 32*cpl pairs), and the channel slots per lane: 4 (one
+// pass of four slots per tile) unless an item holds fewer pairs.
+inline void walk_shape(int nl, int nfr, int& gsize, int& cpl) {
+  const int ng = (nl + kItemLines - 1) / kItemLines;
+  gsize = (nl + ng - 1) / ng;
+  const long long pairs = (long long)gsize * nfr;
+  cpl = pairs <= 32 ? 1 : pairs <= 64 ? 2 : 4;
+}
 
 // Owned device allocation that only grows.
 struct DevBuf {

@@ -192,7 +192,7 @@ template <typename T, int C>
 __global__ void __launch_bounds__(128, WalkMinBlocks<T>::value) k_walk(WalkParams<T> P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  WarpSmem<T, C> W(smem_raw, nw, wib, kGroup * P.nfr, P.list);
+  WarpSmem<T, C> W(smem_raw, nw, wib, kItemLines * P.nfr, P.list);
   WalkCounters wc;
   for (;;) {
     int item = 0;
@@ -213,7 +213,7 @@ __global__ void __launch_bounds__(128, WalkMinBlocks<T>::value) k_walk_jobs(Walk
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ WalkParams<T> jp[4];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  WarpSmem<T, C> W(smem_raw, nw, wib, kGroup * B.max_nfr, B.list);
+  WarpSmem<T, C> W(smem_raw, nw, wib, kItemLines * B.max_nfr, B.list);
   WalkCounters wc;
   int cur = -1;
   const int nq = (B.total + B.stride - 1) / B.stride;
@@ -386,7 +386,7 @@ cudaError_t launch_geometry(const GeoParams& p, const NodeBuf<T>& nb, int ray0, 
 template <typename T, int C>
 static cudaError_t launch_walk_c(const WalkParams<T>& P, int nsm, cudaStream_t s) {
   const int warps = 4, threads = warps * 32;
-  const int capp = (kGroup * P.nfr + 7) & ~7;
+  const int capp = (kItemLines * P.nfr + 7) & ~7;
   const size_t smem = (sizeof(WarpStage<T>) + sizeof(SlotState<T, C>) + sizeof(SubWork<T>)) * warps +
                       (kListInSmem ? sizeof(unsigned short) * (size_t)capp * warps : 0);
   cudaError_t e = cudaFuncSetAttribute(k_walk<T, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -407,7 +407,7 @@ static cudaError_t launch_walk_c(const WalkParams<T>& P, int nsm, cudaStream_t s
 template <typename T, int C>
 static cudaError_t launch_walk_jobs_c(const WalkJobs<T>& B, int nsm, cudaStream_t s) {
   const int warps = 4, threads = warps * 32;
-  const int capp = (kGroup * B.max_nfr + 7) & ~7;
+  const int capp = (kItemLines * B.max_nfr + 7) & ~7;
   const size_t smem = (sizeof(WarpStage<T>) + sizeof(SlotState<T, C>) + sizeof(SubWork<T>)) * warps +
                       (kListInSmem ? sizeof(unsigned short) * (size_t)capp * warps : 0);
   cudaError_t e = cudaFuncSetAttribute(k_walk_jobs<T, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -31,7 +31,7 @@ template <typename T, int C>
 __global__ void __launch_bounds__(128, WalkMinBlocks<T>::value) k_walk_pv(WalkParams<T> P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  WarpSmem<T, C> W(smem_raw, nw, wib, kGroup * P.nfr, P.list);
+  WarpSmem<T, C> W(smem_raw, nw, wib, kItemLines * P.nfr, P.list);
   WalkCounters wc;
   for (;;) {
     int item = 0;
@@ -198,10 +198,10 @@ static int run_posvel(rl_model* md, int iline0, int nl, double* I_out, double* t
     WalkParams<T> P;
     P.nb = nb;
     P.nth = m.nth; P.ncell = m.ncell(); P.nlines = nl; P.nfr = nfr;
+    int cpl = 4;
     {
-      const int ng = (nl + kWalkGroup - 1) / kWalkGroup;
-      P.gsize = (nl + ng - 1) / ng;
-      P.nitems = ng * ntr;
+      walk_shape(nl, nfr, P.gsize, cpl);
+      P.nitems = ((nl + P.gsize - 1) / P.gsize) * ntr;
     }
     P.tab = md->dtab.as<T>(); P.nsum = md->dnsum.as<T>(); P.wch = md->dwch.as<T>(); P.velo = md->dvelo.as<double>();
     P.star = md->dstar.as<T>(); P.lc = md->dlc.as<LineConst<T>>();
@@ -213,8 +213,6 @@ static int run_posvel(rl_model* md, int iline0, int nl, double* I_out, double* t
     P.work = md->dwork.as<int>();
     P.err = md->derr.as<int>();
     P.list = md->dlist.as<unsigned short>();
-    const int need = (P.gsize * nfr + 31) / 32;
-    const int cpl = need <= 1 ? 1 : need <= 2 ? 2 : need <= 4 ? 4 : 8;
     CUDA_TRY(launch_walk_pv<T>(P, cpl, ctx->nsm, s));
     CUDA_TRY(cudaEventRecord(ctx->ev[3], s));
   } else {

@@ -31,9 +31,11 @@ __device__ __forceinline__ void kahan_add(T& s, T& c, T x) {
 // all nodes of the chunk; the slot state lives in shared memory between pairs.
 // PV: also the optical depth of every slot, Kahan-compensated in P.tau / P.tauc (the slot's
 // image position), and no star mixing.
+// The list entries carry item line indices; lbase is the item line of l0 (the tile's first
+// line), so that entry line - lbase indexes the tile's staged lines 0..gl-1.
 template <typename T, int C, bool PV = false>
 __device__ long long walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<T, C>& SS, SubWork<T>& SW, int ray,
-                              int K, int l0, int gl, const unsigned short* list, int nt, int lane) {
+                              int K, int l0, int gl, const unsigned short* list, int nt, int lane, int lbase) {
   const NodeBuf<T>& nb = P.nb;
   const size_t row = (size_t)ray * nb.kmax;
   const int nl = P.nlines;
@@ -45,7 +47,7 @@ __device__ long long walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState
     T w = 0, I = 0;
     if (idx < nt) {
       const unsigned e = list[idx];
-      L = (int)(e >> kChBits);
+      L = (int)(e >> kChBits) - lbase;
       w = P.wch[(size_t)(l0 + L) * P.nfr + (e & (kMaxChannels - 1))];
       I = P.lc[l0 + L].istart;
       if constexpr (PV) {
@@ -297,42 +299,46 @@ __device__ __forceinline__ void walk_item(const WalkParams<T>& P, int item, Warp
   }
   const size_t row = (size_t)ray * nb.kmax;
   // 1. velocity window of the ray per line (telescope.F:4265-4270): node projected
-  //    velocities where N_up + N_low exceeds 1e-3, nodes 0 .. K-2
-  float mn[kGroup], mx[kGroup];
+  //    velocities where N_up + N_low exceeds 1e-3, nodes 0 .. K-2; lines in batches of
+  //    kGroup
+  for (int lb = 0; lb < gl; lb += kGroup) {
+    float mn[kGroup], mx[kGroup];
 #pragma unroll
-  for (int l = 0; l < kGroup; l++) { mn[l] = 1.0f; mx[l] = -1.0f; }
-  __syncwarp();
-  if (!PV && ray != 0) {
-    for (int k = lane; k < K - 1; k += 32) {
-      const size_t o = row + k;
-      const T wr = nb.wr[o], wt = nb.wt[o];
-      const Corners c = corners(nb.c00[o], nb.misc[o], P.nth);
-      const float d = nb.dvf[o];
+    for (int l = 0; l < kGroup; l++) { mn[l] = 1.0f; mx[l] = -1.0f; }
+    if (!PV && ray != 0) {
+      for (int k = lane; k < K - 1; k += 32) {
+        const size_t o = row + k;
+        const T wr = nb.wr[o], wt = nb.wt[o];
+        const Corners c = corners(nb.c00[o], nb.misc[o], P.nth);
+        const float d = nb.dvf[o];
+#pragma unroll
+        for (int l = 0; l < kGroup; l++) {
+          if (lb + l < gl && interp_1(P.nsum, c, nl, l0 + lb + l, wr, wt) > (T)1.0e-3) {
+            mn[l] = fminf(mn[l], d); mx[l] = fmaxf(mx[l], d);
+          }
+        }
+      }
 #pragma unroll
       for (int l = 0; l < kGroup; l++) {
-        if (l < gl && interp_1(P.nsum, c, nl, l0 + l, wr, wt) > (T)1.0e-3) {
-          mn[l] = fminf(mn[l], d); mx[l] = fmaxf(mx[l], d);
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+          mn[l] = fminf(mn[l], __shfl_xor_sync(0xffffffffu, mn[l], off));
+          mx[l] = fmaxf(mx[l], __shfl_xor_sync(0xffffffffu, mx[l], off));
         }
       }
     }
+    if (lane == 0) {
 #pragma unroll
-    for (int l = 0; l < kGroup; l++) {
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) {
-        mn[l] = fminf(mn[l], __shfl_xor_sync(0xffffffffu, mn[l], off));
-        mx[l] = fmaxf(mx[l], __shfl_xor_sync(0xffffffffu, mx[l], off));
-      }
+      for (int l = 0; l < kGroup; l++)
+        if (lb + l < gl) { S.mn[lb + l] = mn[l]; S.mx[lb + l] = mx[l]; }
     }
-  }
-  if (lane == 0) {
-#pragma unroll
-    for (int l = 0; l < kGroup; l++) { S.mn[l] = mn[l]; S.mx[l] = mx[l]; }
   }
   __syncwarp();
   // 2. (line, channel) pairs to integrate: channel 1, the in-window channels and the
   //    channel that supplies the continuum of the others (telescope.F:541-613)
   int nint = 0;
   for (int l = 0; l < gl; l++) {
+    if (lane == 0) S.lineoff[l] = nint;
     int cc = -1;
     const double* velo = P.velo + (size_t)(l0 + l) * P.nfr;
     const double lo = (double)S.mn[l] - 2.0 * P.aksmax_c, hi = (double)S.mx[l] + 2.0 * P.aksmax_c;
@@ -356,11 +362,17 @@ __device__ __forceinline__ void walk_item(const WalkParams<T>& P, int item, Warp
     }
     if (lane == 0) S.cont_ch[l] = cc;
   }
+  if (lane == 0) S.lineoff[gl] = nint;
   __syncwarp();
-  // 3. formal solution of the selected pairs, in tiles of 32*C
-  for (int tb = 0; tb < nint; tb += 32 * C) {
-    const int nt = min(32 * C, nint - tb);
-    wc.steps += walk_ray<T, C, PV>(P, S, SS, SW, ray, K, l0, gl, list + tb, nt, lane);
+  // 3. formal solution of the selected pairs in tiles of at most 32*C pairs spanning at
+  //    most kGroup lines: consecutive lines share a tile, so that the tiles' slots fill up
+  for (int tb = 0; tb < nint;) {
+    const int la = (int)(list[tb] >> kChBits);
+    const int lcap = min(la + kGroup, gl);
+    const int te = min(tb + 32 * C, S.lineoff[lcap]);
+    const int nt = te - tb;
+    const int lz = (int)(list[te - 1] >> kChBits);
+    wc.steps += walk_ray<T, C, PV>(P, S, SS, SW, ray, K, l0 + la, lz - la + 1, list + tb, nt, lane, la);
     for (int j = 0; j < C; j++) {
       const int idx = j * 32 + lane;
       if (idx < nt) {
@@ -371,6 +383,8 @@ __device__ __forceinline__ void walk_item(const WalkParams<T>& P, int item, Warp
         if (c == S.cont_ch[l]) S.contv[l] = Iv;
       }
     }
+    __syncwarp();
+    tb = te;
   }
   wc.integ += nint;
   wc.nodes += (unsigned long long)nint * K;
@@ -404,7 +418,7 @@ __device__ __forceinline__ void walk_item(const WalkParams<T>& P, int item, Warp
     __syncwarp();
     for (int tb = 0; tb < n2; tb += 32 * C) {
       const int nt = min(32 * C, n2 - tb);
-      wc.steps += walk_ray<T, C>(P, S, SS, SW, ray, K, l0, gl, list + tb, nt, lane);
+      wc.steps += walk_ray<T, C>(P, S, SS, SW, ray, K, l0 + l, 1, list + tb, nt, lane, l);
       for (int j = 0; j < C; j++) {
         const int idx = j * 32 + lane;
         if (idx < nt) img[list[tb + idx] & (kMaxChannels - 1)] = SS.I[j][lane];

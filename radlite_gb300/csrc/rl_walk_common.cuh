@@ -132,15 +132,18 @@ template <typename T>
 struct alignas(16) LineVals { T jf, af, jd, ad; };
 
 // Per-warp staging of one 32-node chunk; entry 0 carries the last node of the previous
-// chunk, entries 1..32 the nodes of this chunk.
+// chunk, entries 1..32 the nodes of this chunk. The line tables are staged for the lines of
+// one tile (at most kGroup); the per-line window and continuum data cover the whole item
+// (at most kItemLines lines).
 template <typename T>
 struct WarpStage {
   LineVals<T> lv[kGroup][33];
   T vl[33], hds[33], ds[33], rlw[33], q[33], ids[33], dvs[33], idvs[33], hw3[33], lg[33], ilg[33];
   unsigned flags[33];
-  T contv[kGroup];
-  float mn[kGroup], mx[kGroup];
-  int cont_ch[kGroup];
+  T contv[kItemLines];
+  float mn[kItemLines], mx[kItemLines];
+  int cont_ch[kItemLines];
+  int lineoff[kItemLines + 1];   // first list entry of each line of the item
 };
 
 // Compacted SUBGRID work of one segment: the (slot, lane) channels whose refined window

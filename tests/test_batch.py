@@ -75,13 +75,13 @@ def test_batch_waves_tiles_and_eager(gpu_lib, ctx, model_dir):
     for g, r in zip(got, ref):
         np.testing.assert_allclose(g, r, rtol=1e-6)
     # every tile shape gives the same spectra; the tuner keeps a valid one
-    for lines, slots in ((1, 2), (3, 4), (8, 8)):
+    for lines, slots in ((1, 2), (3, 4), (8, 8), (32, 4)):
         b.set_tiles(lines, slots)
         assert b.tiles() == (lines, slots)
         for g, r in zip(b.run(), ref):
             np.testing.assert_allclose(g, r, rtol=1e-6)
     tune = b.autotune(sample_stride=3)
-    assert tune["lines_per_item"] in (1, 2, 4, 8) and tune["channel_slots"] in (2, 4, 8)
+    assert tune["lines_per_item"] in (2, 8, 16, 32) and tune["channel_slots"] in (2, 4, 8)
     assert tune["sample_ms"] > 0
     b.use_graph(False)
     for g, r in zip(b.run(), ref):
@@ -99,7 +99,7 @@ def test_batch_rejects_bad_jobs(gpu_lib, ctx, model_dir):
     with pytest.raises(gpu_lib.RLError, match="no jobs"):
         b.run()
     with pytest.raises(gpu_lib.RLError, match="lines_per_item"):
-        b.set_tiles(9, 4)
+        b.set_tiles(33, 4)
     b.close()
     m.free()
 
