@@ -22,7 +22,7 @@ template <typename T>
 cudaError_t launch_jobs(const JobLaunch<T>& L, cudaStream_t s);
 cudaError_t measure_peaks(int nsm, cudaStream_t st, double* ffma_per_s, double* ex2_per_s);
 
-constexpr int kWalkGroup = 8;   // lines of one walk tile at most (k_walk's kGroup)
+constexpr int kWalkGroup = 12;   // lines of one walk tile at most (k_walk's kGroup)
 
 // Work-item shape of a line range: balanced items of at most kItemLines lines (their
 // channels are packed into tiles of 32*cpl pairs), and the channel slots per lane: 4 (one

@@ -123,7 +123,7 @@ __device__ __forceinline__ void point_state(const Pt<T>& p, T phi, T& j, T& a, T
 
 // Lines sharing one ray per work item. The integrated (line, channel) pairs of all of
 // them are packed densely over the 32 lanes x C slots of the warp.
-constexpr int kGroup = 8;
+constexpr int kGroup = 12;
 constexpr int kPass = 4;                  // slots walked together (independent chains per lane)
 constexpr int kChBits = 11;               // channel index bits of a packed (line, channel)
 constexpr int kMaxChannels = 1 << kChBits;
