@@ -198,12 +198,14 @@ int rl_batch_destroy(rl_batch* batch);
 int rl_batch_add(rl_batch* batch, rl_model* model, int iline0, int nlines);
 /* Device bytes per memory wave (node records, images, ring sums); 0 = 70% of free memory. */
 int rl_batch_set_memory(rl_batch* batch, double bytes);
-/* Tile shape of the walk: lines per work item (1..8) and channel slots per lane (1, 2, 4, 8;
-   a tile is 32 x slots (line, channel) pairs). */
+/* Tile shape of the walk: lines per work item (1..32; a warp walks the item's (line,
+   channel) pairs in tiles of 32 x slots pairs spanning at most 12 lines) and channel slots
+   per lane (1, 2, 4, 8). Default 32 lines, 4 slots. */
 int rl_batch_set_tiles(rl_batch* batch, int lines_per_item, int channel_slots);
 int rl_batch_get_tiles(rl_batch* batch, int* lines_per_item, int* channel_slots);
-/* Times every tile shape on every sample_stride-th work item of the first wave and keeps the
-   fastest; returns it and the sampled walk time. No counterpart in the reference. */
+/* Times the tile shapes (2, 8, 16, 32 lines per item x 2, 4 slots) on every
+   sample_stride-th work item of the first wave and keeps the fastest; returns it and the
+   sampled walk time. No counterpart in the reference. */
 int rl_batch_autotune(rl_batch* batch, int sample_stride, int* lines_per_item, int* channel_slots,
                       double* sample_ms);
 /* 1 (default): capture the launch sequence in a CUDA graph at the first run, replay after. */

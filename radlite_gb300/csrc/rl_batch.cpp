@@ -415,8 +415,10 @@ int autotune(rl_batch* b, int stride, int* gbest, int* cbest, double* best_ms) {
   }
   int maxnl = 1;
   for (int j : P.waves[0].jobs) maxnl = std::max(maxnl, b->jobs[j]->nl);
+  // eight slots per lane need more shared memory than four 4-warp blocks per SM leave
+  // beside the 12-line stage, so the tuner tries two and four
   const int gc[] = {2, 8, 16, kItemLines};
-  const int cc[] = {2, 4, 8};
+  const int cc[] = {2, 4};
   double best = 1e300;
   int bg = b->gcap, bc = b->cpl;
   for (int g : gc) {
