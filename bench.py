@@ -439,7 +439,7 @@ def extras_case(ctx, cfg, arr, tmp, with_cpu=True):
     return out
 
 
-def batched_case(ctx, n_models, steps, tune_stride=32):
+def batched_case(ctx, n_models, steps, tune_stride=8):
     """Plain per-model launches against one batched, graph-replayed launch sequence on the
     uneven multi-model workload (synth.batch_configs): same spectra, spectra/s of each."""
     import numpy as np

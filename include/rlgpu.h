@@ -204,8 +204,9 @@ int rl_batch_set_memory(rl_batch* batch, double bytes);
 int rl_batch_set_tiles(rl_batch* batch, int lines_per_item, int channel_slots);
 int rl_batch_get_tiles(rl_batch* batch, int* lines_per_item, int* channel_slots);
 /* Times the tile shapes (2, 8, 16, 32 lines per item x 2, 4 slots) on every
-   sample_stride-th work item of the first wave and keeps the fastest; returns it and the
-   sampled walk time. No counterpart in the reference. */
+   sample_stride-th work item of the first wave and keeps the fastest, the default shape
+   unless another beats it by 2% (a stride of 8 or less samples enough items to rank them);
+   returns it and the sampled walk time. No counterpart in the reference. */
 int rl_batch_autotune(rl_batch* batch, int sample_stride, int* lines_per_item, int* channel_slots,
                       double* sample_ms);
 /* 1 (default): capture the launch sequence in a CUDA graph at the first run, replay after. */

@@ -419,7 +419,7 @@ class Batch:
         _check(lib().rl_batch_get_tiles(self.h, C.byref(g), C.byref(c)), self.ctx.h)
         return g.value, c.value
 
-    def autotune(self, sample_stride: int = 16) -> dict:
+    def autotune(self, sample_stride: int = 8) -> dict:
         g, c, ms = C.c_int(), C.c_int(), C.c_double()
         _check(lib().rl_batch_autotune(self.h, sample_stride, C.byref(g), C.byref(c), C.byref(ms)), self.ctx.h)
         return {"lines_per_item": g.value, "channel_slots": c.value, "sample_ms": ms.value}

@@ -419,7 +419,9 @@ int autotune(rl_batch* b, int stride, int* gbest, int* cbest, double* best_ms) {
   // beside the 12-line stage, so the tuner tries two and four
   const int gc[] = {2, 8, 16, kItemLines};
   const int cc[] = {2, 4};
-  double best = 1e300;
+  // A sample of few items ends in a tail that the full walk does not have, so the default
+  // shape (32 lines, 4 slots) keeps its place unless another shape beats it by 2%.
+  double best = 1e300, best_score = 1e300;
   int bg = b->gcap, bc = b->cpl;
   for (int g : gc) {
     if (g > maxnl && g != gc[0]) continue;
@@ -440,7 +442,8 @@ int autotune(rl_batch* b, int stride, int* gbest, int* cbest, double* best_ms) {
         CUDA_TRY(cudaStreamSynchronize(s));
         cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
       }
-      if (ms < best) { best = ms; bg = g; bc = c; }
+      const double score = (g == kItemLines && c == 4) ? 0.98 * ms : ms;
+      if (score < best_score) { best_score = score; best = ms; bg = g; bc = c; }
     }
   }
   b->gcap = bg; b->cpl = bc;
