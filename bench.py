@@ -165,6 +165,17 @@ def dist_setup():
     return world, rank, local, dist
 
 
+def max_over_ranks(x: float, dist) -> float:
+    """The largest of every rank's `x` (the job's time is its slowest replica's); `x`
+    itself with one rank. Replicas exchange nothing else."""
+    if not dist:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def reference_arm(args):
     world, rank, _, dist = dist_setup()
     if rank != 0:
@@ -246,12 +257,7 @@ def ours(args):
             steps_fs = sum(s["steps"] for s in sts)
             integ = sum(s["integrated"] for s in sts)
     wall = (time.perf_counter() - t0) / args.steps
-    ms = sum(dev_ms) / len(dev_ms)
-    if dist:
-        import torch
-        t = torch.tensor([ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(sum(dev_ms) / len(dev_ms), dist)
     nrays = 1 + (abs(cfg.nrrextra) + 10 + cfg.dbdr * (cfg.nr - 1)) * cfg.nphi
     nfr = int(2.0 * cfg.vmax / cfg.dv + 1)
     rc_per_step = nrays * nfr * cfg.nlines * len(INCLS)
@@ -277,7 +283,7 @@ def ours(args):
         h2d = sum(s["h2d_bytes"] for s in sts)
         d2h = sum(s["d2h_bytes"] for s in sts)
         m2.free()
-    e2e = world * rc_per_step / statistics.median(e2e_t)
+    e2e = world * rc_per_step / max_over_ranks(statistics.median(e2e_t), dist)
     # accuracy at full size: FP32 vs FP64 of the first line at the first inclination
     rel = None
     if not args.no_verify:
