@@ -422,18 +422,27 @@ def cell_params(cfg: DiskConfig):
     return (np.log(cell_order(f["temp"])), np.log(cell_order(f["abund"])), cell_order(f["width"]))
 
 
+def lte_populations(E_cm, g, temp):
+    """LTE level populations n_i = g_i exp(-E_i hc/kT) / Q, Q the sum over the given levels,
+    values below 1e-99 set to 0 (pyradlite _prep_mol_forcore, radlite.py:1106-1118, with its
+    interpolated partition-sum table replaced by the level sum). E_cm [nlev] in cm^-1, g
+    [nlev], temp any shape; returns [nlev, *temp.shape]."""
+    temp = np.asarray(temp, dtype=np.float64)
+    ex = -np.multiply.outer(np.asarray(E_cm, dtype=np.float64) * HC_K, 1.0 / temp)
+    lg = np.log(np.asarray(g, dtype=np.float64)).reshape((-1,) + (1,) * temp.ndim)
+    m = (lg + ex).max(axis=0, keepdims=True)
+    w = np.exp(lg + ex - m)
+    pop = w / w.sum(axis=0, keepdims=True)
+    pop[pop < 1e-99] = 0.0
+    return pop
+
+
 def lte_arrays(cfg: DiskConfig) -> dict:
     """model_arrays() with the level populations recomputed in LTE from the energies as the
     molecule file stores them (F12.4 cm^-1), i.e. the populations the differentiable
     raytrace derives from the temperature."""
     f = model_arrays(cfg)
-    E = np.round(f["E"], 4)
-    ex = -np.multiply.outer(E * HC_K, 1.0 / f["temp"])
-    lg = np.log(f["g"])[:, None, None]
-    m = (lg + ex).max(axis=0, keepdims=True)
-    w = np.exp(lg + ex - m)
-    f["pop"] = w / w.sum(axis=0, keepdims=True)
-    f["pop"][f["pop"] < 1e-99] = 0.0
+    f["pop"] = lte_populations(np.round(f["E"], 4), f["g"], f["temp"])
     return f
 
 
