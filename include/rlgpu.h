@@ -78,7 +78,8 @@ typedef struct rl_model_arrays {
   const double* kappa_scat; /* [ncont] */
   double rstar;             /* starinfo.inp [cm] */
   const double* star_flux_1pc; /* [ncont] F_nu at 1 pc (starspectrum.inp) or NULL (no star pumping) */
-  int outer_bc;             /* 0 black, 2 microwave background */
+  int outer_bc;             /* 0 black, 2 microwave background (3, the interstellar field of
+                               interstellfield.inp, only through rl_load_dir) */
   double incl_deg;          /* linespectrum.inp */
   int nphi, dbdr, nrrayextra;  /* radlite.inp circular image */
   double vmax, dv, radvelo; /* passband half width, sampling, radial velocity [km/s] */

@@ -214,6 +214,7 @@ struct rlo_model {
     int nlin; int *lup, *ldn; double *Aud, *lfreq;
     double umass;
     double rstar; double* starcont; int starpump;
+    double* isrf;   /* [1..ncont] interstellfield.inp (outer boundary 3), else NULL */
     int outer_bc, inner_bc, line_dust;
     /* camera & passband */
     double incl_rad; int nphi, dbdr, nrext;
@@ -237,7 +238,7 @@ void rlo_free(rlo_model* m) {
     if (!m) return;
     void* ptrs[] = {m->Rg, m->Tg, m->ridx, m->rho, m->vel, m->lw, m->abun, m->drho, m->dtemp, m->cnu,
                     m->kabs, m->ksca, m->scat, m->pop, m->Ecm, m->g, m->Eerg, m->lup, m->ldn, m->Aud,
-                    m->lfreq, m->starcont, m->x0, m->z0, m->rays_r, m->ri, m->ldsrc, m->ldalp};
+                    m->lfreq, m->starcont, m->isrf, m->x0, m->z0, m->rays_r, m->ri, m->ldsrc, m->ldalp};
     for (size_t i = 0; i < sizeof ptrs / sizeof ptrs[0]; i++) free(ptrs[i]);
     free(m);
 }
@@ -296,7 +297,8 @@ static int read_model(const char* dir, rlo_model* m) {
         if (m->nrext == 0) return fail("radlite.inp: nrrayextra must be non-zero");
         if (dodust != 0 || doline == 0) return fail("radlite.inp: only line transfer is supported");
         m->inner_bc = 2;   /* forced by setup -551 (setup.F:1135) */
-        if (m->outer_bc != 0 && m->outer_bc != 2) return fail("outer boundary type %d not supported", m->outer_bc);
+        if (m->outer_bc != 0 && m->outer_bc != 2 && m->outer_bc != 3)
+            return fail("outer boundary type %d not supported", m->outer_bc);
     }
     /* radius.inp / theta.inp (grid.F:711-819, 1098-1210) */
     if (fr_open(&f, dir, "radius.inp")) return -1;
@@ -343,6 +345,18 @@ static int read_model(const char* dir, rlo_model* m) {
     m->cnu = (double*)calloc((size_t)m->ncont + 2, sizeof(double));   /* 1-based */
     for (int i = 1; i <= m->ncont; i++) if (rd_d(&f, &m->cnu[i])) return -1;
     fr_close(&f);
+    /* interstellfield.inp for outer boundary 3 (read_interstellfield, star.F:690-727): the
+       frequency count, then one intensity per frequency */
+    if (m->outer_bc == 3) {
+        if (!fr_exists(dir, "interstellfield.inp")) return fail("outer boundary type 3 needs interstellfield.inp");
+        if (fr_open(&f, dir, "interstellfield.inp")) return -1;
+        int nf = 0;
+        if (rd_i(&f, &nf)) return -1;
+        if (nf != m->ncont) return fail("interstellfield.inp: frequency count differs from frequency.inp");
+        m->isrf = (double*)calloc((size_t)m->ncont + 2, sizeof(double));
+        for (int i = 1; i <= m->ncont; i++) if (rd_d(&f, &m->isrf[i])) return -1;
+        fr_close(&f);
+    }
     /* line.inp header (line.F:142-200) */
     if (fr_open(&f, dir, "line.inp")) return -1;
     { int fmtl, nsp; if (rd_i(&f, &fmtl)) return -1; if (fmtl == 2 && rd_i(&f, &nsp)) return -1;
@@ -943,6 +957,7 @@ typedef struct {
     const double *dsrc, *dalp;
     double* dnu;   /* [1..nfr] */
     double* star;  /* [1..nfr] */
+    double* isrf;  /* [1..nfr] outer-boundary start intensity (type 3), or NULL: 0 */
     long long steps;
     double tau;        /* char_tau: running optical depth of the current (ray, channel), line.F:4598 */
 } linectx;
@@ -1092,6 +1107,8 @@ static int charint(linectx* L, const traj_t* T, int inu, double rbeam0, float* m
         if (m->outer_bc == 2) {
             double fq = L->lfreq, temp = 2.728;
             I = 1.47455253991e-47 * (fq * fq * fq) / (exp(4.7991598e-11 * fq / temp) - 1.0);
+        } else if (m->outer_bc == 3) {
+            I = L->isrf ? L->isrf[inu] : 0.0;   /* radbnd_interstellfield(inu), telescope.F:4016-4023 */
         } else I = 0.0;
         if (node_values(L, icr, ir, it, dr, dt, T->mu[1], T->phi[1], &sd0, &ad0, &dv0, &lw0, &nu0, &nd0)) return -1;
     }
@@ -1124,7 +1141,11 @@ static int charint(linectx* L, const traj_t* T, int inu, double rbeam0, float* m
     return 0;
 }
 
-static void line_ctx(rlo_model* m, int il, linectx* L) {
+/* with_isrf: fill the interstellar start table as calc_line_spectrum does
+   (line_init_passband_outerbc, line.F:3855-3903, called at telescope.F:1564-1570); the
+   position-velocity path (calc_write_line_posvel, telescope.F:1828-1924) never fills it, so
+   its rays start from the zeros of the untouched table. */
+static int line_ctx(rlo_model* m, int il, linectx* L, int with_isrf) {
     memset(L, 0, sizeof *L);
     L->m = m; L->il = il;
     L->lfreq = m->lfreq[il]; L->nu0abs = fabs(L->lfreq); L->Aud = m->Aud[il];
@@ -1144,6 +1165,25 @@ static void line_ctx(rlo_model* m, int il, linectx* L) {
         if (i == 0 || i == m->ncont) L->star[k] = 0.0;
         else { double w = (fq - m->cnu[i]) / (m->cnu[i + 1] - m->cnu[i]); L->star[k] = (1.0 - w) * m->starcont[i] + w * m->starcont[i + 1]; }
     }
+    if (with_isrf && m->outer_bc == 3) {
+        L->isrf = (double*)calloc((size_t)nfr + 1, sizeof(double));
+        for (int k = 1; k <= nfr; k++) {
+            double fq = L->nu0abs + L->dnu[k];
+            int i = hunt1(m->cnu, m->ncont, fq, 0);
+            /* the zero test is against the channel count freq_nr, not the frequency count */
+            if (i == 0 || i == nfr) L->isrf[k] = 0.0;
+            else if (i >= m->ncont) {
+                free(L->dnu); free(L->star); free(L->isrf);
+                L->dnu = L->star = L->isrf = NULL;
+                return fail("line %d channel %d: above the last frequency of frequency.inp (the reference reads past "
+                            "interstellfield.inp there)", il, k);
+            } else {
+                double w = (fq - m->cnu[i]) / (m->cnu[i + 1] - m->cnu[i]);
+                L->isrf[k] = (1.0 - w) * m->isrf[i] + w * m->isrf[i + 1];
+            }
+        }
+    }
+    return 0;
 }
 
 /* ----------------------------------------------------------------------------------- */
@@ -1202,7 +1242,7 @@ int rlo_line_image(rlo_model* m, int iline, int ray_begin, int ray_end, double* 
                    long long* counts) {
     if (iline < 1 || iline > m->nlin) return fail("line index out of range");
     if (ray_begin < 0 || ray_end > m->nrays || ray_begin > ray_end) return fail("ray range out of bounds");
-    linectx L; line_ctx(m, iline, &L);
+    linectx L; if (line_ctx(m, iline, &L, 1)) return -1;
     int nfr = m->nfr; int rc = 0;
     double* velo = (double*)malloc(sizeof(double) * (nfr + 1));
     for (int k = 1; k <= nfr; k++) velo[k] = L.dnu[k] / L.lfreq;
@@ -1245,17 +1285,18 @@ int rlo_line_image(rlo_model* m, int iline, int ray_begin, int ray_end, double* 
         traj_free(&T);
     }
     if (counts) { counts[0] = L.steps; counts[1] = integ; counts[2] = nodes; }
-    free(velo); free(L.dnu); free(L.star);
+    free(velo); free(L.dnu); free(L.star); free(L.isrf);
     return rc;
 }
 
 /* Every channel of one ray (x0, z0) at the camera's inclination, without the NONREDUNDANT
    window and without central-star mixing: one pixel of the rectangular image
    (make_freq_image_rectang, telescope.F:2061-2150; charintline with rbeam 0). I and the
-   line-of-sight optical depth char_tau per channel. */
+   line-of-sight optical depth char_tau per channel. With outer boundary 3 the rays start
+   at 0: the position-velocity path leaves the interstellar table unfilled. */
 int rlo_ray_spectrum(rlo_model* m, int iline, double x0, double z0, double* I_out, double* tau_out) {
     if (iline < 1 || iline > m->nlin) return fail("line index out of range");
-    linectx L; line_ctx(m, iline, &L);
+    linectx L; if (line_ctx(m, iline, &L, 0)) return -1;
     traj_t T; memset(&T, 0, sizeof T);
     int rc = trajectory(m, x0, z0, m->theta0, &T);
     for (int k = 1; k <= m->nfr && !rc; k++) {

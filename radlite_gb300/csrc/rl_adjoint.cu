@@ -645,7 +645,7 @@ __device__ void adjoint_item(const AdjParams<T>& A, int item, AdjStage<T>& S, Ad
       const int idx = u * 32 + lane;
       ch[u] = idx < nt ? (int)list[tb + idx] : -1;
       w[u] = ch[u] >= 0 ? P.wch[(size_t)l * P.nfr + ch[u]] : (T)0;
-      I[u] = ch[u] >= 0 ? P.lc[l].istart : (T)0;
+      I[u] = ch[u] >= 0 ? (P.isrf ? P.isrf[(size_t)l * P.nfr + ch[u]] : P.lc[l].istart) : (T)0;
       j0[u] = 0; a0[u] = 0; S0[u] = 0;
     }
     for (int cix = 0; cix < nchunk; cix++) {

@@ -217,6 +217,7 @@ int write_descriptors(rl_batch* b) {
       w.gsize = gs; w.nitems = ng * cam.nrays;
       w.tab = J.tab.as<T>(); w.nsum = J.nsum.as<T>(); w.wch = J.wch.as<T>(); w.velo = J.velo.as<double>();
       w.star = J.star.as<T>(); w.lc = J.lc.as<LineConst<T>>();
+      w.isrf = isrf_of(m, w.star, J.nl, J.nfr);
       w.aksmax_c = J.aksmax / 2.99792458e5;
       w.kq = (T)(3.33567e-6 * 2.99792458e5);
       w.fstar = (T)J.fstar;

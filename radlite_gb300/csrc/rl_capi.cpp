@@ -82,7 +82,8 @@ int rl::build_line_tables(const Model& m, int iline0, int nl, LineTables<T>& out
   const bool scaled = std::is_same<T, float>::value;
   out.nl = nl; out.ncell = ncell; out.nfr = nfr;
   out.tab.assign((size_t)nl * ncell * 4, (T)0); out.nsum.assign((size_t)nl * ncell, (T)0);
-  out.wch.assign((size_t)nl * nfr, (T)0); out.star.assign((size_t)nl * nfr, (T)0);
+  const bool isrf = m.outer_bc == 3;
+  out.wch.assign((size_t)nl * nfr, (T)0); out.star.assign((size_t)(isrf ? 2 : 1) * nl * nfr, (T)0);
   out.velo.assign((size_t)nl * nfr, 0.0); out.scale.assign(nl, 1.0); out.lc.assign(nl, LineConst<T>{});
   for (int l = 0; l < nl; l++) {
     LinePrep lp;
@@ -99,6 +100,7 @@ int rl::build_line_tables(const Model& m, int iline0, int nl, LineTables<T>& out
     for (int k = 0; k < nfr; k++) {
       out.wch[(size_t)l * nfr + k] = (T)lp.wch[k];
       out.star[(size_t)l * nfr + k] = (T)lp.star[k];
+      if (isrf) out.star[((size_t)nl + l) * nfr + k] = (T)lp.isrf[k];
       out.velo[(size_t)l * nfr + k] = lp.velo[k];
     }
     out.lc[l].cphi = (T)lp.cphi;
@@ -226,6 +228,7 @@ static int run_lines(rl_model* md, int iline0, int nl, double* flux_out, double*
   if (nfr >= 2048) return set_err(ctx, RL_ERR_ARG, "at most 2047 channels per line are supported");
   P.tab = md->dtab.as<T>(); P.nsum = md->dnsum.as<T>(); P.wch = md->dwch.as<T>(); P.velo = md->dvelo.as<double>();
   P.star = md->dstar.as<T>(); P.lc = md->dlc.as<LineConst<T>>();
+  P.isrf = isrf_of(m, P.star, nl, nfr);
   P.aksmax_c = m.aksmax / 2.99792458e5;
   P.kq = (T)(3.33567e-6 * 2.99792458e5);
   P.fstar = (T)((m.rstar / cam.ri[1]) * (m.rstar / cam.ri[1]));
@@ -401,7 +404,7 @@ int rl_load_arrays(rl_ctx* ctx, const rl_model_arrays* a, rl_model** out) {
   if (a->star_flux_1pc)
     for (int i = 0; i < m.ncont; i++) m.starcont[i] = 3.0308410e36 * a->star_flux_1pc[i] / (m.rstar * m.rstar);
   m.outer_bc = a->outer_bc;
-  if (m.outer_bc != 0 && m.outer_bc != 2) return set_err(ctx, RL_ERR_ARG, "rl_load_arrays: outer boundary 0 or 2");
+  if (m.outer_bc != 0 && m.outer_bc != 2) return set_err(ctx, RL_ERR_ARG, "rl_load_arrays: outer boundary 0 or 2 (type 3 needs interstellfield.inp: use rl_load_dir)");
   m.incl_rad = a->incl_deg * 0.0174532925199;
   m.nphi = a->nphi; m.dbdr = a->dbdr; m.nrext = a->nrrayextra;
   m.vmax = a->vmax; m.dv = a->dv; m.radvelo = a->radvelo;

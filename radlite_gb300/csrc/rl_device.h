@@ -81,6 +81,8 @@ struct WalkParams {
   const T* wch;              // [nlines][nfr] channel velocity in passband units
   const double* velo;        // [nlines][nfr] dnu/nu0 (window test)
   const T* star;             // [nlines][nfr] scaled stellar intensity
+  const T* isrf = nullptr;   // [nlines][nfr] scaled start intensity per channel (outer
+                             //   boundary 3), or null: LineConst::istart for every channel
   const LineConst<T>* lc;    // [nlines]
   double aksmax_c;           // max line width / c
   T kq;                      // 3.33567e-6 * 2.99792458e5

@@ -84,6 +84,7 @@ WalkParams<T> walk_params(const rl_diff* d) {
   P.nitems = ((d->nl + d->gsize - 1) / d->gsize) * d->cam.nrays;
   P.tab = d->tab.as<T>(); P.nsum = d->nsum.as<T>(); P.wch = d->wch.as<T>(); P.velo = d->velo.as<double>();
   P.star = d->star.as<T>(); P.lc = d->lc.as<LineConst<T>>();
+  P.isrf = isrf_of(m, P.star, d->nl, d->nfr);
   P.aksmax_c = m.aksmax / 2.99792458e5;
   P.kq = (T)(3.33567e-6 * 2.99792458e5);
   P.fstar = (T)((m.rstar / d->cam.ri[1]) * (m.rstar / d->cam.ri[1]));

@@ -234,7 +234,8 @@ void read_radlite_inp(const std::string& dir, Model& m) {
   m.starpump = f.i();
   if (dodust != 0 || doline == 0) fail("radlite.inp: only line transfer (dust 0, lines 1) is supported");
   if (m.nrext == 0) fail("radlite.inp: nrrayextra must be non-zero");
-  if (m.outer_bc != 0 && m.outer_bc != 2) fail("radlite.inp: outer boundary type " + std::to_string(m.outer_bc) + " not supported");
+  if (m.outer_bc != 0 && m.outer_bc != 2 && m.outer_bc != 3)
+    fail("radlite.inp: outer boundary type " + std::to_string(m.outer_bc) + " not supported");
 }
 
 void read_grid(const std::string& dir, Model& m) {
@@ -540,6 +541,17 @@ int bracket(const std::vector<double>& xx, double x) {
   return lo;
 }
 
+// interstellfield.inp, the outer boundary of type 3 (read_interstellfield, star.F:690-727):
+// the count of frequency.inp, then one intensity per frequency
+static void read_isrf(const std::string& dir, Model& m) {
+  if (stat_input(dir, "interstellfield.inp").size < 0)
+    fail("radlite.inp: outer boundary type 3 needs the file interstellfield.inp");
+  Records f(dir, "interstellfield.inp");
+  if (f.i() != m.ncont) fail("interstellfield.inp: frequency count differs from frequency.inp");
+  m.isrf.resize(m.ncont);
+  for (auto& v : m.isrf) v = f.d();
+}
+
 void finish_model(Model& m) {
   m.aksmax = 0.0;
   for (double v : m.lw) if (v > m.aksmax) m.aksmax = v;
@@ -558,6 +570,7 @@ static int parse_dir(const std::string& dir, Model& m, std::string& err) {
       m.cnu.resize(m.ncont);
       for (auto& v : m.cnu) v = f.d();
     }
+    if (m.outer_bc == 3) read_isrf(dir, m);
     {
       Records f(dir, "line.inp");
       const int fmt = f.i();
@@ -592,7 +605,7 @@ void visit_model(Model& m, V& v) {
   v(m.umass); v(m.rstar); v(m.starcont); v(m.starpump); v(m.outer_bc); v(m.line_dust); v(m.incl_rad); v(m.nphi);
   v(m.dbdr); v(m.nrext); v(m.vmax); v(m.dv); v(m.radvelo); v(m.nlspec); v(m.ilstart); v(m.style); v(m.nfr);
   v(m.command); v(m.pv.nx); v(m.pv.ny); v(m.pv.szimx); v(m.pv.szimy); v(m.pv.phioff); v(m.pv.xoff); v(m.pv.yoff);
-  v(m.pv.addstar); v(m.aksmax);
+  v(m.pv.addstar); v(m.aksmax); v(m.isrf);
 }
 
 struct Writer {
@@ -653,7 +666,7 @@ struct Hasher {
   }
 };
 
-constexpr char kCacheMagic[8] = {'R', 'L', 'G', 'P', 'U', 'I', 'N', '2'};
+constexpr char kCacheMagic[8] = {'R', 'L', 'G', 'P', 'U', 'I', 'N', '3'};
 
 std::string cache_path(const std::string& cache_dir, const std::string& key) {
   Hasher h;
@@ -889,6 +902,28 @@ int prepare_line(const Model& m, int iline, bool scaled, LinePrep& lp, std::stri
       lp.star[k] = (1.0 - wgt) * m.starcont[i - 1] + wgt * m.starcont[i];
     }
   }
+  // outer boundary type 3: the interstellar field at each channel frequency
+  // (line_init_passband_outerbc, line.F:3855-3903). Unlike the stellar table it zeroes the
+  // channel whose bracket index equals the channel count (freq_nr), not the frequency count;
+  // above the last frequency (other than that) the reference reads past its table.
+  lp.isrf.clear();
+  if (m.outer_bc == 3) {
+    lp.isrf.resize(nfr);
+    for (int k = 0; k < nfr; k++) {
+      const double fq = lp.nu0 + lp.dnu[k];
+      const int i = bracket(m.cnu, fq);
+      if (i == 0 || i == nfr) lp.isrf[k] = 0.0;
+      else if (i >= m.ncont) {
+        err = "line " + std::to_string(iline) + ": channel " + std::to_string(k + 1) +
+              " lies above the last frequency of frequency.inp, where the reference's outer boundary "
+              "type 3 interpolates past the end of interstellfield.inp";
+        return -1;
+      } else {
+        const double wgt = (fq - m.cnu[i - 1]) / (m.cnu[i] - m.cnu[i - 1]);
+        lp.isrf[k] = (1.0 - wgt) * m.isrf[i - 1] + wgt * m.isrf[i];
+      }
+    }
+  }
   // grey dust at the line centre (line.F:3502-3677)
   std::vector<double> jd(ncell, 0.0), ad(ncell, 0.0);
   if (m.line_dust) {
@@ -946,12 +981,14 @@ int prepare_line(const Model& m, int iline, bool scaled, LinePrep& lp, std::stri
       if (af[c] > 0.0) smax = std::max(smax, jf[c] / af[c]);
     }
     for (double v : lp.star) smax = std::max(smax, v);
+    for (double v : lp.isrf) smax = std::max(smax, v);
     smax = std::max(smax, istart);
     if (smax > 0.0 && std::isfinite(smax)) scale = smax;
   }
   lp.scale = scale;
   lp.istart = istart / scale;
   for (auto& v : lp.star) v /= scale;
+  for (auto& v : lp.isrf) v /= scale;
   lp.tab.resize((size_t)ncell * 4);
   for (int c = 0; c < ncell; c++) {
     lp.tab[4 * (size_t)c + 0] = jf[c] / scale;
@@ -960,7 +997,6 @@ int prepare_line(const Model& m, int iline, bool scaled, LinePrep& lp, std::stri
     lp.tab[4 * (size_t)c + 3] = ad[c];
   }
   lp.cphi = 0.56419583546 / (3.33567e-6 * lp.nu0);
-  (void)err;
   return 0;
 }
 

@@ -39,6 +39,7 @@ struct Model {
   // star and boundaries
   double rstar = 0.0;
   std::vector<double> starcont;             // intensity at the stellar surface on cnu
+  std::vector<double> isrf;                 // interstellar field on cnu (outer boundary 3)
   int starpump = 0, outer_bc = 0, line_dust = 1;
   // camera and passband (radlite.inp, linespectrum.inp)
   double incl_rad = 0.0;
@@ -77,6 +78,7 @@ struct PVCamera {
 struct LinePrep {
   double lfreq = 0.0, nu0 = 0.0, Bud = 0.0, Bdu = 0.0, scale = 1.0, istart = 0.0, cphi = 0.0;
   std::vector<double> dnu, velo, wch, star;    // [nfr]
+  std::vector<double> isrf;                    // [nfr] outer-boundary start per channel (type 3), else empty
   std::vector<double> tab;                     // [ncell][4] jfac/scale, afac, jd/scale, ad
   std::vector<double> nsum;                    // [ncell]
 };

@@ -66,13 +66,22 @@ struct LineTables {
   int nl = 0, ncell = 0, nfr = 0;
   std::vector<T> tab;        // [ncell][nl][4]: j-factor*cphi, alpha-factor*cphi, dust j, dust alpha
   std::vector<T> nsum;       // [ncell][nl]
-  std::vector<T> wch, star;  // [nl][nfr]
+  std::vector<T> wch;        // [nl][nfr]
+  std::vector<T> star;       // [nl][nfr] stellar intensity, then (outer boundary 3) [nl][nfr]
+                             // the interstellar start intensity (isrf_of)
   std::vector<double> velo;  // [nl][nfr]
   std::vector<LineConst<T>> lc;
   std::vector<double> scale; // [nl]
 };
 template <typename T>
 int build_line_tables(const Model& m, int iline0, int nl, LineTables<T>& out, std::string& err);
+
+// The per-channel start intensities inside a device copy of LineTables::star (outer
+// boundary 3), or null: the walk then starts every channel at LineConst::istart.
+template <typename T>
+inline const T* isrf_of(const Model& m, const T* dstar, int nl, int nfr) {
+  return m.outer_bc == 3 ? dstar + (size_t)nl * nfr : nullptr;
+}
 
 // Node records of a ray set (NodeBuf's arrays), grown on demand.
 struct NodeStore {

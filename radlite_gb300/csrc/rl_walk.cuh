@@ -49,7 +49,7 @@ __device__ long long walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState
       const unsigned e = list[idx];
       L = (int)(e >> kChBits) - lbase;
       w = P.wch[(size_t)(l0 + L) * P.nfr + (e & (kMaxChannels - 1))];
-      I = P.lc[l0 + L].istart;
+      I = P.isrf ? P.isrf[(size_t)(l0 + L) * P.nfr + (e & (kMaxChannels - 1))] : P.lc[l0 + L].istart;
       if constexpr (PV) {
         const size_t a = ((size_t)(l0 + L) * nb.nrays + ray) * P.nfr + (e & (kMaxChannels - 1));
         P.tau[a] = 0; P.tauc[a] = 0;

@@ -14,6 +14,7 @@ Formats follow the reference readers and the pyradlite writers:
   dustopac.inp / dustopac_1.inp        dust.F:92-447
   frequency.inp        grid.F:1445-1463           starinfo.inp     star.F:543-569
   starspectrum.inp     star.F:449-537             line.inp         line.F:142-367
+  interstellfield.inp  star.F:690-727 (outer boundary 3)
   linespectrum.inp     telescope.F:86-257         moldata.dat      line.F:1826-1985
   levelpop.info / levelpop_moldata.dat line.F:811-950
   radlite.inp (format 104) main.F:488-686 + setup.F:1117-1137, template
@@ -83,7 +84,9 @@ class DiskConfig:
     nrrextra: int = -93               # radlite.inp b_extra (negative: dynamic extra rays)
     perturb_sigma: float = 0.0        # lognormal sigma of per-cell T and rho factors
     seed: int = 0
-    outer_bc: int = 0                 # 0 = black, 2 = CMB
+    outer_bc: int = 0                 # 0 = black, 2 = CMB, 3 = interstellar field (interstellfield.inp)
+    isrf_t: float = 6000.0            # outer boundary 3: diluted blackbody W B_nu(T) on frequency.inp
+    isrf_w: float = 1.0e-3
     starpump: int = 1                 # 1 = read the stellar spectrum (central-ray star)
     nfreq_dust: int = 24
     # linespectrum.inp command 2 (position-velocity cube): pixels, full image size [AU],
@@ -294,6 +297,9 @@ def write_model(cfg: DiskConfig, outdir: str) -> str:
     nf = len(fr)
     with open(P("frequency.inp"), "w") as fh:
         fh.write(f"{nf:12d}\n \n" + _fmt_rows(fr, "%.10e"))
+    if cfg.outer_bc == 3:
+        with open(P("interstellfield.inp"), "w") as fh:
+            fh.write(f"{nf:12d}\n" + _fmt_rows(cfg.isrf_w * planck(fr, cfg.isrf_t), "%.10e"))
     with open(P("dustopac.inp"), "w") as fh:
         fh.write("2               Format number of this file\n"
                  "1               Nr of dust species\n"

@@ -16,7 +16,7 @@ from radlite_gb300 import synth  # noqa: E402
 from oracle import pyoracle  # noqa: E402
 
 CASES = [("tiny_line", {}), ("tiny_band", {}), ("small_line", {}), ("tiny_line", {"incl_deg": 5.0}),
-         ("tiny_line", {"outer_bc": 2, "incl_deg": 80.0})]
+         ("tiny_line", {"outer_bc": 2, "incl_deg": 80.0}), ("tiny_band", {"outer_bc": 3})]
 
 
 def case_name(name, over):
