@@ -498,7 +498,8 @@ static int read_model(const char* dir, rlo_model* m) {
             if (rd_i(&f, &m->pv_nx) || rd_i(&f, &m->pv_ny) || rd_i(&f, &sizespec) || rd_d(&f, &m->pv_szx) ||
                 rd_d(&f, &m->pv_szy) || rd_d(&f, &m->pv_phioff) || rd_d(&f, &m->pv_xoff) || rd_d(&f, &m->pv_yoff) ||
                 rd_i(&f, &m->pv_addstar)) return -1;
-            if (sizespec != 1) return fail("linespectrum.inp: size specifier %d not supported", sizespec);
+            /* 0 (arcsec): the reference warns and reads the sizes as for 1 (telescope.F:207-216) */
+            if (sizespec != 0 && sizespec != 1) return fail("linespectrum.inp: size specifier %d unknown", sizespec);
         }
         m->incl_rad = inc * 0.0174532925199;
         fr_close(&f);

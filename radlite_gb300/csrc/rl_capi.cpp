@@ -547,6 +547,8 @@ int rl_run_dir_ex(const char* dir, int device, int flags, rl_stats* st) {
   rl_model* md = nullptr;
   rc = rl_load_dir(ctx, dir, &md);
   if (rc == 0) run_log(dir, true);
+  if (rc == 0 && md->m.command == 2 && md->m.pv.sizespec == 0)   // telescope.F:207-210
+    std::printf(" While reading linespectrum.inp:\n Size specifier in arcsec not yet implemented\n");
   if (rc == 0 && md->m.command == 2) {
     // one lineposvel file per line (main.F:1061-1074); lines in chunks of at most 2 GB of
     // cube per array

@@ -420,8 +420,9 @@ void read_linespectrum(const std::string& dir, Model& m) {
     pv.xoff = f.d();
     pv.yoff = f.d();
     pv.addstar = f.i();
-    if (sizespec == 0) fail("linespectrum.inp: image size in arcsec is not implemented in the reference either");
-    if (sizespec != 1) fail("linespectrum.inp: size specifier " + std::to_string(sizespec) + " unknown");
+    // 0 (arcsec) draws a warning in the reference, which then reads the sizes as for 1 (cm)
+    if (sizespec != 0 && sizespec != 1) fail("linespectrum.inp: size specifier " + std::to_string(sizespec) + " unknown");
+    pv.sizespec = sizespec;
   }
 }
 
@@ -605,7 +606,7 @@ void visit_model(Model& m, V& v) {
   v(m.umass); v(m.rstar); v(m.starcont); v(m.starpump); v(m.outer_bc); v(m.line_dust); v(m.incl_rad); v(m.nphi);
   v(m.dbdr); v(m.nrext); v(m.vmax); v(m.dv); v(m.radvelo); v(m.nlspec); v(m.ilstart); v(m.style); v(m.nfr);
   v(m.command); v(m.pv.nx); v(m.pv.ny); v(m.pv.szimx); v(m.pv.szimy); v(m.pv.phioff); v(m.pv.xoff); v(m.pv.yoff);
-  v(m.pv.addstar); v(m.aksmax); v(m.isrf);
+  v(m.pv.addstar); v(m.pv.sizespec); v(m.aksmax); v(m.isrf);
 }
 
 struct Writer {

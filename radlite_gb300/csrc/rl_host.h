@@ -11,6 +11,7 @@ struct PVSpec {
   double szimx = 0.0, szimy = 0.0;   // full image size [cm]
   double phioff = 0.0, xoff = 0.0, yoff = 0.0;
   int addstar = 0;
+  int sizespec = 1;                   // linespectrum.inp size specifier (0: arcsec, read as cm)
 };
 
 // Everything the line raytrace reads from the reference's input files.

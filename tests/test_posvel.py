@@ -101,6 +101,23 @@ def test_host_reads_posvel_request(gpu_lib, tmp_path):
     assert m.posvel_spec()["nx"] == 8
 
 
+def test_arcsec_size_specifier_reads_as_cm(gpu_lib, oracle_lib, tmp_path):
+    """Size specifier 0 (arcsec): the reference warns and reads the sizes as for 1
+    (telescope.F:207-216), so both readers take the same request."""
+    d1 = synth.write_model(pv_cfg(), str(tmp_path / "cm"))
+    d0 = synth.write_model(pv_cfg(), str(tmp_path / "as"))
+    p = tmp_path / "as" / "linespectrum.inp"
+    txt = p.read_text()
+    assert "1       image size in cm?" in txt
+    p.write_text(txt.replace("1       image size in cm?", "0       image size in cm?"))
+    m1, m0 = gpu_lib.load_dir_host(d1), gpu_lib.load_dir_host(d0)
+    assert m0.posvel_spec() == m1.posvel_spec()
+    assert oracle_lib.Oracle(d0).pv == oracle_lib.Oracle(d1).pv
+    p.write_text(txt.replace("1       image size in cm?", "2       image size in cm?"))
+    with pytest.raises(gpu_lib.RLError, match="size specifier"):
+        gpu_lib.load_dir_host(d0)
+
+
 # ------------------------------------------------------------------------------------
 # GPU
 # ------------------------------------------------------------------------------------
