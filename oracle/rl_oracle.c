@@ -419,13 +419,38 @@ static int read_model(const char* dir, rlo_model* m) {
             frec g2; if (fr_open(&g2, dir, fn)) return -1;
             char t[2][96]; if (fr_list(&g2, 2, t)) return -1;
             double a0, a1; tok_d(t[0], &a0); tok_d(t[1], &a1);
-            if ((int)a0 == -1) return fail("%s: temperature-dependent opacities not supported", fn);
-            if ((int)a0 != m->ncont) return fail("%s: frequency count mismatch", fn);
-            int nsz = (int)a1; if (nsz != m->nsize[is]) return fail("%s: size count mismatch", fn);
-            for (int i = 1; i <= m->ncont; i++) for (int iz = 0; iz < nsz; iz++)
-                if (rd_d(&g2, &m->kabs[((size_t)is * 4 + iz) * (m->ncont + 2) + i])) return -1;
-            for (int i = 1; i <= m->ncont; i++) for (int iz = 0; iz < nsz; iz++)
-                if (rd_d(&g2, &m->ksca[((size_t)is * 4 + iz) * (m->ncont + 2) + i])) return -1;
+            /* "-1 nfreq", then "nsize idum ntemp" and ntemp tables each after its temperature
+               range (read_dustopac_file, dust.F:320-480, built with DUST_OPAC_TEMPDEP); the
+               line dust uses the first table only (dust_kappawgt_abs(.,1,.,.), line.F:3582) */
+            int nfq = (int)a0, nsz = (int)a1, ntemp = 1, trange = (int)a0 == -1;
+            if (trange) {
+                char t3[3][96]; if (fr_list(&g2, 3, t3)) return -1;
+                double b0, b1, b2; tok_d(t3[0], &b0); tok_d(t3[1], &b1); tok_d(t3[2], &b2);
+                nfq = nsz; nsz = (int)b0; ntemp = (int)b2;
+                if (ntemp < 1) return fail("%s: temperature range count must be positive", fn);
+            }
+            if (nfq != m->ncont) return fail("%s: frequency count mismatch", fn);
+            if (nsz != m->nsize[is]) return fail("%s: size count mismatch", fn);
+            double bold = 0.0, dv;
+            for (int itp = 0; itp < ntemp; itp++) {
+                if (trange) {
+                    char t2[2][96]; double ta, tb;
+                    if (fr_list(&g2, 2, t2)) return -1;
+                    tok_d(t2[0], &ta); tok_d(t2[1], &tb);
+                    if (ta < bold) return fail("%s: temperature ranges overlap", fn);
+                    if (fabs((ta - bold) / (ta + bold)) > 1.0e-3) return fail("%s: gap between temperature ranges", fn);
+                    if (ta < 0.0 || tb < 0.0 || tb < ta) return fail("%s: invalid temperature range", fn);
+                    bold = tb;
+                }
+                for (int i = 1; i <= m->ncont; i++) for (int iz = 0; iz < nsz; iz++) {
+                    if (rd_d(&g2, &dv)) return -1;
+                    if (itp == 0) m->kabs[((size_t)is * 4 + iz) * (m->ncont + 2) + i] = dv;
+                }
+                for (int i = 1; i <= m->ncont; i++) for (int iz = 0; iz < nsz; iz++) {
+                    if (rd_d(&g2, &dv)) return -1;
+                    if (itp == 0) m->ksca[((size_t)is * 4 + iz) * (m->ncont + 2) + i] = dv;
+                }
+            }
             fr_close(&g2);
             if (rd_s(&f, s, sizeof s)) return -1;
         }

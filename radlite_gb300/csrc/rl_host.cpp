@@ -332,13 +332,41 @@ void read_dust(const std::string& dir, Model& m) {
       const std::string fn = "dustopac_" + std::to_string(ifile) + ".inp";
       Records g(dir, fn);
       const auto h = g.head(2);
-      if ((int)h[0] == -1) fail(fn + ": temperature-dependent opacity tables not supported");
-      if ((int)h[0] != m.ncont) fail(fn + ": frequency count differs from frequency.inp");
-      if ((int)h[1] != m.nsize[s]) fail(fn + ": grain size count differs from the dust temperatures");
-      for (int i = 0; i < m.ncont; i++)
-        for (int z = 0; z < m.nsize[s]; z++) m.kabs[((size_t)s * 4 + z) * m.ncont + i] = g.d();
-      for (int i = 0; i < m.ncont; i++)
-        for (int z = 0; z < m.nsize[s]; z++) m.ksca[((size_t)s * 4 + z) * m.ncont + i] = g.d();
+      // "-1 nfreq" then "nsize idum ntemp": tables for ntemp temperature ranges, each
+      // preceded by its range (read_dustopac_file, dust.F:320-480; the reference is built
+      // with DUST_OPAC_TEMPDEP). The line dust reads the first table only (line.F:3582-3605).
+      int nfreq = (int)h[0], nsz = (int)h[1], ntemp = 1;
+      const bool trange = nfreq == -1;
+      if (trange) {
+        nfreq = nsz;
+        const auto h2 = g.head(3);
+        nsz = (int)h2[0];
+        ntemp = (int)h2[2];
+        if (ntemp < 1) fail(fn + ": temperature range count must be positive");
+      }
+      if (nfreq != m.ncont) fail(fn + ": frequency count differs from frequency.inp");
+      if (nsz != m.nsize[s]) fail(fn + ": grain size count differs from the dust temperatures");
+      double bold = 0.0;
+      for (int t = 0; t < ntemp; t++) {
+        if (trange) {
+          const auto ab = g.head(2);
+          const double a = ab[0], b = ab[1];
+          if (a < bold) fail(fn + ": temperature ranges overlap");
+          if (std::fabs((a - bold) / (a + bold)) > 1.0e-3) fail(fn + ": gap between temperature ranges");
+          if (a < 0.0 || b < 0.0 || b < a) fail(fn + ": invalid temperature range");
+          bold = b;
+        }
+        for (int i = 0; i < m.ncont; i++)
+          for (int z = 0; z < nsz; z++) {
+            const double v = g.d();
+            if (t == 0) m.kabs[((size_t)s * 4 + z) * m.ncont + i] = v;
+          }
+        for (int i = 0; i < m.ncont; i++)
+          for (int z = 0; z < nsz; z++) {
+            const double v = g.d();
+            if (t == 0) m.ksca[((size_t)s * 4 + z) * m.ncont + i] = v;
+          }
+      }
       f.s();
     }
   }
