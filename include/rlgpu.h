@@ -121,6 +121,12 @@ int rl_line_image(rl_model* model, int iline, double* image_out, rl_stats* stats
    as channel 1 or inside the ray's velocity window (imcir_cmask, telescope.F:548,575), 0
    where it holds the ray's continuum. */
 int rl_line_image_mask(rl_model* model, int iline, double* image_out, unsigned char* mask_out, rl_stats* stats);
+/* 1 in *detected when the last render of line iline (spectrum, image or position-velocity
+   cube of this model) integrated a segment whose line opacity at its end times its length
+   is below -0.01, the masing test of charintline (telescope.F:4291-4297), after which the
+   reference prints "WARNING: Masing detected!"; else 0. Only lines with a population
+   inversion somewhere are tested; the batch and the differentiable path do not test. */
+int rl_line_masing(rl_model* model, int iline, int* detected);
 
 /* ---- Position-velocity cube (linespectrum.inp command 2): the rectangular image of
    setup_rays_rectang / make_freq_image_rectang / calc_write_line_posvel

@@ -44,6 +44,7 @@ def lib():
         L.rlo_pv_rays.argtypes = [vp, C.c_int, C.c_int] + [C.c_double] * 5 + [C.c_int, _D, _D, _D, _I, _D]
         L.rlo_posvel.argtypes = [vp, C.c_int, C.c_int, C.c_int] + [C.c_double] * 5 + [C.c_int, _D, _D]
         L.rlo_run_dir.argtypes = [C.c_char_p]
+        L.rlo_masing.argtypes = [vp]
         _lib = L
     return _lib
 
@@ -151,6 +152,10 @@ class Oracle:
         if rc != 0:
             raise OracleError(lib().rlo_last_error().decode())
         return flux, velo, {"steps": int(cnt[0]), "integrated": int(cnt[1]), "node_visits": int(cnt[2])}
+
+    def masing(self) -> bool:
+        """Whether the last line spectrum, image or cube met the masing test."""
+        return bool(lib().rlo_masing(self.h))
 
 
 def run_dir(path: str) -> None:

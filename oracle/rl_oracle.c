@@ -215,6 +215,7 @@ struct rlo_model {
     double umass;
     double rstar; double* starcont; int starpump;
     double* isrf;   /* [1..ncont] interstellfield.inp (outer boundary 3), else NULL */
+    int maser;      /* masing found by the last line image or position-velocity cube */
     int outer_bc, inner_bc, line_dust;
     /* camera & passband */
     double incl_rad; int nphi, dbdr, nrext;
@@ -986,6 +987,7 @@ typedef struct {
     double* isrf;  /* [1..nfr] outer-boundary start intensity (type 3), or NULL: 0 */
     long long steps;
     double tau;        /* char_tau: running optical depth of the current (ray, channel), line.F:4598 */
+    int maser;         /* maserflag: some segment had line opacity x length below -0.01 */
 } linectx;
 
 static int node_values(const linectx* L, int icr, int ir, int it, double dr, double dt, double mu, double phi,
@@ -1159,6 +1161,7 @@ static int charint(linectx* L, const traj_t* T, int inu, double rbeam0, float* m
         double sd1, ad1, lw1, dv1, nu1, nd1;
         if (node_values(L, icr, ir, it, dr, dt, T->mu[is], T->phi[is], &sd1, &ad1, &dv1, &lw1, &nu1, &nd1)) return -1;
         clever_integrate(L, inu, &I, ds, sd0, sd1, ad0, ad1, lw0, lw1, dv0, dv1, nu0, nu1, nd0, nd1, &st);
+        if (st.alpl0 * ds < -0.01) L->maser = 1;   /* masing check, telescope.F:4291-4297 */
         if (dv0 < (double)*minvel && nu0 + nd0 > LEVTHRES) *minvel = (float)dv0;
         if (dv0 > (double)*maxvel && nu0 + nd0 > LEVTHRES) *maxvel = (float)dv0;
         sd0 = sd1; ad0 = ad1; lw0 = lw1; dv0 = dv1; nu0 = nu1; nd0 = nd1;
@@ -1311,6 +1314,7 @@ int rlo_line_image(rlo_model* m, int iline, int ray_begin, int ray_end, double* 
         traj_free(&T);
     }
     if (counts) { counts[0] = L.steps; counts[1] = integ; counts[2] = nodes; }
+    m->maser = L.maser;
     free(velo); free(L.dnu); free(L.star); free(L.isrf);
     return rc;
 }
@@ -1331,6 +1335,7 @@ int rlo_ray_spectrum(rlo_model* m, int iline, double x0, double z0, double* I_ou
         rc = charint(&L, &T, k, 0.0, &minv, &maxv, &I_out[k - 1]);
         if (tau_out) tau_out[k - 1] = L.tau;
     }
+    m->maser |= L.maser;
     traj_free(&T);
     free(L.dnu); free(L.star);
     return rc;
@@ -1384,6 +1389,7 @@ int rlo_posvel(rlo_model* m, int iline, int nx, int ny, double szx, double szy, 
     if (!x0) return fail("out of memory");
     double *z0 = x0 + npix, *b = z0 + npix;
     int rc = rlo_pv_rays(m, nx, ny, szx, szy, phioff, xoff, yoff, addstar, x0, z0, b, info, dinfo);
+    m->maser = 0;
     double theta_saved = m->theta0;
     m->theta0 = dinfo[3];
     double rmax = RG(m, m->nr);
@@ -1437,6 +1443,8 @@ int rlo_image_to_spectrum(const rlo_model* m, const double* image, double* flux)
     }
     return 0;
 }
+
+int rlo_masing(const rlo_model* m) { return m->maser; }
 
 int rlo_line_spectrum(rlo_model* m, int iline, double* flux, double* velo_kms, long long* counts) {
     size_t n = (size_t)m->nrays * m->nfr;

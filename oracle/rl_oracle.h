@@ -23,6 +23,9 @@ int rlo_pv_rays(const rlo_model* m, int nx, int ny, double szx, double szy, doub
 int rlo_posvel(rlo_model* m, int iline, int nx, int ny, double szx, double szy, double phioff, double xoff,
                double yoff, int addstar, double* I, double* tau);
 int rlo_run_dir(const char* dir);
+/* 1 when the last line image, line spectrum or position-velocity cube met the masing
+   test of charintline (telescope.F:4291-4297) */
+int rlo_masing(const rlo_model* m);
 #ifdef __cplusplus
 }
 #endif

@@ -95,7 +95,7 @@ EXPORTS = ["rl_create", "rl_destroy", "rl_last_error", "rl_load_dir", "rl_load_a
            "rl_diff_batch_use_graph", "rl_diff_batch_buffers", "rl_diff_batch_layout", "rl_diff_batch_forward",
            "rl_diff_batch_backward",
            "rl_image_to_spectrum_noalloc", "rl_set_posvel", "rl_get_posvel", "rl_posvel",
-           "rl_line_image_mask", "rl_run_dir_ex", "rl_gen_spec_size", "rl_gen_spec",
+           "rl_line_image_mask", "rl_line_masing", "rl_run_dir_ex", "rl_gen_spec_size", "rl_gen_spec",
            "rl_model_checksum"]
 
 _lib = None
@@ -345,6 +345,13 @@ class Model:
         _check(lib().rl_line_image_mask(self.h, iline, _dp(img), msk.ctypes.data_as(C.POINTER(C.c_ubyte)),
                                         C.byref(st)), self._ch)
         return img, msk
+
+    def masing(self, iline: int) -> bool:
+        """Whether the last render of line `iline` met the reference's masing test (a line
+        opacity x segment length below -0.01, telescope.F:4291-4297)."""
+        d = C.c_int()
+        _check(lib().rl_line_masing(self.h, iline, C.byref(d)), self._ch)
+        return bool(d.value)
 
     def set_posvel(self, nx: int, ny: int, szimx: float, szimy: float, phioff: float = 0.0, xoff: float = 0.0,
                    yoff: float = 0.0, addstar: int = 1):

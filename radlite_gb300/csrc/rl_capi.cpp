@@ -85,6 +85,7 @@ int rl::build_line_tables(const Model& m, int iline0, int nl, LineTables<T>& out
   const bool isrf = m.outer_bc == 3;
   out.wch.assign((size_t)nl * nfr, (T)0); out.star.assign((size_t)(isrf ? 2 : 1) * nl * nfr, (T)0);
   out.velo.assign((size_t)nl * nfr, 0.0); out.scale.assign(nl, 1.0); out.lc.assign(nl, LineConst<T>{});
+  out.mase.assign(nl, 0);
   for (int l = 0; l < nl; l++) {
     LinePrep lp;
     if (prepare_line(m, iline0 + l, scaled, lp, err)) return RL_ERR_ARG;
@@ -107,6 +108,7 @@ int rl::build_line_tables(const Model& m, int iline0, int nl, LineTables<T>& out
     out.lc[l].istart = (T)lp.istart;
     out.lc[l].scale = lp.scale;
     out.scale[l] = lp.scale;
+    out.mase[l] = lp.mase;
   }
   return 0;
 }
@@ -176,11 +178,13 @@ static int run_lines(rl_model* md, int iline0, int nl, double* flux_out, double*
   const bool cached = md->tab_line0 == iline0 && md->tab_nl == nl && md->tab_prec == md->precision;
   LineTables<T> lt;
   std::vector<double> scale = md->tab_scale;
+  std::vector<char> mase = md->tab_mase;
   if (!cached) {
     md->tab_line0 = -1;
     std::string err;
     if (build_line_tables<T>(m, iline0, nl, lt, err)) return set_err(ctx, RL_ERR_ARG, err);
     scale = lt.scale;
+    mase = lt.mase;
   }
   const std::vector<T>&tab = lt.tab, &nsum = lt.nsum, &wch = lt.wch, &star = lt.star;
   const std::vector<double>& velo = lt.velo;
@@ -216,9 +220,12 @@ static int run_lines(rl_model* md, int iline0, int nl, double* flux_out, double*
   CUDA_TRY(cudaMemsetAsync(md->dcnt.p, 0, sizeof(unsigned long long) * 4, s));
   CUDA_TRY(cudaMemsetAsync(md->dwork.p, 0, sizeof(int), s));
   CUDA_TRY(cudaMemsetAsync(md->derr.p, 0, sizeof(int), s));
+  MaserFlags mf;
+  CUDA_TRY(mf.arm(md->dmaser, mase, iline0, s));
   CUDA_TRY(cudaEventRecord(ctx->ev[1], s));
   WalkParams<T> P;
   P.nb = node_view<T>(md);
+  P.maser = mf.dev;
   P.nth = m.nth; P.ncell = ncell; P.nlines = nl; P.nfr = nfr;
   int cpl = 4;
   {
@@ -252,7 +259,9 @@ static int run_lines(rl_model* md, int iline0, int nl, double* flux_out, double*
   int kerr = 0;
   CUDA_TRY(d2h(cnt, md->dcnt.p, sizeof(cnt), s));
   CUDA_TRY(d2h(&kerr, md->derr.p, sizeof(int), s));
+  CUDA_TRY(mf.fetch(s));
   CUDA_TRY(cudaStreamSynchronize(s));
+  mf.record(md->masing, m.lfreq.size());
   if (image_out) {
     std::vector<T> img(nimg);
     g_d2h += sizeof(T) * nimg;
@@ -265,6 +274,7 @@ static int run_lines(rl_model* md, int iline0, int nl, double* flux_out, double*
   }
   if (!cached) {
     md->tab_line0 = iline0; md->tab_nl = nl; md->tab_prec = md->precision; md->tab_scale = scale;
+    md->tab_mase = mase;
   }
   if (kerr != 0) return set_err(ctx, RL_ERR_GEOMETRY, "walk: error code " + std::to_string(kerr));
   if (st) {
@@ -539,6 +549,19 @@ static void run_log(const std::string& dir, bool start) {
   std::fclose(fp);
 }
 
+// The reference's warning after each line whose render found masing: calc_line_spectrum
+// writes it with (A35,I10) (telescope.F:1649-1652), calc_write_line_posvel list-directed
+// (telescope.F:2020-2023).
+static void warn_masing(const rl_model* md, int iline0, int nl, bool posvel) {
+  for (int l = 0; l < nl; l++) {
+    const size_t i = (size_t)iline0 - 1 + l;
+    if (i < md->masing.size() && md->masing[i])
+      std::printf("%s\n Will only warn once for this transition.\n",
+                  posvel ? " WARNING: Masing detected!" : "          WARNING: Masing detected!");
+  }
+  std::fflush(stdout);   // in order with the caller's own output
+}
+
 int rl_run_dir_ex(const char* dir, int device, int flags, rl_stats* st) {
   if (flags & ~RL_RUN_SAVE_IMCIR) return set_err(nullptr, RL_ERR_ARG, "rl_run_dir_ex: unknown flags");
   rl_ctx* ctx = nullptr;
@@ -547,8 +570,10 @@ int rl_run_dir_ex(const char* dir, int device, int flags, rl_stats* st) {
   rl_model* md = nullptr;
   rc = rl_load_dir(ctx, dir, &md);
   if (rc == 0) run_log(dir, true);
-  if (rc == 0 && md->m.command == 2 && md->m.pv.sizespec == 0)   // telescope.F:207-210
+  if (rc == 0 && md->m.command == 2 && md->m.pv.sizespec == 0) {   // telescope.F:207-210
     std::printf(" While reading linespectrum.inp:\n Size specifier in arcsec not yet implemented\n");
+    std::fflush(stdout);
+  }
   if (rc == 0 && md->m.command == 2) {
     // one lineposvel file per line (main.F:1061-1074); lines in chunks of at most 2 GB of
     // cube per array
@@ -565,6 +590,7 @@ int rl_run_dir_ex(const char* dir, int device, int flags, rl_stats* st) {
       I.resize(per_line * nl);
       tau.resize(per_line * nl);
       rc = dispatch_posvel(md, m.ilstart + l0, nl, I.data(), tau.data(), st);
+      if (rc == 0) warn_masing(md, m.ilstart + l0, nl, true);
       for (int l = 0; l < nl && rc == 0; l++) {
         const int iline = m.ilstart + l0 + l;
         const std::string name = posvel_file_name(m, iline);
@@ -598,6 +624,7 @@ int rl_run_dir_ex(const char* dir, int device, int flags, rl_stats* st) {
       if (sticky.empty()) sticky.assign(n, 0);
       rc = dispatch_lines(md, iline, 1, &flux[(size_t)l * m.nfr], img.data(), &one, mask.data());
       if (rc) break;
+      warn_masing(md, iline, 1, false);
       for (size_t i = 0; i < n; i++) sticky[i] |= mask[i];
       if (st) {
         st->steps += one.steps; st->integrated += one.integrated; st->node_visits += one.node_visits;
@@ -625,6 +652,7 @@ int rl_run_dir_ex(const char* dir, int device, int flags, rl_stats* st) {
     std::vector<double> flux((size_t)m.nlspec * m.nfr);
     if (st) std::memset(st, 0, sizeof *st);
     rc = dispatch_lines(md, m.ilstart, m.nlspec, flux.data(), nullptr, st);
+    if (rc == 0) warn_masing(md, m.ilstart, m.nlspec, false);
     if (rc == 0) {
       std::vector<int> lines;
       for (int i = 0; i < m.nlspec; i++) lines.push_back(m.ilstart + i);
@@ -642,6 +670,13 @@ int rl_run_dir_ex(const char* dir, int device, int flags, rl_stats* st) {
   rl_model_free(md);
   rl_destroy(ctx);
   return rc;
+}
+
+int rl_line_masing(rl_model* md, int iline, int* detected) {
+  if (!md || !detected) return set_err(nullptr, RL_ERR_ARG, "rl_line_masing: null argument");
+  if (iline < 1 || iline > (int)md->m.lfreq.size()) return set_err(md->ctx, RL_ERR_ARG, "rl_line_masing: line index out of range");
+  *detected = (size_t)iline <= md->masing.size() ? md->masing[(size_t)iline - 1] : 0;
+  return 0;
 }
 
 int rl_measure_peaks(rl_ctx* ctx, double* ffma_per_s, double* ex2_per_s) {

@@ -91,6 +91,8 @@ struct WalkParams {
   T* tau = nullptr;          // position-velocity walk only: [nlines][nrays][nfr] char_tau
   T* tauc = nullptr;         //   and its compensation term (same layout)
   unsigned char* mask = nullptr;  // optional [nlines][nrays][nfr]: 1 = channel 1 or inside the window
+  int* maser = nullptr;      // optional [nlines]: set to 1 where a step's line opacity x segment
+                             //   length falls below -0.01 (only launches with an inverted line)
   unsigned long long* counters;   // [0] steps, [1] integrated channels, [2] node visits
   int* work;                 // dynamic work counter
   int* err;                  // first error code

@@ -993,6 +993,7 @@ int prepare_line(const Model& m, int iline, bool scaled, LinePrep& lp, std::stri
     jf[c] = C1 * nup;
     af[c] = C2 * (ndn * lp.Bdu - nup * lp.Bud);
     lp.nsum[c] = nup + ndn;
+    if (af[c] < 0.0) lp.mase = true;
   }
   // start intensity at the outer boundary (telescope.F:3989-4028)
   double istart = 0.0;

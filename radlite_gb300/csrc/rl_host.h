@@ -80,6 +80,7 @@ struct LinePrep {
   double lfreq = 0.0, nu0 = 0.0, Bud = 0.0, Bdu = 0.0, scale = 1.0, istart = 0.0, cphi = 0.0;
   std::vector<double> dnu, velo, wch, star;    // [nfr]
   std::vector<double> isrf;                    // [nfr] outer-boundary start per channel (type 3), else empty
+  bool mase = false;                           // some cell has a negative line opacity (inversion)
   std::vector<double> tab;                     // [ncell][4] jfac/scale, afac, jd/scale, ad
   std::vector<double> nsum;                    // [ncell]
 };

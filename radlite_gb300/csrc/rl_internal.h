@@ -72,12 +72,40 @@ struct LineTables {
   std::vector<double> velo;  // [nl][nfr]
   std::vector<LineConst<T>> lc;
   std::vector<double> scale; // [nl]
+  std::vector<char> mase;    // [nl] the line has a population inversion somewhere
 };
 template <typename T>
 int build_line_tables(const Model& m, int iline0, int nl, LineTables<T>& out, std::string& err);
 
 // The per-channel start intensities inside a device copy of LineTables::star (outer
 // boundary 3), or null: the walk then starts every channel at LineConst::istart.
+// Masing flags of a launch over lines iline0.. (mase: which of them have an inversion):
+// cleared device flags when any has one, else null (the walk then skips the check).
+// record() stores the flags read back after the launch in rl_model::masing.
+struct MaserFlags {
+  int* dev = nullptr;
+  std::vector<int> host;
+  int iline0 = 1;
+  cudaError_t arm(rl::DevBuf& buf, const std::vector<char>& mase, int line0, cudaStream_t s) {
+    iline0 = line0;
+    host.assign(mase.size(), 0);
+    bool any = false;
+    for (char c : mase) any = any || c;
+    if (!any) { dev = nullptr; return cudaSuccess; }
+    cudaError_t e = buf.ensure(sizeof(int) * mase.size());
+    if (e != cudaSuccess) return e;
+    dev = static_cast<int*>(buf.p);
+    return cudaMemsetAsync(dev, 0, sizeof(int) * mase.size(), s);
+  }
+  cudaError_t fetch(cudaStream_t s) {
+    return dev ? cudaMemcpyAsync(host.data(), dev, sizeof(int) * host.size(), cudaMemcpyDeviceToHost, s) : cudaSuccess;
+  }
+  void record(std::vector<char>& masing, size_t nlines_mol) const {   // after the stream synchronised
+    if (masing.size() != nlines_mol) masing.assign(nlines_mol, 0);
+    for (size_t l = 0; l < host.size(); l++) masing[(size_t)iline0 - 1 + l] = host[l] != 0;
+  }
+};
+
 template <typename T>
 inline const T* isrf_of(const Model& m, const T* dstar, int nl, int nfr) {
   return m.outer_bc == 3 ? dstar + (size_t)nl * nfr : nullptr;
@@ -147,11 +175,15 @@ struct rl_model {
   // per-line tables of the last line range (reused while the range and precision match)
   int tab_line0 = -1, tab_nl = 0, tab_prec = -1;
   std::vector<double> tab_scale;
+  std::vector<char> tab_mase;
+  // masing found by the last render of each line of the molecule (spectrum or cube)
+  std::vector<char> masing;
   // position-velocity cube: the image request and its buffers
   rl::PVSpec pvspec;
   rl::PVBuffers pv;
   // per-call buffers
   rl::DevBuf dmask;   // circular-image integration mask (on request)
+  rl::DevBuf dmaser;  // per-line masing flags (launches with an inverted line)
   rl::DevBuf dtab, dnsum, dwch, dvelo, dstar, dlc, dimg, dring, dflux, dscale, dcnt, dwork, derr, dlist;
 };
 

@@ -155,6 +155,9 @@ static int run_posvel(rl_model* md, int iline0, int nl, double* I_out, double* t
   CUDA_TRY(h2d(B.pix.p, pix.data(), sizeof(int) * npix, s));
   LineTables<T> lt;
   if (build_line_tables<T>(m, iline0, nl, lt, err)) return set_err(ctx, RL_ERR_ARG, err);
+  MaserFlags mf;   // stays clear where no pixel ray crosses the grid
+  mf.iline0 = iline0;
+  mf.host.assign(nl, 0);
   CUDA_TRY(h2d(B.scale.p, lt.scale.data(), sizeof(double) * nl, s));
   if (ntr > 0) {
     const int kmax = rlg::max_nodes(m.nr, m.nth);
@@ -213,6 +216,8 @@ static int run_posvel(rl_model* md, int iline0, int nl, double* I_out, double* t
     P.work = md->dwork.as<int>();
     P.err = md->derr.as<int>();
     P.list = md->dlist.as<unsigned short>();
+    CUDA_TRY(mf.arm(md->dmaser, lt.mase, iline0, s));
+    P.maser = mf.dev;
     CUDA_TRY(launch_walk_pv<T>(P, cpl, ctx->nsm, s));
     CUDA_TRY(cudaEventRecord(ctx->ev[3], s));
   } else {
@@ -233,8 +238,10 @@ static int run_posvel(rl_model* md, int iline0, int nl, double* I_out, double* t
   if (ntr > 0) {
     CUDA_TRY(d2h(cnt, md->dcnt.p, sizeof(cnt), s));
     CUDA_TRY(d2h(&kerr, md->derr.p, sizeof(int), s));
+    CUDA_TRY(mf.fetch(s));
   }
   CUDA_TRY(cudaStreamSynchronize(s));
+  mf.record(md->masing, m.lfreq.size());
   if (kerr != 0) return set_err(ctx, RL_ERR_GEOMETRY, "position-velocity walk: error code " + std::to_string(kerr));
   if (I_out) {
     g_d2h += sizeof(double) * ncube;

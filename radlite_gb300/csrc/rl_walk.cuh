@@ -70,6 +70,7 @@ __device__ long long walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState
     }
   }
   long long steps = 0;
+  unsigned mbits = 0;   // tile lines whose line opacity x segment length fell below -0.01
   T lw_last = 0;
   for (int kb = 0; kb < K; kb += 32) {
     if (kb > 0) {   // carry the last node of the previous chunk into entry 0
@@ -267,6 +268,15 @@ __device__ long long walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState
             if constexpr (PV) kahan_add(tau[u], tcp[u], o.dtau);
           }
         }
+        if (P.maser) {
+          // masing check of charintline (telescope.F:4291-4297): the line opacity at the
+          // segment end (the next step's alpl0) times the segment length. Warp-uniform:
+          // only launches holding a line with a population inversion take it.
+          const T dsm = S.ds[n + 1];
+#pragma unroll
+          for (int u = 0; u < kPass; u++)
+            if (Ls[u] >= 0 && S.lv[Ls[u]][n + 1].af * profile(w[u], vl1, rl, rl) * dsm < (T)-0.01) mbits |= 1u << Ls[u];
+        }
       }
 #pragma unroll
       for (int u = 0; u < kPass; u++) {
@@ -278,6 +288,11 @@ __device__ long long walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState
       }
     }
     __syncwarp();
+  }
+  if (P.maser) {
+    mbits = __reduce_or_sync(0xffffffffu, mbits);
+    if (lane == 0)
+      for (; mbits; mbits &= mbits - 1) atomicExch(&P.maser[l0 + __ffs(mbits) - 1], 1);
   }
   return steps;
 }
