@@ -695,7 +695,7 @@ struct Hasher {
   }
 };
 
-constexpr char kCacheMagic[8] = {'R', 'L', 'G', 'P', 'U', 'I', 'N', '3'};
+constexpr char kCacheMagic[8] = {'R', 'L', 'G', 'P', 'U', 'I', 'N', '4'};
 
 std::string cache_path(const std::string& cache_dir, const std::string& key) {
   Hasher h;
