@@ -94,3 +94,14 @@ def test_run_dir_prints_the_warning(gpu_lib, tmp_path, capfd):
     _, d0 = inverted_model(tmp_path, "run0", None, 0)
     gpu_lib.run_dir(d0)
     assert "Masing" not in capfd.readouterr().out
+
+
+def test_masing_query_arguments(gpu_lib, tmp_path):
+    """Host only: before any render no line is flagged; bad line indices are errors."""
+    cfg, d = inverted_model(tmp_path, "m", 1.001, 22)
+    m = gpu_lib.load_dir_host(d)
+    assert m.masing(cfg.ilinestart) is False
+    for bad in (0, 10 ** 6):
+        with pytest.raises(gpu_lib.RLError, match="line index"):
+            m.masing(bad)
+    m.free()
