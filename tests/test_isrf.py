@@ -95,6 +95,16 @@ def test_readers_reject_bad_field_file(oracle_lib, gpu_lib, tmp_path, damage):
         gpu_lib.load_dir_host(d)
 
 
+def test_oracle_rejects_channels_above_the_table(oracle_lib, tmp_path):
+    """Line 4 of the rotor lies above the dust frequencies (they cover lines 1-3): the
+    reference would interpolate past the end of its table, the oracle stops."""
+    cfg, d = write(tmp_path, "m", outer_bc=3)
+    o = oracle_lib.Oracle(d)
+    o.line_spectrum(cfg.ilinestart)
+    with pytest.raises(Exception, match="above the last frequency"):
+        o.line_spectrum(cfg.ilinestart + 1)
+
+
 def test_host_reader_takes_field(gpu_lib, tmp_path):
     _, d3 = write(tmp_path, "bc3", outer_bc=3)
     _, d0 = write(tmp_path, "bc0")
@@ -134,6 +144,18 @@ def test_gpu_field_spectra_match_oracle(gpu_lib, oracle_lib, tmp_path):
         got.append(mm.calc_line_spectrum(c.ilinestart)[0])
         mm.free()
     assert np.array_equal(got[0], got[1])
+    ctx.close()
+
+
+@pytest.mark.gpu
+def test_gpu_rejects_channels_above_the_table(gpu_lib, tmp_path):
+    cfg, d = write(tmp_path, "m", outer_bc=3)
+    ctx = gpu_lib.Context(0)
+    m = ctx.load_dir(d)
+    m.calc_line_spectrum(cfg.ilinestart)
+    with pytest.raises(gpu_lib.RLError, match="above the last frequency"):
+        m.calc_line_spectrum(cfg.ilinestart + 1)
+    m.free()
     ctx.close()
 
 
