@@ -10,6 +10,7 @@
 //   dusttemp.info/_final.dat setup.F:159-235, 295-420
 //   dustopac.inp, dustopac_N.inp dust.F:92-447  frequency.inp  grid.F:1427-1482
 //   starinfo.inp       star.F:543-569           starspectrum.inp / starspec.inp star.F:449-537
+//   interstellfield.inp star.F:690-727 (outer boundary 3)
 //   scatsource.dat     source.F:494-543         line.inp header line.F:142-200, 3918-3935
 //   linespectrum.inp   telescope.F:86-257       moldata.dat    line.F:1826-1985 (fixed columns)
 //   levelpop.info + levelpop_<mol>.dat line.F:811-950
