@@ -77,18 +77,18 @@ int rl::upload_grid(rl_model* md) {
 }
 
 template <typename T>
-int rl::build_line_tables(const Model& m, int iline0, int nl, LineTables<T>& out, std::string& err) {
+int rl::build_line_tables(const Model& m, int iline0, int nl, LineTables<T>& out, std::string& err, bool with_isrf) {
   const int ncell = m.ncell(), nfr = m.nfr;
   const bool scaled = std::is_same<T, float>::value;
   out.nl = nl; out.ncell = ncell; out.nfr = nfr;
   out.tab.assign((size_t)nl * ncell * 4, (T)0); out.nsum.assign((size_t)nl * ncell, (T)0);
-  const bool isrf = m.outer_bc == 3;
+  const bool isrf = m.outer_bc == 3 && with_isrf;
   out.wch.assign((size_t)nl * nfr, (T)0); out.star.assign((size_t)(isrf ? 2 : 1) * nl * nfr, (T)0);
   out.velo.assign((size_t)nl * nfr, 0.0); out.scale.assign(nl, 1.0); out.lc.assign(nl, LineConst<T>{});
   out.mase.assign(nl, 0);
   for (int l = 0; l < nl; l++) {
     LinePrep lp;
-    if (prepare_line(m, iline0 + l, scaled, lp, err)) return RL_ERR_ARG;
+    if (prepare_line(m, iline0 + l, scaled, lp, err, with_isrf)) return RL_ERR_ARG;
     // cell-major, line-minor: the corners of one node for consecutive lines are contiguous.
     // The line factors carry the profile normalisation (phi = cphi / lwav * e^{-u^2}).
     for (int c = 0; c < ncell; c++) {
@@ -112,8 +112,8 @@ int rl::build_line_tables(const Model& m, int iline0, int nl, LineTables<T>& out
   }
   return 0;
 }
-template int rl::build_line_tables<float>(const Model&, int, int, LineTables<float>&, std::string&);
-template int rl::build_line_tables<double>(const Model&, int, int, LineTables<double>&, std::string&);
+template int rl::build_line_tables<float>(const Model&, int, int, LineTables<float>&, std::string&, bool);
+template int rl::build_line_tables<double>(const Model&, int, int, LineTables<double>&, std::string&, bool);
 
 template <typename T>
 static int build_geometry(rl_model* md, rl_stats* st) {

@@ -909,7 +909,7 @@ int setup_pv_camera(const Model& m, const PVSpec& spec, double incl, PVCamera& c
   return 0;
 }
 
-int prepare_line(const Model& m, int iline, bool scaled, LinePrep& lp, std::string& err) {
+int prepare_line(const Model& m, int iline, bool scaled, LinePrep& lp, std::string& err, bool with_isrf) {
   if (iline < 1 || iline > (int)m.lfreq.size()) { err = "line index out of range"; return -1; }
   const int il = iline - 1, ncell = m.ncell(), nfr = m.nfr;
   lp.lfreq = m.lfreq[il];
@@ -937,7 +937,7 @@ int prepare_line(const Model& m, int iline, bool scaled, LinePrep& lp, std::stri
   // channel whose bracket index equals the channel count (freq_nr), not the frequency count;
   // above the last frequency (other than that) the reference reads past its table.
   lp.isrf.clear();
-  if (m.outer_bc == 3) {
+  if (m.outer_bc == 3 && with_isrf) {
     lp.isrf.resize(nfr);
     for (int k = 0; k < nfr; k++) {
       const double fq = lp.nu0 + lp.dnu[k];

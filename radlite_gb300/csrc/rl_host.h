@@ -91,7 +91,9 @@ int load_dir(const std::string& dir, Model& m, std::string& err);
 unsigned long long model_checksum(const Model& m);
 int setup_camera(const Model& m, double incl_rad, int nphi, int dbdr, int nrext, Camera& cam, std::string& err);
 int setup_pv_camera(const Model& m, const PVSpec& spec, double incl_rad, PVCamera& cam, std::string& err);
-int prepare_line(const Model& m, int iline, bool scaled, LinePrep& lp, std::string& err);
+// with_isrf: build the outer-boundary-3 start table (spectra); the position-velocity path
+// never fills it in the reference (calc_write_line_posvel, telescope.F:1828-1924)
+int prepare_line(const Model& m, int iline, bool scaled, LinePrep& lp, std::string& err, bool with_isrf = true);
 double bplanck(double temp, double nu);                     // setup.F:937-952
 int bracket(const std::vector<double>& xx, double x);      // 1-based j with xx[j-1] < x <= xx[j]
 void finish_model(Model& m);   // derived quantities (aksmax, passband channel count)

@@ -75,7 +75,8 @@ struct LineTables {
   std::vector<char> mase;    // [nl] the line has a population inversion somewhere
 };
 template <typename T>
-int build_line_tables(const Model& m, int iline0, int nl, LineTables<T>& out, std::string& err);
+int build_line_tables(const Model& m, int iline0, int nl, LineTables<T>& out, std::string& err,
+                      bool with_isrf = true);
 
 // The per-channel start intensities inside a device copy of LineTables::star (outer
 // boundary 3), or null: the walk then starts every channel at LineConst::istart.

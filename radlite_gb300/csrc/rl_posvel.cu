@@ -154,7 +154,7 @@ static int run_posvel(rl_model* md, int iline0, int nl, double* I_out, double* t
   CUDA_TRY(cudaEventRecord(ctx->ev[0], s));
   CUDA_TRY(h2d(B.pix.p, pix.data(), sizeof(int) * npix, s));
   LineTables<T> lt;
-  if (build_line_tables<T>(m, iline0, nl, lt, err)) return set_err(ctx, RL_ERR_ARG, err);
+  if (build_line_tables<T>(m, iline0, nl, lt, err, false)) return set_err(ctx, RL_ERR_ARG, err);
   MaserFlags mf;   // stays clear where no pixel ray crosses the grid
   mf.iline0 = iline0;
   mf.host.assign(nl, 0);

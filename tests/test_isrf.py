@@ -105,6 +105,17 @@ def test_oracle_rejects_channels_above_the_table(oracle_lib, tmp_path):
         o.line_spectrum(cfg.ilinestart + 1)
 
 
+def test_oracle_posvel_needs_no_field_table(oracle_lib, tmp_path):
+    """The position-velocity path never builds the field table, so a line above the
+    frequency table renders there (and starts from zeros) where a spectrum stops."""
+    cfg, d3 = write(tmp_path, "bc3", outer_bc=3)
+    _, d0 = write(tmp_path, "bc0")
+    size = 2.0 * float(synth.make_grid(cfg)[0][-1])
+    i3, t3 = oracle_lib.Oracle(d3).posvel(cfg.ilinestart + 1, 6, 6, size, size, addstar=1)
+    i0, t0 = oracle_lib.Oracle(d0).posvel(cfg.ilinestart + 1, 6, 6, size, size, addstar=1)
+    assert np.array_equal(i3, i0) and np.array_equal(t3, t0)
+
+
 def test_host_reader_takes_field(gpu_lib, tmp_path):
     _, d3 = write(tmp_path, "bc3", outer_bc=3)
     _, d0 = write(tmp_path, "bc0")
@@ -190,6 +201,15 @@ def test_gpu_posvel_ignores_field(gpu_lib, tmp_path):
         m.free()
         ctx.close()
     assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+    # a line above the frequency table: no field table, so the cube renders
+    cfg, d = write(tmp_path, "pv_above", outer_bc=3)
+    ctx = gpu_lib.Context(0)
+    m = ctx.load_dir(d)
+    size = 2.0 * float(synth.make_grid(cfg)[0][-1])
+    m.set_posvel(8, 8, size, size, addstar=1)
+    m.posvel(cfg.ilinestart + 1, 1)
+    m.free()
+    ctx.close()
 
 
 @pytest.mark.gpu
