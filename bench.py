@@ -48,6 +48,9 @@ INCLS = (20.0, 60.0)
 # extinction, optical depth, exponential coefficients, bracket, intensity update)
 BUDGET_FP32 = 19
 BUDGET_MUFU = 3
+CONFIG = {"workload": "band_large: 400x200 disk (+-10% lognormal T, rho), 20 band lines x 200 channels, "
+                      "1000x256+1 rays, incl 20+60 deg",
+          "l2": "inputs larger than L2 (node records ~10 GB per inclination)"}
 
 
 def workload():
@@ -104,39 +107,46 @@ class Clocks:
 
 
 # ------------------------------------------------------------------------------------
-# CPU side: the oracle on a bounded sample (one process per core)
+# CPU side: the oracle on a bounded ray sample (one process per core), also the checker
 # ------------------------------------------------------------------------------------
-def _cpu_worker(args):
-    d, iline, rays = args
-    from oracle import pyoracle
-    o = pyoracle.Oracle(d)
-    t0 = time.perf_counter()
-    n = 0
-    for r in rays:
-        o.line_image(iline, int(r), int(r) + 1)
-        n += o.nfr
-    return n, time.perf_counter() - t0
-
-
-def cpu_sample(cfg, stride, procs, tmpdir):
+def model_dirs(tmp):
+    """The band workload written in the reference's file formats, one directory per
+    inclination (the oracle's input, and the GPU model's for the timing and the parity)."""
     from radlite_gb300 import synth
-    import numpy as np
-    d = os.path.join(tmpdir, "band_large_i20")
-    if not os.path.exists(os.path.join(d, "radlite.inp")):
-        synth.write_model(synth.config_by_name("band_large", incl_deg=INCLS[0]), d)
-    from oracle import pyoracle
-    pyoracle.build()
-    nrays = 1 + (abs(cfg.nrrextra) + 10 + cfg.dbdr * (cfg.nr - 1)) * cfg.nphi
-    rays = np.arange(0, nrays, stride)
-    parts = [(d, cfg.ilinestart, rays[i::procs]) for i in range(procs)]
-    ctx = mp.get_context("spawn")
-    with ctx.Pool(procs) as pool:
-        t0 = time.perf_counter()
-        res = pool.map(_cpu_worker, parts)
-        wall = time.perf_counter() - t0
-    n = sum(r[0] for r in res)
-    busy = max(r[1] for r in res)
-    return {"ray_channels": n, "rays": len(rays), "compute_s": busy, "wall_s": wall, "value": n / busy}
+    dirs = {}
+    for inc in INCLS:
+        d = os.path.join(tmp, f"band_large_i{inc:.0f}")
+        if not os.path.exists(os.path.join(d, "radlite.inp")):
+            synth.write_model(synth.config_by_name("band_large", incl_deg=inc), d)
+        dirs[inc] = d
+    return dirs
+
+
+def n_rays(cfg):
+    return 1 + (abs(cfg.nrrextra) + 10 + cfg.dbdr * (cfg.nr - 1)) * cfg.nphi
+
+
+def oracle_sample(pool, dirs, cfg, stride, offset=0):
+    """The oracle's image rows of every stride-th ray (from `offset`) of every line at every
+    inclination: the ray-channels/s of that sample on the pool's host processes, and the
+    rows themselves (per inclination, [nlines, nsel, nfr])."""
+    from oracle import sample
+    rays = sample.ray_sample(n_rays(cfg), stride, offset)
+    lines = range(cfg.ilinestart, cfg.ilinestart + cfg.nlines)
+    nfr = int(2.0 * cfg.vmax / cfg.dv + 1)
+    rows, compute = {}, 0.0
+    for inc, d in dirs.items():
+        r, _, comp, _ = pool.rows(d, lines, rays)
+        rows[inc] = r
+        compute += comp
+    n = len(rays) * nfr * cfg.nlines * len(dirs)
+    return rays, rows, {"ray_channels": n, "rays": len(rays), "compute_s": compute, "value": n / compute}
+
+
+def sample_text(cfg, stride, nsel, offset=0):
+    first = f" from ray {offset % stride}" if offset % stride else ""
+    return (f"every {stride}th ray{first} ({nsel} rays x {int(2.0 * cfg.vmax / cfg.dv + 1)} channels) of all "
+            f"{cfg.nlines} lines at both inclinations ({'+'.join(f'{i:.0f}' for i in INCLS)} deg)")
 
 
 def cpu_model() -> str:
@@ -180,26 +190,27 @@ def reference_arm(args):
     world, rank, _, dist = dist_setup()
     if rank != 0:
         return 0
+    from oracle import sample
     cfg, _ = workload()
     procs = os.cpu_count() or 1
-    stride = args.cpu_stride
-    with tempfile.TemporaryDirectory() as tmp:
+    stride = args.ref_stride
+    with tempfile.TemporaryDirectory() as tmp, sample.OraclePool(procs) as pool:
+        dirs = model_dirs(tmp)
         vals = []
         for i in range(args.warmup + args.steps):
-            s = cpu_sample(cfg, stride, procs, tmp)
+            _, _, st = oracle_sample(pool, dirs, cfg, stride, offset=i)
             if i >= args.warmup:
-                vals.append(s)
+                vals.append(st)
     v = statistics.median(x["value"] for x in vals)
     ms = statistics.median(x["compute_s"] for x in vals) * 1e3
-    sample = (f"band_large line {cfg.ilinestart} (of 20), incl {INCLS[0]:.0f} deg, every {stride}th ray "
-              f"({vals[0]['rays']} rays x 200 channels) per step")
+    smp = (sample_text(cfg, stride, vals[0]["rays"]) + "; step i starts at ray i, so successive steps render "
+           "different rays")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator in the reference file formats)",
-            "config": {"workload": "band_large: 400x200 disk, 20 band lines x 200 channels, 1000x256 rays, "
-                                   "incl 20+60 deg (bounded CPU sample)"},
+            "config": CONFIG,
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": procs, "cpu": cpu_model(), "kind": "port",
-                             "sample": sample},
+                             "sample": smp},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "the reference Fortran cannot be compiled on this image (no Fortran compiler); timed is the "
                     "FP64 C restatement of its raytrace (oracle/), one process per host core"}
@@ -224,14 +235,94 @@ def load_measured():
         return {}
 
 
+def parity_case(ctx, dirs, cfg, rays, ora, stride):
+    """GPU image rows of the oracle's ray sample (same model directories, same rays, FP32
+    transfer) against the oracle's: per spectrum (line, inclination) the sample-spectrum
+    error in every channel above 1e-3 of its peak and the pixel error (oracle/sample.py)."""
+    from oracle import pyoracle, sample
+    per_spec, per_pix, checked, names = [], [], [], []
+    for inc, d in dirs.items():
+        _, _, _, ri = pyoracle.Oracle(d).rays()
+        m = ctx.load_dir(d)
+        _, rows = m.image_rows(cfg.ilinestart, cfg.nlines, rays)
+        m.free()
+        c = sample.compare(rows, ora[inc], rays, ri, cfg.nphi)
+        per_spec += c["spectrum_rel_err"]
+        per_pix += c["pixel_rel_err"]
+        checked += c["channels_checked"]
+        names += [f"line {cfg.ilinestart + k} incl {inc:.0f}" for k in range(cfg.nlines)]
+    return {"criterion": "relative error in every channel above 1e-3 of the peak <= 1e-4 (sample spectrum: the "
+                         "image->F_nu sum over the sampled rays), GPU FP32 transfer vs FP64 oracle",
+            "sample": sample_text(cfg, stride, len(rays)), "spectra": len(per_spec), "spectrum_names": names,
+            "max_spectrum_rel_err": max(per_spec), "per_spectrum_rel_err": per_spec,
+            "max_pixel_rel_err": max(per_pix), "per_spectrum_pixel_rel_err": per_pix,
+            "channels_checked": checked, "channels_checked_total": int(sum(checked)),
+            "pass": bool(max(per_spec) <= 1e-4)}
+
+
+def disk_line_case(ctx, pool, tmp, steps):
+    """The plain single-model configuration: the 100x60 disk, line J=3-2 x 64 channels,
+    400 rings x 128 azimuths + the central beam, incl 45 deg. Device and end-to-end
+    ray-channels/s, and the full spectrum against the oracle's (all 51,201 rays rendered by
+    the host pool and summed by the oracle), FP32 and FP64 transfer."""
+    import numpy as np
+    from radlite_gb300 import synth
+    from oracle import pyoracle, sample
+    cfg = synth.config_by_name("disk_line")
+    d = os.path.join(tmp, "disk_line")
+    synth.write_model(cfg, d)
+    il = cfg.ilinestart
+    m = ctx.load_dir(d)
+    for _ in range(3):
+        m.set_camera(cfg.incl_deg, cfg.nphi, cfg.dbdr, cfg.nrrextra)
+        m.spectra(il, 1)
+    dev = []
+    for _ in range(max(1, steps)):
+        m.set_camera(cfg.incl_deg, cfg.nphi, cfg.dbdr, cfg.nrrextra)
+        f32, st = m.spectra(il, 1, stats=True)
+        dev.append(st["geometry_ms"] + st["upload_ms"] + st["walk_ms"] + st["reduce_ms"])
+    rc = st["ray_channels"]
+    arr = synth.model_arrays(cfg)
+    e2e = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        m2 = ctx.load_arrays(arr, camera(cfg, cfg.incl_deg))
+        m2.spectra(il, 1)
+        e2e.append(time.perf_counter() - t0)
+        m2.free()
+    o = pyoracle.Oracle(d)
+    rows, counts, comp, _ = pool.rows(d, [il], np.arange(o.nrays))
+    ref = o.image_to_spectrum(rows[0])
+    m.set_precision(1)
+    f64, st64 = m.spectra(il, 1, stats=True)
+    m.free()
+    ms = statistics.median(dev)
+    return {"workload": f"disk_line: {cfg.nr}x{cfg.nt} disk, line {il} (J=3-2) x {st['nfr']} channels, "
+                        f"{st['nrays']} rays, incl {cfg.incl_deg:.0f} deg",
+            "ms_per_step": ms, "value": rc / (ms * 1e-3), "unit": UNIT, "spectra_per_s": 1.0 / (ms * 1e-3),
+            "e2e": {"value": rc / statistics.median(e2e), "unit": UNIT},
+            "parity": {"fp32_rel_err": sample.spectrum_relerr(f32[0], ref),
+                       "fp64_rel_err": sample.spectrum_relerr(f64[0], ref),
+                       "fp64_integrated_equal": bool(st64["integrated"] == counts[1]),
+                       "fp64_steps": int(st64["steps"]), "oracle_steps": int(counts[0]),
+                       "criterion": "full spectrum, every channel above 1e-3 of the peak"},
+            "cpu_baseline": {"value": rc / comp, "unit": UNIT, "cores": pool.procs, "kind": "port",
+                             "sample": "every ray and channel (the whole configuration)"}}
+
+
 def ours(args):
     import numpy as np
     import radlite_gb300 as rl
+    from oracle import sample
     world, rank, local, dist = dist_setup()
     cfg, arr = workload()
+    tmpd = tempfile.TemporaryDirectory()
+    dirs = model_dirs(tmpd.name)
+    # the checker's host processes (spawn) start before the first CUDA call
+    pool = sample.OraclePool() if rank == 0 and not args.no_cpu else None
     ctx = rl.Context(local)
     peaks = ctx.measure_peaks()
-    m = ctx.load_arrays(arr, camera(cfg, INCLS[0]))
+    m = ctx.load_dir(dirs[INCLS[0]])
 
     def step(model):
         st_all = []
@@ -258,7 +349,7 @@ def ours(args):
             integ = sum(s["integrated"] for s in sts)
     wall = (time.perf_counter() - t0) / args.steps
     ms = max_over_ranks(sum(dev_ms) / len(dev_ms), dist)
-    nrays = 1 + (abs(cfg.nrrextra) + 10 + cfg.dbdr * (cfg.nr - 1)) * cfg.nphi
+    nrays = n_rays(cfg)
     nfr = int(2.0 * cfg.vmax / cfg.dv + 1)
     rc_per_step = nrays * nfr * cfg.nlines * len(INCLS)
     value = world * rc_per_step / (ms * 1e-3)
@@ -300,32 +391,31 @@ def ours(args):
         batched = batched_case(ctx, args.batch_models, 2)
     if rank == 0 and not args.no_diff:
         adjoint = adjoint_case(ctx)
-        fitting = fit_case(ctx, args.fit_models, 3)
+        fitting = fit_case(ctx, args.fit_models, args.fit_steps)
     out = None
     if rank == 0:
-        cpu = None
+        cpu = parity = disk = None
         extras = {}
-        with tempfile.TemporaryDirectory() as tmp:
-            if not args.no_cpu:
-                s = cpu_sample(cfg, args.cpu_stride, os.cpu_count() or 1, tmp)
-                cpu = {"value": s["value"], "unit": UNIT, "cores": os.cpu_count() or 1, "cpu": cpu_model(), "kind": "port",
-                       "sample": f"band_large line {cfg.ilinestart}, incl {INCLS[0]:.0f} deg, every "
-                                 f"{args.cpu_stride}th ray ({s['rays']} rays x {nfr} channels), FP64 C restatement, "
-                                 f"one process per core"}
-            if not args.no_extras:
-                extras = extras_case(ctx, cfg, arr, tmp, with_cpu=not args.no_cpu)
+        if pool is not None:
+            rays, ora, s = oracle_sample(pool, dirs, cfg, args.cpu_stride)
+            cpu = {"value": s["value"], "unit": UNIT, "cores": pool.procs, "cpu": cpu_model(), "kind": "port",
+                   "sample": sample_text(cfg, args.cpu_stride, s["rays"]) + ", FP64 C restatement, one process per core"}
+            parity = parity_case(ctx, dirs, cfg, rays, ora, args.cpu_stride)
+            del ora
+            disk = disk_line_case(ctx, pool, tmpd.name, args.steps)
+        if not args.no_extras:
+            extras = extras_case(ctx, cfg, arr, dirs[INCLS[0]], tmpd.name, with_cpu=not args.no_cpu)
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": ms, "wall_ms_per_step": wall * 1e3,
                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32 (fp64 geometry)",
                "data": "synthetic (seeded generator in the reference file formats)",
-               "config": {"workload": "band_large: 400x200 disk (+-10% lognormal T, rho), 20 band lines x 200 "
-                                      "channels, 1000x256+1 rays, incl 20+60 deg",
-                          "l2": "inputs larger than L2 (node records ~10 GB per inclination)",
-                          "ray_channels_per_step": rc_per_step, "spectra_per_step": cfg.nlines * len(INCLS)},
+               "config": CONFIG, "ray_channels_per_step": rc_per_step, "spectra_per_step": cfg.nlines * len(INCLS),
                "spectra_per_s": spectra_s,
                "formal_solution_steps_per_step": steps_fs, "integrated_ray_channels_per_step": integ,
                "rel_err_fp32_vs_fp64": rel,
-               "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+               "parity": parity,
+               "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                       "path": "rl_load_arrays from host arrays + rl_spectra per inclination, wall clock"},
                "roofline": {"bound": "mufu_issue" if bound_mufu else "fp32_issue", "achieved": achieved / 1e12,
                             "peak": peak / 1e12, "unit": "Tops/s", "frac": achieved / peak, "traffic": traffic,
                             "kernel": "k_walk<float>", "walk_ms_per_step": wk * 1e3,
@@ -334,6 +424,7 @@ def ours(args):
                             "hbm_side": {"traffic_gb_per_s": traffic_gbs, "peak_gb_per_s": hbm_peak,
                                          "frac_of_measured": (traffic_gbs / hbm_peak
                                                               if traffic_gbs and hbm_peak else None)}},
+               "disk_line": disk,
                "batched": batched,
                "adjoint": adjoint,
                "fit": fitting,
@@ -344,11 +435,14 @@ def ours(args):
                "clocks": clk.summary(),
                "gpu_launches": args.steps * len(INCLS) * 4}
         print(json.dumps(out), flush=True)
+    if pool is not None:
+        pool.close()
     ctx.close()
+    tmpd.cleanup()
     return 0
 
 
-def extras_case(ctx, cfg, arr, tmp, with_cpu=True):
+def extras_case(ctx, cfg, arr, d, tmp, with_cpu=True):
     """The rows beside the raytrace: the position-velocity cube of the band_large disk, the
     spectrum post-processing of a 2000-line band, and the input parsing of the band_large
     directory (text and binary cache). Each with its CPU counterpart where it has one."""
@@ -376,12 +470,8 @@ def extras_case(ctx, cfg, arr, tmp, with_cpu=True):
           "geometry_ms": st["geometry_ms"], "ray_channels_per_s": st["ray_channels"] / (dev_ms * 1e-3),
           "e2e_ray_channels_per_s": st["ray_channels"] / wall, "d2h_bytes": st["d2h_bytes"]}
     m.free()
-    d = os.path.join(tmp, "band_large_i20")
     if with_cpu:
         from oracle import pyoracle
-        if not os.path.exists(os.path.join(d, "radlite.inp")):
-            synth.write_model(synth.config_by_name("band_large", incl_deg=INCLS[0]), d)
-        pyoracle.build()
         o = pyoracle.Oracle(d)
         x0, z0, b, _ = o.pv_rays(npx, npx, size, size, 0.0, 0.0, 0.0, 1)
         inside = np.flatnonzero(b < 0.999 * float(arr["r"][-1]))
@@ -420,8 +510,6 @@ def extras_case(ctx, cfg, arr, tmp, with_cpu=True):
         g["max_rel_diff_vs_cpu"] = float(np.max(np.abs(o2["spectrum"] - ref["spectrum"]) / np.abs(ref["spectrum"]).max()))
     out["genspec"] = g
     # input parsing of the band_large directory: text, then the binary cache
-    if not os.path.exists(os.path.join(d, "radlite.inp")):
-        synth.write_model(synth.config_by_name("band_large", incl_deg=INCLS[0]), d)
     t0 = time.perf_counter()
     rl.load_dir_host(d).free()
     text_s = time.perf_counter() - t0
@@ -587,7 +675,7 @@ def profile_case(args):
         m.free()
         ctx.close()
         return 0
-    cfg = synth.config_by_name(args.workload)
+    cfg = synth.config_by_name(args.workload, **({"nphi": args.nphi} if args.nphi else {}))
     arr = synth.model_arrays(cfg)
     ctx = rl.Context(0)
     m = ctx.load_arrays(arr, camera(cfg, cfg.incl_deg))
@@ -607,14 +695,19 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-stride", type=int, default=16)
+    ap.add_argument("--cpu-stride", type=int, default=32,
+                    help="ray stride of the oracle sample (CPU baseline and parity): all lines, both inclinations")
+    ap.add_argument("--ref-stride", type=int, default=509,
+                    help="ray stride of each step of --impl reference (all lines, both inclinations)")
+    ap.add_argument("--fit-steps", type=int, default=3, help="Adam steps of the fitting measurement")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-verify", action="store_true")
     ap.add_argument("--batch-models", type=int, default=256,
                     help="models of the uneven batched comparison (0 skips it)")
     ap.add_argument("--only-batch", action="store_true", help="run only the batched comparison")
     ap.add_argument("--only-adjoint", action="store_true", help="run only the forward+adjoint timing")
-    ap.add_argument("--nphi", type=int, default=0, help="azimuths of the adjoint timing (0: the workload's)")
+    ap.add_argument("--nphi", type=int, default=0,
+                    help="azimuths of the adjoint timing and of --profile (0: the workload's)")
     ap.add_argument("--only-fit", action="store_true", help="run only the batched fitting-step comparison")
     ap.add_argument("--fit-models", type=int, default=64)
     ap.add_argument("--no-diff", action="store_true", help="skip the adjoint and fitting measurements")

@@ -117,6 +117,14 @@ int rl_spectra(rl_model* model, int iline0, int nlines, double* flux_out, rl_sta
 /* Circular image of one line: [nrays][nfr] intensities (ray 0 = central beam, then
    rings from the inside out, azimuth fastest), as imcir_int. */
 int rl_line_image(rl_model* model, int iline, double* image_out, rl_stats* stats);
+/* Lines iline0 .. iline0+nlines-1 in one launch, as rl_spectra (flux_out [nlines][nfr],
+   may be NULL), also returning the image rows of `nsel` chosen rays: rows_out
+   [nlines][nsel][nfr] holds imcir_int(:, iphi, iring) of rays[i] (ray numbering of
+   rl_line_image), gathered on the device. A ray sample of the circular image of
+   telescope.F:339-631 without reading back the whole image; ray indices outside the
+   camera are rejected. */
+int rl_image_rows(rl_model* model, int iline0, int nlines, int nsel, const int* rays, double* flux_out,
+                  double* rows_out, rl_stats* stats);
 /* The same image and its integration mask [nrays][nfr]: 1 where the channel was integrated
    as channel 1 or inside the ray's velocity window (imcir_cmask, telescope.F:548,575), 0
    where it holds the ray's continuum. */

@@ -95,7 +95,7 @@ EXPORTS = ["rl_create", "rl_destroy", "rl_last_error", "rl_load_dir", "rl_load_a
            "rl_diff_batch_use_graph", "rl_diff_batch_buffers", "rl_diff_batch_layout", "rl_diff_batch_forward",
            "rl_diff_batch_backward",
            "rl_image_to_spectrum_noalloc", "rl_set_posvel", "rl_get_posvel", "rl_posvel",
-           "rl_line_image_mask", "rl_line_masing", "rl_run_dir_ex", "rl_gen_spec_size", "rl_gen_spec",
+           "rl_line_image_mask", "rl_image_rows", "rl_line_masing", "rl_run_dir_ex", "rl_gen_spec_size", "rl_gen_spec",
            "rl_model_checksum"]
 
 _lib = None
@@ -125,6 +125,7 @@ def lib():
         L.rl_run_dir.argtypes = [C.c_char_p, C.c_int, C.POINTER(Stats)]
         L.rl_run_dir_ex.argtypes = [C.c_char_p, C.c_int, C.c_int, C.POINTER(Stats)]
         L.rl_line_image_mask.argtypes = [vp, C.c_int, _D, C.POINTER(C.c_ubyte), C.POINTER(Stats)]
+        L.rl_image_rows.argtypes = [vp, C.c_int, C.c_int, C.c_int, _I, _D, _D, C.POINTER(Stats)]
         L.rl_set_posvel.argtypes = [vp, C.POINTER(PosvelSpec)]
         L.rl_gen_spec_size.argtypes = [C.POINTER(GenspecLines), C.POINTER(GenspecParams), C.POINTER(C.c_longlong)]
         L.rl_gen_spec.argtypes = [vp, C.POINTER(GenspecLines), C.POINTER(GenspecParams)] + [_D] * 5 + [C.POINTER(Stats)]
@@ -345,6 +346,18 @@ class Model:
         _check(lib().rl_line_image_mask(self.h, iline, _dp(img), msk.ctypes.data_as(C.POINTER(C.c_ubyte)),
                                         C.byref(st)), self._ch)
         return img, msk
+
+    def image_rows(self, iline0: int, nlines: int, rays, stats: bool = False):
+        """Lines iline0.. in one launch: their spectra [nlines, nfr] and the image rows of the
+        chosen rays [nlines, len(rays), nfr] (a ray sample of line_image's images)."""
+        n = self.info()["nfr"]
+        r = np.ascontiguousarray(rays, dtype=np.int32)
+        flux = np.zeros((nlines, n))
+        rows = np.zeros((nlines, len(r), n))
+        st = Stats()
+        _check(lib().rl_image_rows(self.h, iline0, nlines, len(r), r.ctypes.data_as(_I), _dp(flux), _dp(rows),
+                                   C.byref(st)), self._ch)
+        return (flux, rows, st.as_dict()) if stats else (flux, rows)
 
     def masing(self, iline: int) -> bool:
         """Whether the last render of line `iline` met the reference's masing test (a line

@@ -162,9 +162,16 @@ static int build_geometry(rl_model* md, rl_stats* st) {
   return 0;
 }
 
+// Image rows of chosen rays, gathered on the device after the walk (rl_image_rows).
+struct RowRequest {
+  const int* rays = nullptr;   // host ray indices
+  int n = 0;
+  double* out = nullptr;       // host [nl][n][nfr]
+};
+
 template <typename T>
 static int run_lines(rl_model* md, int iline0, int nl, double* flux_out, double* image_out, unsigned char* mask_out,
-                     rl_stats* st) {
+                     rl_stats* st, const RowRequest* rows = nullptr) {
   rl_ctx* ctx = md->ctx;
   cudaStream_t s = ctx->stream;
   const Model& m = md->m;
@@ -207,6 +214,14 @@ static int run_lines(rl_model* md, int iline0, int nl, double* flux_out, double*
   CUDA_TRY(md->derr.ensure(sizeof(int)));
   CUDA_TRY(md->dlist.ensure(sizeof(unsigned short) * walk_list_elems(ctx->nsm, nfr)));
   if (mask_out) CUDA_TRY(md->dmask.ensure(nimg));
+  if (rows) {
+    for (int i = 0; i < rows->n; i++)
+      if (rows->rays[i] < 0 || rows->rays[i] >= cam.nrays)
+        return set_err(ctx, RL_ERR_ARG, "rl_image_rows: ray " + std::to_string(rows->rays[i]) + " outside 0.." +
+                                            std::to_string(cam.nrays - 1));
+    CUDA_TRY(md->drows.ensure(sizeof(int) * (size_t)rows->n));
+    CUDA_TRY(md->drowout.ensure(sizeof(T) * (size_t)nl * rows->n * nfr));
+  }
   CUDA_TRY(cudaEventRecord(ctx->ev[0], s));
   if (!cached) {
     CUDA_TRY(h2d(md->dtab.p, tab.data(), sizeof(T) * tab.size(), s));
@@ -253,6 +268,14 @@ static int run_lines(rl_model* md, int iline0, int nl, double* flux_out, double*
   rp.ri = md->dri.as<double>(); rp.dist2 = 3.08572e18 * 3.08572e18; rp.scale = md->dscale.as<double>();
   CUDA_TRY(launch_reduce<T>(rp, md->dimg.as<T>(), md->dring.as<double>(), md->dflux.as<double>(), s));
   CUDA_TRY(cudaEventRecord(ctx->ev[3], s));
+  std::vector<T> rowbuf;
+  if (rows && rows->n > 0) {
+    rowbuf.resize((size_t)nl * rows->n * nfr);
+    CUDA_TRY(h2d(md->drows.p, rows->rays, sizeof(int) * (size_t)rows->n, s));
+    CUDA_TRY(launch_gather_rows<T>(md->dimg.as<T>(), cam.nrays, nfr, nl, md->drows.as<int>(), rows->n,
+                                   md->drowout.as<T>(), s));
+    CUDA_TRY(d2h(rowbuf.data(), md->drowout.p, sizeof(T) * rowbuf.size(), s));
+  }
   if (flux_out)
     CUDA_TRY(d2h(flux_out, md->dflux.p, sizeof(double) * (size_t)nl * nfr, s));
   unsigned long long cnt[4] = {0, 0, 0, 0};
@@ -268,6 +291,8 @@ static int run_lines(rl_model* md, int iline0, int nl, double* flux_out, double*
     CUDA_TRY(cudaMemcpy(img.data(), md->dimg.p, sizeof(T) * nimg, cudaMemcpyDeviceToHost));
     for (size_t i = 0; i < nimg; i++) image_out[i] = (double)img[i] * scale[i / ((size_t)cam.nrays * nfr)];
   }
+  for (size_t i = 0; i < rowbuf.size(); i++)
+    rows->out[i] = (double)rowbuf[i] * scale[i / ((size_t)rows->n * nfr)];
   if (mask_out) {
     g_d2h += nimg;
     CUDA_TRY(cudaMemcpy(mask_out, md->dmask.p, nimg, cudaMemcpyDeviceToHost));
@@ -291,10 +316,10 @@ static int run_lines(rl_model* md, int iline0, int nl, double* flux_out, double*
 }
 
 static int dispatch_lines(rl_model* md, int iline0, int nl, double* flux, double* image, rl_stats* st,
-                          unsigned char* mask = nullptr) {
+                          unsigned char* mask = nullptr, const RowRequest* rows = nullptr) {
   g_h2d = 0; g_d2h = 0;
-  const int rc = md->precision == RL_FP64 ? run_lines<double>(md, iline0, nl, flux, image, mask, st)
-                                          : run_lines<float>(md, iline0, nl, flux, image, mask, st);
+  const int rc = md->precision == RL_FP64 ? run_lines<double>(md, iline0, nl, flux, image, mask, st, rows)
+                                          : run_lines<float>(md, iline0, nl, flux, image, mask, st, rows);
   if (st) { st->h2d_bytes += g_h2d; st->d2h_bytes += g_d2h; }
   return rc;
 }
@@ -512,6 +537,19 @@ int rl_line_image(rl_model* md, int iline, double* image_out, rl_stats* st) {
   CUDA_TRY(cudaSetDevice(ctx->device));
   if (st) std::memset(st, 0, sizeof *st);
   return dispatch_lines(md, iline, 1, nullptr, image_out, st);
+}
+
+int rl_image_rows(rl_model* md, int iline0, int nlines, int nsel, const int* rays, double* flux_out, double* rows_out,
+                  rl_stats* st) {
+  if (!md || (nsel > 0 && (!rays || !rows_out)) || nsel < 0)
+    return set_err(nullptr, RL_ERR_ARG, "rl_image_rows: null argument or negative ray count");
+  rl_ctx* ctx = md->ctx;
+  if (!ctx) return set_err(nullptr, RL_ERR_STATE, "model was loaded without a device context");
+  CUDA_TRY(cudaSetDevice(ctx->device));
+  if (st) std::memset(st, 0, sizeof *st);
+  RowRequest rq;
+  rq.rays = rays; rq.n = nsel; rq.out = rows_out;
+  return dispatch_lines(md, iline0, nlines, flux_out, nullptr, st, nullptr, &rq);
 }
 
 int rl_line_image_mask(rl_model* md, int iline, double* image_out, unsigned char* mask_out, rl_stats* st) {

@@ -20,6 +20,9 @@ template <typename T>
 cudaError_t launch_reduce(const ReduceParams& p, const T* img, double* ring, double* flux, cudaStream_t s);
 template <typename T>
 cudaError_t launch_jobs(const JobLaunch<T>& L, cudaStream_t s);
+template <typename T>
+cudaError_t launch_gather_rows(const T* img, int nrays, int nfr, int nl, const int* rays, int nsel, T* out,
+                               cudaStream_t s);
 cudaError_t measure_peaks(int nsm, cudaStream_t st, double* ffma_per_s, double* ex2_per_s);
 
 constexpr int kWalkGroup = 12;   // lines of one walk tile at most (k_walk's kGroup)
@@ -185,6 +188,7 @@ struct rl_model {
   // per-call buffers
   rl::DevBuf dmask;   // circular-image integration mask (on request)
   rl::DevBuf dmaser;  // per-line masing flags (launches with an inverted line)
+  rl::DevBuf drows, drowout;   // rl_image_rows: chosen ray indices and their gathered rows
   rl::DevBuf dtab, dnsum, dwch, dvelo, dstar, dlc, dimg, dring, dflux, dscale, dcnt, dwork, derr, dlist;
 };
 

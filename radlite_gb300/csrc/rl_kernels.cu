@@ -13,6 +13,7 @@
 //   k_ring_sum / k_spectrum  deterministic FP64 image -> F_nu reduction.
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <algorithm>
 #include "rl_device.h"
 #include "rl_geometry.cuh"
 #include "rl_walk_common.cuh"
@@ -301,6 +302,19 @@ __global__ void k_spectrum_jobs(const RedJob<T>* __restrict__ jobs, const int* _
   for (int k = threadIdx.x; k < J.p.nfr; k += blockDim.x) spectrum_one<T>(J.p, J.img, J.ring, J.flux, line, k);
 }
 
+// rows of chosen rays: out[line][i][k] = img[line][rays[i]][k] (ray indices checked on the host)
+template <typename T>
+__global__ void k_gather_rows(const T* __restrict__ img, int nrays, int nfr, int nl, const int* __restrict__ rays,
+                              int nsel, T* __restrict__ out) {
+  const long long n = (long long)nl * nsel * nfr;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(i % nfr);
+    const long long r = i / nfr;
+    const int sel = (int)(r % nsel), line = (int)(r / nsel);
+    out[i] = img[((size_t)line * nrays + rays[sel]) * nfr + k];
+  }
+}
+
 // ------------------------------------------------------------------------------------
 // pipe-throughput calibration (the denominators of the issue roofline)
 // ------------------------------------------------------------------------------------
@@ -448,6 +462,16 @@ cudaError_t launch_reduce(const ReduceParams& p, const T* img, double* ring, dou
 }
 
 template <typename T>
+cudaError_t launch_gather_rows(const T* img, int nrays, int nfr, int nl, const int* rays, int nsel, T* out,
+                               cudaStream_t s) {
+  const long long n = (long long)nl * nsel * nfr;
+  if (n <= 0) return cudaSuccess;
+  const long long blocks = std::min<long long>((n + 255) / 256, 65536);
+  k_gather_rows<T><<<(unsigned)blocks, 256, 0, s>>>(img, nrays, nfr, nl, rays, nsel, out);
+  return cudaGetLastError();
+}
+
+template <typename T>
 cudaError_t launch_jobs(const JobLaunch<T>& L, cudaStream_t s) {
   if (L.nrays_total > 0) {
     k_geometry_jobs<T><<<(L.nrays_total + 127) / 128, 128, 0, s>>>(L.geo, L.ray_prefix, L.njobs, L.nrays_total);
@@ -476,6 +500,8 @@ template cudaError_t launch_walk<float>(const WalkParams<float>&, int, int, cuda
 template cudaError_t launch_walk<double>(const WalkParams<double>&, int, int, cudaStream_t);
 template cudaError_t launch_reduce<float>(const ReduceParams&, const float*, double*, double*, cudaStream_t);
 template cudaError_t launch_reduce<double>(const ReduceParams&, const double*, double*, double*, cudaStream_t);
+template cudaError_t launch_gather_rows<float>(const float*, int, int, int, const int*, int, float*, cudaStream_t);
+template cudaError_t launch_gather_rows<double>(const double*, int, int, int, const int*, int, double*, cudaStream_t);
 template cudaError_t launch_jobs<float>(const JobLaunch<float>&, cudaStream_t);
 template cudaError_t launch_jobs<double>(const JobLaunch<double>&, cudaStream_t);
 

@@ -1,0 +1,90 @@
+"""GPU parity at the benchmarked sizes, through the C ABI, against the FP64 oracle.
+
+* disk_line: the 100x60 single-line disk (J=3-2, 64 channels, 400 rings x 128 azimuths +
+  the central beam: 51,201 rays) at full size. The oracle renders every ray in a pool of
+  host processes and sums the image with its own calc_freq_flux_observer restatement.
+* band_large: the 400x200 perturbed disk with 20 band lines x 200 channels and 1000 rings x
+  256 azimuths, at inclinations 20 and 60 degrees. The oracle renders a ray sample of every
+  line (every 509th / 1021st ray: all ring radii and azimuths are visited); the GPU renders
+  the full image in one launch and returns the same rays' rows (rl_image_rows).
+
+Tolerances (the reference's spectrum criterion is in every channel above 1e-3 of the peak):
+  FP32 transfer: spectra and sample spectra <= 1e-4 relative; each sampled ray within 2e-4
+                 of its brightest channel.
+  FP64 transfer: spectra <= 1e-9 relative with the oracle's integrated-channel count and
+                 formal-solution step count; sampled rays within 1e-9 of their brightest
+                 channel.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+FP32_TOL = 1e-4
+FP32_PIXEL_TOL = 2e-4
+FP64_TOL = 1e-9
+
+
+@pytest.fixture(scope="module")
+def ctx(gpu_lib):
+    c = gpu_lib.Context(0)
+    yield c
+    c.close()
+
+
+def test_disk_line_full_size(ctx, oracle_lib, model_dir):
+    from oracle import sample
+    d = model_dir("disk_line")
+    o = oracle_lib.Oracle(d)
+    assert (o.nrays, o.nfr, o.nphi) == (51201, 64, 128)
+    il = o.ilinestart
+    rows, counts, _, _ = sample.oracle_rows(d, [il], np.arange(o.nrays))
+    ref = o.image_to_spectrum(rows[0])
+    m = ctx.load_dir(d)
+    got32, _, _ = m.calc_line_spectrum(il, stats=True)
+    assert sample.spectrum_relerr(got32, ref) <= FP32_TOL
+    m.set_precision(1)
+    got64, _, st = m.calc_line_spectrum(il, stats=True)
+    assert sample.spectrum_relerr(got64, ref) <= FP64_TOL
+    assert st["integrated"] == counts[1]
+    assert abs(st["steps"] - counts[0]) <= 1e-6 * counts[0] + 2
+    m.free()
+
+
+@pytest.mark.parametrize("incl,stride", [(20.0, 509), (60.0, 1021)])
+def test_band_large_ray_sample(ctx, oracle_lib, model_dir, incl, stride):
+    from oracle import sample
+    d = model_dir("band_large", incl_deg=incl)
+    o = oracle_lib.Oracle(d)
+    assert (o.nrays, o.nfr, o.nlines_spec) == (256001, 200, 20)
+    lines = list(range(o.ilinestart, o.ilinestart + o.nlines_spec))
+    rays = sample.ray_sample(o.nrays, stride)
+    ref, _, _, _ = sample.oracle_rows(d, lines, rays)
+    _, _, _, ri = o.rays()
+    m = ctx.load_dir(d)
+    _, rows32 = m.image_rows(lines[0], len(lines), rays)
+    c32 = sample.compare(rows32, ref, rays, ri, o.nphi)
+    assert max(c32["spectrum_rel_err"]) <= FP32_TOL, c32
+    assert max(c32["pixel_rel_err"]) <= FP32_PIXEL_TOL, c32
+    assert min(c32["channels_checked"]) > 0
+    m.set_precision(1)
+    _, rows64 = m.image_rows(lines[0], len(lines), rays)
+    c64 = sample.compare(rows64, ref, rays, ri, o.nphi)
+    assert max(c64["spectrum_rel_err"]) <= FP64_TOL, c64
+    assert max(c64["pixel_rel_err"]) <= FP64_TOL, c64
+    m.free()
+
+
+def test_image_rows_match_line_image(ctx, model_dir):
+    """rl_image_rows returns the rows of rl_line_image's image and rl_spectra's spectra."""
+    m = ctx.load_dir(model_dir("tiny_band"))
+    info = m.info()
+    rays = np.array([0, 5, info["nrays"] - 1, 17], dtype=np.int32)
+    flux, rows = m.image_rows(info["ilinestart"], info["nlines_spec"], rays)
+    np.testing.assert_array_equal(flux, m.spectra(info["ilinestart"], info["nlines_spec"]))
+    for k in range(info["nlines_spec"]):
+        img = m.line_image(info["ilinestart"] + k)
+        np.testing.assert_allclose(rows[k], img[rays], rtol=1e-12, atol=0)
+    with pytest.raises(Exception):
+        m.image_rows(info["ilinestart"], 1, [info["nrays"]])
+    m.free()
