@@ -347,6 +347,8 @@ def ours(args):
             walk_ms.append(sum(s["walk_ms"] for s in sts))
             steps_fs = sum(s["steps"] for s in sts)
             integ = sum(s["integrated"] for s in sts)
+            passes = sum(s["node_passes"] for s in sts)
+            packed = sum(s["packed_passes"] for s in sts)
     wall = (time.perf_counter() - t0) / args.steps
     ms = max_over_ranks(sum(dev_ms) / len(dev_ms), dist)
     nrays = n_rays(cfg)
@@ -419,6 +421,7 @@ def ours(args):
                "roofline": {"bound": "mufu_issue" if bound_mufu else "fp32_issue", "achieved": achieved / 1e12,
                             "peak": peak / 1e12, "unit": "Tops/s", "frac": achieved / peak, "traffic": traffic,
                             "kernel": "k_walk<float>", "walk_ms_per_step": wk * 1e3,
+                            "node_passes_per_step": passes, "packed_fraction": packed / passes if passes else None,
                             "budget_per_step": {"fp32": BUDGET_FP32, "mufu": BUDGET_MUFU},
                             "peaks_measured": peaks,
                             "hbm_side": {"traffic_gb_per_s": traffic_gbs, "peak_gb_per_s": hbm_peak,
@@ -681,7 +684,8 @@ def profile_case(args):
     m = ctx.load_arrays(arr, camera(cfg, cfg.incl_deg))
     f, st = m.spectra(cfg.ilinestart, cfg.nlines, stats=True)
     print(json.dumps({"workload": args.workload, "steps": st["steps"], "walk_ms": st["walk_ms"],
-                      "geometry_ms": st["geometry_ms"], "nrays": st["nrays"], "nlines": st["nlines"]}), flush=True)
+                      "geometry_ms": st["geometry_ms"], "nrays": st["nrays"], "nlines": st["nlines"],
+                      "node_passes": st["node_passes"], "packed_passes": st["packed_passes"]}), flush=True)
     m.free()
     ctx.close()
     return 0

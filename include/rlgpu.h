@@ -42,6 +42,9 @@ typedef struct rl_stats {
   double geometry_ms, walk_ms, reduce_ms, upload_ms, total_ms;
   int nrays, nfr, kmax, nlines;
   unsigned long long h2d_bytes, d2h_bytes;   /* host<->device copies made by the call */
+  unsigned long long node_passes;    /* walk: a tile's channel slots taken over one node */
+  unsigned long long packed_passes;  /* of them on the packed FP32 path (positive opacity,
+                                        no state reset, no SUBGRID refinement) */
 } rl_stats;
 
 typedef struct rl_model_info {
@@ -133,7 +136,8 @@ int rl_line_image_mask(rl_model* model, int iline, double* image_out, unsigned c
    cube of this model) integrated a segment whose line opacity at its end times its length
    is below -0.01, the masing test of charintline (telescope.F:4291-4297), after which the
    reference prints "WARNING: Masing detected!"; else 0. Only lines with a population
-   inversion somewhere are tested; the batch and the differentiable path do not test. */
+   inversion somewhere are tested (the batch reports its own with rl_batch_job_masing; the
+   differentiable path's LTE populations have no inversion). */
 int rl_line_masing(rl_model* model, int iline, int* detected);
 
 /* ---- Position-velocity cube (linespectrum.inp command 2): the rectangular image of
@@ -231,6 +235,10 @@ int rl_batch_flux_size(rl_batch* batch, long long* n);
 int rl_batch_job_info(rl_batch* batch, int job, long long* flux_offset, int* nlines, int* nfr);
 /* Renders every job; flux_out receives each job's [nlines][nfr] F_nu at 1 pc in job order. */
 int rl_batch_run(rl_batch* batch, double* flux_out, rl_stats* stats);
+/* Masing test of the last run, per line of job `job` (detected[nlines]: 1 where a segment's
+   line opacity at its end times its length fell below -0.01, as rl_line_masing reports
+   for a model, telescope.F:4291-4297). Only jobs with a population inversion are tested. */
+int rl_batch_job_masing(rl_batch* batch, int job, int* detected);
 /* Memory waves of the last build. */
 int rl_batch_waves(rl_batch* batch, int* nwaves);
 /* The executable's work for every directory listed in `manifest` (one per line, '#'
@@ -298,8 +306,10 @@ int rl_diff_batch_backward(rl_diff_batch* batch, rl_stats* stats);
    doubles, held by every GPU that loads the library until exit); (nrr+1)*nfr above
    2^20 is rejected with RL_ERR_ARG. Nothing in it has to start at zero. Calls that
    overlap on one device (other streams or threads) share that array and race: order
-   them on one stream. The first call on a device looks the array up, which loads the
-   module: make it before any stream capture. Errors: rl_last_error(NULL, ...). */
+   them on one stream. Every call looks the array's address up on the current device
+   (cudaGetSymbolAddress), so a cudaDeviceReset or another current context between calls
+   is safe; the first call in a context loads the module: make it before any stream
+   capture. Errors: rl_last_error(NULL, ...). */
 int rl_image_to_spectrum_noalloc(void* stream, int precision, const void* image, int nlines, int nrays, int nphi,
                                  int nrr, int nfr, const double* ri, const double* scale, double distance_pc,
                                  double* flux);

@@ -144,14 +144,14 @@ def kernel(obsres: float, vres: float):
 def convolve_reflect(x, k):
     """scipy.ndimage.convolve(x, k, mode='reflect') for a symmetric 1-D kernel: the
     flipped kernel centred at len(k)//2, one sample to the left for even lengths, with
-    half-sample symmetric edges (d c b a | a b c d | d c b a)."""
+    half-sample symmetric edges (d c b a | a b c d | d c b a), repeated with period 2n for
+    kernels that reach further than one grid length."""
     n, m = len(x), len(k)
     c = m // 2 - (1 if m % 2 == 0 else 0)
     kf = k[::-1]
     out = np.zeros(n)
     for j in range(m):
-        idx = np.arange(n) + j - c
-        idx = np.where(idx < 0, -idx - 1, idx)
+        idx = np.mod(np.arange(n) + j - c, 2 * n)
         idx = np.where(idx >= n, 2 * n - idx - 1, idx)
         out += x[idx] * kf[j]
     return out

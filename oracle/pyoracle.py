@@ -45,6 +45,7 @@ def lib():
         L.rlo_posvel.argtypes = [vp, C.c_int, C.c_int, C.c_int] + [C.c_double] * 5 + [C.c_int, _D, _D]
         L.rlo_run_dir.argtypes = [C.c_char_p]
         L.rlo_masing.argtypes = [vp]
+        L.rlo_hunt.argtypes = [_D, C.c_int, C.c_double, C.c_int]
         _lib = L
     return _lib
 

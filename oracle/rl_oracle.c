@@ -162,38 +162,47 @@ static double col_num(const char* line, int start, int width, int d) {
 }
 
 /* ----------------------------------------------------------------------------------- */
-/* bracketing search with hunt's semantics (guess, expand, bisect)                       */
-/* xx is 1-based: xx[1..n]                                                              */
+/* bracketing search with the index rules of hunt (nrecip.F:157-197), xx 1-based xx[1..n]: */
+/* with "past j" = x >= xx[j] (x < xx[j] for a descending table), bracket [lo, hi] from the */
+/* guess by probes at distances 2^i - 1 (upwards while past, downwards while not past),    */
+/* then lo + the count of nodes strictly inside the bracket with x > xx[j] (x <= xx[j]    */
+/* descending). An exact hit on a node the bracket stopped on returns that node, one      */
+/* strictly inside returns the node below it.                                            */
 /* ----------------------------------------------------------------------------------- */
-static int hunt1(const double* xx, int n, double x, int jlo) {
-    int ascnd = xx[n] > xx[1];
-    int jhi, inc;
-    if (jlo <= 0 || jlo > n) { jlo = 0; jhi = n + 1; }
-    else {
-        inc = 1;
-        if ((x >= xx[jlo]) == ascnd) {
-            for (;;) {
-                jhi = jlo + inc;
-                if (jhi > n) { jhi = n + 1; break; }
-                else if ((x >= xx[jhi]) == ascnd) { jlo = jhi; inc += inc; }
-                else break;
+static int node_past(const double* xx, int asc, double x, int j) { return asc ? x >= xx[j] : x < xx[j]; }
+static int node_before(const double* xx, int asc, double x, int j) { return asc ? x < xx[j] : x >= xx[j]; }
+static int node_beyond(const double* xx, int asc, double x, int j) { return asc ? x > xx[j] : x <= xx[j]; }
+
+static int hunt1(const double* xx, int n, double x, int guess) {
+    int asc = xx[n] > xx[1];
+    int lo = 0, hi = n + 1;
+    if (guess >= 1 && guess <= n) {
+        int step;
+        if (node_past(xx, asc, x, guess)) {
+            lo = guess;
+            for (step = 1; guess + step <= n; step = 2 * step + 1) {
+                if (!node_past(xx, asc, x, guess + step)) { hi = guess + step; break; }
+                lo = guess + step;
             }
         } else {
-            jhi = jlo;
-            for (;;) {
-                jlo = jhi - inc;
-                if (jlo < 1) { jlo = 0; break; }
-                else if ((x < xx[jlo]) == ascnd) { jhi = jlo; inc += inc; }
-                else break;
+            hi = guess;
+            for (step = 1; guess - step >= 1; step = 2 * step + 1) {
+                if (!node_before(xx, asc, x, guess - step)) { lo = guess - step; break; }
+                hi = guess - step;
             }
         }
     }
-    while (jhi - jlo != 1) {
-        int jm = (jhi + jlo) / 2;
-        if ((x > xx[jm]) == ascnd) jlo = jm; else jhi = jm;
+    /* nodes lo+1 .. hi-1 that x lies beyond precede the others: bisect for their count */
+    int a = lo, b = hi;   /* beyond(a) or a == lo; not beyond(b) or b == hi */
+    while (b - a > 1) {
+        int m = a + (b - a) / 2;
+        if (node_beyond(xx, asc, x, m)) a = m; else b = m;
     }
-    return jlo;
+    return a;
 }
+
+/* hunt1 for tests: the table xx0[0..n-1] as xx[1..n] */
+int rlo_hunt(const double* xx0, int n, double x, int guess) { return hunt1(xx0 - 1, n, x, guess); }
 
 /* ----------------------------------------------------------------------------------- */
 /* model                                                                                 */

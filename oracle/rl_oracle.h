@@ -23,6 +23,8 @@ int rlo_pv_rays(const rlo_model* m, int nx, int ny, double szx, double szy, doub
 int rlo_posvel(rlo_model* m, int iline, int nx, int ny, double szx, double szy, double phioff, double xoff,
                double yoff, int addstar, double* I, double* tau);
 int rlo_run_dir(const char* dir);
+/* bracketing search of the trajectory builder (hunt's index rules) on xx[0..n-1] as 1..n */
+int rlo_hunt(const double* xx, int n, double x, int guess);
 /* 1 when the last line image, line spectrum or position-velocity cube met the masing
    test of charintline (telescope.F:4291-4297) */
 int rlo_masing(const rlo_model* m);

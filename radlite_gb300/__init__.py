@@ -36,7 +36,8 @@ class Stats(C.Structure):
                 ("ray_channels", C.c_ulonglong), ("geometry_ms", C.c_double), ("walk_ms", C.c_double),
                 ("reduce_ms", C.c_double), ("upload_ms", C.c_double), ("total_ms", C.c_double),
                 ("nrays", C.c_int), ("nfr", C.c_int), ("kmax", C.c_int), ("nlines", C.c_int),
-                ("h2d_bytes", C.c_ulonglong), ("d2h_bytes", C.c_ulonglong)]
+                ("h2d_bytes", C.c_ulonglong), ("d2h_bytes", C.c_ulonglong), ("node_passes", C.c_ulonglong),
+                ("packed_passes", C.c_ulonglong)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -89,7 +90,7 @@ EXPORTS = ["rl_create", "rl_destroy", "rl_last_error", "rl_load_dir", "rl_load_a
            "rl_line_image", "rl_run_dir", "rl_debug_trajectory", "rl_measure_peaks",
            "rl_batch_create", "rl_batch_destroy", "rl_batch_add", "rl_batch_set_memory", "rl_batch_set_tiles",
            "rl_batch_get_tiles", "rl_batch_autotune", "rl_batch_use_graph", "rl_batch_flux_size",
-           "rl_batch_job_info", "rl_batch_run", "rl_batch_waves", "rl_run_manifest",
+           "rl_batch_job_info", "rl_batch_job_masing", "rl_batch_run", "rl_batch_waves", "rl_run_manifest",
            "rl_diff_create", "rl_diff_destroy", "rl_diff_info", "rl_diff_set_checkpoint", "rl_diff_forward",
            "rl_diff_backward", "rl_diff_batch_create", "rl_diff_batch_destroy", "rl_diff_batch_add",
            "rl_diff_batch_use_graph", "rl_diff_batch_buffers", "rl_diff_batch_layout", "rl_diff_batch_forward",
@@ -144,6 +145,7 @@ def lib():
         L.rl_batch_flux_size.argtypes = [vp, C.POINTER(C.c_longlong)]
         L.rl_batch_job_info.argtypes = [vp, C.c_int, C.POINTER(C.c_longlong), _I, _I]
         L.rl_batch_run.argtypes = [vp, _D, C.POINTER(Stats)]
+        L.rl_batch_job_masing.argtypes = [vp, C.c_int, _I]
         L.rl_batch_waves.argtypes = [vp, _I]
         L.rl_run_manifest.argtypes = [C.c_char_p, C.c_int, C.POINTER(Stats)]
         L.rl_diff_create.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.POINTER(vp)]
@@ -465,6 +467,14 @@ class Batch:
             _check(lib().rl_batch_job_info(self.h, j, C.byref(off), C.byref(nl), C.byref(nfr)), self.ctx.h)
             out.append(flux[off.value:off.value + nl.value * nfr.value].reshape(nl.value, nfr.value))
         return (out, st.as_dict()) if stats else out
+
+    def masing(self, job: int) -> np.ndarray:
+        """Per line of job `job`: whether the last run met the reference's masing test."""
+        off, nl, nfr = C.c_longlong(), C.c_int(), C.c_int()
+        _check(lib().rl_batch_job_info(self.h, job, C.byref(off), C.byref(nl), C.byref(nfr)), self.ctx.h)
+        d = np.zeros(nl.value, dtype=np.int32)
+        _check(lib().rl_batch_job_masing(self.h, job, d.ctypes.data_as(_I)), self.ctx.h)
+        return d.astype(bool)
 
 
 class Diff:

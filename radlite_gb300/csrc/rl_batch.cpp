@@ -37,6 +37,9 @@ struct BatchJob {
   Camera cam;
   int kmax = 0, nfr = 0, ncell = 0;
   double aksmax = 0.0, fstar = 0.0;
+  bool has_isrf = false;                               // star holds the outer-boundary-3 table too
+  bool inverted = false;                               // some line has a population inversion
+  int line_off = 0;                                    // first flag of the job in the batch's masing flags
   DevBuf x0, z0, ri;                                   // camera
   DevBuf tab, nsum, wch, velo, star, lc, scale;        // line tables of the batch precision
   size_t flux_off = 0;                                 // first value in the batch flux array
@@ -72,7 +75,10 @@ struct rl_batch {
   Plan<float> pf;
   Plan<double> pd;
   DevBuf arena, flux, counters, work, err, list;
+  DevBuf maser;                  // [nlines_total] masing flags (jobs with an inverted line)
+  bool any_inverted = false;
   double* flux_h = nullptr;
+  int* maser_h = nullptr;
   unsigned long long* cnt_h = nullptr;
   int* err_h = nullptr;
   cudaGraph_t graph = nullptr;
@@ -89,6 +95,7 @@ struct rl_batch {
     if (ctx) cudaSetDevice(ctx->device);
     drop_graph();
     if (flux_h) cudaFreeHost(flux_h);
+    if (maser_h) cudaFreeHost(maser_h);
     if (cnt_h) cudaFreeHost(cnt_h);
     if (err_h) cudaFreeHost(err_h);
   }
@@ -120,6 +127,9 @@ int snapshot_job(rl_batch* b, BatchJob& J) {
   J.fstar = (m.rstar / J.cam.ri[1]) * (m.rstar / J.cam.ri[1]);
   LineTables<T> lt;
   if (build_line_tables<T>(m, J.iline0, J.nl, lt, err)) return set_err(ctx, RL_ERR_ARG, err);
+  J.has_isrf = lt.has_isrf;
+  J.inverted = false;
+  for (char c : lt.mase) J.inverted = J.inverted || c;
   cudaStream_t s = ctx->stream;
   const Camera& cam = J.cam;
   CUDA_TRY(J.x0.ensure(sizeof(double) * cam.nrays));
@@ -217,7 +227,7 @@ int write_descriptors(rl_batch* b) {
       w.gsize = gs; w.nitems = ng * cam.nrays;
       w.tab = J.tab.as<T>(); w.nsum = J.nsum.as<T>(); w.wch = J.wch.as<T>(); w.velo = J.velo.as<double>();
       w.star = J.star.as<T>(); w.lc = J.lc.as<LineConst<T>>();
-      w.isrf = isrf_of(m, w.star, J.nl, J.nfr);
+      w.isrf = isrf_of(J.has_isrf, w.star, J.nl, J.nfr);
       w.aksmax_c = J.aksmax / 2.99792458e5;
       w.kq = (T)(3.33567e-6 * 2.99792458e5);
       w.fstar = (T)J.fstar;
@@ -226,6 +236,7 @@ int write_descriptors(rl_batch* b) {
       w.work = b->work.as<int>();
       w.err = b->err.as<int>();
       w.list = b->list.as<unsigned short>();
+      w.maser = J.inverted ? b->maser.as<int>() + J.line_off : nullptr;
       RedJob<T>& r = red[q];
       r.p.nrays = cam.nrays; r.p.nfr = J.nfr; r.p.nphi = cam.nphi; r.p.nrr = cam.nrr; r.p.nlines = J.nl;
       r.p.ri = J.ri.as<double>(); r.p.dist2 = 3.08572e18 * 3.08572e18; r.p.scale = J.scale.as<double>();
@@ -277,6 +288,7 @@ int build(rl_batch* b) {
     int rc = snapshot_job<T>(b, *J);
     if (rc) return rc;
     J->flux_off = b->nflux;
+    J->line_off = b->nlines_total;
     b->nflux += (size_t)J->nl * J->nfr;
     b->ray_channels += (unsigned long long)J->cam.nrays * J->nfr * J->nl;
     b->nlines_total += J->nl;
@@ -302,9 +314,15 @@ int build(rl_batch* b) {
   }
   CUDA_TRY(b->arena.ensure(arena));
   CUDA_TRY(b->flux.ensure(sizeof(double) * b->nflux));
-  CUDA_TRY(b->counters.ensure(sizeof(unsigned long long) * 4));
+  CUDA_TRY(b->counters.ensure(sizeof(unsigned long long) * kWalkCounters));
   CUDA_TRY(b->work.ensure(sizeof(int)));
   CUDA_TRY(b->err.ensure(sizeof(int)));
+  b->any_inverted = false;
+  for (auto& J : b->jobs) b->any_inverted = b->any_inverted || J->inverted;
+  CUDA_TRY(b->maser.ensure(sizeof(int) * std::max(1, b->nlines_total)));
+  if (b->maser_h) { cudaFreeHost(b->maser_h); b->maser_h = nullptr; }
+  CUDA_TRY(cudaMallocHost((void**)&b->maser_h, sizeof(int) * std::max(1, b->nlines_total)));
+  std::memset(b->maser_h, 0, sizeof(int) * std::max(1, b->nlines_total));
   {
     int max_nfr = 0;
     for (auto& J : b->jobs) max_nfr = std::max(max_nfr, J->nfr);
@@ -312,7 +330,7 @@ int build(rl_batch* b) {
   }
   if (b->flux_h) { cudaFreeHost(b->flux_h); b->flux_h = nullptr; }
   CUDA_TRY(cudaMallocHost((void**)&b->flux_h, sizeof(double) * b->nflux));
-  if (!b->cnt_h) CUDA_TRY(cudaMallocHost((void**)&b->cnt_h, sizeof(unsigned long long) * 4));
+  if (!b->cnt_h) CUDA_TRY(cudaMallocHost((void**)&b->cnt_h, sizeof(unsigned long long) * kWalkCounters));
   if (!b->err_h) CUDA_TRY(cudaMallocHost((void**)&b->err_h, sizeof(int)));
   int rc = write_descriptors<T>(b);
   if (rc) return rc;
@@ -326,8 +344,9 @@ int build(rl_batch* b) {
 // a model keeps its camera geometry, and skips the geometry launch afterwards.
 template <typename T>
 cudaError_t enqueue(rl_batch* b, cudaStream_t s, bool skip_geometry) {
-  cudaError_t e = cudaMemsetAsync(b->counters.p, 0, sizeof(unsigned long long) * 4, s);
+  cudaError_t e = cudaMemsetAsync(b->counters.p, 0, sizeof(unsigned long long) * kWalkCounters, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(b->err.p, 0, sizeof(int), s);
+  if (e == cudaSuccess && b->any_inverted) e = cudaMemsetAsync(b->maser.p, 0, sizeof(int) * b->nlines_total, s);
   for (Wave<T>& W : plan_of<T>(b).waves) {
     if (e != cudaSuccess) return e;
     JobLaunch<T> L = W.L;
@@ -336,8 +355,10 @@ cudaError_t enqueue(rl_batch* b, cudaStream_t s, bool skip_geometry) {
   }
   if (e == cudaSuccess) e = cudaMemcpyAsync(b->flux_h, b->flux.p, sizeof(double) * b->nflux, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess)
-    e = cudaMemcpyAsync(b->cnt_h, b->counters.p, sizeof(unsigned long long) * 4, cudaMemcpyDeviceToHost, s);
+    e = cudaMemcpyAsync(b->cnt_h, b->counters.p, sizeof(unsigned long long) * kWalkCounters, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(b->err_h, b->err.p, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess && b->any_inverted)
+    e = cudaMemcpyAsync(b->maser_h, b->maser.p, sizeof(int) * b->nlines_total, cudaMemcpyDeviceToHost, s);
   return e;
 }
 
@@ -375,7 +396,8 @@ int run(rl_batch* b, double* flux_out, rl_stats* st) {
   }
   CUDA_TRY(cudaEventRecord(ctx->ev[1], s));
   CUDA_TRY(cudaStreamSynchronize(s));
-  g_d2h += sizeof(double) * b->nflux + sizeof(unsigned long long) * 4 + sizeof(int);
+  g_d2h += sizeof(double) * b->nflux + sizeof(unsigned long long) * kWalkCounters + sizeof(int) +
+           (b->any_inverted ? sizeof(int) * b->nlines_total : 0);
   if (*b->err_h != 0) {
     b->geo_valid = false;
     return set_err(ctx, RL_ERR_GEOMETRY, "rl_batch: walk error code " + std::to_string(*b->err_h));
@@ -388,6 +410,7 @@ int run(rl_batch* b, double* flux_out, rl_stats* st) {
     st->walk_ms += ms;
     st->total_ms += ms;
     st->steps += b->cnt_h[0]; st->integrated += b->cnt_h[1]; st->node_visits += b->cnt_h[2];
+    st->node_passes += b->cnt_h[3]; st->packed_passes += b->cnt_h[4];
     st->ray_channels += b->ray_channels;
     st->nlines += b->nlines_total;
   }
@@ -436,7 +459,7 @@ int autotune(rl_batch* b, int stride, int* gbest, int* cbest, double* best_ms) {
       L.walk.stride = std::max(1, stride);
       float ms = 0.f;
       for (int rep = 0; rep < 2; rep++) {   // first repetition warms up
-        CUDA_TRY(cudaMemsetAsync(b->counters.p, 0, sizeof(unsigned long long) * 4, s));
+        CUDA_TRY(cudaMemsetAsync(b->counters.p, 0, sizeof(unsigned long long) * kWalkCounters, s));
         CUDA_TRY(cudaEventRecord(ctx->ev[0], s));
         CUDA_TRY(launch_jobs<T>(L, s));
         CUDA_TRY(cudaEventRecord(ctx->ev[1], s));
@@ -608,6 +631,11 @@ int rl_run_manifest(const char* manifest, int device, rl_stats* st) {
   for (size_t i = 0; i < dirs.size() && rc == 0; i++) {
     const BatchJob& J = *b->jobs[i];
     const Model& m = models[i]->m;
+    std::vector<int> det(J.nl, 0);
+    rl_batch_job_masing(b, (int)i, det.data());
+    for (int l = 0; l < J.nl; l++)
+      if (det[l]) std::printf("          WARNING: Masing detected!\n Will only warn once for this transition.\n");
+    std::fflush(stdout);
     std::vector<int> lines;
     for (int l = 0; l < m.nlspec; l++) lines.push_back(m.ilstart + l);
     std::vector<double> f(flux.begin() + J.flux_off, flux.begin() + J.flux_off + (size_t)J.nl * J.nfr);
@@ -624,6 +652,14 @@ int rl_run_manifest(const char* manifest, int device, rl_stats* st) {
   for (rl_model* md : models) rl_model_free(md);
   rl_destroy(ctx);
   return rc;
+}
+
+int rl_batch_job_masing(rl_batch* b, int job, int* detected) {
+  if (!b || !detected) return set_err(nullptr, RL_ERR_ARG, "rl_batch_job_masing: null argument");
+  if (job < 0 || job >= (int)b->jobs.size()) return set_err(b->ctx, RL_ERR_ARG, "rl_batch_job_masing: job index");
+  const BatchJob& J = *b->jobs[job];
+  for (int l = 0; l < J.nl; l++) detected[l] = (b->built && J.inverted && b->maser_h) ? (b->maser_h[J.line_off + l] != 0) : 0;
+  return 0;
 }
 
 int rl_batch_waves(rl_batch* b, int* nwaves) {

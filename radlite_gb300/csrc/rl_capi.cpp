@@ -86,6 +86,7 @@ int rl::build_line_tables(const Model& m, int iline0, int nl, LineTables<T>& out
   out.wch.assign((size_t)nl * nfr, (T)0); out.star.assign((size_t)(isrf ? 2 : 1) * nl * nfr, (T)0);
   out.velo.assign((size_t)nl * nfr, 0.0); out.scale.assign(nl, 1.0); out.lc.assign(nl, LineConst<T>{});
   out.mase.assign(nl, 0);
+  out.has_isrf = isrf;
   for (int l = 0; l < nl; l++) {
     LinePrep lp;
     if (prepare_line(m, iline0 + l, scaled, lp, err, with_isrf)) return RL_ERR_ARG;
@@ -186,12 +187,14 @@ static int run_lines(rl_model* md, int iline0, int nl, double* flux_out, double*
   LineTables<T> lt;
   std::vector<double> scale = md->tab_scale;
   std::vector<char> mase = md->tab_mase;
+  bool has_isrf = md->tab_isrf;
   if (!cached) {
     md->tab_line0 = -1;
     std::string err;
     if (build_line_tables<T>(m, iline0, nl, lt, err)) return set_err(ctx, RL_ERR_ARG, err);
     scale = lt.scale;
     mase = lt.mase;
+    has_isrf = lt.has_isrf;
   }
   const std::vector<T>&tab = lt.tab, &nsum = lt.nsum, &wch = lt.wch, &star = lt.star;
   const std::vector<double>& velo = lt.velo;
@@ -209,7 +212,7 @@ static int run_lines(rl_model* md, int iline0, int nl, double* flux_out, double*
   CUDA_TRY(md->dimg.ensure(sizeof(T) * nimg));
   CUDA_TRY(md->dring.ensure(sizeof(double) * (size_t)nl * (cam.nrr + 1) * nfr));
   CUDA_TRY(md->dflux.ensure(sizeof(double) * (size_t)nl * nfr));
-  CUDA_TRY(md->dcnt.ensure(sizeof(unsigned long long) * 4));
+  CUDA_TRY(md->dcnt.ensure(sizeof(unsigned long long) * kWalkCounters));
   CUDA_TRY(md->dwork.ensure(sizeof(int)));
   CUDA_TRY(md->derr.ensure(sizeof(int)));
   CUDA_TRY(md->dlist.ensure(sizeof(unsigned short) * walk_list_elems(ctx->nsm, nfr)));
@@ -232,7 +235,7 @@ static int run_lines(rl_model* md, int iline0, int nl, double* flux_out, double*
     CUDA_TRY(h2d(md->dlc.p, lc.data(), sizeof(LineConst<T>) * lc.size(), s));
     CUDA_TRY(h2d(md->dscale.p, scale.data(), sizeof(double) * nl, s));
   }
-  CUDA_TRY(cudaMemsetAsync(md->dcnt.p, 0, sizeof(unsigned long long) * 4, s));
+  CUDA_TRY(cudaMemsetAsync(md->dcnt.p, 0, sizeof(unsigned long long) * kWalkCounters, s));
   CUDA_TRY(cudaMemsetAsync(md->dwork.p, 0, sizeof(int), s));
   CUDA_TRY(cudaMemsetAsync(md->derr.p, 0, sizeof(int), s));
   MaserFlags mf;
@@ -250,7 +253,7 @@ static int run_lines(rl_model* md, int iline0, int nl, double* flux_out, double*
   if (nfr >= 2048) return set_err(ctx, RL_ERR_ARG, "at most 2047 channels per line are supported");
   P.tab = md->dtab.as<T>(); P.nsum = md->dnsum.as<T>(); P.wch = md->dwch.as<T>(); P.velo = md->dvelo.as<double>();
   P.star = md->dstar.as<T>(); P.lc = md->dlc.as<LineConst<T>>();
-  P.isrf = isrf_of(m, P.star, nl, nfr);
+  P.isrf = isrf_of(has_isrf, P.star, nl, nfr);
   P.aksmax_c = m.aksmax / 2.99792458e5;
   P.kq = (T)(3.33567e-6 * 2.99792458e5);
   P.fstar = (T)((m.rstar / cam.ri[1]) * (m.rstar / cam.ri[1]));
@@ -278,7 +281,7 @@ static int run_lines(rl_model* md, int iline0, int nl, double* flux_out, double*
   }
   if (flux_out)
     CUDA_TRY(d2h(flux_out, md->dflux.p, sizeof(double) * (size_t)nl * nfr, s));
-  unsigned long long cnt[4] = {0, 0, 0, 0};
+  unsigned long long cnt[kWalkCounters] = {};
   int kerr = 0;
   CUDA_TRY(d2h(cnt, md->dcnt.p, sizeof(cnt), s));
   CUDA_TRY(d2h(&kerr, md->derr.p, sizeof(int), s));
@@ -300,6 +303,7 @@ static int run_lines(rl_model* md, int iline0, int nl, double* flux_out, double*
   if (!cached) {
     md->tab_line0 = iline0; md->tab_nl = nl; md->tab_prec = md->precision; md->tab_scale = scale;
     md->tab_mase = mase;
+    md->tab_isrf = has_isrf;
   }
   if (kerr != 0) return set_err(ctx, RL_ERR_GEOMETRY, "walk: error code " + std::to_string(kerr));
   if (st) {
@@ -309,6 +313,7 @@ static int run_lines(rl_model* md, int iline0, int nl, double* flux_out, double*
     cudaEventElapsedTime(&c, ctx->ev[2], ctx->ev[3]);
     st->upload_ms += a; st->walk_ms += b; st->reduce_ms += c;
     st->steps += cnt[0]; st->integrated += cnt[1]; st->node_visits += cnt[2];
+    st->node_passes += cnt[3]; st->packed_passes += cnt[4];
     st->ray_channels += (unsigned long long)cam.nrays * nfr * nl;
     st->nrays = cam.nrays; st->nfr = nfr; st->kmax = md->kmax; st->nlines += nl;
   }

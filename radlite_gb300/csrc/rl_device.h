@@ -5,6 +5,9 @@
 
 namespace rl {
 
+// Counters of a walk launch (flush_counters): steps, integrated pairs, node visits, node
+// passes, packed node passes, spare.
+constexpr int kWalkCounters = 8;
 // Walk launch shape: 4-warp blocks, at most this many per SM (sizes the list scratch).
 constexpr int kWalkBlocksPerSm = 4;
 constexpr int kWalkWarps = 4;
@@ -23,6 +26,8 @@ constexpr unsigned kFlagHole = 1u << 20;   // segment ending here lies in the ce
 constexpr unsigned kFlagIr1 = 1u << 21;    // node on the innermost radial cell (ir == 1)
 constexpr unsigned kFlagInit = 1u << 22;   // (walk) the segment ending here restarts the line state
 constexpr unsigned kFlagSub = 1u << 23;    // (walk) the segment ending here may need sub-steps
+constexpr unsigned kFlagNeg = 1u << 24;    // (FP32 walk) some staged line lacks a positive opacity at
+                                           // this node or the previous one
 constexpr int kIcrShift = 18;              // bits 18-19: crossing type 1..3
 
 // Node records of all rays of one camera, row-major by ray (row stride kmax).

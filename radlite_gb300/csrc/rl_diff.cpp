@@ -46,6 +46,7 @@ struct rl_diff {
   int ncell = 0, nfr = 0, kmax = 0, cpl = 8, gsize = 1, adj_blocks = 0;
   Camera cam;
   std::vector<double> scale;
+  bool has_isrf = false;   // star holds the outer-boundary-3 start table too
   // node records of this camera (own copy: the widths change with the parameters)
   DevBuf x0, z0, ri, nn, st, ds, dvf, vl, dvs, lw, wr, wt, c00, misc;
   // LTE constants and per-line channel data
@@ -84,7 +85,7 @@ WalkParams<T> walk_params(const rl_diff* d) {
   P.nitems = ((d->nl + d->gsize - 1) / d->gsize) * d->cam.nrays;
   P.tab = d->tab.as<T>(); P.nsum = d->nsum.as<T>(); P.wch = d->wch.as<T>(); P.velo = d->velo.as<double>();
   P.star = d->star.as<T>(); P.lc = d->lc.as<LineConst<T>>();
-  P.isrf = isrf_of(m, P.star, d->nl, d->nfr);
+  P.isrf = isrf_of(d->has_isrf, P.star, d->nl, d->nfr);
   P.aksmax_c = m.aksmax / 2.99792458e5;
   P.kq = (T)(3.33567e-6 * 2.99792458e5);
   P.fstar = (T)((m.rstar / d->cam.ri[1]) * (m.rstar / d->cam.ri[1]));
@@ -145,6 +146,7 @@ int create(rl_diff* d) {
   LineTables<T> lt;
   if (build_line_tables<T>(m, d->iline0, d->nl, lt, err)) return set_err(ctx, RL_ERR_ARG, err);
   d->scale = lt.scale;
+  d->has_isrf = lt.has_isrf;
   // LTE constants
   const int nl = d->nl, ncell = d->ncell;
   std::vector<double> Ek(m.nlev), lng(m.nlev);
@@ -209,7 +211,7 @@ int create(rl_diff* d) {
   CUDA_TRY(d->width.ensure(sizeof(double) * ncell));
   CUDA_TRY(d->img.ensure(sizeof(T) * (size_t)nl * cam.nrays * d->nfr));
   CUDA_TRY(d->ring.ensure(sizeof(double) * (size_t)nl * (cam.nrr + 1) * d->nfr));
-  CUDA_TRY(d->cnt.ensure(sizeof(unsigned long long) * 4));
+  CUDA_TRY(d->cnt.ensure(sizeof(unsigned long long) * kWalkCounters));
   CUDA_TRY(d->work.ensure(sizeof(int)));
   CUDA_TRY(d->err.ensure(sizeof(int)));
   CUDA_TRY(d->list.ensure(sizeof(unsigned short) * walk_list_elems(ctx->nsm, d->nfr)));
@@ -268,7 +270,7 @@ int forward(rl_diff* d, const double* lnT, const double* lnX, const double* widt
   CUDA_TRY(launch_lte<T>(L, s));
   CUDA_TRY(cudaMemcpyAsync(d->width.p, width, sizeof(double) * d->ncell, cudaMemcpyDeviceToDevice, s));
   CUDA_TRY(launch_node_lw<T>(nodes<T>(d), d->width.as<double>(), m.nth, s));
-  CUDA_TRY(cudaMemsetAsync(d->cnt.p, 0, sizeof(unsigned long long) * 4, s));
+  CUDA_TRY(cudaMemsetAsync(d->cnt.p, 0, sizeof(unsigned long long) * kWalkCounters, s));
   CUDA_TRY(cudaMemsetAsync(d->work.p, 0, sizeof(int), s));
   CUDA_TRY(cudaMemsetAsync(d->err.p, 0, sizeof(int), s));
   CUDA_TRY(cudaEventRecord(ctx->ev[1], s));
@@ -418,7 +420,7 @@ int batch_build(rl_diff_batch* b) {
   CUDA_TRY(b->g_width.ensure(sizeof(double) * b->ncell));
   CUDA_TRY(b->flux.ensure(sizeof(double) * b->nflux));
   CUDA_TRY(b->gflux.ensure(sizeof(double) * b->nflux));
-  CUDA_TRY(b->cnt.ensure(sizeof(unsigned long long) * 4));
+  CUDA_TRY(b->cnt.ensure(sizeof(unsigned long long) * kWalkCounters));
   CUDA_TRY(b->acnt.ensure(sizeof(unsigned long long) * 4));
   CUDA_TRY(b->work.ensure(sizeof(int)));
   CUDA_TRY(b->awork.ensure(sizeof(int)));
@@ -507,7 +509,7 @@ cudaError_t batch_enqueue(rl_diff_batch* b, int dir, cudaStream_t s) {
                             cudaMemcpyDeviceToDevice, s);
       if (e == cudaSuccess) e = launch_node_lw<T>(nodes<T>(d), d->width.as<double>(), d->md->m.nth, s);
     }
-    if (e == cudaSuccess) e = cudaMemsetAsync(b->cnt.p, 0, sizeof(unsigned long long) * 4, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->cnt.p, 0, sizeof(unsigned long long) * kWalkCounters, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->err.p, 0, sizeof(int), s);
     if (e == cudaSuccess) e = launch_jobs<T>(launch_of<T>(b), s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(b->cnt_h, b->cnt.p, sizeof(unsigned long long) * 4, cudaMemcpyDeviceToHost, s);

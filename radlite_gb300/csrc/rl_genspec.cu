@@ -140,16 +140,16 @@ __global__ void k_gs_fine(GsParams p) {
 
 // Gaussian smoothing (scipy.ndimage.convolve, mode 'reflect'), normalised by the kernel
 // sum (radlite.py:3147-3152). The kernel is symmetric; its centre is nk/2, one sample to
-// the left for an even length.
+// the left for an even length. The reflected extension (d c b a | a b c d | d c b a)
+// repeats with period 2n, which matters for kernels longer than the grid.
 __global__ void k_gs_smooth(GsParams p) {
   const int n = p.nfine;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     double se = 0.0, sy = 0.0;
     for (int j = 0; j < p.nk; j++) {
-      int t = i + j - p.kc;
-      if (t < 0) t = -t - 1;
+      int t = (i + j - p.kc) % (2 * n);
+      if (t < 0) t += 2 * n;
       if (t >= n) t = 2 * n - t - 1;
-      t = t < 0 ? 0 : (t >= n ? n - 1 : t);   // kernels longer than the grid
       const double w = p.kern[p.nk - 1 - j];
       se = __dadd_rn(se, __dmul_rn(p.full_em[t], w));
       sy = __dadd_rn(sy, __dmul_rn(p.full_y[t], w));

@@ -56,37 +56,56 @@ struct Grid {
 RL_HD double Rg(const Grid& g, int ix) { return g.R[ix + 1]; }
 RL_HD double Tg(const Grid& g, int iy) { return g.TH[iy + 1]; }
 
-// Bracketing search: j with xx(j) <= x < xx(j+1), 0 or n out of range. Starts from a
-// guess, expands, then bisects, like hunt (nrecip.F:157-197); xx is 1-based via acc().
+// Bracketing search of x in the monotonic table xx(1..n) (1-based via acc()) from the guess
+// g, with the index rules of RADLite's hunt (nrecip.F:157-197), stated here:
+//   past(j):   x >= xx(j) in an ascending table (xx(n) > xx(1)), x < xx(j) otherwise
+//   before(j): the opposite comparison, x < xx(j) ascending, x >= xx(j) otherwise
+//   beyond(j): x > xx(j) ascending, x <= xx(j) otherwise
+// 1. Bracket [L, H]. A guess outside 1..n gives L = 0, H = n + 1. Otherwise nodes are
+//    probed at distances 1, 3, 7, 15, ... (2^i - 1) from g: if past(g), upwards while the
+//    probe is <= n and past(probe) (L = the last node passed, g at least; H = the first
+//    probe that is not, n + 1 past the end); else downwards while the probe is >= 1 and
+//    before(probe) (H = the last such probe, g at least; L = the first probe that is not,
+//    0 past the start).
+// 2. Result: L plus the number of nodes strictly inside the bracket that x lies beyond; in
+//    a monotonic table they come first, so a binary search counts them.
+// So x equal to a node value xx(k) gives k when the bracket stopped on k (k = L), and k - 1
+// when k lies strictly inside the bracket: r-crossings land exactly on nodes, and which
+// cell they are assigned to follows these rules.
 template <class Acc>
-RL_HD int hunt(const Acc& acc, int n, double x, int jlo) {
-  const bool ascnd = acc(n) > acc(1);
-  int jhi;
-  if (jlo <= 0 || jlo > n) {
-    jlo = 0;
-    jhi = n + 1;
-  } else {
-    int inc = 1;
-    if ((x >= acc(jlo)) == ascnd) {
-      for (;;) {
-        jhi = jlo + inc;
-        if (jhi > n) { jhi = n + 1; break; }
-        if ((x >= acc(jhi)) == ascnd) { jlo = jhi; inc += inc; } else break;
+RL_HD int hunt(const Acc& acc, int n, double x, int g) {
+  const bool asc = acc(n) > acc(1);
+  int L = 0, H = n + 1;
+  if (g >= 1 && g <= n) {
+    if (asc ? x >= acc(g) : x < acc(g)) {
+      L = g;
+      for (int d = 1; ; d = 2 * d + 1) {
+        const int p = g + d;
+        if (p > n) break;
+        if (!(asc ? x >= acc(p) : x < acc(p))) { H = p; break; }
+        L = p;
       }
     } else {
-      jhi = jlo;
-      for (;;) {
-        jlo = jhi - inc;
-        if (jlo < 1) { jlo = 0; break; }
-        if ((x < acc(jlo)) == ascnd) { jhi = jlo; inc += inc; } else break;
+      H = g;
+      for (int d = 1; ; d = 2 * d + 1) {
+        const int p = g - d;
+        if (p < 1) break;
+        if (!(asc ? x < acc(p) : x >= acc(p))) { L = p; break; }
+        H = p;
       }
     }
   }
-  while (jhi - jlo != 1) {
-    const int jm = (jhi + jlo) / 2;
-    if ((x > acc(jm)) == ascnd) jlo = jm; else jhi = jm;
+  int first = L + 1, count = H - L - 1;   // candidates L+1 .. H-1
+  while (count > 0) {
+    const int half = count >> 1;
+    if (asc ? x > acc(first + half) : x <= acc(first + half)) {
+      first += half + 1;
+      count -= half + 1;
+    } else {
+      count = half;
+    }
   }
-  return jlo;
+  return first - 1;
 }
 
 struct RAcc { const Grid* g; RL_HD double operator()(int j) const { return Rg(*g, j); } };

@@ -76,6 +76,7 @@ struct LineTables {
   std::vector<LineConst<T>> lc;
   std::vector<double> scale; // [nl]
   std::vector<char> mase;    // [nl] the line has a population inversion somewhere
+  bool has_isrf = false;     // star holds the outer-boundary-3 start table after the stellar one
 };
 template <typename T>
 int build_line_tables(const Model& m, int iline0, int nl, LineTables<T>& out, std::string& err,
@@ -111,8 +112,8 @@ struct MaserFlags {
 };
 
 template <typename T>
-inline const T* isrf_of(const Model& m, const T* dstar, int nl, int nfr) {
-  return m.outer_bc == 3 ? dstar + (size_t)nl * nfr : nullptr;
+inline const T* isrf_of(bool has_isrf, const T* dstar, int nl, int nfr) {
+  return has_isrf ? dstar + (size_t)nl * nfr : nullptr;
 }
 
 // Node records of a ray set (NodeBuf's arrays), grown on demand.
@@ -180,6 +181,7 @@ struct rl_model {
   int tab_line0 = -1, tab_nl = 0, tab_prec = -1;
   std::vector<double> tab_scale;
   std::vector<char> tab_mase;
+  bool tab_isrf = false;
   // masing found by the last render of each line of the molecule (spectrum or cube)
   std::vector<char> masing;
   // position-velocity cube: the image request and its buffers

@@ -15,7 +15,6 @@
 #include <cuda_runtime.h>
 
 #include <cstdio>
-#include <mutex>
 #include <string>
 
 #include "../../include/rlgpu.h"
@@ -34,37 +33,19 @@ namespace {
 constexpr size_t kRingScratchDoubles = size_t(1) << 20;
 static __device__ __align__(256) double g_ring_scratch[kRingScratchDoubles];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mu;
-double* g_scratch_addr[kMaxDevices] = {};
-
-// Device address of the scratch on the current device. Looked up once per device, with
-// that device current; the look-up loads the module, so the first call on a device
-// should not happen inside a stream capture.
+// Device address of the scratch on the current device, looked up on every call with that
+// device current. A cached address would outlive a cudaDeviceReset or a change of the
+// current context, after which it no longer names memory of this process; the look-up is
+// cheap once the module is loaded. The first look-up in a context loads the module, so
+// the first call in a context should not happen inside a stream capture.
 int scratch_for_current_device(double** out) {
-  int dev = -1;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) {
-    rl::set_last_error(std::string("rl_image_to_spectrum_noalloc: cudaGetDevice: ") + cudaGetErrorString(e));
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_ring_scratch);
+  if (e != cudaSuccess || !p) {
+    rl::set_last_error(std::string("rl_image_to_spectrum_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
     return RL_ERR_CUDA;
   }
-  if (dev < 0 || dev >= kMaxDevices) {
-    rl::set_last_error("rl_image_to_spectrum_noalloc: device index " + std::to_string(dev) +
-                       " beyond the supported " + std::to_string(kMaxDevices));
-    return RL_ERR_ARG;
-  }
-  std::lock_guard<std::mutex> lk(g_setup_mu);
-  if (!g_scratch_addr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_ring_scratch);
-    if (e != cudaSuccess || !p) {
-      rl::set_last_error(std::string("rl_image_to_spectrum_noalloc: cudaGetSymbolAddress: ") +
-                         cudaGetErrorString(e));
-      return RL_ERR_CUDA;
-    }
-    g_scratch_addr[dev] = static_cast<double*>(p);
-  }
-  *out = g_scratch_addr[dev];
+  *out = static_cast<double*>(p);
   return RL_OK;
 }
 

@@ -176,7 +176,7 @@ static int run_posvel(rl_model* md, int iline0, int nl, double* I_out, double* t
     CUDA_TRY(md->dstar.ensure(sizeof(T) * lt.star.size()));
     CUDA_TRY(md->dvelo.ensure(sizeof(double) * lt.velo.size()));
     CUDA_TRY(md->dlc.ensure(sizeof(LineConst<T>) * lt.lc.size()));
-    CUDA_TRY(md->dcnt.ensure(sizeof(unsigned long long) * 4));
+    CUDA_TRY(md->dcnt.ensure(sizeof(unsigned long long) * kWalkCounters));
     CUDA_TRY(md->dwork.ensure(sizeof(int)));
     CUDA_TRY(md->derr.ensure(sizeof(int)));
     CUDA_TRY(md->dlist.ensure(sizeof(unsigned short) * walk_list_elems(ctx->nsm, nfr)));
@@ -187,7 +187,7 @@ static int run_posvel(rl_model* md, int iline0, int nl, double* I_out, double* t
     CUDA_TRY(h2d(md->dstar.p, lt.star.data(), sizeof(T) * lt.star.size(), s));
     CUDA_TRY(h2d(md->dvelo.p, lt.velo.data(), sizeof(double) * lt.velo.size(), s));
     CUDA_TRY(h2d(md->dlc.p, lt.lc.data(), sizeof(LineConst<T>) * lt.lc.size(), s));
-    CUDA_TRY(cudaMemsetAsync(md->dcnt.p, 0, sizeof(unsigned long long) * 4, s));
+    CUDA_TRY(cudaMemsetAsync(md->dcnt.p, 0, sizeof(unsigned long long) * kWalkCounters, s));
     CUDA_TRY(cudaMemsetAsync(md->dwork.p, 0, sizeof(int), s));
     CUDA_TRY(cudaMemsetAsync(md->derr.p, 0, sizeof(int), s));
     CUDA_TRY(cudaEventRecord(ctx->ev[1], s));

@@ -33,9 +33,84 @@ __device__ __forceinline__ void kahan_add(T& s, T& c, T x) {
 // image position), and no star mixing.
 // The list entries carry item line indices; lbase is the item line of l0 (the tile's first
 // line), so that entry line - lbase indexes the tile's staged lines 0..gl-1.
+// Packed FP32 pairs (sm_100 and later): one instruction works on two independent slots.
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+  unsigned long long ra, rb, rd;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(ra) : "f"(a.x), "f"(a.y));
+  asm("mov.b64 %0, {%1, %2};" : "=l"(rb) : "f"(b.x), "f"(b.y));
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(rd) : "l"(ra), "l"(rb));
+  float2 d;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(d.x), "=f"(d.y) : "l"(rd));
+  return d;
+}
+__device__ __forceinline__ float2 dup2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float ex2(float x) {   // 2^x on the MUFU pipe
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// Math<float>::series and ::direct on a pair of optical depths, with the same roundings
+// per element.
+__device__ __forceinline__ void series2(float2 d, float2& x, float2& a, float2& b) {
+  const float2 nd = make_float2(-d.x, -d.y);
+  float2 t = fma2(d, dup2(-1.f / 5040.f), dup2(1.f / 720.f));
+  t = fma2(nd, t, dup2(1.f / 120.f));
+  t = fma2(nd, t, dup2(1.f / 24.f));
+  t = fma2(nd, t, dup2(1.f / 6.f));
+  t = fma2(nd, t, dup2(0.5f));
+  b = mul2(d, t);
+  const float2 e0 = fma2(nd, b, d);
+  x = sub2(dup2(1.f), e0);
+  a = sub2(e0, b);
+}
+__device__ __forceinline__ void direct2(float2 d, float2& x, float2& a, float2& b) {
+  const float2 m = mul2(d, dup2(-1.4426950408889634f));
+  x = make_float2(ex2(m.x), ex2(m.y));
+  const float2 e0 = sub2(dup2(1.f), x);
+  b = mul2(sub2(d, e0), make_float2(Math<float>::rcp(d.x), Math<float>::rcp(d.y)));
+  a = sub2(e0, b);
+}
+
+// Thin-step switch of qdr_src_2 (transfer.F:1545-1549: Q = 0.5 (j1+j2) ds unless the
+// optical depth exceeds the REAL literal 1e-9) without a compare: sat(2^100 (c - dt)) is 1
+// for dt <= 1e-9f and 0 above (c is the next float above 1e-9f, scaled exactly by 2^100).
+constexpr float kThinScale = 1.2676506002282294e30f;   // 2^100
+constexpr float kThinBias = 1.00000008e-9f * 1.2676506002282294e30f;
+
+// Segment-dependent SUBGRID quantities (line.F:4703-4742): the refinement measure q =
+// |dvmu1 - dvmu0| / (width / c), 1/ds, 1/(vl1 - vl0), the refined window half width
+// 3 l = 3 ds/q and the spacing lg of its 31-point grid.
+template <typename T>
+struct SegGeom { T q, ids, idvs, hw3, lg, ilg; };
+template <typename T>
+__device__ __forceinline__ SegGeom<T> seg_geom(T ds, T dvs, T rlw, T kq) {
+  SegGeom<T> g;
+  g.q = (dvs < (T)0 ? -dvs : dvs) * kq * rlw;
+  g.ids = ds > (T)0 ? Math<T>::div((T)1, ds) : (T)0;
+  const T dls = g.q > (T)0 ? Math<T>::div(ds, g.q) : (T)0;
+  g.idvs = dvs != (T)0 ? Math<T>::div((T)1, dvs) : (T)0;
+  g.hw3 = (T)3 * dls;
+  g.lg = (T)6 * dls / (T)30;
+  g.ilg = dls > (T)0 ? Math<T>::div((T)30, (T)6 * dls) : (T)0;
+  return g;
+}
+
+struct WalkCounters { unsigned long long steps = 0, integ = 0, nodes = 0, passes = 0, packed = 0; };
+
 template <typename T, int C, bool PV = false>
 __device__ long long walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<T, C>& SS, SubWork<T>& SW, int ray,
-                              int K, int l0, int gl, const unsigned short* list, int nt, int lane, int lbase) {
+                              int K, int l0, int gl, const unsigned short* list, int nt, int lane, int lbase,
+                              WalkCounters& wc) {
+  // FP32 circular image: steps whose two nodes have positive opacity in every line of the
+  // tile, with no state reset and no SUBGRID refinement, run packed (two slots per
+  // instruction) without the source-function fallbacks of qdr_src_2, which are the
+  // identity there. All other steps, and the FP64 and position-velocity walks, take the
+  // general path.
+  constexpr bool kFast = sizeof(T) == 4 && !PV;
   const NodeBuf<T>& nb = P.nb;
   const size_t row = (size_t)ray * nb.kmax;
   const int nl = P.nlines;
@@ -70,14 +145,16 @@ __device__ long long walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState
     }
   }
   long long steps = 0;
+  unsigned long long packed = 0, passes = 0;   // packed node passes, all node passes
   unsigned mbits = 0;   // tile lines whose line opacity x segment length fell below -0.01
   T lw_last = 0;
+  bool pos_last = true;
   for (int kb = 0; kb < K; kb += 32) {
     if (kb > 0) {   // carry the last node of the previous chunk into entry 0
       if (lane == 0) {
         S.vl[0] = S.vl[32]; S.hds[0] = S.hds[32]; S.ds[0] = S.ds[32]; S.rlw[0] = S.rlw[32];
-        S.q[0] = S.q[32]; S.ids[0] = S.ids[32]; S.dvs[0] = S.dvs[32]; S.flags[0] = S.flags[32];
-        S.idvs[0] = S.idvs[32]; S.hw3[0] = S.hw3[32]; S.lg[0] = S.lg[32]; S.ilg[0] = S.ilg[32];
+        S.dvs[0] = S.dvs[32]; S.flags[0] = S.flags[32];
+        if constexpr (kFast) { S.hot[0][0] = S.hot[32][0]; S.hot[0][1] = S.hot[32][1]; }
       }
       if (lane < gl) S.lv[lane][0] = S.lv[lane][32];
       __syncwarp();
@@ -85,12 +162,17 @@ __device__ long long walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState
     const int k = kb + lane;
     T vl = 0, ds = 0, dvs = 0, lwk = 0;
     unsigned misc = 0;
+    bool pos = true;   // every staged line has a normal dust opacity and no inversion here
     if (k < K) {
       const size_t o = row + k;
       const T wr = nb.wr[o], wt = nb.wt[o];
       misc = nb.misc[o];
       const Corners c = corners(nb.c00[o], misc, P.nth);
-      for (int l = 0; l < gl; l++) S.lv[l][lane + 1] = interp_lv(P.tab, c, nl, l0 + l, wr, wt);
+      for (int l = 0; l < gl; l++) {
+        const LineVals<T> v = interp_lv(P.tab, c, nl, l0 + l, wr, wt);
+        S.lv[l][lane + 1] = v;
+        if constexpr (kFast) pos = pos && v.ad >= 1.17549435e-38f && v.af >= 0.f;
+      }
       vl = nb.vl[o]; ds = nb.ds[o]; dvs = nb.dvseg[o]; lwk = nb.lw[o];
     }
     T lwp = __shfl_up_sync(0xffffffffu, lwk, 1);
@@ -99,22 +181,23 @@ __device__ long long walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState
     const T lwav = (T)0.5 * (lwp + lwk);
     const T rlw = lwav > (T)0 ? Math<T>::div((T)1, lwav) : (T)0;
     S.vl[lane + 1] = vl; S.hds[lane + 1] = (T)0.5 * ds; S.ds[lane + 1] = ds; S.rlw[lane + 1] = rlw;
-    S.q[lane + 1] = (dvs < (T)0 ? -dvs : dvs) * P.kq * rlw;
-    S.ids[lane + 1] = ds > (T)0 ? Math<T>::div((T)1, ds) : (T)0;
     S.dvs[lane + 1] = dvs;
-    {
-      // refined window half width 3 l = 3 ds/q and the spacing of its 31-point grid
-      const T qv = S.q[lane + 1];
-      const T dls = qv > (T)0 ? Math<T>::div(ds, qv) : (T)0;
-      S.idvs[lane + 1] = dvs != (T)0 ? Math<T>::div((T)1, dvs) : (T)0;
-      S.hw3[lane + 1] = (T)3 * dls;
-      S.lg[lane + 1] = (T)6 * dls / (T)30;
-      S.ilg[lane + 1] = dls > (T)0 ? Math<T>::div((T)30, (T)6 * dls) : (T)0;
-    }
     {
       unsigned f = misc;
       if (k == 1 || (misc & kFlagHole) || k == star_node) f |= kFlagInit;
-      if ((T)6 * S.q[lane + 1] > (T)1) f |= kFlagSub;
+      if ((T)6 * ((dvs < (T)0 ? -dvs : dvs) * P.kq * rlw) > (T)1) f |= kFlagSub;
+      if constexpr (kFast) {
+        // the step ending at this node needs both of its nodes positive
+        bool posp = __shfl_up_sync(0xffffffffu, pos, 1);
+        if (lane == 0) posp = pos_last;
+        pos_last = __shfl_sync(0xffffffffu, pos, 31);
+        if (!(pos && posp)) f |= kFlagNeg;
+        // node values of the packed step, duplicated into pairs: {vl, vl, hds, hds},
+        // {rl, rl} (the profile's 1/width)
+        const float h = 0.5f * (float)ds;
+        S.hot[lane + 1][0] = make_float4((float)vl, (float)vl, h, h);
+        S.hot[lane + 1][1] = make_float4((float)rlw, (float)rlw, 0.f, 0.f);
+      }
       S.flags[lane + 1] = f;
     }
     __syncwarp();
@@ -149,9 +232,84 @@ __device__ long long walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState
           }
         }
       }
+      passes += nn - n0;
       for (int n = n0; n < nn; n++) {
         const int g = kb + n;
         const unsigned fl = S.flags[n + 1];
+        if constexpr (kFast) {
+          bool slow = (fl & (kFlagInit | kFlagNeg)) != 0;
+          if (!slow && (fl & kFlagSub)) {
+            // a SUBGRID window that overlaps the segment sends the node to the general path
+            const T vl0 = S.vl[n], dsf = S.ds[n + 1];
+            const SegGeom<T> G = seg_geom<T>(dsf, S.dvs[n + 1], S.rlw[n + 1], P.kq);
+            bool any = false;
+#pragma unroll
+            for (int u = 0; u < kPass; u++) {
+              const T s_c = dsf * (w[u] - vl0) * G.idvs;
+              any = any || (Ls[u] >= 0 && (s_c + G.hw3 > (T)0) && (s_c - G.hw3 < dsf));
+            }
+            slow = __any_sync(0xffffffffu, any);
+          }
+          if (!slow) {
+            const float4 h0 = S.hot[n + 1][0], h1 = S.hot[n + 1][1];
+            const float2 vl2 = make_float2(h0.x, h0.y), hd2 = make_float2(h0.z, h0.w);
+            const float2 rl2 = make_float2(h1.x, h1.y);
+            float2 j1[2], a1[2], S1[2], dt[2], th[2];
+            bool ser = true, dir = true;
+#pragma unroll
+            for (int p = 0; p < 2; p++) {
+              const LineVals<T> vA = S.lv[lsl[2 * p]][n + 1], vB = S.lv[lsl[2 * p + 1]][n + 1];
+              const float2 u = mul2(sub2(make_float2(w[2 * p], w[2 * p + 1]), vl2), rl2);
+              const float2 m = mul2(mul2(u, u), dup2(-1.4426950408889634f));
+              const float2 ph = mul2(rl2, make_float2(ex2(m.x), ex2(m.y)));
+              j1[p] = make_float2(fmaf(vA.jf, ph.x, vA.jd), fmaf(vB.jf, ph.y, vB.jd));
+              a1[p] = make_float2(fmaf(vA.af, ph.x, vA.ad), fmaf(vB.af, ph.y, vB.ad));
+              S1[p] = mul2(j1[p], make_float2(Math<float>::rcp(a1[p].x), Math<float>::rcp(a1[p].y)));
+              dt[p] = mul2(add2(make_float2(a0[2 * p], a0[2 * p + 1]), a1[p]), hd2);
+              th[p] = mul2(add2(make_float2(j0[2 * p], j0[2 * p + 1]), j1[p]), hd2);
+              const bool sa = dt[p].x < 0.25f, sb = dt[p].y < 0.25f;
+              ser = ser && sa && sb;
+              dir = dir && !sa && !sb;
+            }
+            ser = __all_sync(0xffffffffu, ser);
+            dir = __all_sync(0xffffffffu, dir);
+            float2 x[2], ca[2], cb[2];
+            if (ser) {
+#pragma unroll
+              for (int p = 0; p < 2; p++) series2(dt[p], x[p], ca[p], cb[p]);
+            } else if (dir) {
+#pragma unroll
+              for (int p = 0; p < 2; p++) direct2(dt[p], x[p], ca[p], cb[p]);
+            } else {
+#pragma unroll
+              for (int p = 0; p < 2; p++) {
+                float2 xs, as, bs, xd, ad, bd;
+                series2(dt[p], xs, as, bs);
+                direct2(dt[p], xd, ad, bd);
+                const bool sa = dt[p].x < 0.25f, sb = dt[p].y < 0.25f;
+                x[p] = make_float2(sa ? xs.x : xd.x, sb ? xs.y : xd.y);
+                ca[p] = make_float2(sa ? as.x : ad.x, sb ? as.y : ad.y);
+                cb[p] = make_float2(sa ? bs.x : bd.x, sb ? bs.y : bd.y);
+              }
+            }
+#pragma unroll
+            for (int p = 0; p < 2; p++) {
+              const float2 Q = fma2(ca[p], make_float2(S0[2 * p], S0[2 * p + 1]), mul2(cb[p], S1[p]));
+              const float2 thin = make_float2(__saturatef(fmaf(dt[p].x, -kThinScale, kThinBias)),
+                                              __saturatef(fmaf(dt[p].y, -kThinScale, kThinBias)));
+              const float2 Qb = fma2(thin, dup2(3.0e38f), Q);
+              const float2 q = make_float2(fminf(Qb.x, th[p].x), fminf(Qb.y, th[p].y));
+              const float2 In = fma2(make_float2(I[2 * p], I[2 * p + 1]), x[p], q);
+              I[2 * p] = In.x; I[2 * p + 1] = In.y;
+              j0[2 * p] = j1[p].x; j0[2 * p + 1] = j1[p].y;
+              a0[2 * p] = a1[p].x; a0[2 * p + 1] = a1[p].y;
+              S0[2 * p] = S1[p].x; S0[2 * p + 1] = S1[p].y;
+            }
+            steps += nv;
+            packed++;
+            continue;
+          }
+        }
         if (g == star_node) {
 #pragma unroll
           for (int u = 0; u < kPass; u++)
@@ -168,12 +326,14 @@ __device__ long long walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState
           bool any = false;
 #pragma unroll
           for (int u = 0; u < kPass; u++) ov[u] = false;
+          SegGeom<T> G = {};
           if (fl & kFlagSub) {
-            const T vl0 = S.vl[n], dsf = S.ds[n + 1], hw3 = S.hw3[n + 1];
+            const T vl0 = S.vl[n], dsf = S.ds[n + 1];
+            G = seg_geom<T>(dsf, S.dvs[n + 1], rl, P.kq);
 #pragma unroll
             for (int u = 0; u < kPass; u++) {
-              const T s_c = sizeof(T) == 8 ? dsf * (w[u] - vl0) / S.dvs[n + 1] : dsf * (w[u] - vl0) * S.idvs[n + 1];
-              ov[u] = Ls[u] >= 0 && (s_c + hw3 > (T)0) && (s_c - hw3 < dsf);
+              const T s_c = sizeof(T) == 8 ? dsf * (w[u] - vl0) / S.dvs[n + 1] : dsf * (w[u] - vl0) * G.idvs;
+              ov[u] = Ls[u] >= 0 && (s_c + G.hw3 > (T)0) && (s_c - G.hw3 < dsf);
               any = any || ov[u];
             }
             any = __any_sync(0xffffffffu, any);
@@ -184,8 +344,8 @@ __device__ long long walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState
           for (int u = 0; u < kPass; u++) {
             const LineVals<T> v = S.lv[lsl[u]][n + 1];
             const T ph = profile(w[u], vl1, rl, rl);
-            j1[u] = v.jd + v.jf * ph;
-            a1[u] = v.ad + v.af * ph;
+            j1[u] = fmadd(v.jf, ph, v.jd);
+            a1[u] = fmadd(v.af, ph, v.ad);
             S1[u] = a1[u] > (T)0 ? j1[u] * Math<T>::rcp(a1[u]) : (T)0;
             dt[u] = (a0[u] + a1[u]) * hds;
             th[u] = (j0[u] + j1[u]) * hds;
@@ -210,10 +370,10 @@ __device__ long long walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState
           for (int u = 0; u < kPass; u++) {
             const T src1 = a0[u] > (T)0 ? S0[u] : S1[u];
             const T src2 = a1[u] > (T)0 ? S1[u] : S0[u];
-            T qv = dt[u] > (T)1.0e-9f ? ca[u] * src1 + cb[u] * src2 : th[u];
+            T qv = dt[u] > (T)1.0e-9f ? fmadd(ca[u], src1, cb[u] * src2) : th[u];
             qv = qv < th[u] ? qv : th[u];
             if (!ov[u]) {
-              I[u] = I[u] * x[u] + qv;
+              I[u] = fmadd(I[u], x[u], qv);
               j0[u] = j1[u]; a0[u] = a1[u]; S0[u] = S1[u];
               if constexpr (PV) kahan_add(tau[u], tcp[u], dt[u]);
             }
@@ -234,14 +394,13 @@ __device__ long long walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState
               cnt += __popc(m);
             }
             __syncwarp();
-            const T vl0 = S.vl[n], dsf = S.ds[n + 1], ids = S.ids[n + 1], hw3 = S.hw3[n + 1];
-            const T lgv = S.lg[n + 1], ilg = S.ilg[n + 1], idvs = S.idvs[n + 1], dvsg = S.dvs[n + 1];
+            const T vl0 = S.vl[n], dsf = S.ds[n + 1], dvsg = S.dvs[n + 1];
             for (int p = lane; p < cnt; p += 32) {
               const T wp = SW.w[p];
               const int lp = SW.l[p];
-              const T s_c = sizeof(T) == 8 ? dsf * (wp - vl0) / dvsg : dsf * (wp - vl0) * idvs;
-              const SlotOutT<T, PV> o = slot_sub<T, PV>(wp, S.lv[lp][n], S.lv[lp][n + 1], vl0, vl1, rl, dsf, ids,
-                                                        s_c - hw3, lgv, ilg, SW.I[p], SW.j0[p], SW.a0[p], SW.S0[p]);
+              const T s_c = sizeof(T) == 8 ? dsf * (wp - vl0) / dvsg : dsf * (wp - vl0) * G.idvs;
+              const SlotOutT<T, PV> o = slot_sub<T, PV>(wp, S.lv[lp][n], S.lv[lp][n + 1], vl0, vl1, rl, dsf, G.ids,
+                                                        s_c - G.hw3, G.lg, G.ilg, SW.I[p], SW.j0[p], SW.a0[p], SW.S0[p]);
               SW.I[p] = o.I; SW.j0[p] = o.j0; SW.a0[p] = o.a0; SW.S0[p] = o.S0;
               if constexpr (PV) SW.w[p] = o.dtau;   // the owner keeps w in a register
               steps += o.steps - 1;
@@ -258,12 +417,13 @@ __device__ long long walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState
           }
         } else {
           const bool init = true, sub = fl & kFlagSub;
-          const T vl0 = S.vl[n], q = S.q[n + 1], dsf = S.ds[n + 1], dvs = S.dvs[n + 1], ids = S.ids[n + 1];
+          const T vl0 = S.vl[n], dsf = S.ds[n + 1], dvs = S.dvs[n + 1];
+          const SegGeom<T> G = seg_geom<T>(dsf, dvs, rl, P.kq);
 #pragma unroll
           for (int u = 0; u < kPass; u++) {
             if (Ls[u] < 0) continue;
             const SlotOutT<T, PV> o = slot_slow<T, PV>(init, sub, w[u], S.lv[Ls[u]][n], S.lv[Ls[u]][n + 1], vl0, vl1,
-                                                       rl, hds, q, dsf, dvs, ids, I[u], j0[u], a0[u], S0[u]);
+                                                       rl, hds, G.q, dsf, dvs, G.ids, I[u], j0[u], a0[u], S0[u]);
             I[u] = o.I; j0[u] = o.j0; a0[u] = o.a0; S0[u] = o.S0; steps += o.steps;
             if constexpr (PV) kahan_add(tau[u], tcp[u], o.dtau);
           }
@@ -271,7 +431,8 @@ __device__ long long walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState
         if (P.maser) {
           // masing check of charintline (telescope.F:4291-4297): the line opacity at the
           // segment end (the next step's alpl0) times the segment length. Warp-uniform:
-          // only launches holding a line with a population inversion take it.
+          // only launches holding a line with a population inversion take it. (Packed
+          // steps have no inverted line, so they cannot meet it.)
           const T dsm = S.ds[n + 1];
 #pragma unroll
           for (int u = 0; u < kPass; u++)
@@ -294,10 +455,10 @@ __device__ long long walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState
     if (lane == 0)
       for (; mbits; mbits &= mbits - 1) atomicExch(&P.maser[l0 + __ffs(mbits) - 1], 1);
   }
+  wc.passes += passes;
+  wc.packed += packed;
   return steps;
 }
-
-struct WalkCounters { unsigned long long steps = 0, integ = 0, nodes = 0; };
 
 // One work item: line group g of ray `ray`, item = g * nrays + ray.
 template <typename T, int C, bool PV = false>
@@ -387,7 +548,7 @@ __device__ __forceinline__ void walk_item(const WalkParams<T>& P, int item, Warp
     const int te = min(tb + 32 * C, S.lineoff[lcap]);
     const int nt = te - tb;
     const int lz = (int)(list[te - 1] >> kChBits);
-    wc.steps += walk_ray<T, C, PV>(P, S, SS, SW, ray, K, l0 + la, lz - la + 1, list + tb, nt, lane, la);
+    wc.steps += walk_ray<T, C, PV>(P, S, SS, SW, ray, K, l0 + la, lz - la + 1, list + tb, nt, lane, la, wc);
     for (int j = 0; j < C; j++) {
       const int idx = j * 32 + lane;
       if (idx < nt) {
@@ -433,7 +594,7 @@ __device__ __forceinline__ void walk_item(const WalkParams<T>& P, int item, Warp
     __syncwarp();
     for (int tb = 0; tb < n2; tb += 32 * C) {
       const int nt = min(32 * C, n2 - tb);
-      wc.steps += walk_ray<T, C>(P, S, SS, SW, ray, K, l0 + l, 1, list + tb, nt, lane, l);
+      wc.steps += walk_ray<T, C>(P, S, SS, SW, ray, K, l0 + l, 1, list + tb, nt, lane, l, wc);
       for (int j = 0; j < C; j++) {
         const int idx = j * 32 + lane;
         if (idx < nt) img[list[tb + idx] & (kMaxChannels - 1)] = SS.I[j][lane];
@@ -482,6 +643,9 @@ struct WarpSmem {
   }
 };
 
+// counters[0] formal-solution steps, [1] integrated (line, channel) pairs, [2] node visits
+// (pairs x nodes), [3] node passes of the walk (a pass = the tile's slots over one node),
+// [4] of them taken on the packed FP32 path. The buffers hold kWalkCounters values.
 __device__ __forceinline__ void flush_counters(WalkCounters wc, unsigned long long* counters, int lane) {
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) wc.steps += __shfl_xor_sync(0xffffffffu, wc.steps, off);
@@ -489,6 +653,8 @@ __device__ __forceinline__ void flush_counters(WalkCounters wc, unsigned long lo
     atomicAdd(&counters[0], wc.steps);
     atomicAdd(&counters[1], wc.integ);
     atomicAdd(&counters[2], wc.nodes);
+    atomicAdd(&counters[3], wc.passes);
+    atomicAdd(&counters[4], wc.packed);
   }
 }
 

@@ -23,13 +23,18 @@ __device__ __forceinline__ int find_job(const int* __restrict__ prefix, int njob
 // ------------------------------------------------------------------------------------
 // walk: arithmetic helpers
 // ------------------------------------------------------------------------------------
+// a * b + c with one rounding, written out so that every walk variant (scalar, packed
+// pairs, the adjoint's recomputation) rounds each step alike
+__device__ __forceinline__ float fmadd(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fmadd(double a, double b, double c) { return __fma_rn(a, b, c); }
+
 template <typename T> struct Math;
 
 template <> struct Math<float> {
   // e^{-x} on the MUFU pipe
   static __device__ __forceinline__ float expneg(float x) {
     float y;
-    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(-1.4426950408889634f * x));
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(__fmul_rn(-1.4426950408889634f, x)));
     return y;
   }
   static __device__ __forceinline__ float rcp(float x) {
@@ -53,18 +58,24 @@ template <> struct Math<float> {
   }
   // d < 0.25: b from its Taylor series, e0 = d (1 - b), x = 1 - e0. Below d = 1e-6 the
   // reference uses a = b = d/2, x = 1 - d; the series agrees with that to O(d^2), below
-  // FP32 resolution, so FP32 needs no separate branch.
+  // FP32 resolution, so FP32 needs no separate branch. Horner form with one rounding per
+  // operation, as the packed walk evaluates it.
   static __device__ __forceinline__ void series(float d, float& x, float& a, float& b) {
-    b = d * (0.5f - d * (1.f / 6.f - d * (1.f / 24.f - d * (1.f / 120.f - d * (1.f / 720.f - d * (1.f / 5040.f))))));
-    const float e0 = d - d * b;
-    x = 1.f - e0;
-    a = e0 - b;
+    float t = __fmaf_rn(d, -1.f / 5040.f, 1.f / 720.f);
+    t = __fmaf_rn(-d, t, 1.f / 120.f);
+    t = __fmaf_rn(-d, t, 1.f / 24.f);
+    t = __fmaf_rn(-d, t, 1.f / 6.f);
+    t = __fmaf_rn(-d, t, 0.5f);
+    b = __fmul_rn(d, t);
+    const float e0 = __fmaf_rn(-d, b, d);
+    x = __fsub_rn(1.f, e0);
+    a = __fsub_rn(e0, b);
   }
   static __device__ __forceinline__ void direct(float d, float& x, float& a, float& b) {
     x = expneg(d);
-    const float e0 = 1.f - x;
-    b = (d - e0) * rcp(d);
-    a = e0 - b;
+    const float e0 = __fsub_rn(1.f, x);
+    b = __fmul_rn(__fsub_rn(d, e0), rcp(d));
+    a = __fsub_rn(e0, b);
   }
 };
 
@@ -92,6 +103,11 @@ __device__ __forceinline__ T profile(T w, T vl, T rlw, T nrm) {
   const T u = (w - vl) * rlw;
   return nrm * Math<T>::expneg(u * u);
 }
+template <>
+__device__ __forceinline__ float profile<float>(float w, float vl, float rlw, float nrm) {
+  const float u = __fmul_rn(__fsub_rn(w, vl), rlw);
+  return __fmul_rn(nrm, Math<float>::expneg(__fmul_rn(u, u)));
+}
 
 // One application of the linear-source formal solution (qdr_src_2, transfer.F:1498-1571)
 // from point 0 (j0, a0, S0) to point 1 (j1, a1, S1) over half-length hds. Returns the
@@ -104,9 +120,9 @@ __device__ __forceinline__ T formal(T& I, T j0, T a0, T S0, T j1, T a1, T S1, T 
   Math<T>::coeffs(dtau, x, a, b);
   const T src1 = a0 > (T)0 ? S0 : (a1 > (T)0 ? S1 : (T)0);
   const T src2 = a1 > (T)0 ? S1 : (a0 > (T)0 ? S0 : (T)0);
-  T q = dtau > (T)1.0e-9f ? a * src1 + b * src2 : theo;
+  T q = dtau > (T)1.0e-9f ? fmadd(a, src1, b * src2) : theo;
   q = q < theo ? q : theo;
-  I = I * x + q;
+  I = fmadd(I, x, q);
   return dtau;
 }
 
@@ -116,8 +132,8 @@ struct Pt { T jd, ad, jf, af, vl; };
 // point state: emissivity, extinction and own source function at the walk position
 template <typename T>
 __device__ __forceinline__ void point_state(const Pt<T>& p, T phi, T& j, T& a, T& S) {
-  j = p.jd + p.jf * phi;
-  a = p.ad + p.af * phi;
+  j = fmadd(p.jf, phi, p.jd);
+  a = fmadd(p.af, phi, p.ad);
   S = a > (T)0 ? j * Math<T>::rcp(a) : (T)0;
 }
 
@@ -138,8 +154,9 @@ struct alignas(16) LineVals { T jf, af, jd, ad; };
 template <typename T>
 struct WarpStage {
   LineVals<T> lv[kGroup][33];
-  T vl[33], hds[33], ds[33], rlw[33], q[33], ids[33], dvs[33], idvs[33], hw3[33], lg[33], ilg[33];
+  T vl[33], hds[33], ds[33], rlw[33], dvs[33];
   unsigned flags[33];
+  float4 hot[33][2];   // FP32 walk: per-node values of the packed step, as pairs
   T contv[kItemLines];
   float mn[kItemLines], mx[kItemLines];
   int cont_ch[kItemLines];

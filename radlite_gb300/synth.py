@@ -113,9 +113,10 @@ def config_by_name(name: str, **over) -> DiskConfig:
         "band_large": dict(name="band_large", nr=400, nt=200, perturb_sigma=0.1, seed=1,
                            molecule="band", ilinestart=1, nlines=20, vmax=24.875, dv=0.25,
                            nphi=256, dbdr=2, nrrextra=-192, incl_deg=20.0),
-        # 200x100 disk, 10 rotor lines, 128 channels, 600 rings x 128 azimuths
+        # 200x100 disk, 10 rotor lines, 128 channels (INT(2 vmax/dv + 1) = INT(128.05)),
+        # 600 rings x 128 azimuths
         "adjoint_disk": dict(name="adjoint_disk", nr=200, nt=100, ilinestart=1, nlines=10,
-                             vmax=25.4, dv=0.4, nphi=128, dbdr=2, nrrextra=-192),
+                             vmax=25.41, dv=0.4, nphi=128, dbdr=2, nrrextra=-192),
         # small cases that the FP64 oracle finishes in seconds
         "tiny_line": dict(name="tiny_line", nr=24, nt=12, nphi=16, dbdr=2, nrrextra=-6,
                           vmax=12.0, dv=0.75),
@@ -258,9 +259,13 @@ def _fmt_rows(arr, fmt="%.10e"):
     return "\n".join(fmt % v for v in np.asarray(arr).ravel()) + "\n"
 
 
-def write_model(cfg: DiskConfig, outdir: str) -> str:
+def write_model(cfg: DiskConfig, outdir: str, fields: dict | None = None) -> str:
+    """Write the model in the reference's file formats; `fields` replaces entries of
+    make_fields() (e.g. temp, dust_temp, abund, width, pop on the [it, ir] grid)."""
     os.makedirs(outdir, exist_ok=True)
     f = make_fields(cfg)
+    if fields:
+        f.update(fields)
     nr, nt = cfg.nr, cfg.nt
     P = lambda name: os.path.join(outdir, name)
 
@@ -420,6 +425,22 @@ def model_arrays(cfg: DiskConfig) -> dict:
 def cell_order(a):
     """[nt, nr] field -> the library's cell order (ir-1)*nth + (it-1)."""
     return np.asarray(a).T.ravel()
+
+
+def cells_to_grid(a, cfg: DiskConfig):
+    """The library's cell order (ir-1)*nth + (it-1) -> an [nt, nr] field (cell_order's inverse)."""
+    return np.asarray(a).reshape(cfg.nr, cfg.nt).T.copy()
+
+
+def lte_fields(cfg: DiskConfig, lnT, lnX, width) -> dict:
+    """make_fields() entries for per-cell parameters of the differentiable raytrace (library
+    cell order): gas and dust temperature, abundance, width, and the LTE populations the
+    differentiable path derives from the temperature (lte_arrays' energies). With
+    write_model(cfg, dir, fields=...) the reference's input files of that model."""
+    E, g, _ = molecule_levels(cfg)
+    T = cells_to_grid(np.exp(lnT), cfg)
+    return dict(temp=T, dust_temp=T.copy(), abund=cells_to_grid(np.exp(lnX), cfg), width=cells_to_grid(width, cfg),
+                pop=lte_populations(np.round(E, 4), g, T))
 
 
 def cell_params(cfg: DiskConfig):

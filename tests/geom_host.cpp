@@ -19,6 +19,15 @@ struct Collect {
 };
 }  // namespace
 
+namespace {
+struct Tab {
+  const double* xx;   // xx[0..n-1] as xx(1..n)
+  double operator()(int j) const { return xx[j - 1]; }
+};
+}  // namespace
+
+extern "C" int geom_hunt(const double* xx, int n, double x, int guess) { return rlg::hunt(Tab{xx}, n, x, guess); }
+
 extern "C" int geom_trace(int nr, int nth, const double* R, const double* TH, const double* tan2, double rstar,
                           double x0, double z0, double theta0, int cap, double* s, double* r, double* th, double* mu,
                           int* icr, int* ir, int* it, int* status) {

@@ -1,8 +1,9 @@
 """Writes golden vectors of the spectrum post-processing (RadliteSpectrum.gen_spec) by
 running the reference's own pyradlite code on seeded synthetic line profiles.
 
-Run from the repository root, where the reference tree is present:
-    python tests/golden/make_genspec_golden.py [path/to/pyradlite/pyradlite]
+Run from the repository root, where the reference tree is present, naming the reference's
+pyradlite package directory on the command line or in PYRADLITE_DIR:
+    python tests/golden/make_genspec_golden.py <reference>/pyradlite/pyradlite
 
 pyradlite imports astropy, matplotlib and its radmc helper at module level; none of them is
 installed here and none is used by the two methods exercised (_read_core_radliteoutput,
@@ -20,7 +21,14 @@ import numpy as np
 
 ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 sys.path.insert(0, ROOT)
-DEFAULT_REF = "/root/reference/pyradlite/pyradlite"
+
+
+def reference_path() -> str:
+    """The reference's pyradlite package directory: argv[1], else $PYRADLITE_DIR."""
+    p = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PYRADLITE_DIR")
+    if not p:
+        sys.exit(f"usage: python {sys.argv[0]} <reference>/pyradlite/pyradlite  (or set PYRADLITE_DIR)")
+    return p
 
 
 def _stub_modules():
@@ -122,7 +130,7 @@ def reader_case(radlite):
 
 
 def main():
-    radlite = import_reference(sys.argv[1] if len(sys.argv) > 1 else DEFAULT_REF)
+    radlite = import_reference(reference_path())
     here = os.path.dirname(os.path.abspath(__file__))
     for name, seed, n, groups, obsres, vsamp, dist in CASES:
         lines = synth_lines(seed, n, groups)

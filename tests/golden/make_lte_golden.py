@@ -3,7 +3,7 @@ pyradlite's own _prep_mol_forcore (radlite.py:1022-1121) on the ro-vibrational b
 of the synthetic models.
 
 Run from the repository root, where the reference tree is present:
-    python tests/golden/make_lte_golden.py [path/to/pyradlite/pyradlite]
+    python tests/golden/make_lte_golden.py <reference>/pyradlite/pyradlite   (or set PYRADLITE_DIR)
 
 pyradlite takes the unique levels from a HITRAN line list (lower and upper energies,
 degeneracies and quantum numbers per line) and divides g exp(-E hc/kT) by a partition sum
@@ -22,7 +22,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
-from make_genspec_golden import DEFAULT_REF, import_reference  # noqa: E402
+from make_genspec_golden import import_reference, reference_path  # noqa: E402
 from radlite_gb300 import synth  # noqa: E402
 
 CONFIG = "band_large"
@@ -59,7 +59,7 @@ def inputs():
 
 
 def main():
-    radlite = import_reference(sys.argv[1] if len(sys.argv) > 1 else DEFAULT_REF)
+    radlite = import_reference(reference_path())
     E, g, lines, hitran, temp = inputs()
     hck = radlite.h0 * radlite.c0 / radlite.kB0
     half = temp[: temp.shape[0] // 2]

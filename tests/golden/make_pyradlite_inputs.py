@@ -5,7 +5,7 @@ pyradlite's own writer methods (radlite.py:1739-2230) and its LTE populations
 (_prep_mol_forcore, radlite.py:1022-1121) on a small synthetic band disk.
 
 Run from the repository root, where the reference tree is present:
-    python tests/golden/make_pyradlite_inputs.py [path/to/pyradlite/pyradlite]
+    python tests/golden/make_pyradlite_inputs.py <reference>/pyradlite/pyradlite   (or set PYRADLITE_DIR)
 
 The files pyradlite does not write (grid, dust, frequencies, star, line.inp) come from the
 RADMC side of a real run; the tests take them from radlite_gb300.synth for the same model
@@ -24,7 +24,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
-from make_genspec_golden import DEFAULT_REF, import_reference  # noqa: E402
+from make_genspec_golden import import_reference, reference_path  # noqa: E402
 from radlite_gb300 import synth  # noqa: E402
 
 OUT = os.path.join(HERE, "pyradlite_band")
@@ -54,7 +54,7 @@ def config():
 
 
 def main():
-    radlite = import_reference(sys.argv[1] if len(sys.argv) > 1 else DEFAULT_REF)
+    radlite = import_reference(reference_path())
     cfg = config()
     f = synth.make_fields(cfg)
     E, g, lines = synth.molecule_levels(cfg)

@@ -43,6 +43,20 @@ def test_restatement_reproduces_reference(path):
         np.testing.assert_allclose(out[k], g["out"][k], rtol=1e-14, atol=0)
 
 
+def test_convolve_reflect_matches_scipy():
+    """The smoothing's reflected edges, as scipy.ndimage.convolve(mode='reflect') defines
+    them, also for kernels longer than the grid (period 2n). gen_spec's own grids always
+    make the fine grid longer than the kernel (3 obsres of box on each side)."""
+    nd = pytest.importorskip("scipy.ndimage")
+    from oracle import genspec_ref as G
+    rng = np.random.default_rng(3)
+    for n, m in ((40, 9), (40, 10), (5, 13), (7, 40), (3, 2), (4, 31), (1, 6)):
+        x = rng.random(n)
+        k = rng.random(m)
+        k = k + k[::-1]
+        np.testing.assert_allclose(G.convolve_reflect(x, k), nd.convolve(x, k, mode="reflect"), rtol=1e-13)
+
+
 def test_reader_matches_reference_reader(tmp_path):
     from oracle import genspec_ref as G
     from radlite_gb300 import genspec

@@ -105,3 +105,57 @@ def test_masing_query_arguments(gpu_lib, tmp_path):
         with pytest.raises(gpu_lib.RLError, match="line index"):
             m.masing(bad)
     m.free()
+
+
+@pytest.mark.gpu
+def test_batch_flags_match_oracle(gpu_lib, oracle_lib, tmp_path, capfd):
+    """A batch of the four models: each job's flag equals the oracle's, spectra as the
+    per-model renders; a manifest run prints the warning for the inverted directories."""
+    ctx = gpu_lib.Context(0)
+    models, want, dirs = [], [], []
+    b = gpu_lib.Batch(ctx)
+    for tag, k, shell, flag in CASES:
+        cfg, d = inverted_model(tmp_path, "b" + tag, k, shell)
+        o = oracle_lib.Oracle(d)
+        o.line_spectrum(cfg.ilinestart)
+        assert o.masing() == flag
+        m = ctx.load_dir(d)
+        models.append(m)
+        want.append(flag)
+        dirs.append(d)
+        b.add(m, cfg.ilinestart, 1)
+    for run in range(2):   # the first run and a graph replay
+        b.run()
+        for j, flag in enumerate(want):
+            assert list(b.masing(j)) == [flag], (run, j)
+    b.close()
+    for m in models:
+        m.free()
+    ctx.close()
+    man = tmp_path / "models.txt"
+    # a directory run renders lines 1.. (main.F:204): invert line 1 of one directory
+    _, dinv = inverted_model(tmp_path, "man_inv", 1.001, 20, iline=1)
+    _, dplain = inverted_model(tmp_path, "man_plain", None, 0)
+    man.write_text(dplain + "\n" + dinv + "\n")
+    capfd.readouterr()
+    gpu_lib.run_manifest(str(man))
+    out = capfd.readouterr().out
+    assert out.count("          WARNING: Masing detected!\n Will only warn once for this transition.\n") == 1
+
+
+def test_differentiable_path_has_no_inversion(oracle_lib, tmp_path):
+    """The differentiable path renders LTE populations, whose line opacity
+    C (N_low B_lu - N_up B_ul) = C N_low (g_u/g_l) B_ul (1 - e^{-h nu/kT}) is positive at every
+    T > 0, so the masing test cannot trigger there: the populations it derives hold
+    N_up g_l <= N_low g_u in every cell, and the oracle finds no masing on that model."""
+    cfg = synth.config_by_name("tiny_band")
+    arr = synth.lte_arrays(cfg)
+    _, g, lines = synth.molecule_levels(cfg)
+    pop = arr["pop"]
+    for up, lo, _ in lines[cfg.ilinestart - 1:cfg.ilinestart - 1 + cfg.nlines]:
+        assert np.all(pop[up - 1] * g[lo - 1] <= pop[lo - 1] * g[up - 1])
+    d = synth.write_model(cfg, str(tmp_path / "lte"))
+    o = oracle_lib.Oracle(d)
+    for k in range(cfg.nlines):
+        o.line_spectrum(cfg.ilinestart + k)
+        assert not o.masing()

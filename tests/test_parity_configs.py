@@ -9,11 +9,11 @@
   the full image in one launch and returns the same rays' rows (rl_image_rows).
 
 Tolerances (the reference's spectrum criterion is in every channel above 1e-3 of the peak):
-  FP32 transfer: spectra and sample spectra <= 1e-4 relative; each sampled ray within 2e-4
-                 of its brightest channel.
+  FP32 transfer: spectra and sample spectra <= 1e-4 relative; every sampled pixel within
+                 2e-4 of the line's brightest sampled pixel.
   FP64 transfer: spectra <= 1e-9 relative with the oracle's integrated-channel count and
-                 formal-solution step count; sampled rays within 1e-9 of their brightest
-                 channel.
+                 formal-solution step count; every sampled pixel within 1e-9 of the line's
+                 brightest sampled pixel.
 """
 import numpy as np
 import pytest

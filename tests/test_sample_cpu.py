@@ -25,8 +25,7 @@ def test_error_measures():
     got = ref.copy()
     got[0, 1] += 4e-4
     assert abs(sample.pixel_relerr(got, ref) - 1e-4) < 1e-15
-    got[1, 0] = 1e-30
-    assert sample.pixel_relerr(got, ref) == float("inf")
-    assert sample.spectrum_relerr(np.array([1.0, 2.0002]), np.array([1.0, 2.0])) == 1e-4 or \
-        abs(sample.spectrum_relerr(np.array([1.0, 2.0002]), np.array([1.0, 2.0])) - 1e-4) < 1e-12
+    assert sample.pixel_relerr(np.zeros((1, 2)), np.zeros((1, 2))) == 0.0
+    assert sample.pixel_relerr(np.ones((1, 2)), np.zeros((1, 2))) == float("inf")
+    assert abs(sample.spectrum_relerr(np.array([1.0, 2.0002]), np.array([1.0, 2.0])) - 1e-4) < 1e-12
     assert list(sample.ray_sample(10, 4, 1)) == [1, 5, 9]
