@@ -45,6 +45,9 @@ typedef struct rl_stats {
   unsigned long long node_passes;    /* walk: a tile's channel slots taken over one node */
   unsigned long long packed_passes;  /* of them on the packed FP32 path (positive opacity,
                                         no state reset, no SUBGRID refinement) */
+  unsigned long long empty_steps;    /* steps counted in `steps` whose two nodes have zero
+                                        emissivity and opacity: the intensity passes
+                                        unchanged and no arithmetic is done */
 } rl_stats;
 
 typedef struct rl_model_info {

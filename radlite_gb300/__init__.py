@@ -37,7 +37,7 @@ class Stats(C.Structure):
                 ("reduce_ms", C.c_double), ("upload_ms", C.c_double), ("total_ms", C.c_double),
                 ("nrays", C.c_int), ("nfr", C.c_int), ("kmax", C.c_int), ("nlines", C.c_int),
                 ("h2d_bytes", C.c_ulonglong), ("d2h_bytes", C.c_ulonglong), ("node_passes", C.c_ulonglong),
-                ("packed_passes", C.c_ulonglong)]
+                ("packed_passes", C.c_ulonglong), ("empty_steps", C.c_ulonglong)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

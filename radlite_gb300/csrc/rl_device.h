@@ -6,7 +6,7 @@
 namespace rl {
 
 // Counters of a walk launch (flush_counters): steps, integrated pairs, node visits, node
-// passes, packed node passes, spare.
+// passes, packed node passes, steps of empty segments, spare.
 constexpr int kWalkCounters = 8;
 // Walk launch shape: 4-warp blocks, at most this many per SM (sizes the list scratch).
 constexpr int kWalkBlocksPerSm = 4;
@@ -26,6 +26,8 @@ constexpr unsigned kFlagHole = 1u << 20;   // segment ending here lies in the ce
 constexpr unsigned kFlagIr1 = 1u << 21;    // node on the innermost radial cell (ir == 1)
 constexpr unsigned kFlagInit = 1u << 22;   // (walk) the segment ending here restarts the line state
 constexpr unsigned kFlagSub = 1u << 23;    // (walk) the segment ending here may need sub-steps
+constexpr unsigned kFlagEmpty = 1u << 25;  // (FP32 walk) every staged line has zero emissivity and
+                                           // opacity at this node and the previous one
 constexpr unsigned kFlagNeg = 1u << 24;    // (FP32 walk) some staged line lacks a positive opacity at
                                            // this node or the previous one
 constexpr int kIcrShift = 18;              // bits 18-19: crossing type 1..3

@@ -99,7 +99,7 @@ __device__ __forceinline__ SegGeom<T> seg_geom(T ds, T dvs, T rlw, T kq) {
   return g;
 }
 
-struct WalkCounters { unsigned long long steps = 0, integ = 0, nodes = 0, passes = 0, packed = 0; };
+struct WalkCounters { unsigned long long steps = 0, integ = 0, nodes = 0, passes = 0, packed = 0, skipped = 0; };
 
 template <typename T, int C, bool PV = false>
 __device__ long long walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<T, C>& SS, SubWork<T>& SW, int ray,
@@ -146,9 +146,10 @@ __device__ long long walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState
   }
   long long steps = 0;
   unsigned long long packed = 0, passes = 0;   // packed node passes, all node passes
+  unsigned long long skipped = 0;               // steps of empty segments (no work, counted)
   unsigned mbits = 0;   // tile lines whose line opacity x segment length fell below -0.01
   T lw_last = 0;
-  bool pos_last = true;
+  bool pos_last = true, zero_last = false;
   for (int kb = 0; kb < K; kb += 32) {
     if (kb > 0) {   // carry the last node of the previous chunk into entry 0
       if (lane == 0) {
@@ -162,7 +163,8 @@ __device__ long long walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState
     const int k = kb + lane;
     T vl = 0, ds = 0, dvs = 0, lwk = 0;
     unsigned misc = 0;
-    bool pos = true;   // every staged line has a normal dust opacity and no inversion here
+    bool pos = true;    // every staged line has a normal dust opacity and no inversion here
+    bool zero = true;   // every staged line's emissivity and opacity factors are 0 here
     if (k < K) {
       const size_t o = row + k;
       const T wr = nb.wr[o], wt = nb.wt[o];
@@ -171,7 +173,10 @@ __device__ long long walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState
       for (int l = 0; l < gl; l++) {
         const LineVals<T> v = interp_lv(P.tab, c, nl, l0 + l, wr, wt);
         S.lv[l][lane + 1] = v;
-        if constexpr (kFast) pos = pos && v.ad >= 1.17549435e-38f && v.af >= 0.f;
+        if constexpr (kFast) {
+          pos = pos && v.ad >= 1.17549435e-38f && v.af >= 0.f;
+          zero = zero && v.jd == 0.f && v.jf == 0.f && v.ad == 0.f && v.af == 0.f;
+        }
       }
       vl = nb.vl[o]; ds = nb.ds[o]; dvs = nb.dvseg[o]; lwk = nb.lw[o];
     }
@@ -192,6 +197,13 @@ __device__ long long walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState
         if (lane == 0) posp = pos_last;
         pos_last = __shfl_sync(0xffffffffu, pos, 31);
         if (!(pos && posp)) f |= kFlagNeg;
+        // a segment between two empty nodes leaves the intensity unchanged: j = a = 0 at both
+        // ends gives dtau = 0, x = 1 and Q = 0.5 (j0 + j1) ds = 0, and the carried point
+        // state stays (0, 0, 0)
+        bool zerop = __shfl_up_sync(0xffffffffu, zero, 1);
+        if (lane == 0) zerop = zero_last;
+        zero_last = __shfl_sync(0xffffffffu, zero, 31);
+        if (zero && zerop) f |= kFlagEmpty;
         // node values of the packed step, duplicated into pairs: {vl, vl, hds, hds},
         // {rl, rl} (the profile's 1/width)
         const float h = 0.5f * (float)ds;
@@ -237,6 +249,11 @@ __device__ long long walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState
         const int g = kb + n;
         const unsigned fl = S.flags[n + 1];
         if constexpr (kFast) {
+          if ((fl & (kFlagEmpty | kFlagInit)) == kFlagEmpty) {
+            steps += nv;
+            skipped += nv;
+            continue;
+          }
           bool slow = (fl & (kFlagInit | kFlagNeg)) != 0;
           if (!slow && (fl & kFlagSub)) {
             // a SUBGRID window that overlaps the segment sends the node to the general path
@@ -254,10 +271,10 @@ __device__ long long walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState
             const float4 h0 = S.hot[n + 1][0], h1 = S.hot[n + 1][1];
             const float2 vl2 = make_float2(h0.x, h0.y), hd2 = make_float2(h0.z, h0.w);
             const float2 rl2 = make_float2(h1.x, h1.y);
-            float2 j1[2], a1[2], S1[2], dt[2], th[2];
+            float2 j1[kPass / 2], a1[kPass / 2], S1[kPass / 2], dt[kPass / 2], th[kPass / 2];
             bool ser = true, dir = true;
 #pragma unroll
-            for (int p = 0; p < 2; p++) {
+            for (int p = 0; p < kPass / 2; p++) {
               const LineVals<T> vA = S.lv[lsl[2 * p]][n + 1], vB = S.lv[lsl[2 * p + 1]][n + 1];
               const float2 u = mul2(sub2(make_float2(w[2 * p], w[2 * p + 1]), vl2), rl2);
               const float2 m = mul2(mul2(u, u), dup2(-1.4426950408889634f));
@@ -273,16 +290,16 @@ __device__ long long walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState
             }
             ser = __all_sync(0xffffffffu, ser);
             dir = __all_sync(0xffffffffu, dir);
-            float2 x[2], ca[2], cb[2];
+            float2 x[kPass / 2], ca[kPass / 2], cb[kPass / 2];
             if (ser) {
 #pragma unroll
-              for (int p = 0; p < 2; p++) series2(dt[p], x[p], ca[p], cb[p]);
+              for (int p = 0; p < kPass / 2; p++) series2(dt[p], x[p], ca[p], cb[p]);
             } else if (dir) {
 #pragma unroll
-              for (int p = 0; p < 2; p++) direct2(dt[p], x[p], ca[p], cb[p]);
+              for (int p = 0; p < kPass / 2; p++) direct2(dt[p], x[p], ca[p], cb[p]);
             } else {
 #pragma unroll
-              for (int p = 0; p < 2; p++) {
+              for (int p = 0; p < kPass / 2; p++) {
                 float2 xs, as, bs, xd, ad, bd;
                 series2(dt[p], xs, as, bs);
                 direct2(dt[p], xd, ad, bd);
@@ -293,7 +310,7 @@ __device__ long long walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState
               }
             }
 #pragma unroll
-            for (int p = 0; p < 2; p++) {
+            for (int p = 0; p < kPass / 2; p++) {
               const float2 Q = fma2(ca[p], make_float2(S0[2 * p], S0[2 * p + 1]), mul2(cb[p], S1[p]));
               const float2 thin = make_float2(__saturatef(fmaf(dt[p].x, -kThinScale, kThinBias)),
                                               __saturatef(fmaf(dt[p].y, -kThinScale, kThinBias)));
@@ -457,6 +474,7 @@ __device__ long long walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState
   }
   wc.passes += passes;
   wc.packed += packed;
+  wc.skipped += skipped;
   return steps;
 }
 
@@ -645,7 +663,8 @@ struct WarpSmem {
 
 // counters[0] formal-solution steps, [1] integrated (line, channel) pairs, [2] node visits
 // (pairs x nodes), [3] node passes of the walk (a pass = the tile's slots over one node),
-// [4] of them taken on the packed FP32 path. The buffers hold kWalkCounters values.
+// [4] of them taken on the packed FP32 path, [5] steps of empty segments (counted in [0],
+// no arithmetic). The buffers hold kWalkCounters values.
 __device__ __forceinline__ void flush_counters(WalkCounters wc, unsigned long long* counters, int lane) {
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) wc.steps += __shfl_xor_sync(0xffffffffu, wc.steps, off);
@@ -655,6 +674,7 @@ __device__ __forceinline__ void flush_counters(WalkCounters wc, unsigned long lo
     atomicAdd(&counters[2], wc.nodes);
     atomicAdd(&counters[3], wc.passes);
     atomicAdd(&counters[4], wc.packed);
+    atomicAdd(&counters[5], wc.skipped);
   }
 }
 
