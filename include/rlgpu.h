@@ -94,6 +94,8 @@ typedef struct rl_model_arrays {
 } rl_model_arrays;
 
 int rl_create(rl_ctx** ctx, int device);
+/* Models, batches and differentiable handles made on a context must be released before
+   the context itself. */
 int rl_destroy(rl_ctx* ctx);
 /* Copies the last error message of the context (or of the process for a NULL context). */
 int rl_last_error(rl_ctx* ctx, char* buf, size_t len);

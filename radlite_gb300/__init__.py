@@ -17,6 +17,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import weakref
 
 import numpy as np
 
@@ -189,10 +190,25 @@ class Context:
 
     def __init__(self, device: int = 0):
         self.h = C.c_void_p()
+        self._children = []   # weak references to the models, batches and diffs made on it
         _check(lib().rl_create(C.byref(self.h), device))
 
+    def _adopt(self, obj, rank: int):
+        """Record an object that must be released before the context (lower rank first)."""
+        self._children.append((rank, weakref.ref(obj)))
+
     def close(self):
+        """Release every model, batch and differentiable handle still open on this context,
+        then the context itself (the library's handles must not outlive their context)."""
         if self.h:
+            for _, ref in sorted(self._children, key=lambda t: t[0]):
+                obj = ref()
+                if obj is not None:
+                    try:
+                        obj.free() if hasattr(obj, "free") else obj.close()
+                    except Exception:
+                        pass
+            self._children = []
             lib().rl_destroy(self.h)
             self.h = C.c_void_p()
 
@@ -287,6 +303,8 @@ class Model:
 
     def __init__(self, ctx: Context, h):
         self.ctx, self.h = ctx, h
+        if ctx is not None:
+            ctx._adopt(self, 3)
 
     def free(self):
         if self.h:
@@ -413,6 +431,7 @@ class Batch:
         self.h = C.c_void_p()
         self.models = []
         _check(lib().rl_batch_create(ctx.h, precision, C.byref(self.h)), ctx.h)
+        ctx._adopt(self, 1)
 
     def close(self):
         if self.h:
@@ -486,6 +505,8 @@ class Diff:
         self.model = model
         self.h = C.c_void_p()
         _check(lib().rl_diff_create(model.h, iline0, nlines, precision, C.byref(self.h)), model._ch)
+        if model.ctx is not None:
+            model.ctx._adopt(self, 1)
         nc, nl, nf, nr = C.c_int(), C.c_int(), C.c_int(), C.c_int()
         _check(lib().rl_diff_info(self.h, C.byref(nc), C.byref(nl), C.byref(nf), C.byref(nr)))
         self.ncell, self.nlines, self.nfr, self.nrays = nc.value, nl.value, nf.value, nr.value
@@ -557,6 +578,7 @@ class DiffBatch:
         self.h = C.c_void_p()
         self.diffs = []
         _check(lib().rl_diff_batch_create(ctx.h, C.byref(self.h)), ctx.h)
+        ctx._adopt(self, 0)
         self._views = None
 
     def close(self):

@@ -682,6 +682,12 @@ __device__ void adjoint_item(const AdjParams<T>& A, int item, AdjStage<T>& S, Ad
       lam[u] = (T)(g * wray);
     }
     // 3. reverse, chunk by chunk
+    // the start point of a regular step is the end point of the step before it (same node,
+    // same profile width): kept from one reverse step to the next instead of evaluated twice
+    PV<T> qc[kAdjSlots];
+    bool have_qc[kAdjSlots];
+#pragma unroll
+    for (int u = 0; u < kAdjSlots; u++) have_qc[u] = false;
     for (int cix = nchunk - 1; cix >= 0; cix--) {
       const int kb = cix * 32;
       adj_stage(P, S, row, kb, K, l, star_node, lane);
@@ -736,12 +742,15 @@ __device__ void adjoint_item(const AdjParams<T>& A, int item, AdjStage<T>& S, Ad
                                                   ilgs, Ip, lam[u], cgj[u], cga[u]);
             grl_seg += o.g_rl;
             lam[u] = o.lam; cgj[u] = o.cgj; cga[u] = o.cga;
+            have_qc[u] = false;
 #pragma unroll
             for (int k = 0; k < 4; k++) { acc0[k] += o.acc0[k]; acc1[k] += o.acc1[k]; }
           } else {
             // regular step
             const PV<T> q0 = pv_eval(v0, w[u], vl0, rl0);
-            const PV<T> q1 = pv_eval(v1, w[u], vl1, rl);
+            const PV<T> q1 = have_qc[u] ? qc[u] : pv_eval(v1, w[u], vl1, rl);
+            qc[u] = q0;
+            have_qc[u] = true;
             const StepGrad<T> g = step_back<T>(Ip, lam[u], q0.j, q0.a, q0.S, q1.j, q1.a, q1.S, hds);
             T gv = 0;
             point_back<T>(q1, rl, g.j1 + cgj[u], g.a1 + cga[u], g.S1, acc1, grl_seg, gv);

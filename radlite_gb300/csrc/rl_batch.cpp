@@ -530,7 +530,7 @@ int rl_batch_set_tiles(rl_batch* b, int lines_per_item, int channel_slots) {
   b->cpl = channel_slots;
   if (!b->built) return 0;
   rl_ctx* ctx = b->ctx;
-  CUDA_TRY(cudaSetDevice(ctx->device));
+  CUDA_TRY(rl::enter_device(ctx->device));
   return b->precision == RL_FP64 ? write_descriptors<double>(b) : write_descriptors<float>(b);
 }
 
@@ -550,7 +550,7 @@ int rl_batch_use_graph(rl_batch* b, int enable) {
 int rl_batch_autotune(rl_batch* b, int sample_stride, int* lines_per_item, int* channel_slots, double* sample_ms) {
   if (!b) return set_err(nullptr, RL_ERR_ARG, "rl_batch_autotune: null batch");
   rl_ctx* ctx = b->ctx;
-  CUDA_TRY(cudaSetDevice(ctx->device));
+  CUDA_TRY(rl::enter_device(ctx->device));
   g_h2d = 0; g_d2h = 0;
   return b->precision == RL_FP64 ? autotune<double>(b, sample_stride, lines_per_item, channel_slots, sample_ms)
                                  : autotune<float>(b, sample_stride, lines_per_item, channel_slots, sample_ms);
@@ -577,7 +577,7 @@ int rl_batch_job_info(rl_batch* b, int job, long long* flux_offset, int* nlines,
 int rl_batch_run(rl_batch* b, double* flux_out, rl_stats* st) {
   if (!b) return set_err(nullptr, RL_ERR_ARG, "rl_batch_run: null batch");
   rl_ctx* ctx = b->ctx;
-  CUDA_TRY(cudaSetDevice(ctx->device));
+  CUDA_TRY(rl::enter_device(ctx->device));
   if (st) std::memset(st, 0, sizeof *st);
   g_h2d = 0; g_d2h = 0;
   const int rc = b->precision == RL_FP64 ? run<double>(b, flux_out, st) : run<float>(b, flux_out, st);

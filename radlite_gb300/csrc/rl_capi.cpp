@@ -513,7 +513,7 @@ int rl_line_spectrum(rl_model* md, int iline, double* flux_out, double* velo_out
   if (!md || !flux_out) return set_err(nullptr, RL_ERR_ARG, "rl_line_spectrum: null argument");
   rl_ctx* ctx = md->ctx;
   if (!ctx) return set_err(nullptr, RL_ERR_STATE, "model was loaded without a device context");
-  CUDA_TRY(cudaSetDevice(ctx->device));
+  CUDA_TRY(rl::enter_device(ctx->device));
   if (st) std::memset(st, 0, sizeof *st);
   int rc = dispatch_lines(md, iline, 1, flux_out, nullptr, st);
   if (rc) return rc;
@@ -530,7 +530,7 @@ int rl_spectra(rl_model* md, int iline0, int nlines, double* flux_out, rl_stats*
   if (!md || !flux_out) return set_err(nullptr, RL_ERR_ARG, "rl_spectra: null argument");
   rl_ctx* ctx = md->ctx;
   if (!ctx) return set_err(nullptr, RL_ERR_STATE, "model was loaded without a device context");
-  CUDA_TRY(cudaSetDevice(ctx->device));
+  CUDA_TRY(rl::enter_device(ctx->device));
   if (st) std::memset(st, 0, sizeof *st);
   return dispatch_lines(md, iline0, nlines, flux_out, nullptr, st);
 }
@@ -539,7 +539,7 @@ int rl_line_image(rl_model* md, int iline, double* image_out, rl_stats* st) {
   if (!md || !image_out) return set_err(nullptr, RL_ERR_ARG, "rl_line_image: null argument");
   rl_ctx* ctx = md->ctx;
   if (!ctx) return set_err(nullptr, RL_ERR_STATE, "model was loaded without a device context");
-  CUDA_TRY(cudaSetDevice(ctx->device));
+  CUDA_TRY(rl::enter_device(ctx->device));
   if (st) std::memset(st, 0, sizeof *st);
   return dispatch_lines(md, iline, 1, nullptr, image_out, st);
 }
@@ -550,7 +550,7 @@ int rl_image_rows(rl_model* md, int iline0, int nlines, int nsel, const int* ray
     return set_err(nullptr, RL_ERR_ARG, "rl_image_rows: null argument or negative ray count");
   rl_ctx* ctx = md->ctx;
   if (!ctx) return set_err(nullptr, RL_ERR_STATE, "model was loaded without a device context");
-  CUDA_TRY(cudaSetDevice(ctx->device));
+  CUDA_TRY(rl::enter_device(ctx->device));
   if (st) std::memset(st, 0, sizeof *st);
   RowRequest rq;
   rq.rays = rays; rq.n = nsel; rq.out = rows_out;
@@ -561,7 +561,7 @@ int rl_line_image_mask(rl_model* md, int iline, double* image_out, unsigned char
   if (!md || !image_out || !mask_out) return set_err(nullptr, RL_ERR_ARG, "rl_line_image_mask: null argument");
   rl_ctx* ctx = md->ctx;
   if (!ctx) return set_err(nullptr, RL_ERR_STATE, "model was loaded without a device context");
-  CUDA_TRY(cudaSetDevice(ctx->device));
+  CUDA_TRY(rl::enter_device(ctx->device));
   if (st) std::memset(st, 0, sizeof *st);
   return dispatch_lines(md, iline, 1, nullptr, image_out, st, mask_out);
 }
@@ -724,7 +724,7 @@ int rl_line_masing(rl_model* md, int iline, int* detected) {
 
 int rl_measure_peaks(rl_ctx* ctx, double* ffma_per_s, double* ex2_per_s) {
   if (!ctx || !ffma_per_s || !ex2_per_s) return set_err(ctx, RL_ERR_ARG, "rl_measure_peaks: null argument");
-  CUDA_TRY(cudaSetDevice(ctx->device));
+  CUDA_TRY(rl::enter_device(ctx->device));
   CUDA_TRY(measure_peaks(ctx->nsm, ctx->stream, ffma_per_s, ex2_per_s));
   return 0;
 }
@@ -734,7 +734,7 @@ int rl_debug_trajectory(rl_model* md, int iray, int cap, double* s, double* r, d
   if (!md) return set_err(nullptr, RL_ERR_ARG, "rl_debug_trajectory: null model");
   rl_ctx* ctx = md->ctx;
   if (!ctx) return set_err(nullptr, RL_ERR_STATE, "model was loaded without a device context");
-  CUDA_TRY(cudaSetDevice(ctx->device));
+  CUDA_TRY(rl::enter_device(ctx->device));
   int rc = upload_grid(md);
   if (rc) return rc;
   std::string err;

@@ -621,7 +621,7 @@ int rl_diff_batch_buffers(rl_diff_batch* b, double** lnT, double** lnX, double**
                           double** g_lnT, double** g_lnX, double** g_width, long long* ncell, long long* nflux) {
   if (!b) return set_err(nullptr, RL_ERR_ARG, "rl_diff_batch_buffers: null batch");
   rl_ctx* ctx = b->ctx;
-  CUDA_TRY(cudaSetDevice(ctx->device));
+  CUDA_TRY(rl::enter_device(ctx->device));
   if (!b->built) {
     const int rc = b->precision == RL_FP64 ? batch_build<double>(b) : batch_build<float>(b);
     if (rc) return rc;
@@ -655,7 +655,7 @@ int rl_diff_batch_layout(rl_diff_batch* b, int job, long long* cell_offset, long
 int rl_diff_batch_forward(rl_diff_batch* b, rl_stats* st) {
   if (!b) return set_err(nullptr, RL_ERR_ARG, "rl_diff_batch_forward: null batch");
   rl_ctx* ctx = b->ctx;
-  CUDA_TRY(cudaSetDevice(ctx->device));
+  CUDA_TRY(rl::enter_device(ctx->device));
   if (st) std::memset(st, 0, sizeof *st);
   return b->precision == RL_FP64 ? batch_run<double>(b, 0, st) : batch_run<float>(b, 0, st);
 }
@@ -663,7 +663,7 @@ int rl_diff_batch_forward(rl_diff_batch* b, rl_stats* st) {
 int rl_diff_batch_backward(rl_diff_batch* b, rl_stats* st) {
   if (!b) return set_err(nullptr, RL_ERR_ARG, "rl_diff_batch_backward: null batch");
   rl_ctx* ctx = b->ctx;
-  CUDA_TRY(cudaSetDevice(ctx->device));
+  CUDA_TRY(rl::enter_device(ctx->device));
   if (st) std::memset(st, 0, sizeof *st);
   return b->precision == RL_FP64 ? batch_run<double>(b, 1, st) : batch_run<float>(b, 1, st);
 }
@@ -677,7 +677,7 @@ int rl_diff_create(rl_model* md, int iline0, int nlines, int precision, rl_diff*
   if (precision != RL_FP32 && precision != RL_FP64) return set_err(ctx, RL_ERR_ARG, "rl_diff_create: precision");
   if (nlines < 1 || iline0 < 1 || iline0 + nlines - 1 > (int)md->m.lfreq.size())
     return set_err(ctx, RL_ERR_ARG, "rl_diff_create: line range outside the molecule's line list");
-  CUDA_TRY(cudaSetDevice(ctx->device));
+  CUDA_TRY(rl::enter_device(ctx->device));
   std::unique_ptr<rl_diff> d(new rl_diff);
   d->ctx = ctx; d->md = md; d->iline0 = iline0; d->nl = nlines; d->precision = precision;
   g_h2d = 0; g_d2h = 0;
@@ -698,7 +698,7 @@ int rl_diff_set_checkpoint(rl_diff* d, int every) {
   if (!d) return set_err(nullptr, RL_ERR_ARG, "rl_diff_set_checkpoint: null handle");
   rl_ctx* ctx = d->ctx;
   if (every != 1 && every != 32) return set_err(ctx, RL_ERR_ARG, "rl_diff_set_checkpoint: interval 1 or 32");
-  CUDA_TRY(cudaSetDevice(ctx->device));
+  CUDA_TRY(rl::enter_device(ctx->device));
   d->every = every;
   const long long per = d->precision == RL_FP64 ? adjoint_ckpt_per_warp<double>(d->kmax, every)
                                                 : adjoint_ckpt_per_warp<float>(d->kmax, every);
@@ -720,7 +720,7 @@ int rl_diff_forward(rl_diff* d, const double* lnT, const double* lnX, const doub
                     rl_stats* st) {
   if (!d || !lnT || !lnX || !width || !flux) return set_err(d ? d->ctx : nullptr, RL_ERR_ARG, "rl_diff_forward: null argument");
   rl_ctx* ctx = d->ctx;
-  CUDA_TRY(cudaSetDevice(ctx->device));
+  CUDA_TRY(rl::enter_device(ctx->device));
   if (st) std::memset(st, 0, sizeof *st);
   return d->precision == RL_FP64 ? forward<double>(d, lnT, lnX, width, flux, st)
                                  : forward<float>(d, lnT, lnX, width, flux, st);
@@ -730,7 +730,7 @@ int rl_diff_backward(rl_diff* d, const double* gflux, double* g_lnT, double* g_l
   if (!d || !gflux || !g_lnT || !g_lnX || !g_width)
     return set_err(d ? d->ctx : nullptr, RL_ERR_ARG, "rl_diff_backward: null argument");
   rl_ctx* ctx = d->ctx;
-  CUDA_TRY(cudaSetDevice(ctx->device));
+  CUDA_TRY(rl::enter_device(ctx->device));
   if (st) std::memset(st, 0, sizeof *st);
   return d->precision == RL_FP64 ? backward<double>(d, gflux, g_lnT, g_lnX, g_width, st)
                                  : backward<float>(d, gflux, g_lnT, g_lnX, g_width, st);

@@ -291,7 +291,7 @@ int rl_gen_spec(rl_ctx* ctx, const rl_genspec_lines* in, const rl_genspec_params
                 double* frequency, double* spectrum, double* emission, double* continuum, rl_stats* st) {
   if (!ctx || !in || !p || !wavelength || !frequency || !spectrum || !emission || !continuum)
     return set_err(ctx, RL_ERR_ARG, "rl_gen_spec: null argument");
-  CUDA_TRY(cudaSetDevice(ctx->device));
+  CUDA_TRY(rl::enter_device(ctx->device));
   if (st) std::memset(st, 0, sizeof *st);
   g_h2d = 0; g_d2h = 0;
   GsHost h;

@@ -198,6 +198,14 @@ extern thread_local std::string g_last_error;
 extern thread_local unsigned long long g_h2d, g_d2h;   // bytes copied by the current call
 
 namespace rl {
+// Makes the context's device current at an entry point and drops an error that an
+// earlier, unrelated runtime call left behind, so that the launch checks of this call
+// (cudaGetLastError) report only this call's own launches.
+inline cudaError_t enter_device(int device) {
+  const cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) (void)cudaGetLastError();
+  return e;
+}
 void set_last_error(const std::string& msg);
 int set_err(rl_ctx* c, int code, const std::string& msg);
 cudaError_t h2d(void* dst, const void* src, size_t n, cudaStream_t s);

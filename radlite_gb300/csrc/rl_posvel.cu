@@ -302,7 +302,7 @@ int rl_posvel(rl_model* md, int iline0, int nlines, double* I_out, double* tau_o
   if (!md) return set_err(nullptr, RL_ERR_ARG, "rl_posvel: null model");
   rl_ctx* ctx = md->ctx;
   if (!ctx) return set_err(nullptr, RL_ERR_STATE, "model was loaded without a device context");
-  CUDA_TRY(cudaSetDevice(ctx->device));
+  CUDA_TRY(rl::enter_device(ctx->device));
   if (st) std::memset(st, 0, sizeof *st);
   return dispatch_posvel(md, iline0, nlines, I_out, tau_out, st);
 }
