@@ -113,6 +113,7 @@ __global__ void k_node_lw(NodeBuf<T> nb, const double* __restrict__ b, int nth) 
 // adjoint walk
 // ------------------------------------------------------------------------------------
 constexpr int kAdjSlots = 1;     // slots per lane per tile: 32 (line, channel) pairs
+constexpr int kCoopSubSteps = 6; // refined segments of at least this many sub-steps go to the warp
 
 template <typename T>
 struct AdjStage {
@@ -522,6 +523,167 @@ __device__ __forceinline__ T warp_sum(T v) {
   return v;
 }
 
+// Sub-step grid of a refined or resetting segment, as seg_back_slow and the forward's
+// slot_sub / slot_slow form it: kind 0 one step over the segment, kind 1 the SUBGRID points
+// of a carried-state segment, kind 2 those of a resetting one (kind 0 when the refined window
+// misses the segment); points ia..ib strictly inside (0, ds), then the segment end.
+template <typename T>
+struct SubGrid { int kind, ia, ib, npt; T sleft, lg, ilg; bool halves; };
+
+template <typename T>
+__device__ __forceinline__ SubGrid<T> sub_grid(int kind, T w, T vl0, T q, T dsf, T dvs, T idvs, T hw3s, T lgs,
+                                               T ilgs) {
+  SubGrid<T> G;
+  G.ia = 1; G.ib = 0; G.sleft = 0; G.lg = 0; G.ilg = 0;
+  if (kind == 1) {
+    const T s_c = sizeof(T) == 8 ? dsf * (w - vl0) / dvs : dsf * (w - vl0) * idvs;
+    G.sleft = s_c - hw3s;
+    G.lg = lgs;
+    G.ilg = ilgs;
+  } else if (kind == 2) {
+    const T s_c = dsf * (w - vl0) / dvs;
+    const T dls = dsf / q;
+    const T sright = s_c + (T)3 * dls;
+    G.sleft = s_c - (T)3 * dls;
+    if (sright > (T)0 && G.sleft < dsf) {
+      G.lg = (sright - G.sleft) / (T)30;
+      G.ilg = (T)1 / G.lg;
+    } else {
+      kind = 0;
+      G.sleft = 0;
+    }
+  }
+  if (kind != 0) {
+    int ia = 0;
+    if (!(G.sleft > (T)0)) {
+      ia = (int)(-G.sleft * G.ilg);
+      ia = ia < 0 ? 0 : (ia > 31 ? 31 : ia);
+      while (ia > 0 && G.sleft + (T)(ia - 1) * G.lg > (T)0) ia--;
+      while (ia <= 30 && !(G.sleft + (T)ia * G.lg > (T)0)) ia++;
+    }
+    int ib = 30;
+    if (!(G.sleft + (T)30 * G.lg < dsf)) {
+      ib = (int)((dsf - G.sleft) * G.ilg);
+      ib = ib < -1 ? -1 : (ib > 30 ? 30 : ib);
+      while (ib < 30 && G.sleft + (T)(ib + 1) * G.lg < dsf) ib++;
+      while (ib >= 0 && !(G.sleft + (T)ib * G.lg < dsf)) ib--;
+    }
+    G.ia = ia; G.ib = ib;
+  }
+  G.kind = kind;
+  G.halves = kind == 1 || (kind == 2 && G.ia <= G.ib);
+  G.npt = G.ib - G.ia + 2;
+  return G;
+}
+
+// seg_back_slow for one lane's segment, worked by the whole warp: lane i takes sub-step i
+// (end point ia + i, or the segment end). The intensity entering each sub-step is the
+// segment's input carried through the sub-steps before it, a prefix of the affine maps
+// I -> x I + Q (composed across lanes with shuffles); dL/dI after each sub-step is the
+// segment's output adjoint times the product of the later x (a suffix product). Each lane
+// then takes its step and end point backwards; the point gradients, the corner
+// accumulators and dL/d rl are summed over the lanes. All lanes return the owner's result.
+template <typename T>
+__device__ __noinline__ SlowOut<T> seg_back_coop(const SubGrid<T>& G, bool init, T w, const LineVals<T>& v0,
+                                    const LineVals<T>& v1, T vl0, T vl1, T rl, T rl0, T hds, T q, T dsf, T ids,
+                                    T Iin, T lamo, T cgj_in, T cga_in, int lane) {
+  const unsigned full = 0xffffffffu;
+  const int npt = G.npt;
+  const bool act = lane < npt;
+  const int k = G.ia + lane;                     // index of this lane's end point
+  const bool interior = act && k <= G.ib;
+  const T s = interior ? G.sleft + (T)k * G.lg : dsf;
+  T sp = __shfl_up_sync(full, s, 1);
+  if (lane == 0) sp = 0;
+  const PV<T> p0 = pv_eval(v0, w, vl0, init ? rl : rl0);   // incoming state (lane 0's start)
+  const T e = interior ? s * ids : (T)1;
+  const PV<T> pe = interior ? pv_eval(lerp_lv(v0, v1, e), w, ((T)1 - e) * vl0 + e * vl1, rl) : pv_eval(v1, w, vl1, rl);
+  // start point of this lane's sub-step: the end point of the lane before
+  T j0 = __shfl_up_sync(full, pe.j, 1), a0 = __shfl_up_sync(full, pe.a, 1), S0 = __shfl_up_sync(full, pe.S, 1);
+  if (lane == 0) { j0 = p0.j; a0 = p0.a; S0 = p0.S; }
+  const T h = G.halves ? (T)0.5 * (s - sp) : hds;
+  // the sub-step's affine map (formal's arithmetic)
+  T xm = 1, qm = 0;
+  if (act) {
+    const T dtau = (a0 + pe.a) * h;
+    const T theo = (j0 + pe.j) * h;
+    T x, ca, cb;
+    Math<T>::coeffs(dtau, x, ca, cb);
+    const T src1 = a0 > (T)0 ? S0 : (pe.a > (T)0 ? pe.S : (T)0);
+    const T src2 = pe.a > (T)0 ? pe.S : (a0 > (T)0 ? S0 : (T)0);
+    T qv = dtau > (T)1.0e-9f ? fmadd(ca, src1, cb * src2) : theo;
+    qm = qv < theo ? qv : theo;
+    xm = x;
+  }
+  // inclusive prefix of the maps (earlier lanes first)
+  T X = xm, Q = qm;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const T Xe = __shfl_up_sync(full, X, d), Qe = __shfl_up_sync(full, Q, d);
+    if (lane >= d) { Q = fmadd(Qe, X, Q); X = Xe * X; }
+  }
+  const T Iafter = fmadd(X, Iin, Q);                     // I after this lane's sub-step
+  T Iprev = __shfl_up_sync(full, Iafter, 1);
+  if (lane == 0) Iprev = Iin;
+  // suffix product of the later x: dL/dI after this lane's sub-step
+  T P = xm;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const T Pl = __shfl_down_sync(full, P, d);
+    if (lane + d < 32) P = P * Pl;
+  }
+  T lam = __shfl_down_sync(full, P, 1);
+  if (lane >= npt - 1) lam = (T)1;
+  lam = lam * lamo;
+  StepGrad<T> g = {0, 0, 0, 0, 0, 0, 0};
+  T lam_in = lam;
+  if (act) g = step_back<T>(Iprev, lam_in, j0, a0, S0, pe.j, pe.a, pe.S, h);
+  // the next sub-step's gradients of its start point (this lane's end point)
+  const T nj = __shfl_down_sync(full, g.j0, 1), na = __shfl_down_sync(full, g.a0, 1);
+  const T nS = __shfl_down_sync(full, g.S0, 1), nh = __shfl_down_sync(full, g.h, 1);
+  const bool last = lane == npt - 1;
+  T acc0[4] = {0, 0, 0, 0}, acc1[4] = {0, 0, 0, 0};
+  T g_rl = 0;
+  if (act) {
+    T acc[4] = {0, 0, 0, 0};
+    T gv = 0;
+    point_back<T>(pe, rl, g.j1 + (last ? cgj_in : nj), g.a1 + (last ? cga_in : na), g.S1 + (last ? (T)0 : nS), acc,
+                  g_rl, gv);
+    if (interior) {
+      for (int c = 0; c < 4; c++) { acc0[c] = ((T)1 - e) * acc[c]; acc1[c] = e * acc[c]; }
+      T ge = (T)0.5 * g.h - (T)0.5 * nh;
+      ge += (acc[0] * (v1.jd - v0.jd) + acc[1] * (v1.ad - v0.ad) + acc[2] * (v1.jf - v0.jf) +
+             acc[3] * (v1.af - v0.af) + gv * (vl1 - vl0)) * ids;
+      const T dls = q > (T)0 ? dsf / q : (T)0;
+      if (rl > (T)0) g_rl += ge * ((T)3 - (T)k / (T)5) * dls / rl;
+    } else {
+      for (int c = 0; c < 4; c++) acc1[c] = acc[c];
+    }
+  }
+  // the segment's start point (lane 0's start)
+  SlowOut<T> o;
+  o.cgj = 0; o.cga = 0;
+  if (lane == 0) {
+    if (init) {
+      T gv = 0;
+      point_back<T>(p0, rl, g.j0, g.a0, g.S0, acc0, g_rl, gv);
+    } else {
+      T gj = g.j0, ga = g.a0;
+      if (p0.a > (T)0 && g.S0 != (T)0) {
+        gj += g.S0 * p0.ra;
+        ga -= g.S0 * p0.S * p0.ra;
+      }
+      o.cgj = gj; o.cga = ga;
+    }
+  }
+  o.lam = __shfl_sync(full, lam_in, 0);
+  o.cgj = __shfl_sync(full, o.cgj, 0);
+  o.cga = __shfl_sync(full, o.cga, 0);
+  o.g_rl = warp_sum(g_rl);
+  for (int c = 0; c < 4; c++) { o.acc0[c] = warp_sum(acc0[c]); o.acc1[c] = warp_sum(acc1[c]); }
+  return o;
+}
+
 // Scatter the per-node gradients of staged entries t0..t1 to the cell corners.
 // Scatter the per-node gradients of staged entries t0..t1 to the cell corners, folded
 // into the cell parameters on the way: with the table derivatives dtab of each corner,
@@ -543,6 +705,10 @@ __device__ __forceinline__ void adj_scatter(const AdjParams<T>& A, AdjStage<T>& 
       const double* d = A.dtab + ((size_t)cs[q] * A.W.nlines + l) * 5;
       const double gT = gjf * __ldg(d + 0) + gaf * __ldg(d + 1) + gjd * __ldg(d + 2);
       const double gX = gjf * __ldg(d + 3) + gaf * __ldg(d + 4);
+      if (A.g4) {   // FP32 walk: the three gradients of the corner in one vector atomic
+        atomicAdd(A.g4 + cs[q], make_float4((float)(ws[q] * gT), (float)(ws[q] * gX), (float)(ws[q] * glw), 0.f));
+        continue;
+      }
       if (gT != 0.0) atomicAdd(A.g_lnT + cs[q], ws[q] * gT);
       if (gX != 0.0) atomicAdd(A.g_lnX + cs[q], ws[q] * gX);
       if (glw != 0.0) atomicAdd(A.g_b + cs[q], ws[q] * glw);   // node width: bilinear in all corners
@@ -724,28 +890,35 @@ __device__ void adjoint_item(const AdjParams<T>& A, int item, AdjStage<T>& S, Ad
         T grl_seg = 0;
 #pragma unroll
         for (int u = 0; u < kAdjSlots; u++) {
-          if (ch[u] < 0) continue;
-          const T Ip = every == 1 ? ck[((size_t)cix * 32 + n) * 32 + lane] : SL.Ibuf[n][u][lane];
+          const bool valid = ch[u] >= 0;
+          const T Ip = !valid ? (T)0 : every == 1 ? ck[((size_t)cix * 32 + n) * 32 + lane] : SL.Ibuf[n][u][lane];
           const bool init = (fl & kFlagInit) != 0;
+          const int kind = init ? ((fl & kFlagSub) ? 2 : 0) : 1;
           bool ov = false;
           T hw3 = S.hw3[n + 1], lgs = S.lg[n + 1], ilgs = S.ilg[n + 1];
-          if (!init && (fl & kFlagSub)) {
+          if (valid && !init && (fl & kFlagSub)) {
             const T dsf = S.ds[n + 1];
             const T s_c = sizeof(T) == 8 ? dsf * (w[u] - vl0) / S.dvs[n + 1] : dsf * (w[u] - vl0) * S.idvs[n + 1];
             ov = (s_c + hw3 > (T)0) && (s_c - hw3 < dsf);
           }
-          if (init || ov) {
-            // refined or resetting segment
-            const int kind = init ? ((fl & kFlagSub) ? 2 : 0) : 1;
+          const bool slow = valid && (init || ov);
+          // refined segments of many sub-steps are taken by the whole warp, one at a time
+          bool coop = false;
+          if (slow && kind != 0) {
+            const SubGrid<T> G = sub_grid<T>(kind, w[u], vl0, S.q[n + 1], S.ds[n + 1], S.dvs[n + 1], S.idvs[n + 1],
+                                             hw3, lgs, ilgs);
+            coop = G.npt >= kCoopSubSteps;
+          }
+          if (slow && !coop) {
+            // refined or resetting segment, on this lane
             const SlowOut<T> o = seg_back_slow<T>(init, kind, w[u], v0, v1, vl0, vl1, rl, rl0, hds, S.q[n + 1],
                                                   S.ds[n + 1], S.dvs[n + 1], S.ids[n + 1], S.idvs[n + 1], hw3, lgs,
                                                   ilgs, Ip, lam[u], cgj[u], cga[u]);
             grl_seg += o.g_rl;
             lam[u] = o.lam; cgj[u] = o.cgj; cga[u] = o.cga;
-            have_qc[u] = false;
 #pragma unroll
             for (int k = 0; k < 4; k++) { acc0[k] += o.acc0[k]; acc1[k] += o.acc1[k]; }
-          } else {
+          } else if (valid && !slow) {
             // regular step
             const PV<T> q0 = pv_eval(v0, w[u], vl0, rl0);
             const PV<T> q1 = have_qc[u] ? qc[u] : pv_eval(v1, w[u], vl1, rl);
@@ -762,8 +935,31 @@ __device__ void adjoint_item(const AdjParams<T>& A, int item, AdjStage<T>& S, Ad
             }
             cgj[u] = gj; cga[u] = ga;
           }
-          if (kb + n == star_node) lam[u] *= ((T)1 - fstar);
-          steps++;
+          unsigned tasks = __ballot_sync(0xffffffffu, coop);
+          while (tasks) {
+            const int o = __ffs(tasks) - 1;
+            tasks &= tasks - 1;
+            const T wo = __shfl_sync(0xffffffffu, w[u], o);
+            const T Io = __shfl_sync(0xffffffffu, Ip, o);
+            const T lo = __shfl_sync(0xffffffffu, lam[u], o);
+            const T cjo = __shfl_sync(0xffffffffu, cgj[u], o);
+            const T cao = __shfl_sync(0xffffffffu, cga[u], o);
+            const SubGrid<T> G = sub_grid<T>(kind, wo, vl0, S.q[n + 1], S.ds[n + 1], S.dvs[n + 1], S.idvs[n + 1],
+                                             hw3, lgs, ilgs);
+            const SlowOut<T> r = seg_back_coop<T>(G, init, wo, v0, v1, vl0, vl1, rl, rl0, hds, S.q[n + 1], S.ds[n + 1],
+                                                  S.ids[n + 1], Io, lo, cjo, cao, lane);
+            if (lane == o) {
+              lam[u] = r.lam; cgj[u] = r.cgj; cga[u] = r.cga;
+              grl_seg += r.g_rl;
+#pragma unroll
+              for (int k = 0; k < 4; k++) { acc0[k] += r.acc0[k]; acc1[k] += r.acc1[k]; }
+            }
+          }
+          if (slow) have_qc[u] = false;
+          if (valid) {
+            if (kb + n == star_node) lam[u] *= ((T)1 - fstar);
+            steps++;
+          }
         }
         // width: rl = 1 / (lw_{g-1}/2 + lw_g/2)
         const T glw = -(T)0.5 * rl * rl * grl_seg;
@@ -890,6 +1086,23 @@ cudaError_t launch_adjoint(const AdjJobs<T>& B, int blocks, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(B.work, 0, sizeof(int), s);
   if (e != cudaSuccess) return e;
   k_adjoint_jobs<T><<<blocks, 128, smem, s>>>(B);
+  return cudaGetLastError();
+}
+
+// The FP32 adjoint's accumulated {ln T, ln X, width} gradients into the FP64 outputs.
+__global__ void k_adj_finish(const float4* __restrict__ g4, double* gT, double* gX, double* gb, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float4 v = g4[i];
+    gT[i] = (double)v.x;
+    gX[i] = (double)v.y;
+    gb[i] = (double)v.z;
+  }
+}
+
+cudaError_t launch_adjoint_finish(const float4* g4, double* gT, double* gX, double* gb, long long n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  const long long blocks = (n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096;
+  k_adj_finish<<<(unsigned)blocks, 256, 0, s>>>(g4, gT, gX, gb, n);
   return cudaGetLastError();
 }
 

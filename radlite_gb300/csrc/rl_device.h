@@ -189,6 +189,9 @@ struct AdjParams {
   double* g_lnT;              // [ncell] dL/d ln T, accumulated
   double* g_lnX;              // [ncell] dL/d ln X, accumulated
   double* g_b;                // [ncell] dL/d(cell line width), accumulated
+  float4* g4 = nullptr;       // FP32 walk: [ncell] {dL/d ln T, dL/d ln X, dL/d width, 0} accumulated
+                              //   with one vector atomic per corner instead of g_lnT/g_lnX/g_b
+                              //   (launch_adjoint_finish converts them)
 };
 
 template <typename T>

@@ -35,6 +35,7 @@ template <typename T>
 long long adjoint_ckpt_per_warp(int kmax, int every);
 template <typename T>
 cudaError_t launch_adjoint(const AdjJobs<T>& B, int blocks, cudaStream_t s);
+cudaError_t launch_adjoint_finish(const float4* g4, double* gT, double* gX, double* gb, long long n, cudaStream_t s);
 }  // namespace rl
 
 using namespace rl;
@@ -56,6 +57,7 @@ struct rl_diff {
   DevBuf img, ring, flux, cnt, work, err, list;
   // adjoint
   DevBuf ckpt, ajob, aprefix, acnt, awork;
+  DevBuf g4;   // FP32 adjoint: interleaved gradient accumulator [ncell]
   bool have_forward = false;
   int every = 1;   // adjoint checkpoint interval (nodes)
 };
@@ -311,6 +313,10 @@ int backward(rl_diff* d, const double* gflux, double* g_lnT, double* g_lnX, doub
   A.nphi = d->cam.nphi; A.nrr = d->cam.nrr;
   A.dtab = d->dtab.as<double>();
   A.g_lnT = g_lnT; A.g_lnX = g_lnX; A.g_b = g_width;
+  if (sizeof(T) == 4) {
+    CUDA_TRY(d->g4.ensure(sizeof(float4) * d->ncell));
+    A.g4 = d->g4.as<float4>();
+  }
   AdjJobs<T> B;
   B.jobs = d->ajob.as<AdjParams<T>>();
   B.item_prefix = d->aprefix.as<int>();
@@ -324,10 +330,12 @@ int backward(rl_diff* d, const double* gflux, double* g_lnT, double* g_lnX, doub
   CUDA_TRY(cudaMemsetAsync(g_lnT, 0, sizeof(double) * d->ncell, s));
   CUDA_TRY(cudaMemsetAsync(g_lnX, 0, sizeof(double) * d->ncell, s));
   CUDA_TRY(cudaMemsetAsync(g_width, 0, sizeof(double) * d->ncell, s));
+  if (A.g4) CUDA_TRY(cudaMemsetAsync(A.g4, 0, sizeof(float4) * d->ncell, s));
   CUDA_TRY(cudaMemsetAsync(d->acnt.p, 0, sizeof(unsigned long long) * 4, s));
   CUDA_TRY(cudaMemsetAsync(d->err.p, 0, sizeof(int), s));
   CUDA_TRY(cudaEventRecord(ctx->ev[0], s));
   CUDA_TRY(launch_adjoint<T>(B, d->adj_blocks, s));
+  if (A.g4) CUDA_TRY(launch_adjoint_finish(A.g4, g_lnT, g_lnX, g_width, d->ncell, s));
   CUDA_TRY(cudaEventRecord(ctx->ev[1], s));
   CUDA_TRY(cudaEventRecord(ctx->ev[2], s));
   unsigned long long cnt[4] = {0, 0, 0, 0};
@@ -360,6 +368,7 @@ struct rl_diff_batch {
   int max_nfr = 0, max_kmax = 0, adj_blocks = 0, every = 1;
   bool built = false, use_graph = true;
   DevBuf lnT, lnX, width, flux, gflux, g_lnT, g_lnX, g_width;
+  DevBuf g4;   // FP32 adjoint: interleaved gradient accumulator [ncell]
   DevBuf walkjobs, redjobs, adjjobs, item_prefix, ring_prefix, line_prefix, adj_prefix, cnt, work, err, acnt, awork, ckpt,
       list;
   JobLaunch<float> Lf{};
@@ -416,6 +425,7 @@ int batch_build(rl_diff_batch* b) {
   CUDA_TRY(b->lnX.ensure(sizeof(double) * b->ncell));
   CUDA_TRY(b->width.ensure(sizeof(double) * b->ncell));
   CUDA_TRY(b->g_lnT.ensure(sizeof(double) * b->ncell));
+  CUDA_TRY(b->g4.ensure(sizeof(float4) * b->ncell));
   CUDA_TRY(b->g_lnX.ensure(sizeof(double) * b->ncell));
   CUDA_TRY(b->g_width.ensure(sizeof(double) * b->ncell));
   CUDA_TRY(b->flux.ensure(sizeof(double) * b->nflux));
@@ -453,6 +463,7 @@ int batch_build(rl_diff_batch* b) {
     A.g_lnT = b->g_lnT.as<double>() + b->cell_off[j];
     A.g_lnX = b->g_lnX.as<double>() + b->cell_off[j];
     A.g_b = b->g_width.as<double>() + b->cell_off[j];
+    A.g4 = sizeof(T) == 4 ? b->g4.as<float4>() + b->cell_off[j] : nullptr;
     itemp[j + 1] = itemp[j] + w.nitems;
     ringp[j + 1] = ringp[j] + d->nl * d->cam.nrr;
     linep[j + 1] = linep[j] + d->nl;
@@ -518,9 +529,13 @@ cudaError_t batch_enqueue(rl_diff_batch* b, int dir, cudaStream_t s) {
     e = cudaMemsetAsync(b->g_lnT.p, 0, sizeof(double) * b->ncell, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->g_lnX.p, 0, sizeof(double) * b->ncell, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->g_width.p, 0, sizeof(double) * b->ncell, s);
+    if (e == cudaSuccess && sizeof(T) == 4) e = cudaMemsetAsync(b->g4.p, 0, sizeof(float4) * b->ncell, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->acnt.p, 0, sizeof(unsigned long long) * 4, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->err.p, 0, sizeof(int), s);
     if (e == cudaSuccess) e = launch_adjoint<T>(adj_of<T>(b), b->adj_blocks, s);
+    if (e == cudaSuccess && sizeof(T) == 4)
+      e = launch_adjoint_finish(b->g4.as<float4>(), b->g_lnT.as<double>(), b->g_lnX.as<double>(),
+                                b->g_width.as<double>(), (long long)b->ncell, s);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(b->cnt_h + 4, b->acnt.p, sizeof(unsigned long long) * 4, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(b->err_h + 1, b->err.p, sizeof(int), cudaMemcpyDeviceToHost, s);
