@@ -397,7 +397,7 @@ def ours(args):
         batched = batched_case(ctx, args.batch_models, 2)
     if rank == 0 and not args.no_diff:
         adjoint = adjoint_case(ctx)
-        fitting = fit_case(ctx, args.fit_models, args.fit_steps)
+        fitting = fit_case(ctx, args.fit_models, args.fit_steps, nphi=args.fit_nphi, dbdr=args.fit_dbdr)
     out = None
     if rank == 0:
         cpu = parity = disk = None
@@ -632,17 +632,17 @@ def adjoint_case(ctx, name="adjoint_disk", reps=3, **over):
     return res
 
 
-def fit_case(ctx, n_models=64, steps=5, plain_models=8):
+def fit_case(ctx, n_models=64, steps=5, plain_models=8, nphi=32, dbdr=2, history=False, analyse=False):
     """The batched forward+adjoint fitting step on n uneven models (radlite_gb300.fit)
     against plain per-model forward + central finite differences in the four parameters,
     timed on `plain_models` of the same models."""
     from radlite_gb300 import fit
-    cfgs = fit.fit_configs(n_models)
-    res = fit.run_fit(ctx, cfgs, steps=steps)
+    cfgs = fit.fit_configs(n_models, nphi=nphi, dbdr=dbdr)
+    res = fit.run_fit(ctx, cfgs, steps=steps, history=history, analyse=analyse)
     plain = fit.plain_fd_step_seconds(ctx, cfgs[:plain_models])
     per_spec = plain["seconds"] / plain["spectra"]
     out = {"workload": f"{n_models} uneven disks (nr 100-400, ntheta 50-200), 20 lines x 200 channels, "
-                       f"{cfgs[0].nphi} azimuths, 4 parameters each",
+                       f"{cfgs[0].nphi} azimuths, {dbdr} rings per grid radius, 4 parameters each",
            "batched_forward_adjoint": res,
            "plain_forward_fd": {"models_timed": plain_models, "seconds_per_gradient_spectrum": per_spec,
                                 "spectra_per_s": 1.0 / per_spec}}
@@ -719,7 +719,9 @@ def main():
     ap.add_argument("--nphi", type=int, default=0,
                     help="azimuths of the adjoint timing and of --profile (0: the workload's)")
     ap.add_argument("--only-fit", action="store_true", help="run only the batched fitting-step comparison")
-    ap.add_argument("--fit-models", type=int, default=64)
+    ap.add_argument("--fit-models", type=int, default=16)
+    ap.add_argument("--fit-nphi", type=int, default=32, help="azimuths of the fitting images")
+    ap.add_argument("--fit-dbdr", type=int, default=2, help="rings per grid radius of the fitting images")
     ap.add_argument("--no-diff", action="store_true", help="skip the adjoint and fitting measurements")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the position-velocity, gen_spec and input-parsing measurements")
@@ -727,7 +729,8 @@ def main():
     if args.only_fit:
         import radlite_gb300 as rl
         ctx = rl.Context(0)
-        print(json.dumps(fit_case(ctx, args.fit_models, args.steps)), flush=True)
+        print(json.dumps(fit_case(ctx, args.fit_models, args.fit_steps, nphi=args.fit_nphi, dbdr=args.fit_dbdr,
+                                  history=True, analyse=True, plain_models=min(8, args.fit_models))), flush=True)
         ctx.close()
         return 0
     if args.only_adjoint:

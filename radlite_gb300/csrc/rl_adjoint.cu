@@ -113,7 +113,6 @@ __global__ void k_node_lw(NodeBuf<T> nb, const double* __restrict__ b, int nth) 
 // adjoint walk
 // ------------------------------------------------------------------------------------
 constexpr int kAdjSlots = 1;     // slots per lane per tile: 32 (line, channel) pairs
-constexpr int kCoopSubSteps = 6; // refined segments of at least this many sub-steps go to the warp
 
 template <typename T>
 struct AdjStage {
@@ -127,6 +126,7 @@ struct AdjStage {
 template <typename T>
 struct AdjSlots {
   T Ibuf[33][kAdjSlots][32];   // intensity entering each segment of the current chunk
+  T Isub[33][32];              // intensity entering each sub-step of a lane's refined segment
 };
 
 // d(x, a, b)/d(dtau) of the coefficients Math<T>::coeffs computes.
@@ -261,7 +261,9 @@ struct SlowOut {
 template <typename T>
 __device__ __noinline__ SlowOut<T> seg_back_slow(bool init, int kind, T w, LineVals<T> v0, LineVals<T> v1, T vl0,
                                                   T vl1, T rl, T rl0, T hds, T q, T dsf, T dvs, T ids, T idvs, T hw3s,
-                                                  T lgs, T ilgs, T Iin, T lam, T cgj, T cga) {
+                                                  T lgs, T ilgs, T Iin, T lam, T cgj, T cga, T* Isub) {
+  // Isub: this lane's column of the warp's shared sub-step array (stride 32); the sub-step
+  // positions are formed again in the reverse pass
   T acc0[4] = {0, 0, 0, 0}, acc1[4] = {0, 0, 0, 0};
   const PV<T> p0 = pv_eval(v0, w, vl0, init ? rl : rl0);   // incoming state
   const T j0 = p0.j, a0 = p0.a, S0 = p0.S;
@@ -303,9 +305,11 @@ __device__ __noinline__ SlowOut<T> seg_back_slow(bool init, int kind, T w, LineV
   }
   const bool halves = kind == 1 || (kind == 2 && ia <= ib);   // h = (s - s_prev)/2, else hds
   const T dls = q > (T)0 ? dsf / q : (T)0;
-  T Isub[33];
-  T ssub[33];
   int npt = 0;
+  auto spos = [&](int m) -> T {   // end of sub-step m: grid point ia + m, or the segment end
+    const int i = ia + m;
+    return i <= ib ? sleft + (T)i * lg : dsf;
+  };
   {
     T I = Iin, sj0 = j0, sa0 = a0, sS0 = S0;
     T sp = 0;
@@ -323,8 +327,7 @@ __device__ __noinline__ SlowOut<T> seg_back_slow(bool init, int kind, T w, LineV
       T j1, a1, S1;
       point_vals(pv, w, pvl, rl, j1, a1, S1);
       const T h = halves ? (T)0.5 * (s - sp) : hds;
-      Isub[npt] = I;
-      ssub[npt] = s;
+      Isub[npt * 32] = I;
       npt++;
       formal(I, sj0, sa0, sS0, j1, a1, S1, h);
       sj0 = j1; sa0 = a1; sS0 = S1;
@@ -339,7 +342,7 @@ __device__ __noinline__ SlowOut<T> seg_back_slow(bool init, int kind, T w, LineV
   {
     const int i = ia + npt - 1;
     if (i <= ib) {
-      e = ssub[npt - 1] * ids;
+      e = spos(npt - 1) * ids;
       pe = pv_eval(lerp_lv(v0, v1, e), w, ((T)1 - e) * vl0 + e * vl1, rl);
     } else {
       pe = pv_eval(v1, w, vl1, rl);
@@ -348,8 +351,8 @@ __device__ __noinline__ SlowOut<T> seg_back_slow(bool init, int kind, T w, LineV
   for (int m = npt - 1; m >= 0; m--) {
     const int i = ia + m;
     const bool interior = i <= ib;
-    const T s = ssub[m];
-    const T sp = m > 0 ? ssub[m - 1] : (T)0;
+    const T s = spos(m);
+    const T sp = m > 0 ? spos(m - 1) : (T)0;
     PV<T> ps;
     T es = (T)0;
     if (m > 0) {
@@ -359,7 +362,7 @@ __device__ __noinline__ SlowOut<T> seg_back_slow(bool init, int kind, T w, LineV
       ps = p0;
     }
     const T h = halves ? (T)0.5 * (s - sp) : hds;
-    const StepGrad<T> g = step_back<T>(Isub[m], lam, ps.j, ps.a, ps.S, pe.j, pe.a, pe.S, h);
+    const StepGrad<T> g = step_back<T>(Isub[m * 32], lam, ps.j, ps.a, ps.S, pe.j, pe.a, pe.S, h);
     T acc[4] = {0, 0, 0, 0};
     T gv = 0;
     point_back<T>(pe, rl, g.j1 + gj_next, g.a1 + ga_next, g.S1 + gS_next, acc, g_rl, gv);
@@ -521,167 +524,6 @@ __device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
   return v;
-}
-
-// Sub-step grid of a refined or resetting segment, as seg_back_slow and the forward's
-// slot_sub / slot_slow form it: kind 0 one step over the segment, kind 1 the SUBGRID points
-// of a carried-state segment, kind 2 those of a resetting one (kind 0 when the refined window
-// misses the segment); points ia..ib strictly inside (0, ds), then the segment end.
-template <typename T>
-struct SubGrid { int kind, ia, ib, npt; T sleft, lg, ilg; bool halves; };
-
-template <typename T>
-__device__ __forceinline__ SubGrid<T> sub_grid(int kind, T w, T vl0, T q, T dsf, T dvs, T idvs, T hw3s, T lgs,
-                                               T ilgs) {
-  SubGrid<T> G;
-  G.ia = 1; G.ib = 0; G.sleft = 0; G.lg = 0; G.ilg = 0;
-  if (kind == 1) {
-    const T s_c = sizeof(T) == 8 ? dsf * (w - vl0) / dvs : dsf * (w - vl0) * idvs;
-    G.sleft = s_c - hw3s;
-    G.lg = lgs;
-    G.ilg = ilgs;
-  } else if (kind == 2) {
-    const T s_c = dsf * (w - vl0) / dvs;
-    const T dls = dsf / q;
-    const T sright = s_c + (T)3 * dls;
-    G.sleft = s_c - (T)3 * dls;
-    if (sright > (T)0 && G.sleft < dsf) {
-      G.lg = (sright - G.sleft) / (T)30;
-      G.ilg = (T)1 / G.lg;
-    } else {
-      kind = 0;
-      G.sleft = 0;
-    }
-  }
-  if (kind != 0) {
-    int ia = 0;
-    if (!(G.sleft > (T)0)) {
-      ia = (int)(-G.sleft * G.ilg);
-      ia = ia < 0 ? 0 : (ia > 31 ? 31 : ia);
-      while (ia > 0 && G.sleft + (T)(ia - 1) * G.lg > (T)0) ia--;
-      while (ia <= 30 && !(G.sleft + (T)ia * G.lg > (T)0)) ia++;
-    }
-    int ib = 30;
-    if (!(G.sleft + (T)30 * G.lg < dsf)) {
-      ib = (int)((dsf - G.sleft) * G.ilg);
-      ib = ib < -1 ? -1 : (ib > 30 ? 30 : ib);
-      while (ib < 30 && G.sleft + (T)(ib + 1) * G.lg < dsf) ib++;
-      while (ib >= 0 && !(G.sleft + (T)ib * G.lg < dsf)) ib--;
-    }
-    G.ia = ia; G.ib = ib;
-  }
-  G.kind = kind;
-  G.halves = kind == 1 || (kind == 2 && G.ia <= G.ib);
-  G.npt = G.ib - G.ia + 2;
-  return G;
-}
-
-// seg_back_slow for one lane's segment, worked by the whole warp: lane i takes sub-step i
-// (end point ia + i, or the segment end). The intensity entering each sub-step is the
-// segment's input carried through the sub-steps before it, a prefix of the affine maps
-// I -> x I + Q (composed across lanes with shuffles); dL/dI after each sub-step is the
-// segment's output adjoint times the product of the later x (a suffix product). Each lane
-// then takes its step and end point backwards; the point gradients, the corner
-// accumulators and dL/d rl are summed over the lanes. All lanes return the owner's result.
-template <typename T>
-__device__ __noinline__ SlowOut<T> seg_back_coop(const SubGrid<T>& G, bool init, T w, const LineVals<T>& v0,
-                                    const LineVals<T>& v1, T vl0, T vl1, T rl, T rl0, T hds, T q, T dsf, T ids,
-                                    T Iin, T lamo, T cgj_in, T cga_in, int lane) {
-  const unsigned full = 0xffffffffu;
-  const int npt = G.npt;
-  const bool act = lane < npt;
-  const int k = G.ia + lane;                     // index of this lane's end point
-  const bool interior = act && k <= G.ib;
-  const T s = interior ? G.sleft + (T)k * G.lg : dsf;
-  T sp = __shfl_up_sync(full, s, 1);
-  if (lane == 0) sp = 0;
-  const PV<T> p0 = pv_eval(v0, w, vl0, init ? rl : rl0);   // incoming state (lane 0's start)
-  const T e = interior ? s * ids : (T)1;
-  const PV<T> pe = interior ? pv_eval(lerp_lv(v0, v1, e), w, ((T)1 - e) * vl0 + e * vl1, rl) : pv_eval(v1, w, vl1, rl);
-  // start point of this lane's sub-step: the end point of the lane before
-  T j0 = __shfl_up_sync(full, pe.j, 1), a0 = __shfl_up_sync(full, pe.a, 1), S0 = __shfl_up_sync(full, pe.S, 1);
-  if (lane == 0) { j0 = p0.j; a0 = p0.a; S0 = p0.S; }
-  const T h = G.halves ? (T)0.5 * (s - sp) : hds;
-  // the sub-step's affine map (formal's arithmetic)
-  T xm = 1, qm = 0;
-  if (act) {
-    const T dtau = (a0 + pe.a) * h;
-    const T theo = (j0 + pe.j) * h;
-    T x, ca, cb;
-    Math<T>::coeffs(dtau, x, ca, cb);
-    const T src1 = a0 > (T)0 ? S0 : (pe.a > (T)0 ? pe.S : (T)0);
-    const T src2 = pe.a > (T)0 ? pe.S : (a0 > (T)0 ? S0 : (T)0);
-    T qv = dtau > (T)1.0e-9f ? fmadd(ca, src1, cb * src2) : theo;
-    qm = qv < theo ? qv : theo;
-    xm = x;
-  }
-  // inclusive prefix of the maps (earlier lanes first)
-  T X = xm, Q = qm;
-#pragma unroll
-  for (int d = 1; d < 32; d <<= 1) {
-    const T Xe = __shfl_up_sync(full, X, d), Qe = __shfl_up_sync(full, Q, d);
-    if (lane >= d) { Q = fmadd(Qe, X, Q); X = Xe * X; }
-  }
-  const T Iafter = fmadd(X, Iin, Q);                     // I after this lane's sub-step
-  T Iprev = __shfl_up_sync(full, Iafter, 1);
-  if (lane == 0) Iprev = Iin;
-  // suffix product of the later x: dL/dI after this lane's sub-step
-  T P = xm;
-#pragma unroll
-  for (int d = 1; d < 32; d <<= 1) {
-    const T Pl = __shfl_down_sync(full, P, d);
-    if (lane + d < 32) P = P * Pl;
-  }
-  T lam = __shfl_down_sync(full, P, 1);
-  if (lane >= npt - 1) lam = (T)1;
-  lam = lam * lamo;
-  StepGrad<T> g = {0, 0, 0, 0, 0, 0, 0};
-  T lam_in = lam;
-  if (act) g = step_back<T>(Iprev, lam_in, j0, a0, S0, pe.j, pe.a, pe.S, h);
-  // the next sub-step's gradients of its start point (this lane's end point)
-  const T nj = __shfl_down_sync(full, g.j0, 1), na = __shfl_down_sync(full, g.a0, 1);
-  const T nS = __shfl_down_sync(full, g.S0, 1), nh = __shfl_down_sync(full, g.h, 1);
-  const bool last = lane == npt - 1;
-  T acc0[4] = {0, 0, 0, 0}, acc1[4] = {0, 0, 0, 0};
-  T g_rl = 0;
-  if (act) {
-    T acc[4] = {0, 0, 0, 0};
-    T gv = 0;
-    point_back<T>(pe, rl, g.j1 + (last ? cgj_in : nj), g.a1 + (last ? cga_in : na), g.S1 + (last ? (T)0 : nS), acc,
-                  g_rl, gv);
-    if (interior) {
-      for (int c = 0; c < 4; c++) { acc0[c] = ((T)1 - e) * acc[c]; acc1[c] = e * acc[c]; }
-      T ge = (T)0.5 * g.h - (T)0.5 * nh;
-      ge += (acc[0] * (v1.jd - v0.jd) + acc[1] * (v1.ad - v0.ad) + acc[2] * (v1.jf - v0.jf) +
-             acc[3] * (v1.af - v0.af) + gv * (vl1 - vl0)) * ids;
-      const T dls = q > (T)0 ? dsf / q : (T)0;
-      if (rl > (T)0) g_rl += ge * ((T)3 - (T)k / (T)5) * dls / rl;
-    } else {
-      for (int c = 0; c < 4; c++) acc1[c] = acc[c];
-    }
-  }
-  // the segment's start point (lane 0's start)
-  SlowOut<T> o;
-  o.cgj = 0; o.cga = 0;
-  if (lane == 0) {
-    if (init) {
-      T gv = 0;
-      point_back<T>(p0, rl, g.j0, g.a0, g.S0, acc0, g_rl, gv);
-    } else {
-      T gj = g.j0, ga = g.a0;
-      if (p0.a > (T)0 && g.S0 != (T)0) {
-        gj += g.S0 * p0.ra;
-        ga -= g.S0 * p0.S * p0.ra;
-      }
-      o.cgj = gj; o.cga = ga;
-    }
-  }
-  o.lam = __shfl_sync(full, lam_in, 0);
-  o.cgj = __shfl_sync(full, o.cgj, 0);
-  o.cga = __shfl_sync(full, o.cga, 0);
-  o.g_rl = warp_sum(g_rl);
-  for (int c = 0; c < 4; c++) { o.acc0[c] = warp_sum(acc0[c]); o.acc1[c] = warp_sum(acc1[c]); }
-  return o;
 }
 
 // Scatter the per-node gradients of staged entries t0..t1 to the cell corners.
@@ -848,12 +690,6 @@ __device__ void adjoint_item(const AdjParams<T>& A, int item, AdjStage<T>& S, Ad
       lam[u] = (T)(g * wray);
     }
     // 3. reverse, chunk by chunk
-    // the start point of a regular step is the end point of the step before it (same node,
-    // same profile width): kept from one reverse step to the next instead of evaluated twice
-    PV<T> qc[kAdjSlots];
-    bool have_qc[kAdjSlots];
-#pragma unroll
-    for (int u = 0; u < kAdjSlots; u++) have_qc[u] = false;
     for (int cix = nchunk - 1; cix >= 0; cix--) {
       const int kb = cix * 32;
       adj_stage(P, S, row, kb, K, l, star_node, lane);
@@ -878,6 +714,10 @@ __device__ void adjoint_item(const AdjParams<T>& A, int item, AdjStage<T>& S, Ad
           }
         }
       }
+      // interval 1: this chunk's stored intensities, fetched together into shared memory
+      if (every == 1) {
+        for (int n = n0; n < nn; n++) SL.Ibuf[n][0][lane] = ck[((size_t)cix * 32 + n) * 32 + lane];
+      }
       __syncwarp();
       // walk the segments backwards
       T acc1[5] = {0, 0, 0, 0, 0};    // node kb+n
@@ -891,7 +731,7 @@ __device__ void adjoint_item(const AdjParams<T>& A, int item, AdjStage<T>& S, Ad
 #pragma unroll
         for (int u = 0; u < kAdjSlots; u++) {
           const bool valid = ch[u] >= 0;
-          const T Ip = !valid ? (T)0 : every == 1 ? ck[((size_t)cix * 32 + n) * 32 + lane] : SL.Ibuf[n][u][lane];
+          const T Ip = !valid ? (T)0 : SL.Ibuf[n][u][lane];
           const bool init = (fl & kFlagInit) != 0;
           const int kind = init ? ((fl & kFlagSub) ? 2 : 0) : 1;
           bool ov = false;
@@ -902,28 +742,19 @@ __device__ void adjoint_item(const AdjParams<T>& A, int item, AdjStage<T>& S, Ad
             ov = (s_c + hw3 > (T)0) && (s_c - hw3 < dsf);
           }
           const bool slow = valid && (init || ov);
-          // refined segments of many sub-steps are taken by the whole warp, one at a time
-          bool coop = false;
-          if (slow && kind != 0) {
-            const SubGrid<T> G = sub_grid<T>(kind, w[u], vl0, S.q[n + 1], S.ds[n + 1], S.dvs[n + 1], S.idvs[n + 1],
-                                             hw3, lgs, ilgs);
-            coop = G.npt >= kCoopSubSteps;
-          }
-          if (slow && !coop) {
-            // refined or resetting segment, on this lane
+          if (slow) {
+            // refined or resetting segment
             const SlowOut<T> o = seg_back_slow<T>(init, kind, w[u], v0, v1, vl0, vl1, rl, rl0, hds, S.q[n + 1],
                                                   S.ds[n + 1], S.dvs[n + 1], S.ids[n + 1], S.idvs[n + 1], hw3, lgs,
-                                                  ilgs, Ip, lam[u], cgj[u], cga[u]);
+                                                  ilgs, Ip, lam[u], cgj[u], cga[u], &SL.Isub[0][lane]);
             grl_seg += o.g_rl;
             lam[u] = o.lam; cgj[u] = o.cgj; cga[u] = o.cga;
 #pragma unroll
             for (int k = 0; k < 4; k++) { acc0[k] += o.acc0[k]; acc1[k] += o.acc1[k]; }
-          } else if (valid && !slow) {
+          } else if (valid) {
             // regular step
             const PV<T> q0 = pv_eval(v0, w[u], vl0, rl0);
-            const PV<T> q1 = have_qc[u] ? qc[u] : pv_eval(v1, w[u], vl1, rl);
-            qc[u] = q0;
-            have_qc[u] = true;
+            const PV<T> q1 = pv_eval(v1, w[u], vl1, rl);
             const StepGrad<T> g = step_back<T>(Ip, lam[u], q0.j, q0.a, q0.S, q1.j, q1.a, q1.S, hds);
             T gv = 0;
             point_back<T>(q1, rl, g.j1 + cgj[u], g.a1 + cga[u], g.S1, acc1, grl_seg, gv);
@@ -935,27 +766,6 @@ __device__ void adjoint_item(const AdjParams<T>& A, int item, AdjStage<T>& S, Ad
             }
             cgj[u] = gj; cga[u] = ga;
           }
-          unsigned tasks = __ballot_sync(0xffffffffu, coop);
-          while (tasks) {
-            const int o = __ffs(tasks) - 1;
-            tasks &= tasks - 1;
-            const T wo = __shfl_sync(0xffffffffu, w[u], o);
-            const T Io = __shfl_sync(0xffffffffu, Ip, o);
-            const T lo = __shfl_sync(0xffffffffu, lam[u], o);
-            const T cjo = __shfl_sync(0xffffffffu, cgj[u], o);
-            const T cao = __shfl_sync(0xffffffffu, cga[u], o);
-            const SubGrid<T> G = sub_grid<T>(kind, wo, vl0, S.q[n + 1], S.ds[n + 1], S.dvs[n + 1], S.idvs[n + 1],
-                                             hw3, lgs, ilgs);
-            const SlowOut<T> r = seg_back_coop<T>(G, init, wo, v0, v1, vl0, vl1, rl, rl0, hds, S.q[n + 1], S.ds[n + 1],
-                                                  S.ids[n + 1], Io, lo, cjo, cao, lane);
-            if (lane == o) {
-              lam[u] = r.lam; cgj[u] = r.cgj; cga[u] = r.cga;
-              grl_seg += r.g_rl;
-#pragma unroll
-              for (int k = 0; k < 4; k++) { acc0[k] += r.acc0[k]; acc1[k] += r.acc1[k]; }
-            }
-          }
-          if (slow) have_qc[u] = false;
           if (valid) {
             if (kb + n == star_node) lam[u] *= ((T)1 - fstar);
             steps++;

@@ -25,9 +25,10 @@ from . import synth
 PARAMS = ("lnT0", "q", "lnX0", "lnf")
 
 
-def fit_configs(n: int = 64, seed: int = 4, nphi: int = 4, nlines: int = 20, nch: int = 200) -> list:
+def fit_configs(n: int = 64, seed: int = 4, nphi: int = 4, nlines: int = 20, nch: int = 200, dbdr: int = 1) -> list:
     """n uneven disks: nr ~ U[100,400], ntheta ~ U[50,200], 20 ro-vibrational lines x 200
-    channels, inclination ~ U[5,85] deg, stellar mass ~ U[0.3,2.5] Msun; nphi azimuths."""
+    channels, inclination ~ U[5,85] deg, stellar mass ~ U[0.3,2.5] Msun; nphi azimuths and
+    dbdr rings per grid radius."""
     rng = np.random.default_rng(seed)
     out = []
     dv = 0.25
@@ -37,7 +38,7 @@ def fit_configs(n: int = 64, seed: int = 4, nphi: int = 4, nlines: int = 20, nch
         out.append(synth.DiskConfig(
             name=f"fit{i:02d}", nr=nr, nt=nt, mstar=float(rng.uniform(0.3, 2.5)),
             incl_deg=float(rng.uniform(5.0, 85.0)), molecule="band", band_nj=nlines // 2, ilinestart=1,
-            nlines=nlines, dv=dv, vmax=((nch - 1) + 0.05) * dv / 2.0, nphi=nphi, dbdr=1,
+            nlines=nlines, dv=dv, vmax=((nch - 1) + 0.05) * dv / 2.0, nphi=nphi, dbdr=dbdr,
             nrrextra=-max(8, nr // 8), seed=seed * 1000 + i))
     return out
 
@@ -141,8 +142,38 @@ class DiskFit:
             m.free()
 
 
-def run_fit(ctx, cfgs, steps: int = 200, lr: float = 0.02, precision: int = 0, log=None) -> dict:
-    """Adam on all models at once; returns throughput and parameter recovery."""
+def gauss_newton(fit, p, rel: float = 1e-3) -> dict:
+    """Which parameter combinations the spectra constrain at p: per model the Jacobian J of
+    its normalised spectra (F / |F_target|) in the four parameters, by central differences
+    of the batched forward (each parameter moved in every model at once: a model's spectra
+    depend on its own parameters only), and the eigenvalues of J^T J, the Gauss-Newton
+    Hessian of the loss. A small eigenvalue marks a combination the spectra hardly change
+    with (a degeneracy); its eigenvector names the combination."""
+    import torch
+    cols = []
+    for k in range(4):
+        q = p.detach().clone()
+        q[:, k] += rel
+        fp = fit.render(q)
+        q[:, k] -= 2 * rel
+        fm = fit.render(q)
+        cols.append([((a - b) / (2 * rel)).flatten() / math.sqrt(tn) for a, b, tn in zip(fp, fm, fit.tnorm)])
+    out = {"eigenvalues": [], "weakest_direction": [], "condition": []}
+    for j in range(len(fit.cfgs)):
+        J = torch.stack([cols[k][j] for k in range(4)], dim=1)
+        ev, vec = torch.linalg.eigh(J.T @ J)
+        ev = ev.cpu().numpy()
+        out["eigenvalues"].append([float(x) for x in ev])
+        out["weakest_direction"].append([float(x) for x in vec[:, 0].cpu().numpy()])
+        out["condition"].append(float(ev[-1] / max(ev[0], 1e-300)))
+    return out
+
+
+def run_fit(ctx, cfgs, steps: int = 200, lr: float = 0.02, precision: int = 0, log=None, history: bool = False,
+            analyse: bool = False) -> dict:
+    """Adam on all models at once; returns throughput and parameter recovery (with
+    history=True the largest error of each parameter every 10 steps; with analyse=True the
+    Gauss-Newton eigen-analysis at the end point)."""
     import torch
     fit = DiskFit(ctx, cfgs, precision=precision)
     fit.set_target()
@@ -151,7 +182,7 @@ def run_fit(ctx, cfgs, steps: int = 200, lr: float = 0.02, precision: int = 0, l
     err0 = (fit.p0 - fit.p_true).abs().max(dim=0).values.cpu().numpy()
     fw_ms = bw_ms = 0.0
     t0 = time.perf_counter()
-    losses = []
+    losses, hist = [], []
     for it in range(steps):
         loss, g, fst, bst = fit.loss_and_grad(p)
         fw_ms += fst["total_ms"]
@@ -160,10 +191,15 @@ def run_fit(ctx, cfgs, steps: int = 200, lr: float = 0.02, precision: int = 0, l
         p.grad = g
         opt.step()
         losses.append(loss)
+        if history and (it % 10 == 0 or it == steps - 1):
+            e = (p.detach() - fit.p_true).abs()
+            hist.append({"step": it + 1, "loss": loss, "max_abs_error": dict(zip(PARAMS, map(float, e.max(dim=0).values))),
+                         "median_abs_error": dict(zip(PARAMS, map(float, e.median(dim=0).values)))})
         if log and (it % 20 == 0 or it == steps - 1):
             log(f"step {it} loss {loss:.4e}")
     wall = time.perf_counter() - t0
     err = (p.detach() - fit.p_true).abs().max(dim=0).values.cpu().numpy()
+    errm = (p.detach() - fit.p_true).abs().median(dim=0).values.cpu().numpy()
     nspec = sum(c.nlines for c in cfgs)
     res = {"models": len(cfgs), "steps": steps, "spectra_per_step": nspec,
            "loss_first": losses[0], "loss_last": losses[-1],
@@ -171,7 +207,12 @@ def run_fit(ctx, cfgs, steps: int = 200, lr: float = 0.02, precision: int = 0, l
            "wall_s": wall, "forward_adjoint_spectra_per_s": nspec * steps / ((fw_ms + bw_ms) * 1e-3),
            "wall_spectra_per_s": nspec * steps / wall,
            "max_abs_param_error_start": dict(zip(PARAMS, map(float, err0))),
-           "max_abs_param_error_end": dict(zip(PARAMS, map(float, err)))}
+           "max_abs_param_error_end": dict(zip(PARAMS, map(float, err))),
+           "median_abs_param_error_end": dict(zip(PARAMS, map(float, errm)))}
+    if history:
+        res["history"] = hist
+    if analyse:
+        res["gauss_newton"] = gauss_newton(fit, p)
     fit.close()
     return res
 

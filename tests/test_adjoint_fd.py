@@ -11,7 +11,8 @@
   central difference of the linear loss sum(gflux * F) against the GPU's FP64 adjoint at
   the same gflux: <= 1e-3 relative on at least 32 cells per parameter whose +-h renders
   keep the base render's discrete decisions (step and integrated-channel counts); relative
-  step 1e-4, 1e-5 where a kink of the piecewise forward lies within the larger step.
+  step 1e-4, then 1e-5 and 1e-6 where a kink of the piecewise forward lies within the
+  larger step.
 """
 import os
 
@@ -133,18 +134,25 @@ def test_adjoint_vs_oracle_finite_differences(gpu_lib, ctx, oracle_lib):
         return out
 
     # relative step 1e-4; where that difference disagrees (a kink of the piecewise forward,
-    # e.g. the source bracket switching, within +-h) once more at 1e-5, which the text
-    # formats still resolve
+    # e.g. the source bracket switching or a sub-step moving, within +-h) again at 1e-5 and
+    # 1e-6, which the text formats still resolve for the temperature and the width (not for
+    # the abundance's 9 digits, whose differences agree at 1e-4)
     with mp.get_context("spawn").Pool(os.cpu_count() or 1) as pool:
         first = fd_round([(pi, c) for pi in range(3) for c in cells[pi]], 1e-4, pool)
-        again = fd_round([k for k, e in first.items() if e > FD_TOL], 1e-5, pool)
+        again = dict(first)
+        for h in (1e-5, 1e-6):
+            redo = [k for k, e in again.items() if e > FD_TOL and names[k[0]] != "lnX"]
+            if not redo:
+                break
+            finer = fd_round(redo, h, pool)
+            for k in redo:
+                if k in finer:
+                    again[k] = finer[k]
+                else:
+                    again.pop(k)          # the finer step met a decision change
     report = {n: [] for n in names}
     worst = []
-    for (pi, c), e in first.items():
-        if e > FD_TOL and (pi, c) in again:
-            e = again[(pi, c)]
-        elif e > FD_TOL:
-            continue                      # the finer step met a decision change
+    for (pi, c), e in again.items():
         report[names[pi]].append(e)
         worst.append((e, pi, int(c)))
     summary = {n: (len(e), max(e) if e else None) for n, e in report.items()}
@@ -153,7 +161,7 @@ def test_adjoint_vs_oracle_finite_differences(gpu_lib, ctx, oracle_lib):
         # the same central difference of the GPU's own FP64 forward, for the message
         params = [lnT, lnX, b]
         for e, pi, c in bad:
-            step = 1e-5 if names[pi] != "width" else 1e-5 * p0[2][c]
+            step = 1e-6 if names[pi] != "width" else 1e-6 * p0[2][c]
             vals = []
             for sgn in (1.0, -1.0):
                 q = [t.clone() for t in params]
