@@ -150,7 +150,6 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
   unsigned mbits = 0;   // tile lines whose line opacity x segment length fell below -0.01
   T lw_last = 0;
   bool pos_last = true, zero_last = false;
-  float amax_last = 0.f, amin_last = 0.f;
   for (int kb = 0; kb < K; kb += 32) {
     if (kb > 0) {   // carry the last node of the previous chunk into entry 0
       if (lane == 0) {
@@ -166,7 +165,6 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
     unsigned misc = 0;
     bool pos = true;    // every staged line has a normal dust opacity and no inversion here
     bool zero = true;   // every staged line's emissivity and opacity factors are 0 here
-    float amin = 3.0e38f;   // smallest dust opacity of the staged lines here
     if (k < K) {
       const size_t o = row + k;
       const T wr = nb.wr[o], wt = nb.wt[o];
@@ -178,25 +176,9 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
         if constexpr (kFast) {
           pos = pos && v.ad >= 1.17549435e-38f && v.af >= 0.f;
           zero = zero && v.jd == 0.f && v.jf == 0.f && v.ad == 0.f && v.af == 0.f;
-          amin = fminf(amin, (float)v.ad);
         }
       }
       vl = nb.vl[o]; ds = nb.ds[o]; dvs = nb.dvseg[o]; lwk = nb.lw[o];
-    }
-    if constexpr (kFast) {
-      // the next chunk's node records, into L2 while this chunk is walked
-      const int kn = k + 32;
-      if (kn < K) {
-        const size_t o = row + kn;
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(nb.wr + o));
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(nb.wt + o));
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(nb.misc + o));
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(nb.c00 + o));
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(nb.vl + o));
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(nb.ds + o));
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(nb.dvseg + o));
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(nb.lw + o));
-      }
     }
     T lwp = __shfl_up_sync(0xffffffffu, lwk, 1);
     if (lane == 0) lwp = lw_last;
@@ -222,24 +204,6 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
         if (lane == 0) zerop = zero_last;
         zero_last = __shfl_sync(0xffffffffu, zero, 31);
         if (zero && zerop) f |= kFlagEmpty;
-        // bounds of every slot's optical depth over the segment ending here: the opacity at a
-        // node lies in [min ad, max (ad + af rl)] of the staged lines (the profile is at most
-        // rl, up to the exponential's last bit), so (a0 + a1) hds is bracketed by the same
-        // sums, rounded alike; a bracket below 0.25 (with a margin for that bit) or at and
-        // above it fixes the coefficient form of every slot in advance
-        float amax = 0.f;
-        if (k < K)
-          for (int l = 0; l < gl; l++) {
-            const LineVals<T> v = S.lv[l][lane + 1];
-            amax = fmaxf(amax, fmadd((float)v.af, (float)rlw, (float)v.ad));
-          }
-        float amaxp = __shfl_up_sync(0xffffffffu, amax, 1), aminp = __shfl_up_sync(0xffffffffu, amin, 1);
-        if (lane == 0) { amaxp = amax_last; aminp = amin_last; }
-        amax_last = __shfl_sync(0xffffffffu, amax, 31);
-        amin_last = __shfl_sync(0xffffffffu, amin, 31);
-        const float hh = 0.5f * (float)ds;
-        if (__fmul_rn(__fadd_rn(amaxp, amax), hh) < 0.2499f) f |= kFlagSer;
-        else if (__fmul_rn(__fadd_rn(aminp, amin), hh) >= 0.25f) f |= kFlagDir;
         // node values of the packed step, duplicated into pairs: {vl, vl, hds, hds},
         // {rl, rl} (the profile's 1/width)
         const float h = 0.5f * (float)ds;
@@ -322,20 +286,12 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
               S1[p] = mul2(j1[p], make_float2(Math<float>::rcp(a1[p].x), Math<float>::rcp(a1[p].y)));
               dt[p] = mul2(add2(make_float2(a0[2 * p], a0[2 * p + 1]), a1[p]), hd2);
               th[p] = mul2(add2(make_float2(j0[2 * p], j0[2 * p + 1]), j1[p]), hd2);
+              const bool sa = dt[p].x < 0.25f, sb = dt[p].y < 0.25f;
+              ser = ser && sa && sb;
+              dir = dir && !sa && !sb;
             }
-            if (fl & (kFlagSer | kFlagDir)) {   // decided at staging for every slot
-              ser = (fl & kFlagSer) != 0;
-              dir = !ser;
-            } else {
-#pragma unroll
-              for (int p = 0; p < kPass / 2; p++) {
-                const bool sa = dt[p].x < 0.25f, sb = dt[p].y < 0.25f;
-                ser = ser && sa && sb;
-                dir = dir && !sa && !sb;
-              }
-              ser = __all_sync(0xffffffffu, ser);
-              dir = __all_sync(0xffffffffu, dir);
-            }
+            ser = __all_sync(0xffffffffu, ser);
+            dir = __all_sync(0xffffffffu, dir);
             float2 x[kPass / 2], ca[kPass / 2], cb[kPass / 2];
             if (ser) {
 #pragma unroll
