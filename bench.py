@@ -398,6 +398,8 @@ def ours(args):
     if rank == 0 and not args.no_diff:
         adjoint = adjoint_case(ctx)
         fitting = fit_case(ctx, args.fit_models, args.fit_steps, nphi=args.fit_nphi, dbdr=args.fit_dbdr)
+        if args.recovery_steps > 0:
+            fitting["recovery"] = recovery_case(ctx, steps=args.recovery_steps)
     out = None
     if rank == 0:
         cpu = parity = disk = None
@@ -650,6 +652,19 @@ def fit_case(ctx, n_models=64, steps=5, plain_models=8, nphi=32, dbdr=2, history
     return out
 
 
+def recovery_case(ctx, n_models=8, steps=200, nphi=8, dbdr=1):
+    """Parameter recovery of the fitting loop: `steps` Adam steps on n uneven disks of the
+    fitting workload (smaller images, so that 200 steps stay within a minute or two), the
+    error of each parameter every 10 steps, and the Gauss-Newton eigen-analysis at the end
+    point (which parameter combinations the spectra constrain)."""
+    from radlite_gb300 import fit
+    cfgs = fit.fit_configs(n_models, nphi=nphi, dbdr=dbdr)
+    res = fit.run_fit(ctx, cfgs, steps=steps, history=True, analyse=True)
+    res["workload"] = (f"{n_models} uneven disks (nr 100-400, ntheta 50-200), 20 lines x 200 channels, {nphi} "
+                       f"azimuths, {dbdr} ring per grid radius, 4 parameters each, {steps} Adam steps (lr 0.02)")
+    return res
+
+
 def profile_case(args):
     """One pass of a named workload (geometry, walk, reduction), for profiler captures.
     "posvel_disk": the 200x100 disk's 128x128-pixel position-velocity cube of 2 lines;
@@ -710,6 +725,8 @@ def main():
     ap.add_argument("--ref-stride", type=int, default=509,
                     help="ray stride of each step of --impl reference (all lines, both inclinations)")
     ap.add_argument("--fit-steps", type=int, default=3, help="Adam steps of the fitting measurement")
+    ap.add_argument("--recovery-steps", type=int, default=200,
+                    help="Adam steps of the parameter-recovery study (0 skips it)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-verify", action="store_true")
     ap.add_argument("--batch-models", type=int, default=256,
@@ -719,6 +736,7 @@ def main():
     ap.add_argument("--nphi", type=int, default=0,
                     help="azimuths of the adjoint timing and of --profile (0: the workload's)")
     ap.add_argument("--only-fit", action="store_true", help="run only the batched fitting-step comparison")
+    ap.add_argument("--only-recovery", action="store_true", help="run only the parameter-recovery study")
     ap.add_argument("--fit-models", type=int, default=16)
     ap.add_argument("--fit-nphi", type=int, default=32, help="azimuths of the fitting images")
     ap.add_argument("--fit-dbdr", type=int, default=2, help="rings per grid radius of the fitting images")
@@ -726,6 +744,12 @@ def main():
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the position-velocity, gen_spec and input-parsing measurements")
     args = ap.parse_args()
+    if args.only_recovery:
+        import radlite_gb300 as rl
+        ctx = rl.Context(0)
+        print(json.dumps(recovery_case(ctx, steps=args.recovery_steps)), flush=True)
+        ctx.close()
+        return 0
     if args.only_fit:
         import radlite_gb300 as rl
         ctx = rl.Context(0)
