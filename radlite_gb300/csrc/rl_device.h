@@ -28,8 +28,6 @@ constexpr unsigned kFlagInit = 1u << 22;   // (walk) the segment ending here res
 constexpr unsigned kFlagSub = 1u << 23;    // (walk) the segment ending here may need sub-steps
 constexpr unsigned kFlagEmpty = 1u << 25;  // (FP32 walk) every staged line has zero emissivity and
                                            // opacity at this node and the previous one
-constexpr unsigned kFlagClear = 1u << 26;  // (FP32 walk) every staged line has zero opacity factors at
-                                           // this node and the previous one (emission only)
 constexpr unsigned kFlagNeg = 1u << 24;    // (FP32 walk) some staged line lacks a positive opacity at
                                            // this node or the previous one
 constexpr int kIcrShift = 18;              // bits 18-19: crossing type 1..3

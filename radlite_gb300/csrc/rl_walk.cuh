@@ -146,10 +146,10 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
   }
   // per-call counts (32-bit: a call walks one tile of one ray): formal-solution steps, node
   // passes, of them on the general path and empty, and the steps of empty segments
-  unsigned steps = 0, passes = 0, general = 0, emptyp = 0, skipped = 0, clearp_n = 0;
+  unsigned steps = 0, passes = 0, general = 0, emptyp = 0, skipped = 0;
   unsigned mbits = 0;   // tile lines whose line opacity x segment length fell below -0.01
   T lw_last = 0;
-  bool pos_last = true, zero_last = false, clear_last = false;
+  bool pos_last = true, zero_last = false;
   for (int kb = 0; kb < K; kb += 32) {
     if (kb > 0) {   // carry the last node of the previous chunk into entry 0
       if (lane == 0) {
@@ -165,7 +165,6 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
     unsigned misc = 0;
     bool pos = true;    // every staged line has a normal dust opacity and no inversion here
     bool zero = true;   // every staged line's emissivity and opacity factors are 0 here
-    bool clear = true;  // every staged line's opacity factors are 0 here
     if (k < K) {
       const size_t o = row + k;
       const T wr = nb.wr[o], wt = nb.wt[o];
@@ -176,8 +175,7 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
         S.lv[l][lane + 1] = v;
         if constexpr (kFast) {
           pos = pos && v.ad >= 1.17549435e-38f && v.af >= 0.f;
-          clear = clear && v.ad == 0.f && v.af == 0.f;
-          zero = zero && clear && v.jd == 0.f && v.jf == 0.f;
+          zero = zero && v.jd == 0.f && v.jf == 0.f && v.ad == 0.f && v.af == 0.f;
         }
       }
       vl = nb.vl[o]; ds = nb.ds[o]; dvs = nb.dvseg[o]; lwk = nb.lw[o];
@@ -206,12 +204,6 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
         if (lane == 0) zerop = zero_last;
         zero_last = __shfl_sync(0xffffffffu, zero, 31);
         if (zero && zerop) f |= kFlagEmpty;
-        // a segment between two nodes without opacity but with emission: dtau = 0, x = 1, and
-        // the step adds Q = 0.5 (j0 + j1) ds
-        bool clearp = __shfl_up_sync(0xffffffffu, clear, 1);
-        if (lane == 0) clearp = clear_last;
-        clear_last = __shfl_sync(0xffffffffu, clear, 31);
-        if (clear && clearp && !(zero && zerop)) f |= kFlagClear;
         // node values of the packed step, duplicated into pairs: {vl, vl, hds, hds},
         // {rl, rl} (the profile's 1/width)
         const float h = 0.5f * (float)ds;
@@ -264,7 +256,7 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
             emptyp++;
             continue;
           }
-          bool slow = (fl & kFlagInit) != 0 || (fl & (kFlagNeg | kFlagClear)) == kFlagNeg;
+          bool slow = (fl & (kFlagInit | kFlagNeg)) != 0;
           if (!slow && (fl & kFlagSub)) {
             // a SUBGRID window that overlaps the segment sends the node to the general path
             const T vl0 = S.vl[n], dsf = S.ds[n + 1];
@@ -276,29 +268,6 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
               any = any || (Ls[u] >= 0 && (s_c + G.hw3 > (T)0) && (s_c - G.hw3 < dsf));
             }
             slow = __any_sync(0xffffffffu, any);
-          }
-          if (!slow && (fl & kFlagClear)) {
-            // no opacity at either node: the general step reduces to I += 0.5 (j0 + j1) ds with
-            // the carried opacity and source function zero (same roundings)
-            const float4 h0 = S.hot[n + 1][0], h1 = S.hot[n + 1][1];
-            const float2 vl2 = make_float2(h0.x, h0.y), hd2 = make_float2(h0.z, h0.w);
-            const float2 rl2 = make_float2(h1.x, h1.y);
-#pragma unroll
-            for (int p = 0; p < kPass / 2; p++) {
-              const LineVals<T> vA = S.lv[lsl[2 * p]][n + 1], vB = S.lv[lsl[2 * p + 1]][n + 1];
-              const float2 u = mul2(sub2(make_float2(w[2 * p], w[2 * p + 1]), vl2), rl2);
-              const float2 m = mul2(mul2(u, u), dup2(-1.4426950408889634f));
-              const float2 ph = mul2(rl2, make_float2(ex2(m.x), ex2(m.y)));
-              const float2 j1 = make_float2(fmaf(vA.jf, ph.x, vA.jd), fmaf(vB.jf, ph.y, vB.jd));
-              const float2 th = mul2(add2(make_float2(j0[2 * p], j0[2 * p + 1]), j1), hd2);
-              const float2 In = fma2(make_float2(I[2 * p], I[2 * p + 1]), dup2(1.f), th);
-              I[2 * p] = In.x; I[2 * p + 1] = In.y;
-              j0[2 * p] = j1.x; j0[2 * p + 1] = j1.y;
-              a0[2 * p] = 0.f; a0[2 * p + 1] = 0.f;
-              S0[2 * p] = 0.f; S0[2 * p + 1] = 0.f;
-            }
-            clearp_n++;
-            continue;
           }
           if (!slow) {
             const float4 h0 = S.hot[n + 1][0], h1 = S.hot[n + 1][1];
@@ -504,7 +473,7 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
       for (; mbits; mbits &= mbits - 1) atomicExch(&P.maser[l0 + __ffs(mbits) - 1], 1);
   }
   wc.passes += passes;
-  wc.packed += kFast ? passes - general - emptyp - clearp_n : 0u;
+  wc.packed += kFast ? passes - general - emptyp : 0u;
   wc.skipped += skipped;
   return steps;
 }
