@@ -148,7 +148,8 @@ def gauss_newton(fit, p, rel: float = 1e-3) -> dict:
     of the batched forward (each parameter moved in every model at once: a model's spectra
     depend on its own parameters only), and the eigenvalues of J^T J, the Gauss-Newton
     Hessian of the loss. A small eigenvalue marks a combination the spectra hardly change
-    with (a degeneracy); its eigenvector names the combination."""
+    with (a degeneracy); its eigenvector names the combination. "vectors" holds each model's
+    eigenvectors as columns, weakest first."""
     import torch
     cols = []
     for k in range(4):
@@ -158,14 +159,35 @@ def gauss_newton(fit, p, rel: float = 1e-3) -> dict:
         q[:, k] -= 2 * rel
         fm = fit.render(q)
         cols.append([((a - b) / (2 * rel)).flatten() / math.sqrt(tn) for a, b, tn in zip(fp, fm, fit.tnorm)])
-    out = {"eigenvalues": [], "weakest_direction": [], "condition": []}
+    out = {"eigenvalues": [], "weakest_direction": [], "condition": [], "vectors": []}
     for j in range(len(fit.cfgs)):
         J = torch.stack([cols[k][j] for k in range(4)], dim=1)
         ev, vec = torch.linalg.eigh(J.T @ J)
         ev = ev.cpu().numpy()
         out["eigenvalues"].append([float(x) for x in ev])
         out["weakest_direction"].append([float(x) for x in vec[:, 0].cpu().numpy()])
+        out["vectors"].append(vec.cpu().numpy().tolist())
         out["condition"].append(float(ev[-1] / max(ev[0], 1e-300)))
+    return out
+
+
+def error_in_eigenbasis(gn: dict, e_start, e_end) -> dict:
+    """The parameter error of each model at the start and the end of a fit, split over the
+    eigenvectors of its end-point Gauss-Newton Hessian H = J^T J: the component along the
+    weakest eigenvector (the combination the spectra hardly constrain) and the error the
+    spectra do see, sqrt(e^T H e) (the first-order change of the normalised spectra, in
+    units of the loss's norm). A fit that reduces the second while the first stays put or
+    grows has recovered everything the spectra determine."""
+    out = {"weak_component_start": [], "weak_component_end": [], "seen_error_start": [], "seen_error_end": []}
+    for j, (ev, vec) in enumerate(zip(gn["eigenvalues"], gn["vectors"])):
+        v = np.asarray(vec)
+        lam = np.asarray(ev)
+        for tag, e in (("start", e_start[j]), ("end", e_end[j])):
+            c = v.T @ e
+            out[f"weak_component_{tag}"].append(float(c[0]))
+            out[f"seen_error_{tag}"].append(float(math.sqrt(max(float(np.sum(lam * c * c)), 0.0))))
+    out["median_seen_error_ratio_end_over_start"] = float(np.median(
+        np.asarray(out["seen_error_end"]) / np.maximum(np.asarray(out["seen_error_start"]), 1e-300)))
     return out
 
 
@@ -212,7 +234,10 @@ def run_fit(ctx, cfgs, steps: int = 200, lr: float = 0.02, precision: int = 0, l
     if history:
         res["history"] = hist
     if analyse:
-        res["gauss_newton"] = gauss_newton(fit, p)
+        gn = gauss_newton(fit, p)
+        res["gauss_newton"] = gn
+        res["error_in_eigenbasis"] = error_in_eigenbasis(gn, (fit.p0 - fit.p_true).cpu().numpy(),
+                                                         (p.detach() - fit.p_true).cpu().numpy())
     fit.close()
     return res
 
