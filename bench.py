@@ -629,6 +629,11 @@ def adjoint_case(ctx, name="adjoint_disk", reps=3, **over):
            "spectra": cfg.nlines}
     res["adjoint_over_forward"] = res["adjoint_ms"] / res["forward_ms"]
     res["forward_adjoint_spectra_per_s"] = cfg.nlines / ((res["forward_ms"] + res["adjoint_ms"]) * 1e-3)
+    # the same gradient by central differences: two forwards per cell parameter
+    npar = 3 * int(lnT.numel())
+    res["parameters"] = npar
+    res["speedup_vs_central_differences"] = ((2 * npar + 1) * res["forward_ms"]
+                                             / (res["forward_ms"] + res["adjoint_ms"]))
     d.close()
     m.free()
     return res
@@ -649,6 +654,10 @@ def fit_case(ctx, n_models=64, steps=5, plain_models=8, nphi=32, dbdr=2, history
            "plain_forward_fd": {"models_timed": plain_models, "seconds_per_gradient_spectrum": per_spec,
                                 "spectra_per_s": 1.0 / per_spec}}
     out["speedup_vs_plain_fd"] = res["forward_adjoint_spectra_per_s"] * per_spec
+    # four parameters: central differences cost 9 forwards per gradient, the batched
+    # forward + adjoint this many forwards' time
+    out["forward_equivalents_per_gradient"] = ((res["forward_ms_per_step"] + res["adjoint_ms_per_step"])
+                                               / res["forward_ms_per_step"])
     return out
 
 

@@ -227,7 +227,8 @@ int rl_batch_set_memory(rl_batch* batch, double bytes);
    per lane (1, 2, 4, 8). Default 32 lines, 4 slots. */
 int rl_batch_set_tiles(rl_batch* batch, int lines_per_item, int channel_slots);
 int rl_batch_get_tiles(rl_batch* batch, int* lines_per_item, int* channel_slots);
-/* Times the tile shapes (2, 8, 16, 32 lines per item x 2, 4 slots) on every
+/* Times the tile shapes (2, 8, 16, 32 lines per item, 4 slots: the walk steps four slots
+   per lane together) on every
    sample_stride-th work item of the first wave and keeps the fastest, the default shape
    unless another beats it by 2% (a stride of 8 or less samples enough items to rank them);
    returns it and the sampled walk time. No counterpart in the reference. */

@@ -841,6 +841,38 @@ __global__ void __launch_bounds__(128) k_adjoint_jobs(AdjJobs<T> B) {
   }
 }
 
+// The same for one job whose parameters are a kernel argument (the constant bank) rather
+// than a shared-memory copy: the single-model adjoint.
+template <typename T>
+__global__ void __launch_bounds__(128) k_adjoint_one(AdjParams<T> A, AdjJobs<T> B) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  AdjStage<T>* stages = reinterpret_cast<AdjStage<T>*>(smem_raw);
+  AdjSlots<T>* slots = reinterpret_cast<AdjSlots<T>*>(smem_raw + sizeof(AdjStage<T>) * nw);
+  unsigned short* lists =
+      reinterpret_cast<unsigned short*>(smem_raw + (sizeof(AdjStage<T>) + sizeof(AdjSlots<T>)) * nw);
+  const int capp = (B.max_nfr + 7) & ~7;
+  unsigned short* list = lists + (size_t)wib * capp;
+  T* ck = B.ckpt + ((size_t)blockIdx.x * nw + wib) * (size_t)B.ckpt_warp;
+  unsigned long long steps = 0, zc = 0;
+  for (;;) {
+    int item = 0;
+    if (lane == 0) item = atomicAdd(B.work, 1);
+    item = __shfl_sync(0xffffffffu, item, 0);
+    if (item >= B.total) break;
+    adjoint_item<T>(A, item, stages[wib], slots[wib], list, ck, B.ckpt_warp, B.every, lane, steps, zc);
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    steps += __shfl_xor_sync(0xffffffffu, steps, off);
+    zc += __shfl_xor_sync(0xffffffffu, zc, off);
+  }
+  if (lane == 0) {
+    atomicAdd(&B.counters[0], steps);
+    if (zc) atomicAdd(&B.counters[1], zc);
+  }
+}
+
 // ------------------------------------------------------------------------------------
 // launchers
 // ------------------------------------------------------------------------------------
@@ -878,9 +910,14 @@ cudaError_t adjoint_grid(int nsm, int max_nfr, int* blocks) {
   const size_t smem = adjoint_smem<T>(max_nfr);
   cudaError_t e = cudaFuncSetAttribute(k_adjoint_jobs<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  int per_sm = 0;
+  e = cudaFuncSetAttribute(k_adjoint_one<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  int per_sm = 0, per_sm1 = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_adjoint_jobs<T>, 128, smem);
   if (e != cudaSuccess) return e;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm1, k_adjoint_one<T>, 128, smem);
+  if (e != cudaSuccess) return e;
+  per_sm = per_sm1 < per_sm ? per_sm1 : per_sm;   // the scratch is sized for the smaller grid
   *blocks = nsm * (per_sm < 1 ? 1 : per_sm);
   return cudaSuccess;
 }
@@ -896,6 +933,15 @@ cudaError_t launch_adjoint(const AdjJobs<T>& B, int blocks, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(B.work, 0, sizeof(int), s);
   if (e != cudaSuccess) return e;
   k_adjoint_jobs<T><<<blocks, 128, smem, s>>>(B);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_adjoint_one(const AdjParams<T>& A, const AdjJobs<T>& B, int blocks, cudaStream_t s) {
+  const size_t smem = adjoint_smem<T>(B.max_nfr);
+  cudaError_t e = cudaMemsetAsync(B.work, 0, sizeof(int), s);
+  if (e != cudaSuccess) return e;
+  k_adjoint_one<T><<<blocks, 128, smem, s>>>(A, B);
   return cudaGetLastError();
 }
 
@@ -926,5 +972,7 @@ template long long adjoint_ckpt_per_warp<float>(int, int);
 template long long adjoint_ckpt_per_warp<double>(int, int);
 template cudaError_t launch_adjoint<float>(const AdjJobs<float>&, int, cudaStream_t);
 template cudaError_t launch_adjoint<double>(const AdjJobs<double>&, int, cudaStream_t);
+template cudaError_t launch_adjoint_one<float>(const AdjParams<float>&, const AdjJobs<float>&, int, cudaStream_t);
+template cudaError_t launch_adjoint_one<double>(const AdjParams<double>&, const AdjJobs<double>&, int, cudaStream_t);
 
 }  // namespace rl

@@ -29,6 +29,10 @@ using namespace rl;
 namespace {
 
 constexpr size_t kAlign = 256;
+// Streams the per-job walk launches of a run are spread over: a job's persistent launch
+// holds the whole GPU until its work counter runs dry, and the launches queued on the
+// other streams fill the SMs its tail leaves idle.
+constexpr int kSideStreams = 4;
 inline size_t align_up(size_t x) { return (x + kAlign - 1) & ~(kAlign - 1); }
 
 struct BatchJob {
@@ -53,6 +57,8 @@ struct Wave {
   size_t bytes = 0;
   DevBuf dgeo, dwalk, dred, dray, ditem, dring, dline;
   JobLaunch<T> L{};
+  std::vector<WalkParams<T>> hwalk;   // per-job walk launches, in queue order
+  std::vector<int> side;              // stream of each of them
 };
 
 template <typename T>
@@ -75,6 +81,9 @@ struct rl_batch {
   Plan<float> pf;
   Plan<double> pd;
   DevBuf arena, flux, counters, work, err, list;
+  DevBuf jwork;                  // one work counter per job of a wave (per-job walk launches)
+  cudaStream_t side[kSideStreams] = {};
+  cudaEvent_t fork = nullptr, join[kSideStreams] = {};
   DevBuf maser;                  // [nlines_total] masing flags (jobs with an inverted line)
   bool any_inverted = false;
   double* flux_h = nullptr;
@@ -94,6 +103,11 @@ struct rl_batch {
   ~rl_batch() {
     if (ctx) cudaSetDevice(ctx->device);
     drop_graph();
+    for (int k = 0; k < kSideStreams; k++) {
+      if (side[k]) cudaStreamDestroy(side[k]);
+      if (join[k]) cudaEventDestroy(join[k]);
+    }
+    if (fork) cudaEventDestroy(fork);
     if (flux_h) cudaFreeHost(flux_h);
     if (maser_h) cudaFreeHost(maser_h);
     if (cnt_h) cudaFreeHost(cnt_h);
@@ -191,6 +205,27 @@ int write_descriptors(rl_batch* b) {
     std::vector<WalkParams<T>> walk(nj);
     std::vector<RedJob<T>> red(nj);
     std::vector<int> rayp(nj + 1, 0), itemp(nj + 1, 0), ringp(nj + 1, 0), linep(nj + 1, 0);
+    // per-job launches: each job to the stream with the least work queued so far (largest
+    // jobs first), so that the streams end together
+    W.side.assign(nj, 0);
+    {
+      double load[kSideStreams] = {};
+      std::vector<int> order(nj);
+      std::iota(order.begin(), order.end(), 0);
+      auto job_cost = [&](int q) {
+        const BatchJob& J = *b->jobs[W.jobs[q]];
+        int ng, gs;
+        job_groups(J.nl, b->gcap, ng, gs);
+        return (double)ng * J.cam.nrays * item_cost(J, b->gcap);
+      };
+      std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return job_cost(x) > job_cost(y); });
+      for (int q : order) {
+        const int k = (int)(std::min_element(load, load + kSideStreams) - load);
+        W.side[q] = k;
+        load[k] += job_cost(q);
+      }
+    }
+    const size_t list_stride = walk_list_elems(ctx->nsm, max_nfr);
     for (int q = 0; q < nj; q++) {
       BatchJob& J = *b->jobs[W.jobs[q]];
       size_t off = J.arena_off;   // fixed at build time: independent of the queue order
@@ -233,9 +268,9 @@ int write_descriptors(rl_batch* b) {
       w.fstar = (T)J.fstar;
       w.img = img;
       w.counters = b->counters.as<unsigned long long>();
-      w.work = b->work.as<int>();
+      w.work = b->jwork.as<int>() + q;              // the per-job launch's own queue
       w.err = b->err.as<int>();
-      w.list = b->list.as<unsigned short>();
+      w.list = b->list.as<unsigned short>() + list_stride * W.side[q];   // its stream's list rows
       w.maser = J.inverted ? b->maser.as<int>() + J.line_off : nullptr;
       RedJob<T>& r = red[q];
       r.p.nrays = cam.nrays; r.p.nfr = J.nfr; r.p.nphi = cam.nphi; r.p.nrr = cam.nrr; r.p.nlines = J.nl;
@@ -270,6 +305,7 @@ int write_descriptors(rl_batch* b) {
     L.reduce = true;
     L.red = static_cast<RedJob<T>*>(W.dred.p); L.ring_prefix = static_cast<int*>(W.dring.p); L.line_prefix = static_cast<int*>(W.dline.p);
     L.nring_blocks = ringp[nj]; L.nline_blocks = linep[nj];
+    W.hwalk = walk;
   }
   CUDA_TRY(cudaStreamSynchronize(s));
   b->drop_graph();
@@ -326,8 +362,18 @@ int build(rl_batch* b) {
   {
     int max_nfr = 0;
     for (auto& J : b->jobs) max_nfr = std::max(max_nfr, J->nfr);
-    CUDA_TRY(b->list.ensure(sizeof(unsigned short) * walk_list_elems(ctx->nsm, max_nfr)));
+    CUDA_TRY(b->list.ensure(sizeof(unsigned short) * walk_list_elems(ctx->nsm, max_nfr) * kSideStreams));
   }
+  {
+    size_t maxj = 1;
+    for (const Wave<T>& W : P.waves) maxj = std::max(maxj, W.jobs.size());
+    CUDA_TRY(b->jwork.ensure(sizeof(int) * maxj));
+  }
+  for (int k = 0; k < kSideStreams; k++) {
+    if (!b->side[k]) CUDA_TRY(cudaStreamCreateWithFlags(&b->side[k], cudaStreamNonBlocking));
+    if (!b->join[k]) CUDA_TRY(cudaEventCreateWithFlags(&b->join[k], cudaEventDisableTiming));
+  }
+  if (!b->fork) CUDA_TRY(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
   if (b->flux_h) { cudaFreeHost(b->flux_h); b->flux_h = nullptr; }
   CUDA_TRY(cudaMallocHost((void**)&b->flux_h, sizeof(double) * b->nflux));
   if (!b->cnt_h) CUDA_TRY(cudaMallocHost((void**)&b->cnt_h, sizeof(unsigned long long) * kWalkCounters));
@@ -350,7 +396,26 @@ cudaError_t enqueue(rl_batch* b, cudaStream_t s, bool skip_geometry) {
   for (Wave<T>& W : plan_of<T>(b).waves) {
     if (e != cudaSuccess) return e;
     JobLaunch<T> L = W.L;
-    if (skip_geometry) L.nrays_total = 0;
+    if (!skip_geometry) {   // the geometry of every job of the wave in one launch
+      L.walk_jobs = false;
+      L.reduce = false;
+      e = launch_jobs<T>(L, s);
+      if (e != cudaSuccess) return e;
+    }
+    // one walk launch per job (the single-model kernel), spread over the side streams
+    const int nj = (int)W.hwalk.size();
+    e = cudaMemsetAsync(b->jwork.p, 0, sizeof(int) * nj, s);
+    if (e == cudaSuccess) e = cudaEventRecord(b->fork, s);
+    for (int k = 0; k < kSideStreams && e == cudaSuccess; k++) e = cudaStreamWaitEvent(b->side[k], b->fork, 0);
+    for (int q = 0; q < nj && e == cudaSuccess; q++) e = launch_walk<T>(W.hwalk[q], b->cpl, L.nsm, b->side[W.side[q]]);
+    for (int k = 0; k < kSideStreams && e == cudaSuccess; k++) {
+      e = cudaEventRecord(b->join[k], b->side[k]);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(s, b->join[k], 0);
+    }
+    if (e != cudaSuccess) return e;
+    L.nrays_total = 0;
+    L.walk_jobs = false;
+    L.reduce = true;
     e = launch_jobs<T>(L, s);
   }
   if (e == cudaSuccess) e = cudaMemcpyAsync(b->flux_h, b->flux.p, sizeof(double) * b->nflux, cudaMemcpyDeviceToHost, s);
@@ -439,10 +504,11 @@ int autotune(rl_batch* b, int stride, int* gbest, int* cbest, double* best_ms) {
   }
   int maxnl = 1;
   for (int j : P.waves[0].jobs) maxnl = std::max(maxnl, b->jobs[j]->nl);
-  // eight slots per lane need more shared memory than four 4-warp blocks per SM leave
-  // beside the 12-line stage, so the tuner tries two and four
+  // the walk steps four slots per lane together, so fewer slots per tile leave
+  // lanes of every pass empty, and eight need more shared memory than four 4-warp blocks
+  // per SM leave beside the 12-line stage: the tuner varies the lines per item only
   const int gc[] = {2, 8, 16, kItemLines};
-  const int cc[] = {2, 4};
+  const int cc[] = {4};
   // A sample of few items ends in a tail that the full walk does not have, so the default
   // shape (32 lines, 4 slots) keeps its place unless another shape beats it by 2%.
   double best = 1e300, best_score = 1e300;

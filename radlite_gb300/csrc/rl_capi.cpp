@@ -67,9 +67,13 @@ int rl::upload_grid(rl_model* md) {
   CUDA_TRY(h2d(md->dvel.p, m.vel.data(), sizeof(double) * m.vel.size(), s));
   CUDA_TRY(h2d(md->dlw.p, m.lw.data(), sizeof(double) * m.lw.size(), s));
   std::vector<float> velf(m.vel.begin(), m.vel.end()), lwf(m.lw.begin(), m.lw.end());
+  std::vector<float> vell(m.vel.size());   // float-float low parts of the velocities
+  for (size_t i = 0; i < vell.size(); i++) vell[i] = (float)(m.vel[i] - (double)velf[i]);
   CUDA_TRY(md->dvelf.ensure(sizeof(float) * velf.size()));
+  CUDA_TRY(md->dvell.ensure(sizeof(float) * vell.size()));
   CUDA_TRY(md->dlwf.ensure(sizeof(float) * lwf.size()));
   CUDA_TRY(h2d(md->dvelf.p, velf.data(), sizeof(float) * velf.size(), s));
+  CUDA_TRY(h2d(md->dvell.p, vell.data(), sizeof(float) * vell.size(), s));
   CUDA_TRY(h2d(md->dlwf.p, lwf.data(), sizeof(float) * lwf.size(), s));
   CUDA_TRY(cudaStreamSynchronize(s));
   md->grid_ready = true;
@@ -767,7 +771,7 @@ int rl_debug_trajectory(rl_model* md, int iray, int cap, double* s, double* r, d
   p.nr = m.nr; p.nth = m.nth; p.ny = m.ny; p.rstar = m.rstar; p.theta0 = cam.theta0;
   p.R = md->dR.as<double>(); p.TH = md->dTH.as<double>(); p.tan2 = md->dtan2.as<double>();
   p.vel = md->dvel.as<double>(); p.lw = md->dlw.as<double>(); p.x0 = bx0.as<double>(); p.z0 = bz0.as<double>();
-  p.velf = md->dvelf.as<float>(); p.lwf = md->dlwf.as<float>();
+  p.velf = md->dvelf.as<float>(); p.vell = md->dvell.as<float>(); p.lwf = md->dlwf.as<float>();
   NodeBuf<double> nb;
   nb.nrays = 1; nb.kmax = kmax; nb.nnodes = bnn.as<int>(); nb.status = bst.as<int>();
   nb.ds = bds.as<double>(); nb.dvf = bdvf.as<float>(); nb.vl = bvl.as<double>(); nb.dvseg = bdvs.as<double>();

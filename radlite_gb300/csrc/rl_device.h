@@ -64,6 +64,7 @@ struct GeoParams {
   const double* vel;    // [ncell*3]
   const double* lw;     // [ncell]
   const float* velf;    // [ncell*3] FP32 copies for the FP32 build's node values
+  const float* vell;    // [ncell*3] their low parts, vel - (double)velf (float-float velocity)
   const float* lwf;     // [ncell]
   const double* x0;     // [nrays]
   const double* z0;     // [nrays]
@@ -147,6 +148,7 @@ struct JobLaunch {
   const int* ray_prefix;
   int nrays_total;
   WalkJobs<T> walk;
+  bool walk_jobs = true;     // false: no walk launch (the jobs are walked by per-job launches)
   bool reduce;
   const RedJob<T>* red;      // [njobs] (device)
   const int* ring_prefix;    // [njobs+1] (line, ring) pairs

@@ -35,6 +35,8 @@ template <typename T>
 long long adjoint_ckpt_per_warp(int kmax, int every);
 template <typename T>
 cudaError_t launch_adjoint(const AdjJobs<T>& B, int blocks, cudaStream_t s);
+template <typename T>
+cudaError_t launch_adjoint_one(const AdjParams<T>& A, const AdjJobs<T>& B, int blocks, cudaStream_t s);
 cudaError_t launch_adjoint_finish(const float4* g4, double* gT, double* gX, double* gb, long long n, cudaStream_t s);
 }  // namespace rl
 
@@ -334,7 +336,7 @@ int backward(rl_diff* d, const double* gflux, double* g_lnT, double* g_lnX, doub
   CUDA_TRY(cudaMemsetAsync(d->acnt.p, 0, sizeof(unsigned long long) * 4, s));
   CUDA_TRY(cudaMemsetAsync(d->err.p, 0, sizeof(int), s));
   CUDA_TRY(cudaEventRecord(ctx->ev[0], s));
-  CUDA_TRY(launch_adjoint<T>(B, d->adj_blocks, s));
+  CUDA_TRY(launch_adjoint_one<T>(A, B, d->adj_blocks, s));
   if (A.g4) CUDA_TRY(launch_adjoint_finish(A.g4, g_lnT, g_lnX, g_width, d->ncell, s));
   CUDA_TRY(cudaEventRecord(ctx->ev[1], s));
   CUDA_TRY(cudaEventRecord(ctx->ev[2], s));

@@ -114,7 +114,8 @@ struct TAcc { const Grid* g; RL_HD double operator()(int j) const { return Tg(*g
 struct Ray {
   double x0, z0, costh0, sinth0, costh02, sinth02, pitheta0, bimpact;
   double bnew, znew;                    // direction(): impact distance and offset in the ray plane
-  float bnew_f, znew_f, costh0_f;       // FP32 copies for direction_f
+  float bnew_f, znew_f, costh0_f;       // FP32 copies for direction_ff (high parts)
+  float bnew_l, znew_l, costh0_l;       //   and their low parts (x - (double)x_f)
   int iy0, isnr, isdblnr, caseA, iup;   // theta crossings
   int ir_min, ir_amount, ith_amount;    // r crossings
 };
@@ -122,7 +123,8 @@ struct Ray {
 // One emitted node of the trajectory.
 struct Node {
   double s, r, th, mu, sinmu, sinphi, cosphi;   // sinmu = sqrt(1 - mu^2)
-  float mu_f, sinmu_f, sinphi_f, cosphi_f;      // the same from direction_f (FP32 node values)
+  float mu_f, sinmu_f, sinphi_f, cosphi_f;      // the same from direction_ff (FP32 node values):
+  float mu_l, sinmu_l, sinphi_l, cosphi_l;      //   high and low parts of a float-float value
   int icr, ir, it;
 };
 
@@ -143,6 +145,9 @@ RL_HD int init_ray(const Grid& g, double x0, double z0, double theta0, Ray& y) {
   y.znew = z0 * y.sinth02;
   y.bnew = sqrt(x0 * x0 + z0 * z0 * y.sinth02);
   y.bnew_f = (float)y.bnew; y.znew_f = (float)y.znew; y.costh0_f = (float)y.costh0;
+  y.bnew_l = (float)(y.bnew - (double)y.bnew_f);
+  y.znew_l = (float)(y.znew - (double)y.znew_f);
+  y.costh0_l = (float)(y.costh0 - (double)y.costh0_f);
   // theta=const cones with two crossings: contiguous suffix iy0..nth of the stored half
   int first = 0, count = 0;
   for (int iy = 1; iy <= g.nth; iy++) {
@@ -353,41 +358,105 @@ RL_HD void direction(const Ray& y, double s, double& mu, double& sinmu, double& 
   cosphi = (y.x0 < 0.0) ? c : -c;
 }
 
-// direction() in FP32 from the FP64 position along the ray: the FP32 build stores the
-// projected velocity in FP32, so its direction needs no more.
-// Every operation is spelled out (no contraction left to the compiler), so that all
-// kernels that inline it produce the same bits.
+// The FP32 build's node values come from float-float ("double-single") arithmetic: a
+// value is hi + lo with |lo| <= ulp(hi)/2, about 44 significant bits, built on the
+// error-free transformations of Knuth (two-sum) and Dekker (two-product, here with a
+// fused multiply-add). The projected velocity rounded to FP32 then equals the FP64
+// value rounded to FP32 except within about 1e-13 of a rounding boundary, so the FP32
+// build takes the reference's velocity-window decisions (REAL minvel/maxvel of the
+// FP64 omega.v, telescope.F:4260-4265) as the FP64 build does.
+// Every operation is spelled out (no contraction left to the compiler): the
+// transformations need each rounding where it is written.
 #ifdef __CUDA_ARCH__
 #define RL_FMA(a, b, c) __fmaf_rn(a, b, c)
 #define RL_MUL(a, b) __fmul_rn(a, b)
 #define RL_ADD(a, b) __fadd_rn(a, b)
 #define RL_SUB(a, b) __fsub_rn(a, b)
+#define RL_DIV(a, b) __fdiv_rn(a, b)
+#define RL_SQRT(a) __fsqrt_rn(a)
 #else
 #define RL_FMA(a, b, c) fmaf(a, b, c)
 #define RL_MUL(a, b) ((a) * (b))
 #define RL_ADD(a, b) ((a) + (b))
 #define RL_SUB(a, b) ((a) - (b))
+#define RL_DIV(a, b) ((a) / (b))
+#define RL_SQRT(a) sqrtf(a)
 #endif
-RL_HD void direction_f(const Ray& y, double s, float& mu, float& sinmu, float& sinphi, float& cosphi) {
-  const float snew = (float)(s + y.z0 * y.costh0);
-  const float bnew = y.bnew_f, znew = y.znew_f;
-  const float rr2 = RL_FMA(snew, snew, RL_MUL(bnew, bnew));
-  const float irad = 1.0f / sqrtf(rr2);
-  mu = fminf(1.0f, fmaxf(-1.0f, RL_MUL(snew, irad)));
-  sinmu = RL_MUL(bnew, irad);
-  const float q = RL_FMA(snew, y.costh0_f, znew);
-  const float dummy = RL_MUL(bnew, sqrtf(fmaxf(RL_FMA(-q, q, rr2), 0.0f)));
-  const float num = RL_FMA(RL_MUL(bnew, bnew), y.costh0_f, -RL_MUL(znew, snew));
-  const float sp = (dummy > 0.0f) ? num / dummy : (float)(1.0e1 * kTelEps);
-  sinphi = sp;
-  const float c = sqrtf(fmaxf(RL_FMA(-sp, sp, 1.0f), 0.0f));
-  cosphi = (y.x0 < 0.0) ? c : -c;
+struct ff { float hi, lo; };
+RL_HD ff ff_of(double x) {
+  ff r;
+  r.hi = (float)x;
+  r.lo = (float)(x - (double)r.hi);
+  return r;
+}
+RL_HD ff ff_c(float x) { return ff{x, 0.0f}; }
+// a + b for |a| >= |b| (or a = 0): the rounded sum and its exact error
+RL_HD ff ff_fast_two_sum(float a, float b) {
+  const float s = RL_ADD(a, b);
+  return ff{s, RL_SUB(b, RL_SUB(s, a))};
+}
+RL_HD ff ff_two_sum(float a, float b) {
+  const float s = RL_ADD(a, b);
+  const float bb = RL_SUB(s, a);
+  return ff{s, RL_ADD(RL_SUB(a, RL_SUB(s, bb)), RL_SUB(b, bb))};
+}
+RL_HD ff ff_add(ff x, ff y) {
+  const ff s = ff_two_sum(x.hi, y.hi);
+  return ff_fast_two_sum(s.hi, RL_ADD(s.lo, RL_ADD(x.lo, y.lo)));
+}
+RL_HD ff ff_neg(ff x) { return ff{-x.hi, -x.lo}; }
+RL_HD ff ff_sub(ff x, ff y) { return ff_add(x, ff_neg(y)); }
+RL_HD ff ff_mul(ff x, ff y) {
+  const float p = RL_MUL(x.hi, y.hi);
+  float e = RL_FMA(x.hi, y.hi, -p);
+  e = RL_FMA(x.hi, y.lo, e);
+  e = RL_FMA(x.lo, y.hi, e);
+  return ff_fast_two_sum(p, e);
+}
+RL_HD ff ff_div(ff x, ff y) {
+  const float q1 = RL_DIV(x.hi, y.hi);
+  const ff r = ff_sub(x, ff_mul(ff_c(q1), y));
+  return ff_fast_two_sum(q1, RL_DIV(r.hi, y.hi));
+}
+// sqrt(x) for x >= 0 (0 for x <= 0): one correction of the FP32 root s by (x - s^2)/(2s)
+RL_HD ff ff_sqrt(ff x) {
+  if (!(x.hi > 0.0f)) return ff_c(0.0f);
+  const float s = RL_SQRT(x.hi);
+  const float p = RL_MUL(s, s);
+  const float e = RL_FMA(s, s, -p);
+  const float r = RL_ADD(RL_SUB(RL_SUB(x.hi, p), e), x.lo);
+  return ff_fast_two_sum(s, RL_DIV(r, RL_ADD(s, s)));
+}
+
+// direction() in float-float from the FP64 position along the ray, the same formulas in
+// the same order.
+RL_HD void direction_ff(const Ray& y, double s, ff& mu, ff& sinmu, ff& sinphi, ff& cosphi) {
+  const ff bnew{y.bnew_f, y.bnew_l}, znew{y.znew_f, y.znew_l}, c0{y.costh0_f, y.costh0_l};
+  const ff snew = ff_of(s + y.z0 * y.costh0);
+  const ff rr2 = ff_add(ff_mul(bnew, bnew), ff_mul(snew, snew));
+  const ff irad = ff_div(ff_c(1.0f), ff_sqrt(rr2));
+  mu = ff_mul(snew, irad);
+  if (mu.hi > 1.0f || (mu.hi == 1.0f && mu.lo > 0.0f)) mu = ff_c(1.0f);
+  if (mu.hi < -1.0f || (mu.hi == -1.0f && mu.lo < 0.0f)) mu = ff_c(-1.0f);
+  sinmu = ff_mul(bnew, irad);
+  const ff q = ff_add(znew, ff_mul(snew, c0));
+  const ff dummy = ff_mul(bnew, ff_sqrt(ff_sub(rr2, ff_mul(q, q))));
+  sinphi = dummy.hi > 0.0f ? ff_div(ff_sub(ff_mul(ff_mul(bnew, bnew), c0), ff_mul(znew, snew)), dummy)
+                           : ff_of(1.0e1 * kTelEps);
+  const ff c = ff_sqrt(ff_sub(ff_c(1.0f), ff_mul(sinphi, sinphi)));
+  cosphi = (y.x0 < 0.0) ? c : ff_neg(c);
 }
 
 template <bool kFp32>
 RL_HD void set_direction(const Ray& y, Node& nd) {
-  if (kFp32) direction_f(y, nd.s, nd.mu_f, nd.sinmu_f, nd.sinphi_f, nd.cosphi_f);
-  else direction(y, nd.s, nd.mu, nd.sinmu, nd.sinphi, nd.cosphi);
+  if (kFp32) {
+    ff mu, sinmu, sinphi, cosphi;
+    direction_ff(y, nd.s, mu, sinmu, sinphi, cosphi);
+    nd.mu_f = mu.hi; nd.mu_l = mu.lo; nd.sinmu_f = sinmu.hi; nd.sinmu_l = sinmu.lo;
+    nd.sinphi_f = sinphi.hi; nd.sinphi_l = sinphi.lo; nd.cosphi_f = cosphi.hi; nd.cosphi_l = cosphi.lo;
+  } else {
+    direction(y, nd.s, nd.mu, nd.sinmu, nd.sinphi, nd.cosphi);
+  }
 }
 
 // Walk the merged node sequence, calling emit(const Node&) for each accepted node.

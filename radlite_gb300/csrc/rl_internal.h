@@ -169,7 +169,7 @@ struct rl_model {
   int nphi = 0, dbdr = 1, nrext = 0;
   // device copies of the grid and cell fields (uploaded once)
   bool grid_ready = false;
-  rl::DevBuf dR, dTH, dtan2, dvel, dlw, dvelf, dlwf;
+  rl::DevBuf dR, dTH, dtan2, dvel, dlw, dvelf, dvell, dlwf;
   // camera geometry cache
   bool geo_ready = false;
   int geo_prec = -1;
@@ -220,7 +220,7 @@ inline GeoParams geo_params(const rl_model* md) {
   p.nr = m.nr; p.nth = m.nth; p.ny = m.ny; p.rstar = m.rstar; p.theta0 = md->cam.theta0;
   p.R = md->dR.as<double>(); p.TH = md->dTH.as<double>(); p.tan2 = md->dtan2.as<double>();
   p.vel = md->dvel.as<double>(); p.lw = md->dlw.as<double>();
-  p.velf = md->dvelf.as<float>(); p.lwf = md->dlwf.as<float>();
+  p.velf = md->dvelf.as<float>(); p.vell = md->dvell.as<float>(); p.lwf = md->dlwf.as<float>();
   p.x0 = md->dx0.as<double>(); p.z0 = md->dz0.as<double>();
   return p;
 }

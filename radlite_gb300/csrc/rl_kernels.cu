@@ -35,8 +35,8 @@ __device__ __forceinline__ int ridx_dev(int it, int ny) {
 template <typename T>
 struct NodeEmitter {
   // The FP32 build stores every node value in FP32, so it forms the direction, the
-  // projected velocity, the interpolation weights and the width in FP32 from the FP64
-  // positions and cell differences; the FP64 build does all of it in FP64.
+  // projected velocity and the interpolation weights in float-float and the width in FP32
+  // from the FP64 positions and cell differences; the FP64 build does all of it in FP64.
   static constexpr bool kFp32Direction = sizeof(T) == 4;
   const GeoParams* p;
   const rlg::Grid* g;
@@ -46,7 +46,7 @@ struct NodeEmitter {
   int k, status;
   int ir_prev, icr_prev;
   double s_prev, dvmu_prev;
-  float dvmu_prev_f;
+  rlg::ff dvmu_prev_ff;
 
   __device__ bool operator()(const rlg::Node& n) {
     if (k >= nb->kmax) return false;
@@ -106,8 +106,11 @@ struct NodeEmitter {
     const int nr = p->nr, nth = p->nth, ny = p->ny;
     const double R0 = rlg::Rg(*g, n.ir), R1 = rlg::Rg(*g, n.ir + 1);
     const double T0 = rlg::Tg(*g, n.it), T1 = rlg::Tg(*g, n.it + 1);
-    const float dr = (float)(n.r - R0) / (float)(R1 - R0);
-    const float dt = (float)(n.th - T0) / (float)(T1 - T0);
+    // interpolation weights in float-float from the FP64 differences
+    using rlg::ff;
+    const ff drf = rlg::ff_div(rlg::ff_of(n.r - R0), rlg::ff_of(R1 - R0));
+    const ff dtf = rlg::ff_div(rlg::ff_of(n.th - T0), rlg::ff_of(T1 - T0));
+    const float dr = drf.hi, dt = dtf.hi;
     if (!(dr >= 0.0f && dr <= 1.0f) || !(dt >= 0.0f && dt <= 1.0f)) { status = rlg::kGeoRange; return false; }
     if (k == 0 && n.ir == 0) { status = rlg::kGeoStarStart; return false; }
     int r1;
@@ -122,13 +125,23 @@ struct NodeEmitter {
     auto bil = [&](float f00, float f01, float f10, float f11) {
       return RL_FMA(dr, RL_FMA(dt, f11, RL_MUL(at, f10)), RL_MUL(ar, RL_FMA(dt, f01, RL_MUL(at, f00))));
     };
-    float v[3];
-    for (int i = 0; i < 3; i++)
-      v[i] = bil(p->velf[3 * c00 + i], p->velf[3 * c01 + i], p->velf[3 * c10 + i], p->velf[3 * c11 + i]);
     const float lwv = bil(p->lwf[c00], p->lwf[c01], p->lwf[c10], p->lwf[c11]);
-    const float tang = RL_FMA(v[1], n.sinphi_f, RL_MUL(v[2], n.cosphi_f));
-    const float dvmu = RL_MUL(3.335668e-11f, RL_FMA(n.mu_f, v[0], RL_MUL(n.sinmu_f, tang)));
-    const float kv = (float)(1.0 / 3.33567e-6);
+    // the velocity and its projection omega.v/c in float-float, the FP64 formulas in the
+    // same order: the window test, the segment velocity differences and the Doppler
+    // offsets follow the FP64 values to FP32 rounding
+    const ff arf = rlg::ff_sub(rlg::ff_c(1.0f), drf), atf = rlg::ff_sub(rlg::ff_c(1.0f), dtf);
+    ff v[3];
+    for (int i = 0; i < 3; i++) {
+      const ff f00{p->velf[3 * c00 + i], p->vell[3 * c00 + i]}, f01{p->velf[3 * c01 + i], p->vell[3 * c01 + i]};
+      const ff f10{p->velf[3 * c10 + i], p->vell[3 * c10 + i]}, f11{p->velf[3 * c11 + i], p->vell[3 * c11 + i]};
+      v[i] = rlg::ff_add(rlg::ff_mul(arf, rlg::ff_add(rlg::ff_mul(atf, f00), rlg::ff_mul(dtf, f01))),
+                         rlg::ff_mul(drf, rlg::ff_add(rlg::ff_mul(atf, f10), rlg::ff_mul(dtf, f11))));
+    }
+    const ff mu{n.mu_f, n.mu_l}, sinmu{n.sinmu_f, n.sinmu_l};
+    const ff sinphi{n.sinphi_f, n.sinphi_l}, cosphi{n.cosphi_f, n.cosphi_l};
+    const ff tang = rlg::ff_add(rlg::ff_mul(v[1], sinphi), rlg::ff_mul(v[2], cosphi));
+    const ff dvmu = rlg::ff_mul(rlg::ff_of(3.335668e-11), rlg::ff_add(rlg::ff_mul(mu, v[0]), rlg::ff_mul(sinmu, tang)));
+    const ff kv = rlg::ff_of(1.0 / 3.33567e-6);
     unsigned flags = 0;
     double ds = 0.0;
     if (k > 0) {
@@ -140,15 +153,15 @@ struct NodeEmitter {
     if (n.ir <= 1) flags |= kFlagIr1;
     const size_t o = row + k;
     nb->ds[o] = (T)ds;
-    nb->dvf[o] = dvmu;
-    nb->vl[o] = (T)RL_MUL(dvmu, kv);
-    nb->dvseg[o] = (T)(k > 0 ? RL_MUL(RL_SUB(dvmu, dvmu_prev_f), kv) : 0.0f);
+    nb->dvf[o] = dvmu.hi;
+    nb->vl[o] = (T)rlg::ff_mul(dvmu, kv).hi;
+    nb->dvseg[o] = (T)(k > 0 ? rlg::ff_mul(rlg::ff_sub(dvmu, dvmu_prev_ff), kv).hi : 0.0f);
     nb->lw[o] = (T)lwv;
     nb->wr[o] = (T)dr;
     nb->wt[o] = (T)dt;
     nb->c00[o] = c00;
     nb->misc[o] = (unsigned)(dto + 32768) | ((unsigned)(dro + 1) << 16) | ((unsigned)n.icr << kIcrShift) | flags;
-    s_prev = n.s; dvmu_prev_f = dvmu; ir_prev = n.ir; icr_prev = n.icr;
+    s_prev = n.s; dvmu_prev_ff = dvmu; ir_prev = n.ir; icr_prev = n.icr;
     k++;
     return true;
   }
@@ -161,7 +174,7 @@ __device__ __forceinline__ void geometry_ray(const GeoParams& p, NodeBuf<T>& nb,
   NodeEmitter<T> em;
   em.p = &p; em.g = &g; em.nb = &nb; em.dbg = dbg; em.row = (size_t)ray * nb.kmax;
   em.k = 0; em.status = 0; em.ir_prev = -1; em.icr_prev = -1; em.s_prev = 0.0; em.dvmu_prev = 0.0;
-  em.dvmu_prev_f = 0.0f;
+  em.dvmu_prev_ff = rlg::ff_c(0.0f);
   int st = rlg::trace(g, p.x0[ray], p.z0[ray], p.theta0, em);
   if (em.status != 0) st = em.status;
   nb.nnodes[ray] = em.k;
@@ -478,13 +491,16 @@ cudaError_t launch_jobs(const JobLaunch<T>& L, cudaStream_t s) {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
-  cudaError_t e = cudaMemsetAsync(L.walk.work, 0, sizeof(int), s);
-  if (e != cudaSuccess) return e;
-  switch (L.cpl) {
-    case 1: e = launch_walk_jobs_c<T, 1>(L.walk, L.nsm, s); break;
-    case 2: e = launch_walk_jobs_c<T, 2>(L.walk, L.nsm, s); break;
-    case 4: e = launch_walk_jobs_c<T, 4>(L.walk, L.nsm, s); break;
-    default: e = launch_walk_jobs_c<T, 8>(L.walk, L.nsm, s); break;
+  cudaError_t e = cudaSuccess;
+  if (L.walk_jobs) {
+    e = cudaMemsetAsync(L.walk.work, 0, sizeof(int), s);
+    if (e != cudaSuccess) return e;
+    switch (L.cpl) {
+      case 1: e = launch_walk_jobs_c<T, 1>(L.walk, L.nsm, s); break;
+      case 2: e = launch_walk_jobs_c<T, 2>(L.walk, L.nsm, s); break;
+      case 4: e = launch_walk_jobs_c<T, 4>(L.walk, L.nsm, s); break;
+      default: e = launch_walk_jobs_c<T, 8>(L.walk, L.nsm, s); break;
+    }
   }
   if (e != cudaSuccess || !L.reduce) return e;
   k_ring_sum_jobs<T><<<L.nring_blocks, 256, 0, s>>>(L.red, L.ring_prefix, L.njobs);

@@ -81,7 +81,7 @@ def test_batch_waves_tiles_and_eager(gpu_lib, ctx, model_dir):
         for g, r in zip(b.run(), ref):
             np.testing.assert_allclose(g, r, rtol=1e-6)
     tune = b.autotune(sample_stride=3)
-    assert tune["lines_per_item"] in (2, 8, 16, 32) and tune["channel_slots"] in (2, 4)
+    assert tune["lines_per_item"] in (2, 8, 16, 32) and tune["channel_slots"] == 4
     assert tune["sample_ms"] > 0
     b.use_graph(False)
     for g, r in zip(b.run(), ref):

@@ -8,6 +8,9 @@
   line (every 509th / 1021st ray: all ring radii and azimuths are visited); the GPU renders
   the full image in one launch and returns the same rays' rows (rl_image_rows).
 
+* window decisions: the FP32 build's velocity windows (the integration mask of every ray and
+  line) equal the FP64 build's on the band workload at 32 azimuths, both inclinations.
+
 Tolerances (the reference's spectrum criterion is in every channel above 1e-3 of the peak):
   FP32 transfer: spectra and sample spectra <= 1e-4 relative; every sampled pixel within
                  2e-4 of the line's brightest sampled pixel.
@@ -87,4 +90,22 @@ def test_image_rows_match_line_image(ctx, model_dir):
         np.testing.assert_allclose(rows[k], img[rays], rtol=1e-12, atol=0)
     with pytest.raises(Exception):
         m.image_rows(info["ilinestart"], 1, [info["nrays"]])
+    m.free()
+
+
+@pytest.mark.parametrize("incl", [20.0, 60.0])
+def test_band_window_decisions_fp32_equal_fp64(ctx, model_dir, incl):
+    """The FP32 build forms the projected velocity of the window test in float-float, so
+    its windows are the FP64 build's (which are the oracle's): same integration mask for
+    every (line, ray, channel)."""
+    m = ctx.load_dir(model_dir("band_large", incl_deg=incl, nphi=32))
+    info = m.info()
+    lines = range(info["ilinestart"], info["ilinestart"] + info["nlines_spec"])
+    masks32 = [m.line_image(il, mask=True)[1] for il in lines]
+    m.set_precision(1)
+    flips = 0
+    for il, m32 in zip(lines, masks32):
+        m64 = m.line_image(il, mask=True)[1]
+        flips += int(np.count_nonzero(m32 != m64))
+    assert flips == 0, f"{flips} (line, ray, channel) window decisions differ"
     m.free()
