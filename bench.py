@@ -350,6 +350,8 @@ def ours(args):
             passes = sum(s["node_passes"] for s in sts)
             packed = sum(s["packed_passes"] for s in sts)
             empty = sum(s["empty_steps"] for s in sts)
+            refined = sum(s["refined_passes"] for s in sts)
+            substeps = sum(s["sub_steps"] for s in sts)
     wall = (time.perf_counter() - t0) / args.steps
     ms = max_over_ranks(sum(dev_ms) / len(dev_ms), dist)
     nrays = n_rays(cfg)
@@ -429,6 +431,8 @@ def ours(args):
                             "kernel": "k_walk<float>", "walk_ms_per_step": wk * 1e3,
                             "executed_steps_per_step": executed, "empty_steps_per_step": empty,
                             "node_passes_per_step": passes, "packed_fraction": packed / passes if passes else None,
+                            "refined_fraction": refined / passes if passes else None,
+                            "sub_steps_per_step": substeps,
                             "budget_per_step": {"fp32": BUDGET_FP32, "mufu": BUDGET_MUFU},
                             "peaks_measured": peaks,
                             "hbm_side": {"traffic_gb_per_s": traffic_gbs, "peak_gb_per_s": hbm_peak,
@@ -627,6 +631,16 @@ def adjoint_case(ctx, name="adjoint_disk", reps=3, **over):
                        "gradients w.r.t. per-cell ln T, ln X, width",
            "forward_ms": statistics.median(fw[1:]), "adjoint_ms": statistics.median(bw[1:]),
            "spectra": cfg.nlines}
+    # the reverse sweep over stored intensities (checkpoint interval 1) on the same forward
+    d.set_checkpoint(1)
+    flux = d.forward(lnT, lnX, b)
+    gflux = 2.0 * (flux - target) / target.abs().max() ** 2
+    rv = []
+    for _ in range(2):
+        _, sb = d.backward(gflux, stats=True)
+        rv.append(sb["total_ms"])
+    d.set_checkpoint(0)
+    res["reverse_sweep_ms"] = min(rv)
     res["adjoint_over_forward"] = res["adjoint_ms"] / res["forward_ms"]
     res["forward_adjoint_spectra_per_s"] = cfg.nlines / ((res["forward_ms"] + res["adjoint_ms"]) * 1e-3)
     # the same gradient by central differences: two forwards per cell parameter
@@ -715,7 +729,8 @@ def profile_case(args):
     print(json.dumps({"workload": args.workload, "steps": st["steps"], "walk_ms": st["walk_ms"],
                       "geometry_ms": st["geometry_ms"], "nrays": st["nrays"], "nlines": st["nlines"],
                       "node_passes": st["node_passes"], "packed_passes": st["packed_passes"],
-                      "empty_steps": st["empty_steps"]}), flush=True)
+                      "empty_steps": st["empty_steps"], "refined_passes": st["refined_passes"],
+                      "sub_steps": st["sub_steps"]}), flush=True)
     m.free()
     ctx.close()
     return 0

@@ -48,6 +48,10 @@ typedef struct rl_stats {
   unsigned long long empty_steps;    /* steps counted in `steps` whose two nodes have zero
                                         emissivity and opacity: the intensity passes
                                         unchanged and no arithmetic is done */
+  unsigned long long refined_passes; /* node passes in which some channel needed SUBGRID
+                                        refinement (line.F:4733-4742) */
+  unsigned long long sub_steps;      /* steps counted in `steps` that refined channels take
+                                        inside such segments */
 } rl_stats;
 
 typedef struct rl_model_info {
@@ -266,16 +270,19 @@ typedef struct rl_diff rl_diff;
 int rl_diff_create(rl_model* model, int iline0, int nlines, int precision, rl_diff** diff);
 int rl_diff_destroy(rl_diff* diff);
 int rl_diff_info(rl_diff* diff, int* ncell, int* nlines, int* nfr, int* nrays);
-/* Adjoint checkpoints along each ray: every 32 nodes (the chunk is walked again in the
-   reverse sweep; per-warp scratch of 32 values a chunk) or every node (1, the default:
-   each intensity is kept, 32 values a node per resident warp, about 0.1-0.4 GB). */
+/* How the backward call walks the rays. 0 (the default): the gradient sweep in walk
+   order, no stored intensities: a first pass sums each channel's optical depth along the
+   ray, a second recomputes every step and takes its gradient with the multiplier
+   e^{-(optical depth still ahead)}. 1 or 32: the reverse sweep, which keeps the intensity
+   entering every node (1: 32 values a node per resident warp, about 0.1-0.4 GB) or every
+   32nd node (the chunk is walked again). All give the same gradient. */
 int rl_diff_set_checkpoint(rl_diff* diff, int every);
 /* flux [nlines][nfr]: F_nu at 1 pc for the parameters lnT, lnX, width [ncell]. */
 int rl_diff_forward(rl_diff* diff, const double* lnT, const double* lnX, const double* width, double* flux,
                     rl_stats* stats);
 /* Gradient of a loss L at the last forward's parameters: given gflux = dL/dflux
-   [nlines][nfr], writes dL/dlnT, dL/dlnX, dL/dwidth [ncell] (adjoint walk with
-   checkpoints every 32 nodes per ray). */
+   [nlines][nfr], writes dL/dlnT, dL/dlnX, dL/dwidth [ncell] (the adjoint walk chosen by
+   rl_diff_set_checkpoint). */
 int rl_diff_backward(rl_diff* diff, const double* gflux, double* g_lnT, double* g_lnX, double* g_width,
                      rl_stats* stats);
 

@@ -38,7 +38,8 @@ class Stats(C.Structure):
                 ("reduce_ms", C.c_double), ("upload_ms", C.c_double), ("total_ms", C.c_double),
                 ("nrays", C.c_int), ("nfr", C.c_int), ("kmax", C.c_int), ("nlines", C.c_int),
                 ("h2d_bytes", C.c_ulonglong), ("d2h_bytes", C.c_ulonglong), ("node_passes", C.c_ulonglong),
-                ("packed_passes", C.c_ulonglong), ("empty_steps", C.c_ulonglong)]
+                ("packed_passes", C.c_ulonglong), ("empty_steps", C.c_ulonglong),
+                ("refined_passes", C.c_ulonglong), ("sub_steps", C.c_ulonglong)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -513,7 +514,8 @@ class Diff:
         self.version = 0
 
     def set_checkpoint(self, every: int):
-        """Adjoint checkpoint interval along each ray: 1 (every node) or 32 nodes."""
+        """How the adjoint walks each ray: 0 (default) the gradient sweep in walk order;
+        1 or 32 the reverse sweep with intensities stored every node or every 32 nodes."""
         _check(lib().rl_diff_set_checkpoint(self.h, every), self.model._ch)
 
     def close(self):

@@ -27,6 +27,7 @@
 #include <stdint.h>
 #include "rl_device.h"
 #include "rl_walk_common.cuh"
+#include "rl_grad.cuh"
 
 namespace rl {
 
@@ -87,12 +88,12 @@ __global__ void k_lte_lines(LteParams<R> P) {
   tb[2] = (R)t2;
   tb[3] = (R)du3[2];
   P.nsum[(size_t)c * P.nl + l] = (R)(nup + ndn);
-  double* dt = P.dtab + ((size_t)c * P.nl + l) * 5;
-  dt[0] = t0 * du;
-  dt[1] = L.C2 * L.cphi * (ndn * L.Bdu * dd - nup * L.Bud * du);
-  dt[2] = du3[0] * TdB / L.scale;
-  dt[3] = t0;
-  dt[4] = t1;
+  R* dt = P.dtab + ((size_t)c * P.nl + l) * 5;
+  dt[0] = (R)(t0 * du);
+  dt[1] = (R)(L.C2 * L.cphi * (ndn * L.Bdu * dd - nup * L.Bud * du));
+  dt[2] = (R)(du3[0] * TdB / L.scale);
+  dt[3] = (R)t0;
+  dt[4] = (R)t1;
 }
 
 // Node line widths from cell widths, with the weights the geometry stored (the same
@@ -526,7 +527,6 @@ __device__ __forceinline__ T warp_sum(T v) {
   return v;
 }
 
-// Scatter the per-node gradients of staged entries t0..t1 to the cell corners.
 // Scatter the per-node gradients of staged entries t0..t1 to the cell corners, folded
 // into the cell parameters on the way: with the table derivatives dtab of each corner,
 // dL/d ln T += w (g_jf dtab0 + g_af dtab1 + g_jd dtab2), dL/d ln X += w (g_jf tab0 +
@@ -537,6 +537,24 @@ __device__ __forceinline__ void adj_scatter(const AdjParams<T>& A, AdjStage<T>& 
     const T* g = S.gacc[t];
     if (g[0] == (T)0 && g[2] == (T)0 && g[3] == (T)0 && g[4] == (T)0) continue;
     const Corners c = corners(S.c00[t], S.misc[t], A.W.nth);
+    if constexpr (sizeof(T) == 4) {
+      // FP32 walk: weights and products in FP32 (the FP64 pipe of this GPU is a small
+      // fraction of the FP32 one), the three gradients of a corner in one vector atomic
+      const float wr = S.wr[t], wt = S.wt[t];
+      const float ar = 1.f - wr, at = 1.f - wt;
+      const int cs[4] = {c.c00, c.c01, c.c10, c.c11};
+      const float ws[4] = {ar * at, ar * wt, wr * at, wr * wt};
+      const float gjd = g[0], gjf = g[2], gaf = g[3], glw = g[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        if (ws[q] == 0.f) continue;
+        const float* d = A.dtab + ((size_t)cs[q] * A.W.nlines + l) * 5;
+        const float gT = gjf * __ldg(d + 0) + gaf * __ldg(d + 1) + gjd * __ldg(d + 2);
+        const float gX = gjf * __ldg(d + 3) + gaf * __ldg(d + 4);
+        atomicAdd(A.g4 + cs[q], make_float4(ws[q] * gT, ws[q] * gX, ws[q] * glw, 0.f));
+      }
+      continue;
+    }
     const double wr = (double)S.wr[t], wt = (double)S.wt[t];
     const double ar = 1.0 - wr, at = 1.0 - wt;
     const int cs[4] = {c.c00, c.c01, c.c10, c.c11};
@@ -544,13 +562,9 @@ __device__ __forceinline__ void adj_scatter(const AdjParams<T>& A, AdjStage<T>& 
     const double gjd = (double)g[0], gjf = (double)g[2], gaf = (double)g[3], glw = (double)g[4];
     for (int q = 0; q < 4; q++) {
       if (ws[q] == 0.0) continue;
-      const double* d = A.dtab + ((size_t)cs[q] * A.W.nlines + l) * 5;
-      const double gT = gjf * __ldg(d + 0) + gaf * __ldg(d + 1) + gjd * __ldg(d + 2);
-      const double gX = gjf * __ldg(d + 3) + gaf * __ldg(d + 4);
-      if (A.g4) {   // FP32 walk: the three gradients of the corner in one vector atomic
-        atomicAdd(A.g4 + cs[q], make_float4((float)(ws[q] * gT), (float)(ws[q] * gX), (float)(ws[q] * glw), 0.f));
-        continue;
-      }
+      const T* d = A.dtab + ((size_t)cs[q] * A.W.nlines + l) * 5;
+      const double gT = gjf * (double)__ldg(d + 0) + gaf * (double)__ldg(d + 1) + gjd * (double)__ldg(d + 2);
+      const double gX = gjf * (double)__ldg(d + 3) + gaf * (double)__ldg(d + 4);
       if (gT != 0.0) atomicAdd(A.g_lnT + cs[q], ws[q] * gT);
       if (gX != 0.0) atomicAdd(A.g_lnX + cs[q], ws[q] * gX);
       if (glw != 0.0) atomicAdd(A.g_b + cs[q], ws[q] * glw);   // node width: bilinear in all corners
@@ -873,6 +887,76 @@ __global__ void __launch_bounds__(128) k_adjoint_one(AdjParams<T> A, AdjJobs<T> 
   }
 }
 
+// The gradient sweep (rl_grad.cuh): one warp per (ray, line group) item from the queue;
+// the list of each warp's item sits in its row of the job-wide scratch.
+// FP32: three blocks per SM (at most 168 registers); FP64 keeps its registers
+template <typename T> struct GradMinBlocks { static constexpr int value = sizeof(T) == 4 ? 3 : 1; };
+
+template <typename T>
+__global__ void __launch_bounds__(128, GradMinBlocks<T>::value) k_grad_jobs(AdjJobs<T> B) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ AdjParams<T> jp[4];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  GradStage<T>* stages = reinterpret_cast<GradStage<T>*>(smem_raw);
+  GradWork<T>* works = reinterpret_cast<GradWork<T>*>(smem_raw + sizeof(GradStage<T>) * nw);
+  unsigned short* list =
+      reinterpret_cast<unsigned short*>(B.ckpt + ((size_t)blockIdx.x * nw + wib) * (size_t)B.ckpt_warp);
+  unsigned long long steps = 0, zc = 0;
+  int cur = -1;
+  for (;;) {
+    int item = 0;
+    if (lane == 0) item = atomicAdd(B.work, 1);
+    item = __shfl_sync(0xffffffffu, item, 0);
+    if (item >= B.total) break;
+    const int j = find_job(B.item_prefix, B.njobs, item);
+    if (j != cur) {
+      __syncwarp();
+      const int* src = reinterpret_cast<const int*>(B.jobs + j);
+      int* dst = reinterpret_cast<int*>(&jp[wib]);
+      for (int w = lane; w < (int)(sizeof(AdjParams<T>) / 4); w += 32) dst[w] = __ldg(src + w);
+      __syncwarp();
+      cur = j;
+    }
+    grad_item<T>(jp[wib], item - __ldg(&B.item_prefix[j]), stages[wib], works[wib], list, lane, steps, zc);
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    steps += __shfl_xor_sync(0xffffffffu, steps, off);
+    zc += __shfl_xor_sync(0xffffffffu, zc, off);
+  }
+  if (lane == 0) {
+    atomicAdd(&B.counters[0], steps);
+    if (zc) atomicAdd(&B.counters[1], zc);
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128, GradMinBlocks<T>::value) k_grad_one(AdjParams<T> A, AdjJobs<T> B) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  GradStage<T>* stages = reinterpret_cast<GradStage<T>*>(smem_raw);
+  GradWork<T>* works = reinterpret_cast<GradWork<T>*>(smem_raw + sizeof(GradStage<T>) * nw);
+  unsigned short* list =
+      reinterpret_cast<unsigned short*>(B.ckpt + ((size_t)blockIdx.x * nw + wib) * (size_t)B.ckpt_warp);
+  unsigned long long steps = 0, zc = 0;
+  for (;;) {
+    int item = 0;
+    if (lane == 0) item = atomicAdd(B.work, 1);
+    item = __shfl_sync(0xffffffffu, item, 0);
+    if (item >= B.total) break;
+    grad_item<T>(A, item, stages[wib], works[wib], list, lane, steps, zc);
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    steps += __shfl_xor_sync(0xffffffffu, steps, off);
+    zc += __shfl_xor_sync(0xffffffffu, zc, off);
+  }
+  if (lane == 0) {
+    atomicAdd(&B.counters[0], steps);
+    if (zc) atomicAdd(&B.counters[1], zc);
+  }
+}
+
 // ------------------------------------------------------------------------------------
 // launchers
 // ------------------------------------------------------------------------------------
@@ -904,44 +988,68 @@ size_t adjoint_smem(int max_nfr) {
   return (sizeof(AdjStage<T>) + sizeof(AdjSlots<T>)) * warps + sizeof(unsigned short) * (size_t)capp * warps;
 }
 
-// Blocks of the persistent adjoint launch (the checkpoint scratch holds one region per warp).
 template <typename T>
-cudaError_t adjoint_grid(int nsm, int max_nfr, int* blocks) {
-  const size_t smem = adjoint_smem<T>(max_nfr);
-  cudaError_t e = cudaFuncSetAttribute(k_adjoint_jobs<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(k_adjoint_one<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
+size_t grad_smem() { return (sizeof(GradStage<T>) + sizeof(GradWork<T>)) * 4; }
+
+// Blocks of the persistent adjoint launch of checkpoint interval `every` (0: the gradient
+// sweep); the scratch holds one region per warp.
+template <typename T>
+cudaError_t adjoint_grid(int nsm, int max_nfr, int every, int* blocks) {
   int per_sm = 0, per_sm1 = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_adjoint_jobs<T>, 128, smem);
-  if (e != cudaSuccess) return e;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm1, k_adjoint_one<T>, 128, smem);
+  cudaError_t e;
+  if (every == 0) {
+    const size_t smem = grad_smem<T>();
+    e = cudaFuncSetAttribute(k_grad_jobs<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_grad_one<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_grad_jobs<T>, 128, smem);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm1, k_grad_one<T>, 128, smem);
+  } else {
+    const size_t smem = adjoint_smem<T>(max_nfr);
+    e = cudaFuncSetAttribute(k_adjoint_jobs<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_adjoint_one<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_adjoint_jobs<T>, 128, smem);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm1, k_adjoint_one<T>, 128, smem);
+  }
   if (e != cudaSuccess) return e;
   per_sm = per_sm1 < per_sm ? per_sm1 : per_sm;   // the scratch is sized for the smaller grid
   *blocks = nsm * (per_sm < 1 ? 1 : per_sm);
   return cudaSuccess;
 }
 
+// Scratch per warp in elements of T: the reverse sweep's stored intensities (interval 1:
+// every node, 32: every chunk start), or the gradient sweep's (line, channel) list.
 template <typename T>
-long long adjoint_ckpt_per_warp(int kmax, int every) {
+long long adjoint_ckpt_per_warp(int kmax, int max_nfr, int every) {
+  if (every == 0) return ((long long)kGG * max_nfr * (long long)sizeof(unsigned short) + sizeof(T) - 1) / sizeof(T) + 8;
   return (long long)((kmax + 31) / 32) * 32 * (every == 1 ? 32 : kAdjSlots);
+}
+
+// Work items of one job: (line group, ray) for the gradient sweep, (line, ray) otherwise.
+int adjoint_items(int nlines, int nrays, int every) {
+  return (every == 0 ? (nlines + kGG - 1) / kGG : nlines) * nrays;
 }
 
 template <typename T>
 cudaError_t launch_adjoint(const AdjJobs<T>& B, int blocks, cudaStream_t s) {
-  const size_t smem = adjoint_smem<T>(B.max_nfr);
   cudaError_t e = cudaMemsetAsync(B.work, 0, sizeof(int), s);
   if (e != cudaSuccess) return e;
-  k_adjoint_jobs<T><<<blocks, 128, smem, s>>>(B);
+  if (B.every == 0) k_grad_jobs<T><<<blocks, 128, grad_smem<T>(), s>>>(B);
+  else k_adjoint_jobs<T><<<blocks, 128, adjoint_smem<T>(B.max_nfr), s>>>(B);
   return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t launch_adjoint_one(const AdjParams<T>& A, const AdjJobs<T>& B, int blocks, cudaStream_t s) {
-  const size_t smem = adjoint_smem<T>(B.max_nfr);
   cudaError_t e = cudaMemsetAsync(B.work, 0, sizeof(int), s);
   if (e != cudaSuccess) return e;
-  k_adjoint_one<T><<<blocks, 128, smem, s>>>(A, B);
+  if (B.every == 0) k_grad_one<T><<<blocks, 128, grad_smem<T>(), s>>>(A, B);
+  else k_adjoint_one<T><<<blocks, 128, adjoint_smem<T>(B.max_nfr), s>>>(A, B);
   return cudaGetLastError();
 }
 
@@ -966,10 +1074,10 @@ template cudaError_t launch_lte<float>(const LteParams<float>&, cudaStream_t);
 template cudaError_t launch_lte<double>(const LteParams<double>&, cudaStream_t);
 template cudaError_t launch_node_lw<float>(const NodeBuf<float>&, const double*, int, cudaStream_t);
 template cudaError_t launch_node_lw<double>(const NodeBuf<double>&, const double*, int, cudaStream_t);
-template cudaError_t adjoint_grid<float>(int, int, int*);
-template cudaError_t adjoint_grid<double>(int, int, int*);
-template long long adjoint_ckpt_per_warp<float>(int, int);
-template long long adjoint_ckpt_per_warp<double>(int, int);
+template cudaError_t adjoint_grid<float>(int, int, int, int*);
+template cudaError_t adjoint_grid<double>(int, int, int, int*);
+template long long adjoint_ckpt_per_warp<float>(int, int, int);
+template long long adjoint_ckpt_per_warp<double>(int, int, int);
 template cudaError_t launch_adjoint<float>(const AdjJobs<float>&, int, cudaStream_t);
 template cudaError_t launch_adjoint<double>(const AdjJobs<double>&, int, cudaStream_t);
 template cudaError_t launch_adjoint_one<float>(const AdjParams<float>&, const AdjJobs<float>&, int, cudaStream_t);

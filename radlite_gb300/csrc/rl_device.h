@@ -178,7 +178,7 @@ struct LteParams {
   double* Emean;              // [ncell] mean level energy / kT (work)
   T* tab;                     // [ncell][nl][4] walk table
   T* nsum;                    // [ncell][nl] N_up + N_low
-  double* dtab;               // [ncell][nl][5]: d tab[0..2] / d lnT, tab[0], tab[1] (FP64)
+  T* dtab;                    // [ncell][nl][5]: d tab[0..2] / d lnT, tab[0], tab[1]
 };
 
 template <typename T>
@@ -187,7 +187,7 @@ struct AdjParams {
   const double* gflux;        // [nl][nfr] dL/dF_nu (F_nu at 1 pc)
   const double* ri;           // [nrr+2] ring edges
   int nphi, nrr;
-  const double* dtab;         // [ncell][nl][5] table derivatives of the LTE tables (LteParams::dtab)
+  const T* dtab;              // [ncell][nl][5] table derivatives of the LTE tables (LteParams::dtab)
   double* g_lnT;              // [ncell] dL/d ln T, accumulated
   double* g_lnX;              // [ncell] dL/d ln X, accumulated
   double* g_b;                // [ncell] dL/d(cell line width), accumulated

@@ -30,9 +30,10 @@ cudaError_t launch_lte(const LteParams<T>& P, cudaStream_t s);
 template <typename T>
 cudaError_t launch_node_lw(const NodeBuf<T>& nb, const double* b, int nth, cudaStream_t s);
 template <typename T>
-cudaError_t adjoint_grid(int nsm, int max_nfr, int* blocks);
+cudaError_t adjoint_grid(int nsm, int max_nfr, int every, int* blocks);
 template <typename T>
-long long adjoint_ckpt_per_warp(int kmax, int every);
+long long adjoint_ckpt_per_warp(int kmax, int max_nfr, int every);
+int adjoint_items(int nlines, int nrays, int every);
 template <typename T>
 cudaError_t launch_adjoint(const AdjJobs<T>& B, int blocks, cudaStream_t s);
 template <typename T>
@@ -61,7 +62,8 @@ struct rl_diff {
   DevBuf ckpt, ajob, aprefix, acnt, awork;
   DevBuf g4;   // FP32 adjoint: interleaved gradient accumulator [ncell]
   bool have_forward = false;
-  int every = 1;   // adjoint checkpoint interval (nodes)
+  int every = 0;   // adjoint: 0 the gradient sweep in walk order; 1 or 32 the reverse sweep
+                   // with stored intensities every node or every 32 nodes
 };
 
 namespace {
@@ -211,7 +213,7 @@ int create(rl_diff* d) {
   CUDA_TRY(d->dscale.ensure(sizeof(double) * nl));
   CUDA_TRY(d->tab.ensure(sizeof(T) * (size_t)ncell * nl * 4));
   CUDA_TRY(d->nsum.ensure(sizeof(T) * (size_t)ncell * nl));
-  CUDA_TRY(d->dtab.ensure(sizeof(double) * (size_t)ncell * nl * 5));
+  CUDA_TRY(d->dtab.ensure(sizeof(T) * (size_t)ncell * nl * 5));
   CUDA_TRY(d->width.ensure(sizeof(double) * ncell));
   CUDA_TRY(d->img.ensure(sizeof(T) * (size_t)nl * cam.nrays * d->nfr));
   CUDA_TRY(d->ring.ensure(sizeof(double) * (size_t)nl * (cam.nrr + 1) * d->nfr));
@@ -235,10 +237,10 @@ int create(rl_diff* d) {
   CUDA_TRY(h2d(d->dscale.p, lt.scale.data(), sizeof(double) * nl, s));
   // walk shape as the plain path: balanced groups of up to 8 lines
   walk_shape(nl, d->nfr, d->gsize, d->cpl);
-  CUDA_TRY(adjoint_grid<T>(ctx->nsm, d->nfr, &d->adj_blocks));
-  const long long per = adjoint_ckpt_per_warp<T>(d->kmax, d->every);
+  CUDA_TRY(adjoint_grid<T>(ctx->nsm, d->nfr, d->every, &d->adj_blocks));
+  const long long per = adjoint_ckpt_per_warp<T>(d->kmax, d->nfr, d->every);
   CUDA_TRY(d->ckpt.ensure(sizeof(T) * (size_t)per * d->adj_blocks * 4));
-  const int pre[2] = {0, nl * cam.nrays};
+  const int pre[2] = {0, adjoint_items(nl, cam.nrays, d->every)};
   CUDA_TRY(h2d(d->aprefix.p, pre, sizeof(pre), s));
   CUDA_TRY(cudaStreamSynchronize(s));
   return 0;
@@ -252,7 +254,7 @@ LteParams<T> lte_params(const rl_diff* d, const double* lnT, const double* lnX) 
   L.lnT = lnT; L.lnX = lnX; L.rho_m = d->rho_m.as<double>(); L.Ek = d->Ek.as<double>(); L.lng = d->lng.as<double>();
   L.lines = d->lines.as<LteLine>(); L.dust = d->dust.as<double>();
   L.lnQ = d->lnQ.as<double>(); L.Emean = d->Emean.as<double>();
-  L.tab = d->tab.as<T>(); L.nsum = d->nsum.as<T>(); L.dtab = d->dtab.as<double>();
+  L.tab = d->tab.as<T>(); L.nsum = d->nsum.as<T>(); L.dtab = d->dtab.as<T>();
   return L;
 }
 
@@ -313,7 +315,7 @@ int backward(rl_diff* d, const double* gflux, double* g_lnT, double* g_lnX, doub
   A.gflux = gflux;
   A.ri = d->ri.as<double>();
   A.nphi = d->cam.nphi; A.nrr = d->cam.nrr;
-  A.dtab = d->dtab.as<double>();
+  A.dtab = d->dtab.as<T>();
   A.g_lnT = g_lnT; A.g_lnX = g_lnX; A.g_b = g_width;
   if (sizeof(T) == 4) {
     CUDA_TRY(d->g4.ensure(sizeof(float4) * d->ncell));
@@ -322,9 +324,9 @@ int backward(rl_diff* d, const double* gflux, double* g_lnT, double* g_lnX, doub
   AdjJobs<T> B;
   B.jobs = d->ajob.as<AdjParams<T>>();
   B.item_prefix = d->aprefix.as<int>();
-  B.njobs = 1; B.total = d->nl * d->cam.nrays; B.max_nfr = d->nfr;
+  B.njobs = 1; B.total = adjoint_items(d->nl, d->cam.nrays, d->every); B.max_nfr = d->nfr;
   B.ckpt = d->ckpt.as<T>();
-  B.ckpt_warp = adjoint_ckpt_per_warp<T>(d->kmax, d->every);
+  B.ckpt_warp = adjoint_ckpt_per_warp<T>(d->kmax, d->nfr, d->every);
   B.every = d->every;
   B.work = d->awork.as<int>();
   B.counters = d->acnt.as<unsigned long long>();
@@ -367,7 +369,7 @@ struct rl_diff_batch {
   std::vector<rl_diff*> jobs;
   std::vector<size_t> cell_off, flux_off;
   size_t ncell = 0, nflux = 0;
-  int max_nfr = 0, max_kmax = 0, adj_blocks = 0, every = 1;
+  int max_nfr = 0, max_kmax = 0, adj_blocks = 0, every = 0;   // every: as rl_diff::every
   bool built = false, use_graph = true;
   DevBuf lnT, lnX, width, flux, gflux, g_lnT, g_lnX, g_width;
   DevBuf g4;   // FP32 adjoint: interleaved gradient accumulator [ncell]
@@ -461,7 +463,7 @@ int batch_build(rl_diff_batch* b) {
     A.gflux = b->gflux.as<double>() + b->flux_off[j];
     A.ri = d->ri.as<double>();
     A.nphi = d->cam.nphi; A.nrr = d->cam.nrr;
-    A.dtab = d->dtab.as<double>();
+    A.dtab = d->dtab.as<T>();
     A.g_lnT = b->g_lnT.as<double>() + b->cell_off[j];
     A.g_lnX = b->g_lnX.as<double>() + b->cell_off[j];
     A.g_b = b->g_width.as<double>() + b->cell_off[j];
@@ -469,7 +471,7 @@ int batch_build(rl_diff_batch* b) {
     itemp[j + 1] = itemp[j] + w.nitems;
     ringp[j + 1] = ringp[j] + d->nl * d->cam.nrr;
     linep[j + 1] = linep[j] + d->nl;
-    adjp[j + 1] = adjp[j] + d->nl * d->cam.nrays;
+    adjp[j + 1] = adjp[j] + adjoint_items(d->nl, d->cam.nrays, b->every);
   }
   CUDA_TRY(b->walkjobs.ensure(sizeof(WalkParams<T>) * nj));
   CUDA_TRY(b->redjobs.ensure(sizeof(RedJob<T>) * nj));
@@ -485,8 +487,8 @@ int batch_build(rl_diff_batch* b) {
   CUDA_TRY(h2d(b->ring_prefix.p, ringp.data(), sizeof(int) * (nj + 1), s));
   CUDA_TRY(h2d(b->line_prefix.p, linep.data(), sizeof(int) * (nj + 1), s));
   CUDA_TRY(h2d(b->adj_prefix.p, adjp.data(), sizeof(int) * (nj + 1), s));
-  CUDA_TRY(adjoint_grid<T>(ctx->nsm, b->max_nfr, &b->adj_blocks));
-  const long long per = adjoint_ckpt_per_warp<T>(b->max_kmax, b->every);
+  CUDA_TRY(adjoint_grid<T>(ctx->nsm, b->max_nfr, b->every, &b->adj_blocks));
+  const long long per = adjoint_ckpt_per_warp<T>(b->max_kmax, b->max_nfr, b->every);
   CUDA_TRY(b->ckpt.ensure(sizeof(T) * (size_t)per * b->adj_blocks * 4));
   JobLaunch<T>& L = launch_of<T>(b);
   L = JobLaunch<T>{};
@@ -714,13 +716,20 @@ int rl_diff_destroy(rl_diff* d) {
 int rl_diff_set_checkpoint(rl_diff* d, int every) {
   if (!d) return set_err(nullptr, RL_ERR_ARG, "rl_diff_set_checkpoint: null handle");
   rl_ctx* ctx = d->ctx;
-  if (every != 1 && every != 32) return set_err(ctx, RL_ERR_ARG, "rl_diff_set_checkpoint: interval 1 or 32");
+  if (every != 0 && every != 1 && every != 32)
+    return set_err(ctx, RL_ERR_ARG, "rl_diff_set_checkpoint: 0 (gradient sweep), 1 or 32");
   CUDA_TRY(rl::enter_device(ctx->device));
   d->every = every;
-  const long long per = d->precision == RL_FP64 ? adjoint_ckpt_per_warp<double>(d->kmax, every)
-                                                : adjoint_ckpt_per_warp<float>(d->kmax, every);
-  const size_t el = d->precision == RL_FP64 ? sizeof(double) : sizeof(float);
+  const bool f64 = d->precision == RL_FP64;
+  CUDA_TRY(f64 ? adjoint_grid<double>(ctx->nsm, d->nfr, every, &d->adj_blocks)
+               : adjoint_grid<float>(ctx->nsm, d->nfr, every, &d->adj_blocks));
+  const long long per = f64 ? adjoint_ckpt_per_warp<double>(d->kmax, d->nfr, every)
+                            : adjoint_ckpt_per_warp<float>(d->kmax, d->nfr, every);
+  const size_t el = f64 ? sizeof(double) : sizeof(float);
   CUDA_TRY(d->ckpt.ensure(el * (size_t)per * d->adj_blocks * 4));
+  const int pre[2] = {0, adjoint_items(d->nl, d->cam.nrays, every)};
+  CUDA_TRY(h2d(d->aprefix.p, pre, sizeof(pre), ctx->stream));
+  CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return 0;
 }
 

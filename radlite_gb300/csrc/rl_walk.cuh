@@ -99,7 +99,9 @@ __device__ __forceinline__ SegGeom<T> seg_geom(T ds, T dvs, T rlw, T kq) {
   return g;
 }
 
-struct WalkCounters { unsigned long long steps = 0, integ = 0, nodes = 0, passes = 0, packed = 0, skipped = 0; };
+struct WalkCounters {
+  unsigned long long steps = 0, integ = 0, nodes = 0, passes = 0, packed = 0, skipped = 0, refined = 0, substeps = 0;
+};
 
 template <typename T, int C, bool PV = false>
 __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<T, C>& SS, SubWork<T>& SW, int ray,
@@ -146,7 +148,7 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
   }
   // per-call counts (32-bit: a call walks one tile of one ray): formal-solution steps, node
   // passes, of them on the general path and empty, and the steps of empty segments
-  unsigned steps = 0, passes = 0, general = 0, emptyp = 0, skipped = 0;
+  unsigned steps = 0, passes = 0, general = 0, emptyp = 0, skipped = 0, refined = 0, substeps = 0;
   unsigned mbits = 0;   // tile lines whose line opacity x segment length fell below -0.01
   T lw_last = 0;
   bool pos_last = true, zero_last = false;
@@ -421,7 +423,9 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
               SW.I[p] = o.I; SW.j0[p] = o.j0; SW.a0[p] = o.a0; SW.S0[p] = o.S0;
               if constexpr (PV) SW.w[p] = o.dtau;   // the owner keeps w in a register
               steps += o.steps - 1;
+              substeps += o.steps;
             }
+            refined++;
             __syncwarp();
 #pragma unroll
             for (int u = 0; u < kPass; u++) {
@@ -475,6 +479,8 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
   wc.passes += passes;
   wc.packed += kFast ? passes - general - emptyp : 0u;
   wc.skipped += skipped;
+  wc.refined += refined;
+  wc.substeps += substeps;
   return steps;
 }
 
@@ -664,10 +670,14 @@ struct WarpSmem {
 // counters[0] formal-solution steps, [1] integrated (line, channel) pairs, [2] node visits
 // (pairs x nodes), [3] node passes of the walk (a pass = the tile's slots over one node),
 // [4] of them taken on the packed FP32 path, [5] steps of empty segments (counted in [0],
-// no arithmetic). The buffers hold kWalkCounters values.
+// no arithmetic), [6] node passes with SUBGRID refinement, [7] the sub-steps of the refined
+// channels. The buffers hold kWalkCounters values.
 __device__ __forceinline__ void flush_counters(WalkCounters wc, unsigned long long* counters, int lane) {
 #pragma unroll
-  for (int off = 16; off > 0; off >>= 1) wc.steps += __shfl_xor_sync(0xffffffffu, wc.steps, off);
+  for (int off = 16; off > 0; off >>= 1) {   // steps and sub-steps are per lane, the rest warp-uniform
+    wc.steps += __shfl_xor_sync(0xffffffffu, wc.steps, off);
+    wc.substeps += __shfl_xor_sync(0xffffffffu, wc.substeps, off);
+  }
   if (lane == 0) {
     atomicAdd(&counters[0], wc.steps);
     atomicAdd(&counters[1], wc.integ);
@@ -675,6 +685,8 @@ __device__ __forceinline__ void flush_counters(WalkCounters wc, unsigned long lo
     atomicAdd(&counters[3], wc.passes);
     atomicAdd(&counters[4], wc.packed);
     atomicAdd(&counters[5], wc.skipped);
+    atomicAdd(&counters[6], wc.refined);
+    atomicAdd(&counters[7], wc.substeps);
   }
 }
 
