@@ -52,6 +52,7 @@ typedef struct rl_stats {
                                         refinement (line.F:4733-4742) */
   unsigned long long sub_steps;      /* steps counted in `steps` that refined channels take
                                         inside such segments */
+  unsigned long long refined_channels; /* (channel, segment) pairs refined in those passes */
 } rl_stats;
 
 typedef struct rl_model_info {

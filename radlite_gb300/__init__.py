@@ -39,7 +39,8 @@ class Stats(C.Structure):
                 ("nrays", C.c_int), ("nfr", C.c_int), ("kmax", C.c_int), ("nlines", C.c_int),
                 ("h2d_bytes", C.c_ulonglong), ("d2h_bytes", C.c_ulonglong), ("node_passes", C.c_ulonglong),
                 ("packed_passes", C.c_ulonglong), ("empty_steps", C.c_ulonglong),
-                ("refined_passes", C.c_ulonglong), ("sub_steps", C.c_ulonglong)]
+                ("refined_passes", C.c_ulonglong), ("sub_steps", C.c_ulonglong),
+                ("refined_channels", C.c_ulonglong)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -889,6 +889,24 @@ __global__ void __launch_bounds__(128) k_adjoint_one(AdjParams<T> A, AdjJobs<T> 
 
 // The gradient sweep (rl_grad.cuh): one warp per (ray, line group) item from the queue;
 // the list of each warp's item sits in its row of the job-wide scratch.
+// Counters of the gradient sweep: [0] steps, [1] zero continuum channels (per lane), [2]
+// node passes with refined or resetting segments, [3] those segments (warp-uniform).
+template <typename T>
+__device__ __forceinline__ void grad_flush(const AdjJobs<T>& B, int lane, unsigned long long steps,
+                                           unsigned long long zc, unsigned long long rp, unsigned long long rc) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    steps += __shfl_xor_sync(0xffffffffu, steps, off);
+    zc += __shfl_xor_sync(0xffffffffu, zc, off);
+  }
+  if (lane == 0) {
+    atomicAdd(&B.counters[0], steps);
+    if (zc) atomicAdd(&B.counters[1], zc);
+    atomicAdd(&B.counters[2], rp);
+    atomicAdd(&B.counters[3], rc);
+  }
+}
+
 // FP32: three blocks per SM (at most 168 registers); FP64 keeps its registers
 template <typename T> struct GradMinBlocks { static constexpr int value = sizeof(T) == 4 ? 3 : 1; };
 
@@ -901,7 +919,7 @@ __global__ void __launch_bounds__(128, GradMinBlocks<T>::value) k_grad_jobs(AdjJ
   GradWork<T>* works = reinterpret_cast<GradWork<T>*>(smem_raw + sizeof(GradStage<T>) * nw);
   unsigned short* list =
       reinterpret_cast<unsigned short*>(B.ckpt + ((size_t)blockIdx.x * nw + wib) * (size_t)B.ckpt_warp);
-  unsigned long long steps = 0, zc = 0;
+  unsigned long long steps = 0, zc = 0, rp = 0, rc = 0;
   int cur = -1;
   for (;;) {
     int item = 0;
@@ -917,17 +935,9 @@ __global__ void __launch_bounds__(128, GradMinBlocks<T>::value) k_grad_jobs(AdjJ
       __syncwarp();
       cur = j;
     }
-    grad_item<T>(jp[wib], item - __ldg(&B.item_prefix[j]), stages[wib], works[wib], list, lane, steps, zc);
+    grad_item<T>(jp[wib], item - __ldg(&B.item_prefix[j]), stages[wib], works[wib], list, lane, steps, zc, rp, rc);
   }
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    steps += __shfl_xor_sync(0xffffffffu, steps, off);
-    zc += __shfl_xor_sync(0xffffffffu, zc, off);
-  }
-  if (lane == 0) {
-    atomicAdd(&B.counters[0], steps);
-    if (zc) atomicAdd(&B.counters[1], zc);
-  }
+  grad_flush(B, lane, steps, zc, rp, rc);
 }
 
 template <typename T>
@@ -938,23 +948,15 @@ __global__ void __launch_bounds__(128, GradMinBlocks<T>::value) k_grad_one(AdjPa
   GradWork<T>* works = reinterpret_cast<GradWork<T>*>(smem_raw + sizeof(GradStage<T>) * nw);
   unsigned short* list =
       reinterpret_cast<unsigned short*>(B.ckpt + ((size_t)blockIdx.x * nw + wib) * (size_t)B.ckpt_warp);
-  unsigned long long steps = 0, zc = 0;
+  unsigned long long steps = 0, zc = 0, rp = 0, rc = 0;
   for (;;) {
     int item = 0;
     if (lane == 0) item = atomicAdd(B.work, 1);
     item = __shfl_sync(0xffffffffu, item, 0);
     if (item >= B.total) break;
-    grad_item<T>(A, item, stages[wib], works[wib], list, lane, steps, zc);
+    grad_item<T>(A, item, stages[wib], works[wib], list, lane, steps, zc, rp, rc);
   }
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    steps += __shfl_xor_sync(0xffffffffu, steps, off);
-    zc += __shfl_xor_sync(0xffffffffu, zc, off);
-  }
-  if (lane == 0) {
-    atomicAdd(&B.counters[0], steps);
-    if (zc) atomicAdd(&B.counters[1], zc);
-  }
+  grad_flush(B, lane, steps, zc, rp, rc);
 }
 
 // ------------------------------------------------------------------------------------

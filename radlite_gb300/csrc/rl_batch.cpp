@@ -477,6 +477,7 @@ int run(rl_batch* b, double* flux_out, rl_stats* st) {
     st->steps += b->cnt_h[0]; st->integrated += b->cnt_h[1]; st->node_visits += b->cnt_h[2];
     st->node_passes += b->cnt_h[3]; st->packed_passes += b->cnt_h[4]; st->empty_steps += b->cnt_h[5];
     st->refined_passes += b->cnt_h[6]; st->sub_steps += b->cnt_h[7];
+    st->refined_channels += b->cnt_h[8];
     st->ray_channels += b->ray_channels;
     st->nlines += b->nlines_total;
   }

@@ -318,7 +318,7 @@ static int run_lines(rl_model* md, int iline0, int nl, double* flux_out, double*
     st->upload_ms += a; st->walk_ms += b; st->reduce_ms += c;
     st->steps += cnt[0]; st->integrated += cnt[1]; st->node_visits += cnt[2];
     st->node_passes += cnt[3]; st->packed_passes += cnt[4]; st->empty_steps += cnt[5];
-    st->refined_passes += cnt[6]; st->sub_steps += cnt[7];
+    st->refined_passes += cnt[6]; st->sub_steps += cnt[7]; st->refined_channels += cnt[8];
     st->ray_channels += (unsigned long long)cam.nrays * nfr * nl;
     st->nrays = cam.nrays; st->nfr = nfr; st->kmax = md->kmax; st->nlines += nl;
   }

@@ -6,8 +6,9 @@
 namespace rl {
 
 // Counters of a walk launch (flush_counters): steps, integrated pairs, node visits, node
-// passes, packed node passes, steps of empty segments, spare.
-constexpr int kWalkCounters = 8;
+// passes, packed node passes, steps of empty segments, refined passes, their sub-steps,
+// their refined channels.
+constexpr int kWalkCounters = 9;
 // Walk launch shape: 4-warp blocks, at most this many per SM (sizes the list scratch).
 constexpr int kWalkBlocksPerSm = 4;
 constexpr int kWalkWarps = 4;

@@ -355,6 +355,7 @@ int backward(rl_diff* d, const double* gflux, double* g_lnT, double* g_lnX, doub
     st->walk_ms += a; st->reduce_ms += b; st->total_ms += a + b;
     st->steps += cnt[0];
     st->integrated += cnt[1];   // items whose continuum channel was zero (their copies get no gradient)
+    if (d->every == 0) { st->refined_passes += cnt[2]; st->refined_channels += cnt[3]; }
     st->nrays = d->cam.nrays; st->nfr = d->nfr; st->kmax = d->kmax; st->nlines += d->nl;
   }
   return 0;
@@ -440,7 +441,7 @@ int batch_build(rl_diff_batch* b) {
   CUDA_TRY(b->awork.ensure(sizeof(int)));
   CUDA_TRY(b->err.ensure(sizeof(int)));
   CUDA_TRY(b->list.ensure(sizeof(unsigned short) * walk_list_elems(ctx->nsm, b->max_nfr)));
-  if (!b->cnt_h) CUDA_TRY(cudaMallocHost((void**)&b->cnt_h, sizeof(unsigned long long) * 8));
+  if (!b->cnt_h) CUDA_TRY(cudaMallocHost((void**)&b->cnt_h, sizeof(unsigned long long) * kWalkCounters));
   if (!b->err_h) CUDA_TRY(cudaMallocHost((void**)&b->err_h, sizeof(int) * 2));
   std::vector<WalkParams<T>> walk(nj);
   std::vector<RedJob<T>> red(nj);

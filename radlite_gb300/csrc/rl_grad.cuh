@@ -413,6 +413,121 @@ __device__ __forceinline__ void gstep_regular(GState<T>& st, const LineVals<T>& 
   st.j0 = p1.j; st.a0 = p1.a; st.S0 = p1.S; st.ra0 = p1.ra; st.E0 = p1.E;
 }
 
+// FP32: the regular steps of a lane's two slots as packed pairs (both slots belong to one
+// line, so the node values are shared operands). Every element is rounded as in
+// gstep_regular: the optical depths equal the first sweep's. Slots that refine (skip) keep
+// their state and contribute nothing here.
+__device__ __forceinline__ float2 sel2(bool a, bool b, float2 t, float2 f) {
+  return make_float2(a ? t.x : f.x, b ? t.y : f.y);
+}
+__device__ __forceinline__ void gstep_regular2(GState<float>* st, const LineVals<float>& v0, const LineVals<float>& v1,
+                                               const float* w, float vl0, float vl1, float rl, float rl0, float hds,
+                                               const float* lamf, const float* sN, const float* cN, const bool* skip,
+                                               GAcc<float>& ac) {
+  const float2 w2 = make_float2(w[0], w[1]);
+  // the node point
+  const float2 u1 = mul2(sub2(w2, dup2(vl1)), dup2(rl));
+  const float2 m1 = mul2(dup2(-1.4426950408889634f), mul2(u1, u1));
+  const float2 E1 = make_float2(ex2(m1.x), ex2(m1.y));
+  const float2 ph1 = mul2(dup2(rl), E1);
+  const float2 a1 = fma2(dup2(v1.af), ph1, dup2(v1.ad));
+  const float2 j1 = fma2(dup2(v1.jf), ph1, dup2(v1.jd));
+  const bool p1x = a1.x > 0.f, p1y = a1.y > 0.f;
+  const float2 ra1 = make_float2(p1x ? Math<float>::rcp(a1.x) : 0.f, p1y ? Math<float>::rcp(a1.y) : 0.f);
+  const float2 S1 = sel2(p1x, p1y, mul2(j1, ra1), dup2(0.f));
+  // the step
+  const float2 a0 = make_float2(st[0].a0, st[1].a0), j0 = make_float2(st[0].j0, st[1].j0);
+  const float2 S0 = make_float2(st[0].S0, st[1].S0);
+  const float2 dt = mul2(add2(a0, a1), dup2(hds));
+  const float2 th = mul2(add2(j0, j1), dup2(hds));
+  float2 xs, as, bs, xd, ad, bd;
+  series2(dt, xs, as, bs);
+  direct2(dt, xd, ad, bd);
+  const bool sx = dt.x < 0.25f, sy = dt.y < 0.25f;
+  const float2 x = sel2(sx, sy, xs, xd), ca = sel2(sx, sy, as, ad), cb = sel2(sx, sy, bs, bd);
+  const bool p0x = a0.x > 0.f, p0y = a0.y > 0.f;
+  const float2 src1 = sel2(p0x, p0y, S0, S1);
+  const float2 src2 = sel2(p1x, p1y, S1, S0);
+  const float2 qraw = fma2(ca, src1, mul2(cb, src2));
+  const bool tx = dt.x > 1.0e-9f, ty = dt.y > 1.0e-9f;
+  float2 qv = sel2(tx, ty, qraw, th);
+  qv = sel2(qv.x < th.x, qv.y < th.y, qv, th);
+  const float2 Ip = make_float2(st[0].I, st[1].I);
+  const float2 In = fma2(Ip, x, qv);
+  // optical depth walked and the multiplier
+  float2 s2 = make_float2(st[0].s, st[1].s), c2 = make_float2(st[0].c, st[1].c);
+  {
+    const float2 y = sub2(dt, c2);
+    const float2 t = add2(s2, y);
+    c2 = sub2(sub2(t, s2), y);
+    s2 = t;
+  }
+  const float2 D = sub2(sub2(make_float2(sN[0], sN[1]), s2), sub2(make_float2(cN[0], cN[1]), c2));
+  const float2 mD = mul2(dup2(-1.4426950408889634f), D);
+  const bool lx = lamf[0] != 0.f && !skip[0], ly = lamf[1] != 0.f && !skip[1];
+  const float2 lam = sel2(lx, ly, mul2(make_float2(lamf[0], lamf[1]), make_float2(ex2(mD.x), ex2(mD.y))), dup2(0.f));
+  // gradient of the step (gstep_back, two slots)
+  const float2 r = make_float2(Math<float>::rcp(dt.x), Math<float>::rcp(dt.y));
+  const float2 nd = make_float2(-dt.x, -dt.y);
+  float2 dbs = fma2(nd, dup2(1.f / 840.f), dup2(1.f / 144.f));
+  dbs = fma2(nd, dbs, dup2(1.f / 30.f));
+  dbs = fma2(nd, dbs, dup2(1.f / 8.f));
+  dbs = fma2(nd, dbs, dup2(1.f / 3.f));
+  dbs = fma2(nd, dbs, dup2(0.5f));
+  const float2 de0 = fma2(nd, dbs, sub2(dup2(1.f), cb));
+  const float2 dbd = mul2(ca, r);
+  const float2 db = sel2(sx, sy, dbs, dbd);
+  const float2 dx = sel2(sx, sy, make_float2(-de0.x, -de0.y), make_float2(-x.x, -x.y));
+  const float2 da = sel2(sx, sy, sub2(de0, dbs), sub2(x, dbd));
+  const bool nx = tx && qraw.x < th.x, ny = ty && qraw.y < th.y;   // the linear-source branch
+  const float2 g_dt = fma2(mul2(lam, Ip), dx, sel2(nx, ny, mul2(lam, fma2(src1, da, mul2(src2, db))), dup2(0.f)));
+  const float2 g_th = sel2(nx, ny, dup2(0.f), lam);
+  const float2 g1 = sel2(nx, ny, mul2(lam, ca), dup2(0.f)), g2 = sel2(nx, ny, mul2(lam, cb), dup2(0.f));
+  const float2 gS0 = add2(sel2(p0x, p0y, g1, dup2(0.f)), sel2(p1x, p1y, dup2(0.f), g2));
+  const float2 gS1 = add2(sel2(p0x, p0y, dup2(0.f), g1), sel2(p1x, p1y, g2, dup2(0.f)));
+  const float2 ga = mul2(g_dt, dup2(hds)), gj = mul2(g_th, dup2(hds));
+  // the carried point is complete: its pending part, this step's part, dL/dS folded in
+  const float2 ra0 = make_float2(st[0].ra0, st[1].ra0);
+  float2 gjs = add2(make_float2(st[0].pgj, st[1].pgj), gj), gas = add2(make_float2(st[0].pga, st[1].pga), ga);
+  {
+    const bool fx = p0x && gS0.x != 0.f, fy = p0y && gS0.y != 0.f;
+    const float2 t = mul2(gS0, ra0);
+    gjs = add2(gjs, sel2(fx, fy, t, dup2(0.f)));
+    gas = sub2(gas, sel2(fx, fy, mul2(t, S0), dup2(0.f)));
+  }
+  gjs = sel2(skip[0], skip[1], dup2(0.f), gjs);
+  gas = sel2(skip[0], skip[1], dup2(0.f), gas);
+  {
+    const float2 u0 = mul2(sub2(w2, dup2(vl0)), dup2(rl0));
+    const float2 E0 = make_float2(st[0].E0, st[1].E0);
+    const float2 phi0 = mul2(dup2(rl0), E0);
+    const float2 gjp = mul2(gjs, phi0), gap = mul2(gas, phi0);
+    ac.p[0] += gjs.x + gjs.y;
+    ac.p[1] += gjp.x + gjp.y;
+    ac.p[2] += gap.x + gap.y;
+    const float2 gphi = fma2(gjs, dup2(v0.jf), mul2(gas, dup2(v0.af)));
+    const float2 grl = mul2(mul2(gphi, E0), fma2(dup2(-2.f), mul2(u0, u0), dup2(1.f)));
+    ac.rp += grl.x + grl.y;
+  }
+  // the node point carries this step's part
+  float2 pgj = gj, pga = ga;
+  {
+    const bool fx = p1x && gS1.x != 0.f, fy = p1y && gS1.y != 0.f;
+    const float2 t = mul2(gS1, ra1);
+    pgj = add2(pgj, sel2(fx, fy, t, dup2(0.f)));
+    pga = sub2(pga, sel2(fx, fy, mul2(t, S1), dup2(0.f)));
+  }
+#pragma unroll
+  for (int u = 0; u < 2; u++) {
+    if (skip[u]) continue;
+    st[u].I = u == 0 ? In.x : In.y;
+    st[u].s = u == 0 ? s2.x : s2.y; st[u].c = u == 0 ? c2.x : c2.y;
+    st[u].pgj = u == 0 ? pgj.x : pgj.y; st[u].pga = u == 0 ? pga.x : pga.y;
+    st[u].j0 = u == 0 ? j1.x : j1.y; st[u].a0 = u == 0 ? a1.x : a1.y; st[u].S0 = u == 0 ? S1.x : S1.y;
+    st[u].ra0 = u == 0 ? ra1.x : ra1.y; st[u].E0 = u == 0 ? E1.x : E1.y;
+  }
+}
+
 // Stage nodes kb-1 .. kb+31 of a ray (entries 0..32) for lines l0 .. l0+gl-1.
 template <typename T>
 __device__ __forceinline__ void grad_stage(const WalkParams<T>& P, GradStage<T>& S, size_t row, int kb, int K, int l0,
@@ -479,7 +594,8 @@ __device__ __forceinline__ void gscatter(const AdjParams<T>& A, int l, int c00, 
 // One gradient work item: line group gi of ray `ray`.
 template <typename T>
 __device__ void grad_item(const AdjParams<T>& A, int item, GradStage<T>& S, GradWork<T>& W, unsigned short* list,
-                          int lane, unsigned long long& steps, unsigned long long& zero_cont) {
+                          int lane, unsigned long long& steps, unsigned long long& zero_cont, unsigned long long& rpass,
+                          unsigned long long& rch) {
   const WalkParams<T>& P = A.W;
   const NodeBuf<T>& nb = P.nb;
   const int nrays = nb.nrays;
@@ -706,10 +822,19 @@ __device__ void grad_item(const AdjParams<T>& A, int item, GradStage<T>& S, Grad
               ov = ch[u] >= 0 && addr(sc, G.hw3) > (T)0 && subr(sc, G.hw3) < dsf;
             }
             need[u] = ch[u] >= 0 && (init || ov);
-            if (!init && !ov) {
-              gstep_regular(st[u], v0, v1, w[u], vl0, vl1, rl, rl0, hds, ch[u] < 0 ? (T)0 : keep * seed[u], sN[u], cN[u],
-                            ac);
-              if (ch[u] >= 0) steps++;
+            if constexpr (!(sizeof(T) == 4 && kGS == 2)) {
+              if (!init && !ov) {
+                gstep_regular(st[u], v0, v1, w[u], vl0, vl1, rl, rl0, hds, ch[u] < 0 ? (T)0 : keep * seed[u], sN[u],
+                              cN[u], ac);
+                if (ch[u] >= 0) steps++;
+              }
+            }
+          }
+          if constexpr (sizeof(T) == 4 && kGS == 2) {
+            if (!init) {
+              const float lf[2] = {ch[0] < 0 ? 0.f : keep * seed[0], ch[1] < 0 ? 0.f : keep * seed[1]};
+              gstep_regular2(st, v0, v1, w, vl0, vl1, rl, rl0, hds, lf, sN, cN, need, ac);
+              steps += (ch[0] >= 0 && !need[0]) + (ch[1] >= 0 && !need[1]);
             }
           }
           // refined and resetting segments: the slots that need one, compacted over the
@@ -722,6 +847,7 @@ __device__ void grad_item(const AdjParams<T>& A, int item, GradStage<T>& S, Grad
             cnt += __popc(mk);
           }
           const int kind = init ? (sub ? 2 : 0) : 1;
+          if (cnt > 0) { rpass++; rch += cnt; }   // warp-uniform counts
           for (int r0 = 0; r0 < cnt; r0 += 32) {
 #pragma unroll
             for (int u = 0; u < kGS; u++) {

@@ -24,57 +24,6 @@ __device__ __forceinline__ void kahan_add(T& s, T& c, T x) {
   s = t;
 }
 
-// Formal solution of the (line, channel) pairs list[0..nt) of lines l0.. of one ray.
-// The per-line tables carry the profile normalisation 0.56419583546/(3.33567e-6 nu0), so
-// the profile of every slot is rlw * exp(-u^2) with the node's shared 1/linewidth.
-// Work order: per 32-node chunk, per pair of slots (two independent channels per lane),
-// all nodes of the chunk; the slot state lives in shared memory between pairs.
-// PV: also the optical depth of every slot, Kahan-compensated in P.tau / P.tauc (the slot's
-// image position), and no star mixing.
-// The list entries carry item line indices; lbase is the item line of l0 (the tile's first
-// line), so that entry line - lbase indexes the tile's staged lines 0..gl-1.
-// Packed FP32 pairs (sm_100 and later): one instruction works on two independent slots.
-__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
-__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
-  unsigned long long ra, rb, rd;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(ra) : "f"(a.x), "f"(a.y));
-  asm("mov.b64 %0, {%1, %2};" : "=l"(rb) : "f"(b.x), "f"(b.y));
-  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(rd) : "l"(ra), "l"(rb));
-  float2 d;
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(d.x), "=f"(d.y) : "l"(rd));
-  return d;
-}
-__device__ __forceinline__ float2 dup2(float a) { return make_float2(a, a); }
-__device__ __forceinline__ float ex2(float x) {   // 2^x on the MUFU pipe
-  float y;
-  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
-}
-
-// Math<float>::series and ::direct on a pair of optical depths, with the same roundings
-// per element.
-__device__ __forceinline__ void series2(float2 d, float2& x, float2& a, float2& b) {
-  const float2 nd = make_float2(-d.x, -d.y);
-  float2 t = fma2(d, dup2(-1.f / 5040.f), dup2(1.f / 720.f));
-  t = fma2(nd, t, dup2(1.f / 120.f));
-  t = fma2(nd, t, dup2(1.f / 24.f));
-  t = fma2(nd, t, dup2(1.f / 6.f));
-  t = fma2(nd, t, dup2(0.5f));
-  b = mul2(d, t);
-  const float2 e0 = fma2(nd, b, d);
-  x = sub2(dup2(1.f), e0);
-  a = sub2(e0, b);
-}
-__device__ __forceinline__ void direct2(float2 d, float2& x, float2& a, float2& b) {
-  const float2 m = mul2(d, dup2(-1.4426950408889634f));
-  x = make_float2(ex2(m.x), ex2(m.y));
-  const float2 e0 = sub2(dup2(1.f), x);
-  b = mul2(sub2(d, e0), make_float2(Math<float>::rcp(d.x), Math<float>::rcp(d.y)));
-  a = sub2(e0, b);
-}
-
 // Thin-step switch of qdr_src_2 (transfer.F:1545-1549: Q = 0.5 (j1+j2) ds unless the
 // optical depth exceeds the REAL literal 1e-9) without a compare: sat(2^100 (c - dt)) is 1
 // for dt <= 1e-9f and 0 above (c is the next float above 1e-9f, scaled exactly by 2^100).
@@ -100,9 +49,19 @@ __device__ __forceinline__ SegGeom<T> seg_geom(T ds, T dvs, T rlw, T kq) {
 }
 
 struct WalkCounters {
-  unsigned long long steps = 0, integ = 0, nodes = 0, passes = 0, packed = 0, skipped = 0, refined = 0, substeps = 0;
+  unsigned long long steps = 0, integ = 0, nodes = 0, passes = 0, packed = 0, skipped = 0, refined = 0, substeps = 0,
+                     refch = 0;
 };
 
+// Formal solution of the (line, channel) pairs list[0..nt) of lines l0.. of one ray.
+// The per-line tables carry the profile normalisation 0.56419583546/(3.33567e-6 nu0), so
+// the profile of every slot is rlw * exp(-u^2) with the node's shared 1/linewidth.
+// Work order: per 32-node chunk, per pair of slots (two independent channels per lane),
+// all nodes of the chunk; the slot state lives in shared memory between pairs.
+// PV: also the optical depth of every slot, Kahan-compensated in P.tau / P.tauc (the slot's
+// image position), and no star mixing.
+// The list entries carry item line indices; lbase is the item line of l0 (the tile's first
+// line), so that entry line - lbase indexes the tile's staged lines 0..gl-1.
 template <typename T, int C, bool PV = false>
 __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<T, C>& SS, SubWork<T>& SW, int ray,
                               int K, int l0, int gl, const unsigned short* list, int nt, int lane, int lbase,
@@ -148,7 +107,7 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
   }
   // per-call counts (32-bit: a call walks one tile of one ray): formal-solution steps, node
   // passes, of them on the general path and empty, and the steps of empty segments
-  unsigned steps = 0, passes = 0, general = 0, emptyp = 0, skipped = 0, refined = 0, substeps = 0;
+  unsigned steps = 0, passes = 0, general = 0, emptyp = 0, skipped = 0, refined = 0, substeps = 0, refch = 0;
   unsigned mbits = 0;   // tile lines whose line opacity x segment length fell below -0.01
   T lw_last = 0;
   bool pos_last = true, zero_last = false;
@@ -426,6 +385,7 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
               substeps += o.steps;
             }
             refined++;
+            refch += cnt;
             __syncwarp();
 #pragma unroll
             for (int u = 0; u < kPass; u++) {
@@ -481,6 +441,7 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
   wc.skipped += skipped;
   wc.refined += refined;
   wc.substeps += substeps;
+  wc.refch += refch;
   return steps;
 }
 
@@ -671,7 +632,7 @@ struct WarpSmem {
 // (pairs x nodes), [3] node passes of the walk (a pass = the tile's slots over one node),
 // [4] of them taken on the packed FP32 path, [5] steps of empty segments (counted in [0],
 // no arithmetic), [6] node passes with SUBGRID refinement, [7] the sub-steps of the refined
-// channels. The buffers hold kWalkCounters values.
+// channels, [8] the refined channels of those passes. The buffers hold kWalkCounters values.
 __device__ __forceinline__ void flush_counters(WalkCounters wc, unsigned long long* counters, int lane) {
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {   // steps and sub-steps are per lane, the rest warp-uniform
@@ -687,6 +648,7 @@ __device__ __forceinline__ void flush_counters(WalkCounters wc, unsigned long lo
     atomicAdd(&counters[5], wc.skipped);
     atomicAdd(&counters[6], wc.refined);
     atomicAdd(&counters[7], wc.substeps);
+    atomicAdd(&counters[8], wc.refch);
   }
 }
 

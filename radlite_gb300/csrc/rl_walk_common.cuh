@@ -98,6 +98,48 @@ template <> struct Math<double> {
   }
 };
 
+// Packed FP32 pairs (sm_100 and later): one instruction works on two independent slots.
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+  unsigned long long ra, rb, rd;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(ra) : "f"(a.x), "f"(a.y));
+  asm("mov.b64 %0, {%1, %2};" : "=l"(rb) : "f"(b.x), "f"(b.y));
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(rd) : "l"(ra), "l"(rb));
+  float2 d;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(d.x), "=f"(d.y) : "l"(rd));
+  return d;
+}
+__device__ __forceinline__ float2 dup2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float ex2(float x) {   // 2^x on the MUFU pipe
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// Math<float>::series and ::direct on a pair of optical depths, with the same roundings
+// per element.
+__device__ __forceinline__ void series2(float2 d, float2& x, float2& a, float2& b) {
+  const float2 nd = make_float2(-d.x, -d.y);
+  float2 t = fma2(d, dup2(-1.f / 5040.f), dup2(1.f / 720.f));
+  t = fma2(nd, t, dup2(1.f / 120.f));
+  t = fma2(nd, t, dup2(1.f / 24.f));
+  t = fma2(nd, t, dup2(1.f / 6.f));
+  t = fma2(nd, t, dup2(0.5f));
+  b = mul2(d, t);
+  const float2 e0 = fma2(nd, b, d);
+  x = sub2(dup2(1.f), e0);
+  a = sub2(e0, b);
+}
+__device__ __forceinline__ void direct2(float2 d, float2& x, float2& a, float2& b) {
+  const float2 m = mul2(d, dup2(-1.4426950408889634f));
+  x = make_float2(ex2(m.x), ex2(m.y));
+  const float2 e0 = sub2(dup2(1.f), x);
+  b = mul2(sub2(d, e0), make_float2(Math<float>::rcp(d.x), Math<float>::rcp(d.y)));
+  a = sub2(e0, b);
+}
+
 template <typename T>
 __device__ __forceinline__ T profile(T w, T vl, T rlw, T nrm) {
   const T u = (w - vl) * rlw;
