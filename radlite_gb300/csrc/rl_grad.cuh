@@ -48,8 +48,9 @@ __device__ __forceinline__ void kadd(T& s, T& c, T x) {   // compensated s += x 
 // kb - 1 + t), the node data of the scatter, and the item's window and lane layout.
 template <typename T>
 struct GradStage {
-  LineVals<T> lv[kGG][33];
+  LineVals<T> lv[kGG][33];   // the lines of the current tile
   T vl[33], hds[33], ds[33], rlw[33], dvs[33], wr[33], wt[33];
+  T gq[33], gids[33], gidvs[33], gdls[33], ghw3[33], glg[33], gilg[33];   // segment geometry (GSeg)
   int c00[33];
   unsigned misc[33], flags[33];
   double gcopy[kGG];      // gradient of the channels copied from the continuum channel
@@ -528,6 +529,15 @@ __device__ __forceinline__ void gstep_regular2(GState<float>* st, const LineVals
   }
 }
 
+// the staged segment geometry of entry t
+template <typename T>
+__device__ __forceinline__ GSeg<T> stage_seg(const GradStage<T>& S, int t) {
+  GSeg<T> g;
+  g.q = S.gq[t]; g.ids = S.gids[t]; g.idvs = S.gidvs[t]; g.dls = S.gdls[t]; g.hw3 = S.ghw3[t]; g.lg = S.glg[t];
+  g.ilg = S.gilg[t];
+  return g;
+}
+
 // Stage nodes kb-1 .. kb+31 of a ray (entries 0..32) for lines l0 .. l0+gl-1.
 template <typename T>
 __device__ __forceinline__ void grad_stage(const WalkParams<T>& P, GradStage<T>& S, size_t row, int kb, int K, int l0,
@@ -541,6 +551,7 @@ __device__ __forceinline__ void grad_stage(const WalkParams<T>& P, GradStage<T>&
       const LineVals<T> z = {0, 0, 0, 0};
       for (int l = 0; l < gl; l++) S.lv[l][t] = z;
       S.vl[t] = 0; S.hds[t] = 0; S.ds[t] = 0; S.rlw[t] = 0; S.dvs[t] = 0; S.wr[t] = 0; S.wt[t] = 0;
+      S.gq[t] = 0; S.gids[t] = 0; S.gidvs[t] = 0; S.gdls[t] = 0; S.ghw3[t] = 0; S.glg[t] = 0; S.gilg[t] = 0;
       S.c00[t] = 0; S.misc[t] = 0; S.flags[t] = 0;
       continue;
     }
@@ -556,9 +567,12 @@ __device__ __forceinline__ void grad_stage(const WalkParams<T>& P, GradStage<T>&
     const T rlw = lwav > (T)0 ? Math<T>::div((T)1, lwav) : (T)0;
     S.vl[t] = vl; S.hds[t] = (T)0.5 * ds; S.ds[t] = ds; S.rlw[t] = rlw; S.dvs[t] = dvs;
     S.wr[t] = wr; S.wt[t] = wt; S.misc[t] = misc; S.c00[t] = c00;
+    const GSeg<T> G = gseg<T>(ds, dvs, rlw, P.kq);
+    S.gq[t] = G.q; S.gids[t] = G.ids; S.gidvs[t] = G.idvs; S.gdls[t] = G.dls; S.ghw3[t] = G.hw3; S.glg[t] = G.lg;
+    S.gilg[t] = G.ilg;
     unsigned f = misc;
     if (k == 1 || (misc & kFlagHole) || k == star_node) f |= kFlagInit;
-    if ((T)6 * gseg<T>(ds, dvs, rlw, P.kq).q > (T)1) f |= kFlagSub;
+    if ((T)6 * G.q > (T)1) f |= kFlagSub;
     S.flags[t] = f;
   }
   __syncwarp();
@@ -712,7 +726,18 @@ __device__ void grad_item(const AdjParams<T>& A, int item, GradStage<T>& S, Grad
       pb = S.lineoff[li] + (L - S.lanepre[li]) * kGS;
       m = min(kGS, S.lineoff[li + 1] - pb);
     }
-    const int lsafe = li < 0 ? 0 : li;
+    // the tile's lines: from the line of its first lane to that of its last; only those
+    // are staged
+    int tl0 = 0, tl1 = 0;
+    {
+      const int Lb = tile * 32, Le = min(tile * 32 + 31, lanes - 1);
+      while (S.lanepre[tl0 + 1] <= Lb) tl0++;
+      tl1 = tl0;
+      while (S.lanepre[tl1 + 1] <= Le) tl1++;
+    }
+    const int tgl = tl1 - tl0 + 1;
+    const int lit = li < 0 ? tl0 : li;   // the lane's line in the item (a staged one for idle lanes)
+    const int lsafe = lit - tl0;         // and among the staged lines
     // segmented sums over the lanes of each line: lanes lane+d of the same line
     unsigned same = 0;
 #pragma unroll
@@ -726,7 +751,7 @@ __device__ void grad_item(const AdjParams<T>& A, int item, GradStage<T>& S, Grad
     T w[kGS], seed[kGS], sN[kGS], cN[kGS];
     int ch[kGS];
     GState<T> st[kGS];
-    const T istart = P.lc[l0 + lsafe].istart;
+    const T istart = P.lc[l0 + lit].istart;
 #pragma unroll
     for (int u = 0; u < kGS; u++) {
       ch[u] = -1; w[u] = 0; seed[u] = 0;
@@ -746,7 +771,7 @@ __device__ void grad_item(const AdjParams<T>& A, int item, GradStage<T>& S, Grad
     // 3a. first sweep: the optical depth of the whole ray per slot
     for (int cix = 0; cix < nchunk; cix++) {
       const int kb = cix * 32;
-      grad_stage(P, S, row, kb, K, l0, gl, star_node, lane);
+      grad_stage(P, S, row, kb, K, l0 + tl0, tgl, star_node, lane);
       const int nn = min(32, K - kb);
       const int n0 = kb == 0 ? 1 : 0;
       for (int n = n0; n < nn; n++) {
@@ -756,7 +781,7 @@ __device__ void grad_item(const AdjParams<T>& A, int item, GradStage<T>& S, Grad
         const LineVals<T> v0 = S.lv[lsafe][n], v1 = S.lv[lsafe][n + 1];
         const bool init = (fl & kFlagInit) != 0, sub = (fl & kFlagSub) != 0;
         GSeg<T> G = {};
-        if (init || sub) G = gseg<T>(dsf, dvs, rl, P.kq);
+        if (init || sub) G = stage_seg(S, n + 1);
 #pragma unroll
         for (int u = 0; u < kGS; u++) {
           bool ov = false;
@@ -794,7 +819,7 @@ __device__ void grad_item(const AdjParams<T>& A, int item, GradStage<T>& S, Grad
     bool hheld = false;
     for (int cix = 0; cix < nchunk; cix++) {
       const int kb = cix * 32;
-      grad_stage(P, S, row, kb, K, l0, gl, star_node, lane);
+      grad_stage(P, S, row, kb, K, l0 + tl0, tgl, star_node, lane);
       const int nn = min(32, K - kb);
       const int n0 = kb == 0 ? 1 : 0;
       for (int n = n0; n <= nn; n++) {
@@ -809,13 +834,13 @@ __device__ void grad_item(const AdjParams<T>& A, int item, GradStage<T>& S, Grad
           const LineVals<T> v0 = S.lv[lsafe][n], v1 = S.lv[lsafe][n + 1];
           const bool init = (fl & kFlagInit) != 0, sub = (fl & kFlagSub) != 0;
           GSeg<T> G = {};
-          if (init || sub) G = gseg<T>(dsf, dvs, rl, P.kq);
+          if (init || sub) G = stage_seg(S, n + 1);
           bool need[kGS];
           if (kb + n == star_node) keep = (T)1;
 #pragma unroll
           for (int u = 0; u < kGS; u++) {
             if (kb + n == star_node)
-              st[u].I = ((T)1 - P.fstar) * st[u].I + P.fstar * P.star[(size_t)(l0 + lsafe) * P.nfr + (ch[u] < 0 ? 0 : ch[u])];
+              st[u].I = ((T)1 - P.fstar) * st[u].I + P.fstar * P.star[(size_t)(l0 + lit) * P.nfr + (ch[u] < 0 ? 0 : ch[u])];
             bool ov = false;
             if (!init && sub) {
               const T sc = gsc(w[u], vl0, dsf, dvs, G);
