@@ -291,7 +291,7 @@ __device__ __forceinline__ GState<T> gw_get(const GradWork<T>& W, int q) {
 // SUBGRID points of a resetting segment. rl0: width with which the carried start point
 // was evaluated.
 template <typename T>
-__device__ __noinline__ GRes<T> gseg_refined(int kind, bool init, T w, LineVals<T> v0, LineVals<T> v1, T vl0, T vl1,
+__device__ __forceinline__ GRes<T> gseg_refined(int kind, bool init, T w, LineVals<T> v0, LineVals<T> v1, T vl0, T vl1,
                                              T rl, T rl0, T hds, T dsf, T dvs, GSeg<T> G, T seed, T sN, T cN,
                                              GState<T> st, GAcc<T> ac) {
   T tmp[4];
@@ -782,6 +782,7 @@ __device__ void grad_item(const AdjParams<T>& A, int item, GradStage<T>& S, Grad
         const bool init = (fl & kFlagInit) != 0, sub = (fl & kFlagSub) != 0;
         GSeg<T> G = {};
         if (init || sub) G = stage_seg(S, n + 1);
+        bool need[kGS];
 #pragma unroll
         for (int u = 0; u < kGS; u++) {
           bool ov = false;
@@ -789,17 +790,46 @@ __device__ void grad_item(const AdjParams<T>& A, int item, GradStage<T>& S, Grad
             const T sc = gsc(w[u], vl0, dsf, dvs, G);
             ov = ch[u] >= 0 && addr(sc, G.hw3) > (T)0 && subr(sc, G.hw3) < dsf;
           }
-          if (init || ov) {
-            // (the second sweep leaves empty slots alone at resetting nodes: so does this one)
-            if (ch[u] >= 0)
-              st[u].a0 = gseg_tau<T>(init ? (sub ? 2 : 0) : 1, init, w[u], v0, v1, vl0, vl1, rl, hds, dsf, dvs, G,
-                                     st[u].a0, st[u].s, st[u].c);
-          } else {
+          // (the second sweep leaves empty slots alone at resetting nodes: so does this one)
+          need[u] = ch[u] >= 0 && (init || ov);
+          if (!init && !ov) {
             T E;
             const T a1 = gpt_a(v1, w[u], vl1, rl, E);
             kadd(st[u].s, st[u].c, mulr(addr(st[u].a0, a1), hds));
             st[u].a0 = a1;
           }
+        }
+        // refined and resetting segments, compacted over the warp as in the second sweep
+        int pos[kGS], cnt = 0;
+#pragma unroll
+        for (int u = 0; u < kGS; u++) {
+          const unsigned mk = __ballot_sync(0xffffffffu, need[u]);
+          pos[u] = cnt + __popc(mk & lanemask_lt());
+          cnt += __popc(mk);
+        }
+        for (int r0 = 0; r0 < cnt; r0 += 32) {
+#pragma unroll
+          for (int u = 0; u < kGS; u++) {
+            const int q = pos[u] - r0;
+            if (need[u] && q >= 0 && q < 32) {
+              W.k[0][q] = w[u]; W.st[2][q] = st[u].a0; W.st[8][q] = st[u].s; W.st[9][q] = st[u].c; W.line[q] = lsafe;
+            }
+          }
+          __syncwarp();
+          if (lane < cnt - r0) {
+            const int lq = W.line[lane];
+            T sq = W.st[8][lane], cq = W.st[9][lane];
+            W.st[2][lane] = gseg_tau<T>(init ? (sub ? 2 : 0) : 1, init, W.k[0][lane], S.lv[lq][n], S.lv[lq][n + 1], vl0,
+                                        vl1, rl, hds, dsf, dvs, G, W.st[2][lane], sq, cq);
+            W.st[8][lane] = sq; W.st[9][lane] = cq;
+          }
+          __syncwarp();
+#pragma unroll
+          for (int u = 0; u < kGS; u++) {
+            const int q = pos[u] - r0;
+            if (need[u] && q >= 0 && q < 32) { st[u].a0 = W.st[2][q]; st[u].s = W.st[8][q]; st[u].c = W.st[9][q]; }
+          }
+          __syncwarp();
         }
       }
       __syncwarp();
