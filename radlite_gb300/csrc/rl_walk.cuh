@@ -124,7 +124,7 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
     const int k = kb + lane;
     T vl = 0, ds = 0, dvs = 0, lwk = 0;
     unsigned misc = 0;
-    bool pos = true;    // every staged line has a normal dust opacity and no inversion here
+    bool pos = true;    // every staged line has a positive dust opacity and no inversion here
     bool zero = true;   // every staged line's emissivity and opacity factors are 0 here
     if (k < K) {
       const size_t o = row + k;
@@ -135,7 +135,9 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
         const LineVals<T> v = interp_lv(P.tab, c, nl, l0 + l, wr, wt);
         S.lv[l][lane + 1] = v;
         if constexpr (kFast) {
-          pos = pos && v.ad >= 1.17549435e-38f && v.af >= 0.f;
+          // a positive dust opacity (subnormal ones included: their reciprocal is +inf in both
+          // forms of the step, and the source brackets pick the same values) and no inversion
+          pos = pos && v.ad > 0.f && v.af >= 0.f;
           zero = zero && v.jd == 0.f && v.jf == 0.f && v.ad == 0.f && v.af == 0.f;
         }
       }
