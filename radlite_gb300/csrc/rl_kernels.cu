@@ -208,6 +208,8 @@ __global__ void __launch_bounds__(128, WalkMinBlocks<T>::value) k_walk(WalkParam
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
   WarpSmem<T, C> W(smem_raw, nw, wib, kItemLines * P.nfr, P.list);
   WalkCounters wc;
+  if (lane == 0) { W.SW->rstat[0] = 0; W.SW->rstat[1] = 0; W.SW->rstat[2] = 0; }
+  __syncwarp();
   for (;;) {
     int item = 0;
     if (lane == 0) item = atomicAdd(P.work, 1);
@@ -215,7 +217,8 @@ __global__ void __launch_bounds__(128, WalkMinBlocks<T>::value) k_walk(WalkParam
     if (item >= P.nitems) break;
     walk_item<T, C>(P, item, *W.S, *W.SS, *W.SW, W.list, lane, wc);
   }
-  flush_counters(wc, P.counters, lane);
+  __syncwarp();
+  flush_counters(wc, *W.SW, P.counters, lane);
 }
 
 // Walk of many jobs (model, camera, line range) from one device queue: queue entry i
@@ -229,6 +232,8 @@ __global__ void __launch_bounds__(128, WalkMinBlocks<T>::value) k_walk_jobs(Walk
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
   WarpSmem<T, C> W(smem_raw, nw, wib, kItemLines * B.max_nfr, B.list);
   WalkCounters wc;
+  if (lane == 0) { W.SW->rstat[0] = 0; W.SW->rstat[1] = 0; W.SW->rstat[2] = 0; }
+  __syncwarp();
   int cur = -1;
   const int nq = (B.total + B.stride - 1) / B.stride;
   for (;;) {
@@ -248,7 +253,8 @@ __global__ void __launch_bounds__(128, WalkMinBlocks<T>::value) k_walk_jobs(Walk
     }
     walk_item<T, C>(jp[wib], item - __ldg(&B.item_prefix[j]), *W.S, *W.SS, *W.SW, W.list, lane, wc);
   }
-  flush_counters(wc, B.counters, lane);
+  __syncwarp();
+  flush_counters(wc, *W.SW, B.counters, lane);
 }
 
 // ------------------------------------------------------------------------------------

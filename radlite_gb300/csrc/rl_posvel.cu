@@ -33,6 +33,8 @@ __global__ void __launch_bounds__(128, WalkMinBlocks<T>::value) k_walk_pv(WalkPa
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
   WarpSmem<T, C> W(smem_raw, nw, wib, kItemLines * P.nfr, P.list);
   WalkCounters wc;
+  if (lane == 0) { W.SW->rstat[0] = 0; W.SW->rstat[1] = 0; W.SW->rstat[2] = 0; }
+  __syncwarp();
   for (;;) {
     int item = 0;
     if (lane == 0) item = atomicAdd(P.work, 1);
@@ -40,7 +42,8 @@ __global__ void __launch_bounds__(128, WalkMinBlocks<T>::value) k_walk_pv(WalkPa
     if (item >= P.nitems) break;
     walk_item<T, C, true>(P, item, *W.S, *W.SS, *W.SW, W.list, lane, wc);
   }
-  flush_counters(wc, P.counters, lane);
+  __syncwarp();
+  flush_counters(wc, *W.SW, P.counters, lane);
 }
 
 struct CubeParams {

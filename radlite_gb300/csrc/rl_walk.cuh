@@ -48,10 +48,7 @@ __device__ __forceinline__ SegGeom<T> seg_geom(T ds, T dvs, T rlw, T kq) {
   return g;
 }
 
-struct WalkCounters {
-  unsigned long long steps = 0, integ = 0, nodes = 0, passes = 0, packed = 0, skipped = 0, refined = 0, substeps = 0,
-                     refch = 0;
-};
+struct WalkCounters { unsigned long long steps = 0, integ = 0, nodes = 0, passes = 0, packed = 0, skipped = 0; };
 
 // Formal solution of the (line, channel) pairs list[0..nt) of lines l0.. of one ray.
 // The per-line tables carry the profile normalisation 0.56419583546/(3.33567e-6 nu0), so
@@ -107,7 +104,7 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
   }
   // per-call counts (32-bit: a call walks one tile of one ray): formal-solution steps, node
   // passes, of them on the general path and empty, and the steps of empty segments
-  unsigned steps = 0, passes = 0, general = 0, emptyp = 0, skipped = 0, refined = 0, substeps = 0, refch = 0;
+  unsigned steps = 0, passes = 0, general = 0, emptyp = 0, skipped = 0;
   unsigned mbits = 0;   // tile lines whose line opacity x segment length fell below -0.01
   T lw_last = 0;
   bool pos_last = true, zero_last = false;
@@ -375,6 +372,7 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
             }
             __syncwarp();
             const T vl0 = S.vl[n], dsf = S.ds[n + 1], dvsg = S.dvs[n + 1];
+            unsigned mysub = 0;
             for (int p = lane; p < cnt; p += 32) {
               const T wp = SW.w[p];
               const int lp = SW.l[p];
@@ -384,10 +382,11 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
               SW.I[p] = o.I; SW.j0[p] = o.j0; SW.a0[p] = o.a0; SW.S0[p] = o.S0;
               if constexpr (PV) SW.w[p] = o.dtau;   // the owner keeps w in a register
               steps += o.steps - 1;
-              substeps += o.steps;
+              mysub += o.steps;
             }
-            refined++;
-            refch += cnt;
+            // refinement statistics in shared memory (this path is rare; registers are not)
+            mysub = __reduce_add_sync(0xffffffffu, mysub);
+            if (lane == 0) { SW.rstat[0] += 1; SW.rstat[1] += mysub; SW.rstat[2] += cnt; }
             __syncwarp();
 #pragma unroll
             for (int u = 0; u < kPass; u++) {
@@ -441,9 +440,6 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
   wc.passes += passes;
   wc.packed += kFast ? passes - general - emptyp : 0u;
   wc.skipped += skipped;
-  wc.refined += refined;
-  wc.substeps += substeps;
-  wc.refch += refch;
   return steps;
 }
 
@@ -635,12 +631,11 @@ struct WarpSmem {
 // [4] of them taken on the packed FP32 path, [5] steps of empty segments (counted in [0],
 // no arithmetic), [6] node passes with SUBGRID refinement, [7] the sub-steps of the refined
 // channels, [8] the refined channels of those passes. The buffers hold kWalkCounters values.
-__device__ __forceinline__ void flush_counters(WalkCounters wc, unsigned long long* counters, int lane) {
+template <typename T>
+__device__ __forceinline__ void flush_counters(WalkCounters wc, const SubWork<T>& SW, unsigned long long* counters,
+                                               int lane) {
 #pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {   // steps and sub-steps are per lane, the rest warp-uniform
-    wc.steps += __shfl_xor_sync(0xffffffffu, wc.steps, off);
-    wc.substeps += __shfl_xor_sync(0xffffffffu, wc.substeps, off);
-  }
+  for (int off = 16; off > 0; off >>= 1) wc.steps += __shfl_xor_sync(0xffffffffu, wc.steps, off);   // per lane
   if (lane == 0) {
     atomicAdd(&counters[0], wc.steps);
     atomicAdd(&counters[1], wc.integ);
@@ -648,9 +643,9 @@ __device__ __forceinline__ void flush_counters(WalkCounters wc, unsigned long lo
     atomicAdd(&counters[3], wc.passes);
     atomicAdd(&counters[4], wc.packed);
     atomicAdd(&counters[5], wc.skipped);
-    atomicAdd(&counters[6], wc.refined);
-    atomicAdd(&counters[7], wc.substeps);
-    atomicAdd(&counters[8], wc.refch);
+    atomicAdd(&counters[6], (unsigned long long)SW.rstat[0]);
+    atomicAdd(&counters[7], (unsigned long long)SW.rstat[1]);
+    atomicAdd(&counters[8], (unsigned long long)SW.rstat[2]);
   }
 }
 
