@@ -207,18 +207,16 @@ __global__ void __launch_bounds__(128, WalkMinBlocks<T>::value) k_walk(WalkParam
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
   WarpSmem<T, C> W(smem_raw, nw, wib, kItemLines * P.nfr, P.list);
-  WalkCounters wc;
-  if (lane == 0) { W.SW->rstat[0] = 0; W.SW->rstat[1] = 0; W.SW->rstat[2] = 0; }
-  __syncwarp();
+  unsigned long long steps = 0;   // this lane's formal-solution steps
+  zero_counters(*W.SW, lane);
   for (;;) {
     int item = 0;
     if (lane == 0) item = atomicAdd(P.work, 1);
     item = __shfl_sync(0xffffffffu, item, 0);
     if (item >= P.nitems) break;
-    walk_item<T, C>(P, item, *W.S, *W.SS, *W.SW, W.list, lane, wc);
+    walk_item<T, C>(P, item, *W.S, *W.SS, *W.SW, W.list, lane, steps);
   }
-  __syncwarp();
-  flush_counters(wc, *W.SW, P.counters, lane);
+  flush_counters(steps, *W.SW, P.counters, lane);
 }
 
 // Walk of many jobs (model, camera, line range) from one device queue: queue entry i
@@ -231,9 +229,8 @@ __global__ void __launch_bounds__(128, WalkMinBlocks<T>::value) k_walk_jobs(Walk
   __shared__ WalkParams<T> jp[4];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
   WarpSmem<T, C> W(smem_raw, nw, wib, kItemLines * B.max_nfr, B.list);
-  WalkCounters wc;
-  if (lane == 0) { W.SW->rstat[0] = 0; W.SW->rstat[1] = 0; W.SW->rstat[2] = 0; }
-  __syncwarp();
+  unsigned long long steps = 0;   // this lane's formal-solution steps
+  zero_counters(*W.SW, lane);
   int cur = -1;
   const int nq = (B.total + B.stride - 1) / B.stride;
   for (;;) {
@@ -251,10 +248,9 @@ __global__ void __launch_bounds__(128, WalkMinBlocks<T>::value) k_walk_jobs(Walk
       __syncwarp();
       cur = j;
     }
-    walk_item<T, C>(jp[wib], item - __ldg(&B.item_prefix[j]), *W.S, *W.SS, *W.SW, W.list, lane, wc);
+    walk_item<T, C>(jp[wib], item - __ldg(&B.item_prefix[j]), *W.S, *W.SS, *W.SW, W.list, lane, steps);
   }
-  __syncwarp();
-  flush_counters(wc, *W.SW, B.counters, lane);
+  flush_counters(steps, *W.SW, B.counters, lane);
 }
 
 // ------------------------------------------------------------------------------------

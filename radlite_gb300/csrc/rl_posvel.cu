@@ -32,18 +32,16 @@ __global__ void __launch_bounds__(128, WalkMinBlocks<T>::value) k_walk_pv(WalkPa
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
   WarpSmem<T, C> W(smem_raw, nw, wib, kItemLines * P.nfr, P.list);
-  WalkCounters wc;
-  if (lane == 0) { W.SW->rstat[0] = 0; W.SW->rstat[1] = 0; W.SW->rstat[2] = 0; }
-  __syncwarp();
+  unsigned long long steps = 0;   // this lane's formal-solution steps
+  zero_counters(*W.SW, lane);
   for (;;) {
     int item = 0;
     if (lane == 0) item = atomicAdd(P.work, 1);
     item = __shfl_sync(0xffffffffu, item, 0);
     if (item >= P.nitems) break;
-    walk_item<T, C, true>(P, item, *W.S, *W.SS, *W.SW, W.list, lane, wc);
+    walk_item<T, C, true>(P, item, *W.S, *W.SS, *W.SW, W.list, lane, steps);
   }
-  __syncwarp();
-  flush_counters(wc, *W.SW, P.counters, lane);
+  flush_counters(steps, *W.SW, P.counters, lane);
 }
 
 struct CubeParams {

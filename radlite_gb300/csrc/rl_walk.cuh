@@ -48,7 +48,13 @@ __device__ __forceinline__ SegGeom<T> seg_geom(T ds, T dvs, T rlw, T kq) {
   return g;
 }
 
-struct WalkCounters { unsigned long long steps = 0, integ = 0, nodes = 0, passes = 0, packed = 0, skipped = 0; };
+// zero a warp's launch totals (SubWork::ctr, rstat) before its first item
+template <typename T>
+__device__ __forceinline__ void zero_counters(SubWork<T>& SW, int lane) {
+  if (lane < 5) SW.ctr[lane] = 0;
+  if (lane < 3) SW.rstat[lane] = 0;
+  __syncwarp();
+}
 
 // Formal solution of the (line, channel) pairs list[0..nt) of lines l0.. of one ray.
 // The per-line tables carry the profile normalisation 0.56419583546/(3.33567e-6 nu0), so
@@ -62,7 +68,7 @@ struct WalkCounters { unsigned long long steps = 0, integ = 0, nodes = 0, passes
 template <typename T, int C, bool PV = false>
 __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<T, C>& SS, SubWork<T>& SW, int ray,
                               int K, int l0, int gl, const unsigned short* list, int nt, int lane, int lbase,
-                              WalkCounters& wc) {
+                              unsigned long long& steps_total) {
   // FP32 circular image: steps whose two nodes have positive opacity in every line of the
   // tile, with no state reset and no SUBGRID refinement, run packed (two slots per
   // instruction) without the source-function fallbacks of qdr_src_2, which are the
@@ -437,16 +443,20 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
     if (lane == 0)
       for (; mbits; mbits &= mbits - 1) atomicExch(&P.maser[l0 + __ffs(mbits) - 1], 1);
   }
-  wc.passes += passes;
-  wc.packed += kFast ? passes - general - emptyp : 0u;
-  wc.skipped += skipped;
+  if (lane == 0) {
+    SW.ctr[2] += passes;
+    SW.ctr[3] += kFast ? passes - general - emptyp : 0u;
+    SW.ctr[4] += skipped;
+  }
+  steps_total += steps;
   return steps;
 }
 
 // One work item: line group g of ray `ray`, item = g * nrays + ray.
 template <typename T, int C, bool PV = false>
 __device__ __forceinline__ void walk_item(const WalkParams<T>& P, int item, WarpStage<T>& S, SlotState<T, C>& SS,
-                                          SubWork<T>& SW, unsigned short* list, int lane, WalkCounters& wc) {
+                                          SubWork<T>& SW, unsigned short* list, int lane,
+                                          unsigned long long& steps) {
   const NodeBuf<T>& nb = P.nb;
   const int nl = P.nlines;
   const int g = item / nb.nrays, ray = item - g * nb.nrays;
@@ -531,7 +541,7 @@ __device__ __forceinline__ void walk_item(const WalkParams<T>& P, int item, Warp
     const int te = min(tb + 32 * C, S.lineoff[lcap]);
     const int nt = te - tb;
     const int lz = (int)(list[te - 1] >> kChBits);
-    wc.steps += walk_ray<T, C, PV>(P, S, SS, SW, ray, K, l0 + la, lz - la + 1, list + tb, nt, lane, la, wc);
+    walk_ray<T, C, PV>(P, S, SS, SW, ray, K, l0 + la, lz - la + 1, list + tb, nt, lane, la, steps);
     for (int j = 0; j < C; j++) {
       const int idx = j * 32 + lane;
       if (idx < nt) {
@@ -545,8 +555,7 @@ __device__ __forceinline__ void walk_item(const WalkParams<T>& P, int item, Warp
     __syncwarp();
     tb = te;
   }
-  wc.integ += nint;
-  wc.nodes += (unsigned long long)nint * K;
+  if (lane == 0) { SW.ctr[0] += nint; SW.ctr[1] += (unsigned long long)nint * K; }
   __syncwarp();
   // 4. continuum copy for the other channels of each line
   for (int l = 0; l < gl; l++) {
@@ -577,14 +586,13 @@ __device__ __forceinline__ void walk_item(const WalkParams<T>& P, int item, Warp
     __syncwarp();
     for (int tb = 0; tb < n2; tb += 32 * C) {
       const int nt = min(32 * C, n2 - tb);
-      wc.steps += walk_ray<T, C>(P, S, SS, SW, ray, K, l0 + l, 1, list + tb, nt, lane, l, wc);
+      walk_ray<T, C>(P, S, SS, SW, ray, K, l0 + l, 1, list + tb, nt, lane, l, steps);
       for (int j = 0; j < C; j++) {
         const int idx = j * 32 + lane;
         if (idx < nt) img[list[tb + idx] & (kMaxChannels - 1)] = SS.I[j][lane];
       }
     }
-    wc.integ += n2;
-    wc.nodes += (unsigned long long)n2 * K;
+    if (lane == 0) { SW.ctr[0] += n2; SW.ctr[1] += (unsigned long long)n2 * K; }
     __syncwarp();
     if (lane == 0) {
       T cur = 0;
@@ -632,17 +640,15 @@ struct WarpSmem {
 // no arithmetic), [6] node passes with SUBGRID refinement, [7] the sub-steps of the refined
 // channels, [8] the refined channels of those passes. The buffers hold kWalkCounters values.
 template <typename T>
-__device__ __forceinline__ void flush_counters(WalkCounters wc, const SubWork<T>& SW, unsigned long long* counters,
-                                               int lane) {
+__device__ __forceinline__ void flush_counters(unsigned long long steps, const SubWork<T>& SW,
+                                               unsigned long long* counters, int lane) {
+  __syncwarp();
 #pragma unroll
-  for (int off = 16; off > 0; off >>= 1) wc.steps += __shfl_xor_sync(0xffffffffu, wc.steps, off);   // per lane
+  for (int off = 16; off > 0; off >>= 1) steps += __shfl_xor_sync(0xffffffffu, steps, off);   // per lane
   if (lane == 0) {
-    atomicAdd(&counters[0], wc.steps);
-    atomicAdd(&counters[1], wc.integ);
-    atomicAdd(&counters[2], wc.nodes);
-    atomicAdd(&counters[3], wc.passes);
-    atomicAdd(&counters[4], wc.packed);
-    atomicAdd(&counters[5], wc.skipped);
+    atomicAdd(&counters[0], steps);
+#pragma unroll
+    for (int i = 0; i < 5; i++) atomicAdd(&counters[1 + i], SW.ctr[i]);
     atomicAdd(&counters[6], (unsigned long long)SW.rstat[0]);
     atomicAdd(&counters[7], (unsigned long long)SW.rstat[1]);
     atomicAdd(&counters[8], (unsigned long long)SW.rstat[2]);

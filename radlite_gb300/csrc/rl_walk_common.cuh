@@ -211,7 +211,11 @@ template <typename T>
 struct SubWork {
   T I[128], j0[128], a0[128], S0[128], w[128];
   unsigned char l[128];
-  unsigned rstat[3];   // refined passes, their sub-steps, their refined channels (a warp's totals of a launch)
+  // a warp's totals of a launch, kept here rather than in registers: integrated pairs, node
+  // visits, node passes, packed passes, steps of empty segments; refined passes, their
+  // sub-steps, their refined channels
+  unsigned long long ctr[5];
+  unsigned rstat[3];
 };
 
 // Per-lane state of the walk slots between chunks and slot pairs.
