@@ -691,7 +691,8 @@ def recovery_case(ctx, n_models=8, steps=200, nphi=8, dbdr=1):
 def profile_case(args):
     """One pass of a named workload (geometry, walk, reduction), for profiler captures.
     "posvel_disk": the 200x100 disk's 128x128-pixel position-velocity cube of 2 lines;
-    "genspec_band": gen_spec of 500 lines x 201 channels."""
+    "genspec_band": gen_spec of 500 lines x 201 channels; "adjoint_grad": forward and
+    backward of the differentiable 200x100 disk, both adjoint modes."""
     import numpy as np
     import radlite_gb300 as rl
     from radlite_gb300 import synth
@@ -718,6 +719,28 @@ def profile_case(args):
         print(json.dumps({"workload": args.workload, "steps": st["steps"], "walk_ms": st["walk_ms"],
                           "geometry_ms": st["geometry_ms"], "nrays": st["nrays"], "ray_channels": st["ray_channels"]}),
               flush=True)
+        m.free()
+        ctx.close()
+        return 0
+    if args.workload == "adjoint_grad":
+        # one differentiable forward and one backward of the 200x100 disk per adjoint mode:
+        # the gradient sweep (checkpoint interval 0), then the reverse sweep (interval 1)
+        import torch
+        cfg = synth.config_by_name("adjoint_disk", **({"nphi": args.nphi} if args.nphi else {}))
+        ctx = rl.Context(0)
+        m = ctx.load_arrays(synth.lte_arrays(cfg), camera(cfg, cfg.incl_deg))
+        lnT, lnX, b = (torch.tensor(a, dtype=torch.float64, device="cuda") for a in synth.cell_params(cfg))
+        d = rl.Diff(m, cfg.ilinestart, cfg.nlines, precision=0)
+        target = d.forward(lnT + 0.05, lnX, b)
+        flux, fst = d.forward(lnT, lnX, b, stats=True)
+        gflux = 2.0 * (flux - target) / target.abs().max() ** 2
+        out = {"workload": args.workload, "nrays": d.nrays, "forward_ms": fst["total_ms"]}
+        for every in (0, 1):
+            d.set_checkpoint(every)
+            _, st = d.backward(gflux, stats=True)
+            out[f"interval_{every}"] = {k: st[k] for k in ("total_ms", "steps", "refined_passes", "refined_channels")}
+        print(json.dumps(out), flush=True)
+        d.close()
         m.free()
         ctx.close()
         return 0
