@@ -737,6 +737,7 @@ def profile_case(args):
         out = {"workload": args.workload, "nrays": d.nrays, "forward_ms": fst["total_ms"]}
         for every in (0, 1):
             d.set_checkpoint(every)
+            d.forward(lnT, lnX, b)      # each adjoint mode differentiates a forward of its own
             _, st = d.backward(gflux, stats=True)
             out[f"interval_{every}"] = {k: st[k] for k in ("total_ms", "steps", "refined_passes", "refined_channels")}
         print(json.dumps(out), flush=True)

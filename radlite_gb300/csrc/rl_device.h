@@ -97,8 +97,10 @@ struct WalkParams {
   T kq;                      // 3.33567e-6 * 2.99792458e5
   T fstar;                   // (R*/ri(1))^2 for the central beam
   T* img;                    // [nlines][nrays][nfr]
-  T* tau = nullptr;          // position-velocity walk only: [nlines][nrays][nfr] char_tau
-  T* tauc = nullptr;         //   and its compensation term (same layout)
+  T* tau = nullptr;          // [nlines][nrays][nfr] optical depth of each walked channel along the
+  T* tauc = nullptr;         //   ray (char_tau) and its compensation term: the position-velocity
+                             //   walk, and the walk of the differentiable forward (for the
+                             //   gradient sweep); null otherwise
   unsigned char* mask = nullptr;  // optional [nlines][nrays][nfr]: 1 = channel 1 or inside the window
   int* maser = nullptr;      // optional [nlines]: set to 1 where a step's line opacity x segment
                              //   length falls below -0.01 (only launches with an inverted line)
@@ -132,6 +134,7 @@ struct WalkJobs {
   int* work;                  // queue counter
   unsigned long long* counters;
   unsigned short* list;       // per-warp list rows, as WalkParams::list with max_nfr
+  bool tau = false;           // the jobs' walks also keep each channel's optical depth
 };
 
 template <typename T>

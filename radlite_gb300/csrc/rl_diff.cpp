@@ -58,6 +58,7 @@ struct rl_diff {
   // tables of the last forward
   DevBuf tab, nsum, dtab, width;
   DevBuf img, ring, flux, cnt, work, err, list;
+  DevBuf tau, tauc;   // the gradient sweep: each walked channel's optical depth from the forward
   // adjoint
   DevBuf ckpt, ajob, aprefix, acnt, awork;
   DevBuf g4;   // FP32 adjoint: interleaved gradient accumulator [ncell]
@@ -100,7 +101,19 @@ WalkParams<T> walk_params(const rl_diff* d) {
   P.work = d->work.as<int>();
   P.err = d->err.as<int>();
   P.list = d->list.as<unsigned short>();
+  if (d->every == 0) { P.tau = d->tau.as<T>(); P.tauc = d->tauc.as<T>(); }
   return P;
+}
+
+// The gradient sweep takes each channel's optical depth along the ray from the forward
+// walk: image-shaped buffers, allocated when that adjoint mode is in use.
+template <typename T>
+cudaError_t ensure_tau(rl_diff* d, bool need) {
+  if (!need) return cudaSuccess;
+  const size_t n = (size_t)d->nl * d->cam.nrays * d->nfr;
+  cudaError_t e = d->tau.ensure(sizeof(T) * n);
+  if (e == cudaSuccess) e = d->tauc.ensure(sizeof(T) * n);
+  return e;
 }
 
 template <typename T>
@@ -280,6 +293,7 @@ int forward(rl_diff* d, const double* lnT, const double* lnX, const double* widt
   CUDA_TRY(cudaMemsetAsync(d->work.p, 0, sizeof(int), s));
   CUDA_TRY(cudaMemsetAsync(d->err.p, 0, sizeof(int), s));
   CUDA_TRY(cudaEventRecord(ctx->ev[1], s));
+  CUDA_TRY(ensure_tau<T>(d, d->every == 0));
   const WalkParams<T> P = walk_params<T>(d);
   CUDA_TRY(launch_walk<T>(P, d->cpl, ctx->nsm, s));
   CUDA_TRY(cudaEventRecord(ctx->ev[2], s));
@@ -448,8 +462,11 @@ int batch_build(rl_diff_batch* b) {
   std::vector<AdjParams<T>> adj(nj);
   std::vector<int> itemp(nj + 1, 0), ringp(nj + 1, 0), linep(nj + 1, 0), adjp(nj + 1, 0);
   for (int j = 0; j < nj; j++) {
-    const rl_diff* d = b->jobs[j];
+    rl_diff* d = b->jobs[j];
+    CUDA_TRY(ensure_tau<T>(d, b->every == 0));   // the batch's adjoint mode, whatever the model's own
     WalkParams<T> w = walk_params<T>(d);
+    w.tau = b->every == 0 ? d->tau.as<T>() : nullptr;
+    w.tauc = b->every == 0 ? d->tauc.as<T>() : nullptr;
     w.counters = b->cnt.as<unsigned long long>();
     w.work = b->work.as<int>();
     w.err = b->err.as<int>();
@@ -499,6 +516,7 @@ int batch_build(rl_diff_batch* b) {
   L.walk.njobs = nj; L.walk.total = itemp[nj]; L.walk.stride = 1; L.walk.max_nfr = b->max_nfr;
   L.walk.work = b->work.as<int>(); L.walk.counters = b->cnt.as<unsigned long long>();
   L.walk.list = b->list.as<unsigned short>();
+  L.walk.tau = b->every == 0;
   L.reduce = true;
   L.red = b->redjobs.as<RedJob<T>>(); L.ring_prefix = b->ring_prefix.as<int>(); L.line_prefix = b->line_prefix.as<int>();
   L.nring_blocks = ringp[nj]; L.nline_blocks = linep[nj];
@@ -721,6 +739,7 @@ int rl_diff_set_checkpoint(rl_diff* d, int every) {
     return set_err(ctx, RL_ERR_ARG, "rl_diff_set_checkpoint: 0 (gradient sweep), 1 or 32");
   CUDA_TRY(rl::enter_device(ctx->device));
   d->every = every;
+  d->have_forward = false;   // the forward of the other mode does not keep what this one needs
   const bool f64 = d->precision == RL_FP64;
   CUDA_TRY(f64 ? adjoint_grid<double>(ctx->nsm, d->nfr, every, &d->adj_blocks)
                : adjoint_grid<float>(ctx->nsm, d->nfr, every, &d->adj_blocks));

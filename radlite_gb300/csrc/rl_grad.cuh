@@ -4,10 +4,13 @@
 // lam_{k-1} = lam_k x_k, and x_k = e^{-dtau_k}: the multiplier of every step is the
 // seed times e^{-D_k}, with D_k the optical depth that the ray still crosses after step k
 // (line.F:4598's char_tau counted from the observer's end). So the gradient needs no
-// reverse walk: a first sweep along the ray sums the optical depth of every step and
-// sub-step (compensated, so that differences of two partial sums keep their digits), a
-// second sweep walks the ray again, recomputes each step forward and takes its gradient
-// at once with lam_k = seed e^{-(T_N - T_k)}. No intensities are stored.
+// reverse walk: the forward walk sums each channel's optical depth along the ray
+// (compensated, so that differences of two partial sums keep their digits; the walk's TAU
+// instances), and this sweep walks the ray again, recomputes each step and takes its
+// gradient at once with lam_k = seed e^{-(T_N - T_k)}, T_k summed alike as it goes. No
+// intensities are stored. (T_k rounds a little differently from the walk's sum where the
+// walk adds a refined segment's sub-steps before compensating: D_k is then off by a few
+// units in the last place of that segment's optical depth.)
 //
 // Work layout: one warp per (ray, group of up to kGG lines). The integrated (line,
 // channel) pairs of the group are dealt to the lanes so that every lane holds up to kGS
@@ -26,7 +29,7 @@ namespace rl {
 constexpr int kGS = 2;        // channel slots per lane (one line per lane)
 constexpr int kGG = kGroup;   // lines per gradient work item
 
-// explicitly rounded arithmetic: the two sweeps must form every optical depth alike
+// explicitly rounded arithmetic, as the walk rounds each operation of a step
 __device__ __forceinline__ float mulr(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ double mulr(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ float addr(float a, float b) { return __fadd_rn(a, b); }
@@ -365,32 +368,7 @@ __device__ __forceinline__ GRes<T> gseg_refined(int kind, bool init, T w, LineVa
   return r;
 }
 
-// The optical depth of the same segment (first sweep): every step and sub-step of
-// gseg_refined, formed alike. Returns the opacity of the end point.
-template <typename T>
-__device__ __noinline__ T gseg_tau(int kind, bool init, T w, LineVals<T> v0, LineVals<T> v1, T vl0, T vl1, T rl, T hds,
-                                   T dsf, T dvs, GSeg<T> G, T a0, T& s, T& c) {
-  T E;
-  if (init) a0 = gpt_a(v0, w, vl0, rl, E);
-  const GGrid<T> gr = ggrid<T>(kind, w, vl0, dsf, dvs, G);
-  T sp = 0;
-  for (int i = gr.ia; i <= gr.ib + 1; i++) {
-    T sv = dsf, pvl = vl1;
-    LineVals<T> v = v1;
-    if (i <= gr.ib) {
-      sv = gpos(gr, i);
-      glerp(v0, v1, vl0, vl1, mulr(sv, G.ids), v, pvl);
-    }
-    const T a1 = gpt_a(v, w, pvl, rl, E);
-    const T h = gr.halves ? mulr((T)0.5, subr(sv, sp)) : hds;
-    kadd(s, c, mulr(addr(a0, a1), h));
-    a0 = a1;
-    sp = sv;
-  }
-  return a0;
-}
-
-// One regular step of one slot in the second sweep: the step of the walk from the carried
+// One regular step of one slot in the sweep: the step of the walk from the carried
 // point to the node point, its gradient with the multiplier lamf e^{-D} (D the optical
 // depth still ahead), the carried point completed (contributions to node g-1 and to the
 // width of the segment ending there), and the node point carried on.
@@ -416,7 +394,7 @@ __device__ __forceinline__ void gstep_regular(GState<T>& st, const LineVals<T>& 
 
 // FP32: the regular steps of a lane's two slots as packed pairs (both slots belong to one
 // line, so the node values are shared operands). Every element is rounded as in
-// gstep_regular: the optical depths equal the first sweep's. Slots that refine (skip) keep
+// gstep_regular, so the optical depths equal the forward walk's. Slots that refine (skip) keep
 // their state and contribute nothing here.
 __device__ __forceinline__ float2 sel2(bool a, bool b, float2 t, float2 f) {
   return make_float2(a ? t.x : f.x, b ? t.y : f.y);
@@ -768,78 +746,16 @@ __device__ void grad_item(const AdjParams<T>& A, int item, GradStage<T>& S, Grad
       st[u].I = I0; st[u].j0 = 0; st[u].a0 = 0; st[u].S0 = 0; st[u].ra0 = 0; st[u].E0 = 0;
       st[u].pgj = 0; st[u].pga = 0; st[u].s = 0; st[u].c = 0;
     }
-    // 3a. first sweep: the optical depth of the whole ray per slot
-    for (int cix = 0; cix < nchunk; cix++) {
-      const int kb = cix * 32;
-      grad_stage(P, S, row, kb, K, l0 + tl0, tgl, star_node, lane);
-      const int nn = min(32, K - kb);
-      const int n0 = kb == 0 ? 1 : 0;
-      for (int n = n0; n < nn; n++) {
-        const unsigned fl = S.flags[n + 1];
-        const T vl0 = S.vl[n], vl1 = S.vl[n + 1], rl = S.rlw[n + 1], hds = S.hds[n + 1];
-        const T dsf = S.ds[n + 1], dvs = S.dvs[n + 1];
-        const LineVals<T> v0 = S.lv[lsafe][n], v1 = S.lv[lsafe][n + 1];
-        const bool init = (fl & kFlagInit) != 0, sub = (fl & kFlagSub) != 0;
-        GSeg<T> G = {};
-        if (init || sub) G = stage_seg(S, n + 1);
-        bool need[kGS];
-#pragma unroll
-        for (int u = 0; u < kGS; u++) {
-          bool ov = false;
-          if (!init && sub) {
-            const T sc = gsc(w[u], vl0, dsf, dvs, G);
-            ov = ch[u] >= 0 && addr(sc, G.hw3) > (T)0 && subr(sc, G.hw3) < dsf;
-          }
-          // (the second sweep leaves empty slots alone at resetting nodes: so does this one)
-          need[u] = ch[u] >= 0 && (init || ov);
-          if (!init && !ov) {
-            T E;
-            const T a1 = gpt_a(v1, w[u], vl1, rl, E);
-            kadd(st[u].s, st[u].c, mulr(addr(st[u].a0, a1), hds));
-            st[u].a0 = a1;
-          }
-        }
-        // refined and resetting segments, compacted over the warp as in the second sweep
-        int pos[kGS], cnt = 0;
-#pragma unroll
-        for (int u = 0; u < kGS; u++) {
-          const unsigned mk = __ballot_sync(0xffffffffu, need[u]);
-          pos[u] = cnt + __popc(mk & lanemask_lt());
-          cnt += __popc(mk);
-        }
-        for (int r0 = 0; r0 < cnt; r0 += 32) {
-#pragma unroll
-          for (int u = 0; u < kGS; u++) {
-            const int q = pos[u] - r0;
-            if (need[u] && q >= 0 && q < 32) {
-              W.k[0][q] = w[u]; W.st[2][q] = st[u].a0; W.st[8][q] = st[u].s; W.st[9][q] = st[u].c; W.line[q] = lsafe;
-            }
-          }
-          __syncwarp();
-          if (lane < cnt - r0) {
-            const int lq = W.line[lane];
-            T sq = W.st[8][lane], cq = W.st[9][lane];
-            W.st[2][lane] = gseg_tau<T>(init ? (sub ? 2 : 0) : 1, init, W.k[0][lane], S.lv[lq][n], S.lv[lq][n + 1], vl0,
-                                        vl1, rl, hds, dsf, dvs, G, W.st[2][lane], sq, cq);
-            W.st[8][lane] = sq; W.st[9][lane] = cq;
-          }
-          __syncwarp();
-#pragma unroll
-          for (int u = 0; u < kGS; u++) {
-            const int q = pos[u] - r0;
-            if (need[u] && q >= 0 && q < 32) { st[u].a0 = W.st[2][q]; st[u].s = W.st[8][q]; st[u].c = W.st[9][q]; }
-          }
-          __syncwarp();
-        }
-      }
-      __syncwarp();
-    }
+    // 3a. the optical depth of the whole ray per slot, as the forward walk summed it
 #pragma unroll
     for (int u = 0; u < kGS; u++) {
-      sN[u] = st[u].s; cN[u] = st[u].c;
-      st[u].a0 = 0; st[u].s = 0; st[u].c = 0;
+      sN[u] = 0; cN[u] = 0;
+      if (ch[u] >= 0) {
+        const size_t a = ((size_t)(l0 + li) * nrays + ray) * P.nfr + ch[u];
+        sN[u] = P.tau[a]; cN[u] = P.tauc[a];
+      }
     }
-    // 3b. second sweep: forward and gradient
+    // 3b. the sweep: forward and gradient
     T keep = keep0;                // multiplier factor of the steps before the star node
     T carry[4] = {0, 0, 0, 0};     // this lane's contributions to the next node (jd, jf, af) and segment
     T hP[3] = {0, 0, 0}, hglw = 0; // head lane: the node awaiting its scatter

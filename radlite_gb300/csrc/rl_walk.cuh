@@ -65,7 +65,9 @@ __device__ __forceinline__ void zero_counters(SubWork<T>& SW, int lane) {
 // image position), and no star mixing.
 // The list entries carry item line indices; lbase is the item line of l0 (the tile's first
 // line), so that entry line - lbase indexes the tile's staged lines 0..gl-1.
-template <typename T, int C, bool PV = false>
+// TAU (circular image): the slots' optical depth is kept as in the position-velocity walk
+// (for the gradient sweep of the differentiable path); nothing else changes.
+template <typename T, int C, bool PV = false, bool TAU = false>
 __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<T, C>& SS, SubWork<T>& SW, int ray,
                               int K, int l0, int gl, const unsigned short* list, int nt, int lane, int lbase,
                               unsigned long long& steps_total) {
@@ -75,6 +77,7 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
   // identity there. All other steps, and the FP64 and position-velocity walks, take the
   // general path.
   constexpr bool kFast = sizeof(T) == 4 && !PV;
+  constexpr bool kTau = PV || TAU;
   const NodeBuf<T>& nb = P.nb;
   const size_t row = (size_t)ray * nb.kmax;
   const int nl = P.nlines;
@@ -89,7 +92,7 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
       L = (int)(e >> kChBits) - lbase;
       w = P.wch[(size_t)(l0 + L) * P.nfr + (e & (kMaxChannels - 1))];
       I = P.isrf ? P.isrf[(size_t)(l0 + L) * P.nfr + (e & (kMaxChannels - 1))] : P.lc[l0 + L].istart;
-      if constexpr (PV) {
+      if constexpr (kTau) {
         const size_t a = ((size_t)(l0 + L) * nb.nrays + ray) * P.nfr + (e & (kMaxChannels - 1));
         P.tau[a] = 0; P.tauc[a] = 0;
       }
@@ -199,7 +202,7 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
       }
       T tau[kPass], tcp[kPass];
       size_t ta[kPass];
-      if constexpr (PV) {
+      if constexpr (kTau) {
 #pragma unroll
         for (int u = 0; u < kPass; u++) {
           tau[u] = 0; tcp[u] = 0; ta[u] = 0;
@@ -286,6 +289,10 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
               const float2 q = make_float2(fminf(Qb.x, th[p].x), fminf(Qb.y, th[p].y));
               const float2 In = fma2(make_float2(I[2 * p], I[2 * p + 1]), x[p], q);
               I[2 * p] = In.x; I[2 * p + 1] = In.y;
+              if constexpr (TAU) {
+                kahan_add(tau[2 * p], tcp[2 * p], dt[p].x);
+                kahan_add(tau[2 * p + 1], tcp[2 * p + 1], dt[p].y);
+              }
               j0[2 * p] = j1[p].x; j0[2 * p + 1] = j1[p].y;
               a0[2 * p] = a1[p].x; a0[2 * p + 1] = a1[p].y;
               S0[2 * p] = S1[p].x; S0[2 * p + 1] = S1[p].y;
@@ -359,7 +366,7 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
             if (!ov[u]) {
               I[u] = fmadd(I[u], x[u], qv);
               j0[u] = j1[u]; a0[u] = a1[u]; S0[u] = S1[u];
-              if constexpr (PV) kahan_add(tau[u], tcp[u], dt[u]);
+              if constexpr (kTau) kahan_add(tau[u], tcp[u], dt[u]);
             }
           }
           if (any) {
@@ -383,10 +390,10 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
               const T wp = SW.w[p];
               const int lp = SW.l[p];
               const T s_c = sizeof(T) == 8 ? dsf * (wp - vl0) / dvsg : dsf * (wp - vl0) * G.idvs;
-              const SlotOutT<T, PV> o = slot_sub<T, PV>(wp, S.lv[lp][n], S.lv[lp][n + 1], vl0, vl1, rl, dsf, G.ids,
+              const SlotOutT<T, kTau> o = slot_sub<T, kTau>(wp, S.lv[lp][n], S.lv[lp][n + 1], vl0, vl1, rl, dsf, G.ids,
                                                         s_c - G.hw3, G.lg, G.ilg, SW.I[p], SW.j0[p], SW.a0[p], SW.S0[p]);
               SW.I[p] = o.I; SW.j0[p] = o.j0; SW.a0[p] = o.a0; SW.S0[p] = o.S0;
-              if constexpr (PV) SW.w[p] = o.dtau;   // the owner keeps w in a register
+              if constexpr (kTau) SW.w[p] = o.dtau;   // the owner keeps w in a register
               steps += o.steps - 1;
               mysub += o.steps;
             }
@@ -398,7 +405,7 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
             for (int u = 0; u < kPass; u++) {
               if (ov[u]) {
                 I[u] = SW.I[pos[u]]; j0[u] = SW.j0[pos[u]]; a0[u] = SW.a0[pos[u]]; S0[u] = SW.S0[pos[u]];
-                if constexpr (PV) kahan_add(tau[u], tcp[u], SW.w[pos[u]]);
+                if constexpr (kTau) kahan_add(tau[u], tcp[u], SW.w[pos[u]]);
               }
             }
             __syncwarp();
@@ -410,10 +417,10 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
 #pragma unroll
           for (int u = 0; u < kPass; u++) {
             if (Ls[u] < 0) continue;
-            const SlotOutT<T, PV> o = slot_slow<T, PV>(init, sub, w[u], S.lv[Ls[u]][n], S.lv[Ls[u]][n + 1], vl0, vl1,
+            const SlotOutT<T, kTau> o = slot_slow<T, kTau>(init, sub, w[u], S.lv[Ls[u]][n], S.lv[Ls[u]][n + 1], vl0, vl1,
                                                        rl, hds, G.q, dsf, dvs, G.ids, I[u], j0[u], a0[u], S0[u]);
             I[u] = o.I; j0[u] = o.j0; a0[u] = o.a0; S0[u] = o.S0; steps += o.steps - 1;
-            if constexpr (PV) kahan_add(tau[u], tcp[u], o.dtau);
+            if constexpr (kTau) kahan_add(tau[u], tcp[u], o.dtau);
           }
         }
         if (P.maser) {
@@ -431,7 +438,7 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
       for (int u = 0; u < kPass; u++) {
         const int j = kPass * pq + u;
         if (j < C) { SS.I[j][lane] = I[u]; SS.j0[j][lane] = j0[u]; SS.a0[j][lane] = a0[u]; SS.S0[j][lane] = S0[u]; }
-        if constexpr (PV) {
+        if constexpr (kTau) {
           if (Ls[u] >= 0) { P.tau[ta[u]] = tau[u]; P.tauc[ta[u]] = tcp[u]; }
         }
       }
@@ -453,7 +460,7 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
 }
 
 // One work item: line group g of ray `ray`, item = g * nrays + ray.
-template <typename T, int C, bool PV = false>
+template <typename T, int C, bool PV = false, bool TAU = false>
 __device__ __forceinline__ void walk_item(const WalkParams<T>& P, int item, WarpStage<T>& S, SlotState<T, C>& SS,
                                           SubWork<T>& SW, unsigned short* list, int lane,
                                           unsigned long long& steps) {
@@ -541,7 +548,7 @@ __device__ __forceinline__ void walk_item(const WalkParams<T>& P, int item, Warp
     const int te = min(tb + 32 * C, S.lineoff[lcap]);
     const int nt = te - tb;
     const int lz = (int)(list[te - 1] >> kChBits);
-    walk_ray<T, C, PV>(P, S, SS, SW, ray, K, l0 + la, lz - la + 1, list + tb, nt, lane, la, steps);
+    walk_ray<T, C, PV, TAU>(P, S, SS, SW, ray, K, l0 + la, lz - la + 1, list + tb, nt, lane, la, steps);
     for (int j = 0; j < C; j++) {
       const int idx = j * 32 + lane;
       if (idx < nt) {
