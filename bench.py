@@ -631,17 +631,23 @@ def adjoint_case(ctx, name="adjoint_disk", reps=3, **over):
                        "gradients w.r.t. per-cell ln T, ln X, width",
            "forward_ms": statistics.median(fw[1:]), "adjoint_ms": statistics.median(bw[1:]),
            "spectra": cfg.nlines}
-    # the reverse sweep over stored intensities (checkpoint interval 1) on the same forward
+    # the reverse sweep over stored intensities (checkpoint interval 1), whose forward is the
+    # plain walk (the gradient sweep's forward also keeps each channel's optical depth)
     d.set_checkpoint(1)
-    flux = d.forward(lnT, lnX, b)
+    fp = []
+    for _ in range(2):
+        flux, sf = d.forward(lnT, lnX, b, stats=True)
+        fp.append(sf["total_ms"])
     gflux = 2.0 * (flux - target) / target.abs().max() ** 2
     rv = []
     for _ in range(2):
         _, sb = d.backward(gflux, stats=True)
         rv.append(sb["total_ms"])
     d.set_checkpoint(0)
+    res["forward_plain_walk_ms"] = min(fp)
     res["reverse_sweep_ms"] = min(rv)
     res["adjoint_over_forward"] = res["adjoint_ms"] / res["forward_ms"]
+    res["forward_adjoint_over_plain_forward"] = (res["forward_ms"] + res["adjoint_ms"]) / res["forward_plain_walk_ms"]
     res["forward_adjoint_spectra_per_s"] = cfg.nlines / ((res["forward_ms"] + res["adjoint_ms"]) * 1e-3)
     # the same gradient by central differences: two forwards per cell parameter
     npar = 3 * int(lnT.numel())

@@ -200,8 +200,17 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
         lsl[u] = Ls[u] < 0 ? 0 : Ls[u];
         nv += Ls[u] >= 0 ? 1 : 0;
       }
-      T tau[kPass], tcp[kPass];
+      // optical depth: the position-velocity walk adds every step compensated; the TAU walk
+      // sums a pass's steps plainly (part) and adds that sum compensated at the pass end,
+      // so that the loads below are needed only then
+      T tau[kPass], tcp[kPass], part[kPass];
       size_t ta[kPass];
+#pragma unroll
+      for (int u = 0; u < kPass; u++) part[u] = 0;
+      auto add_tau = [&](int u, T x) {
+        if constexpr (PV) kahan_add(tau[u], tcp[u], x);
+        else if constexpr (TAU) part[u] += x;
+      };
       if constexpr (kTau) {
 #pragma unroll
         for (int u = 0; u < kPass; u++) {
@@ -289,10 +298,7 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
               const float2 q = make_float2(fminf(Qb.x, th[p].x), fminf(Qb.y, th[p].y));
               const float2 In = fma2(make_float2(I[2 * p], I[2 * p + 1]), x[p], q);
               I[2 * p] = In.x; I[2 * p + 1] = In.y;
-              if constexpr (TAU) {
-                kahan_add(tau[2 * p], tcp[2 * p], dt[p].x);
-                kahan_add(tau[2 * p + 1], tcp[2 * p + 1], dt[p].y);
-              }
+              if constexpr (TAU) { part[2 * p] += dt[p].x; part[2 * p + 1] += dt[p].y; }
               j0[2 * p] = j1[p].x; j0[2 * p + 1] = j1[p].y;
               a0[2 * p] = a1[p].x; a0[2 * p + 1] = a1[p].y;
               S0[2 * p] = S1[p].x; S0[2 * p + 1] = S1[p].y;
@@ -366,7 +372,7 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
             if (!ov[u]) {
               I[u] = fmadd(I[u], x[u], qv);
               j0[u] = j1[u]; a0[u] = a1[u]; S0[u] = S1[u];
-              if constexpr (kTau) kahan_add(tau[u], tcp[u], dt[u]);
+              if constexpr (kTau) add_tau(u, dt[u]);
             }
           }
           if (any) {
@@ -405,7 +411,7 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
             for (int u = 0; u < kPass; u++) {
               if (ov[u]) {
                 I[u] = SW.I[pos[u]]; j0[u] = SW.j0[pos[u]]; a0[u] = SW.a0[pos[u]]; S0[u] = SW.S0[pos[u]];
-                if constexpr (kTau) kahan_add(tau[u], tcp[u], SW.w[pos[u]]);
+                if constexpr (kTau) add_tau(u, SW.w[pos[u]]);
               }
             }
             __syncwarp();
@@ -420,7 +426,7 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
             const SlotOutT<T, kTau> o = slot_slow<T, kTau>(init, sub, w[u], S.lv[Ls[u]][n], S.lv[Ls[u]][n + 1], vl0, vl1,
                                                        rl, hds, G.q, dsf, dvs, G.ids, I[u], j0[u], a0[u], S0[u]);
             I[u] = o.I; j0[u] = o.j0; a0[u] = o.a0; S0[u] = o.S0; steps += o.steps - 1;
-            if constexpr (kTau) kahan_add(tau[u], tcp[u], o.dtau);
+            if constexpr (kTau) add_tau(u, o.dtau);
           }
         }
         if (P.maser) {
@@ -439,6 +445,7 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
         const int j = kPass * pq + u;
         if (j < C) { SS.I[j][lane] = I[u]; SS.j0[j][lane] = j0[u]; SS.a0[j][lane] = a0[u]; SS.S0[j][lane] = S0[u]; }
         if constexpr (kTau) {
+          if constexpr (!PV) kahan_add(tau[u], tcp[u], part[u]);
           if (Ls[u] >= 0) { P.tau[ta[u]] = tau[u]; P.tauc[ta[u]] = tcp[u]; }
         }
       }
