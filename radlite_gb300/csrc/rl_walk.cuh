@@ -78,6 +78,12 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
   // general path.
   constexpr bool kFast = sizeof(T) == 4 && !PV;
   constexpr bool kTau = PV || TAU;
+  // TAU with one pass per chunk (at most kPass slots per lane): the sums stay in registers
+  // over the whole ray and are stored once at its end
+  constexpr bool kTauReg = TAU && !PV && C <= kPass;
+  T tauR[kPass], tcpR[kPass];
+#pragma unroll
+  for (int u = 0; u < kPass; u++) { tauR[u] = 0; tcpR[u] = 0; }
   const NodeBuf<T>& nb = P.nb;
   const size_t row = (size_t)ray * nb.kmax;
   const int nl = P.nlines;
@@ -92,7 +98,7 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
       L = (int)(e >> kChBits) - lbase;
       w = P.wch[(size_t)(l0 + L) * P.nfr + (e & (kMaxChannels - 1))];
       I = P.isrf ? P.isrf[(size_t)(l0 + L) * P.nfr + (e & (kMaxChannels - 1))] : P.lc[l0 + L].istart;
-      if constexpr (kTau) {
+      if constexpr (kTau && !kTauReg) {
         const size_t a = ((size_t)(l0 + L) * nb.nrays + ray) * P.nfr + (e & (kMaxChannels - 1));
         P.tau[a] = 0; P.tauc[a] = 0;
       }
@@ -211,7 +217,7 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
         if constexpr (PV) kahan_add(tau[u], tcp[u], x);
         else if constexpr (TAU) part[u] += x;
       };
-      if constexpr (kTau) {
+      if constexpr (kTau && !kTauReg) {
 #pragma unroll
         for (int u = 0; u < kPass; u++) {
           tau[u] = 0; tcp[u] = 0; ta[u] = 0;
@@ -444,13 +450,26 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
       for (int u = 0; u < kPass; u++) {
         const int j = kPass * pq + u;
         if (j < C) { SS.I[j][lane] = I[u]; SS.j0[j][lane] = j0[u]; SS.a0[j][lane] = a0[u]; SS.S0[j][lane] = S0[u]; }
-        if constexpr (kTau) {
+        if constexpr (kTauReg) {
+          kahan_add(tauR[u], tcpR[u], part[u]);
+        } else if constexpr (kTau) {
           if constexpr (!PV) kahan_add(tau[u], tcp[u], part[u]);
           if (Ls[u] >= 0) { P.tau[ta[u]] = tau[u]; P.tauc[ta[u]] = tcp[u]; }
         }
       }
     }
     __syncwarp();
+  }
+  if constexpr (kTauReg) {
+#pragma unroll
+    for (int u = 0; u < kPass; u++) {
+      const int idx = u * 32 + lane;
+      if (u < C && idx < nt) {
+        const unsigned e = list[idx];
+        const size_t a = ((size_t)(l0 + (int)(e >> kChBits) - lbase) * nb.nrays + ray) * P.nfr + (e & (kMaxChannels - 1));
+        P.tau[a] = tauR[u]; P.tauc[a] = tcpR[u];
+      }
+    }
   }
   if (P.maser) {
     mbits = __reduce_or_sync(0xffffffffu, mbits);
