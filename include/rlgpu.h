@@ -272,11 +272,12 @@ int rl_diff_create(rl_model* model, int iline0, int nlines, int precision, rl_di
 int rl_diff_destroy(rl_diff* diff);
 int rl_diff_info(rl_diff* diff, int* ncell, int* nlines, int* nfr, int* nrays);
 /* How the backward call walks the rays. 0 (the default): the gradient sweep in walk
-   order, no stored intensities: a first pass sums each channel's optical depth along the
-   ray, a second recomputes every step and takes its gradient with the multiplier
-   e^{-(optical depth still ahead)}. 1 or 32: the reverse sweep, which keeps the intensity
-   entering every node (1: 32 values a node per resident warp, about 0.1-0.4 GB) or every
-   32nd node (the chunk is walked again). All give the same gradient. */
+   order, no stored intensities: the forward also keeps each channel's optical depth along
+   the ray (two image-sized buffers), and the backward recomputes every step and takes its
+   gradient with the multiplier e^{-(optical depth still ahead)}. 1 or 32: the reverse
+   sweep, which keeps the intensity entering every node (1: 32 values a node per resident
+   warp, about 0.1-0.4 GB) or every 32nd node (the chunk is walked again). All give the
+   same gradient. A change of mode needs a new rl_diff_forward before rl_diff_backward. */
 int rl_diff_set_checkpoint(rl_diff* diff, int every);
 /* flux [nlines][nfr]: F_nu at 1 pc for the parameters lnT, lnX, width [ncell]. */
 int rl_diff_forward(rl_diff* diff, const double* lnT, const double* lnX, const double* width, double* flux,

@@ -176,6 +176,21 @@ def test_gradient_sweep_matches_reverse_sweep(gpu_lib, ctx, name, over, prec):
     m.free()
 
 
+@pytest.mark.parametrize("prec", [1, 0])
+def test_forward_keeping_optical_depths_is_the_plain_walk(gpu_lib, ctx, prec):
+    """The forward of the gradient sweep (the walk that also keeps each channel's optical
+    depth) renders exactly what the plain walk renders (the reverse sweep's forward)."""
+    cfg, m, lnT, lnX, b = _setup(gpu_lib, ctx, "adjoint_disk", nphi=4, nlines=3)
+    out = []
+    for every in (0, 1):
+        d = gpu_lib.Diff(m, cfg.ilinestart, cfg.nlines, precision=prec)
+        d.set_checkpoint(every)
+        out.append(d.forward(lnT, lnX, b).cpu().numpy())
+        d.close()
+    assert np.array_equal(out[0], out[1])
+    m.free()
+
+
 def test_autograd_function(gpu_lib, ctx):
     import torch
     cfg, m, lnT, lnX, b = _setup(gpu_lib, ctx)
