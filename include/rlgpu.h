@@ -53,6 +53,11 @@ typedef struct rl_stats {
   unsigned long long sub_steps;      /* steps counted in `steps` that refined channels take
                                         inside such segments */
   unsigned long long refined_channels; /* (channel, segment) pairs refined in those passes */
+  unsigned long long overshoots;     /* steps counted in `steps` whose quadrature before the
+                                        bracket exceeded twice the theoretical maximum
+                                        (transerr_overshoot, transfer.F:1548-1553); counted
+                                        with RL_CHECK_OVERSHOOT set (rl_set_checks), by
+                                        position-velocity cubes and by rl_run_dir; 0 otherwise */
 } rl_stats;
 
 typedef struct rl_model_info {
@@ -120,6 +125,13 @@ int rl_model_get_info(rl_model* model, rl_model_info* info);
 int rl_set_camera(rl_model* model, double incl_deg, int nphi, int dbdr, int nrrayextra);
 /* RL_FP32 (default): FP64 geometry, FP32 transfer. RL_FP64: FP64 throughout. */
 int rl_set_precision(rl_model* model, int precision);
+/* Diagnostics of the model's line renders (spectra, images, image rows), off by default.
+   RL_CHECK_OVERSHOOT: take the reference's overshoot test on every formal-solution step,
+   the check its default build compiles in (transfer.F:1548-1553, not SRCQDR_NO_ERRCHECK),
+   and count the steps that fail it in rl_stats.overshoots. The results are unchanged; the
+   FP32 walk takes about 10% longer (13.1 -> 14.4 ms on a 400x200 band disk of 20 lines). */
+#define RL_CHECK_OVERSHOOT 1
+int rl_set_checks(rl_model* model, int flags);
 
 /* F_nu at 1 pc of line `iline` (1-based line of moldata.dat), channel order of the
    passband (ascending frequency), like spec_flux_observer after calc_line_spectrum.
@@ -195,7 +207,12 @@ int rl_gen_spec(rl_ctx* ctx, const rl_genspec_lines* lines, const rl_genspec_par
 /* The RADlite executable's work in `dir`: read the inputs and render the lines requested
    by linespectrum.inp (starting at line 1, main.F:204). Command 0 writes
    linespectrum_<mol>.dat (main.F:1034-1049), command 2 one lineposvel_<mol>_<iline>.dat
-   per line (main.F:1061-1074); both then write radlite.success. */
+   per line (main.F:1061-1074); both then write radlite.success. The run takes the
+   overshoot test on every step (RL_CHECK_OVERSHOOT) and, like the reference, appends the
+   run's record to radlite.log: the start stamp, this build's switches and the problem
+   setup before the render, the warnings (the overshoot warning of main.F:1547-1552 when a
+   step failed the test) and the finish stamp after it (write_logmessage_start/_end,
+   main.F:1121-1588). */
 int rl_run_dir(const char* dir, int device, rl_stats* stats);
 /* rl_run_dir with options. RL_RUN_SAVE_IMCIR: as a reference build with SAVE_IMCIR
    (configure_image.h:57), also write lineposvelcirc_<mol>_<iline>.dat, the circular image

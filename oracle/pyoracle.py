@@ -45,6 +45,8 @@ def lib():
         L.rlo_posvel.argtypes = [vp, C.c_int, C.c_int, C.c_int] + [C.c_double] * 5 + [C.c_int, _D, _D]
         L.rlo_run_dir.argtypes = [C.c_char_p]
         L.rlo_masing.argtypes = [vp]
+        L.rlo_overshoots.argtypes = [vp]
+        L.rlo_overshoots.restype = C.c_longlong
         L.rlo_hunt.argtypes = [_D, C.c_int, C.c_double, C.c_int]
         _lib = L
     return _lib
@@ -157,6 +159,11 @@ class Oracle:
     def masing(self) -> bool:
         """Whether the last line spectrum, image or cube met the masing test."""
         return bool(lib().rlo_masing(self.h))
+
+    def overshoots(self) -> int:
+        """Formal-solution steps of the last line spectrum, image or cube whose quadrature
+        exceeded twice the theoretical maximum before the bracket."""
+        return int(lib().rlo_overshoots(self.h))
 
 
 def run_dir(path: str) -> None:

@@ -225,6 +225,7 @@ struct rlo_model {
     double rstar; double* starcont; int starpump;
     double* isrf;   /* [1..ncont] interstellfield.inp (outer boundary 3), else NULL */
     int maser;      /* masing found by the last line image or position-velocity cube */
+    long long overshoot;   /* quadrature overshoots of the last line image or cube */
     int outer_bc, inner_bc, line_dust;
     /* camera & passband */
     double incl_rad; int nphi, dbdr, nrext;
@@ -997,6 +998,7 @@ typedef struct {
     long long steps;
     double tau;        /* char_tau: running optical depth of the current (ray, channel), line.F:4598 */
     int maser;         /* maserflag: some segment had line opacity x length below -0.01 */
+    long long overshoot;   /* transerr_overshoot: steps whose quadrature exceeded twice theomax */
 } linectx;
 
 static int node_values(const linectx* L, int icr, int ir, int it, double dr, double dt, double mu, double phi,
@@ -1059,7 +1061,10 @@ static double voigt(double nu00, double aks, double dnu) {
     return norm * exp(-(u * u));
 }
 
-static double qdr_src_2(double in, double js1, double alp1, double js2, double alp2, double ds) {
+/* The overshoot test (transfer.F:1548-1553, on in the reference's default build): the
+   quadrature before the bracket above twice the theoretical maximum; counted, then bracketed
+   as usual. */
+static double qdr_src_2(double in, double js1, double alp1, double js2, double alp2, double ds, long long* nover) {
     double dtau1 = 0.5 * (alp1 + alp2) * ds;
     double theomax = 0.5 * (js1 + js2) * ds;
     double xp, a, b;
@@ -1069,6 +1074,7 @@ static double qdr_src_2(double in, double js1, double alp1, double js2, double a
     if (alp1 > 0.0) src1 = js1 / alp1; else if (alp2 > 0.0) src1 = js2 / alp2; else src1 = 0.0;
     if (alp2 > 0.0) src2 = js2 / alp2; else if (alp1 > 0.0) src2 = js1 / alp1; else src2 = 0.0;
     if (dtau1 > (double)1e-9f) q = a * src1 + b * src2; else q = 0.5 * (js1 + js2) * ds;
+    if (q > 2.0 * theomax) (*nover)++;
     if (q > theomax) q = theomax;
     return in * xp + q;
 }
@@ -1088,7 +1094,7 @@ static void integrate_el(linectx* L, int inu, double* I, double ds, double sd0, 
     if (st->init == 1) st->alpl0 = 5.27296241956e-28 * L->lfreq * st->phiprof0 * (nd0 * L->Bdu - nu0 * L->Bud);
     double alpl1 = 5.27296241956e-28 * L->lfreq * phi1 * (nd1 * L->Bdu - nu1 * L->Bud);
     double src0 = sd0 + st->srcl0, src1 = sd1 + srcl1, alp0 = ad0 + st->alpl0, alp1 = ad1 + alpl1;
-    *I = qdr_src_2(*I, src0, alp0, src1, alp1, ds);
+    *I = qdr_src_2(*I, src0, alp0, src1, alp1, ds, &L->overshoot);
     L->tau = L->tau + 0.5 * (alp0 + alp1) * ds;
     st->phiprof0 = phi1; st->srcl0 = srcl1; st->alpl0 = alpl1; st->init = 0;
     L->steps++;
@@ -1324,6 +1330,7 @@ int rlo_line_image(rlo_model* m, int iline, int ray_begin, int ray_end, double* 
     }
     if (counts) { counts[0] = L.steps; counts[1] = integ; counts[2] = nodes; }
     m->maser = L.maser;
+    m->overshoot = L.overshoot;
     free(velo); free(L.dnu); free(L.star); free(L.isrf);
     return rc;
 }
@@ -1345,6 +1352,7 @@ int rlo_ray_spectrum(rlo_model* m, int iline, double x0, double z0, double* I_ou
         if (tau_out) tau_out[k - 1] = L.tau;
     }
     m->maser |= L.maser;
+    m->overshoot += L.overshoot;
     traj_free(&T);
     free(L.dnu); free(L.star);
     return rc;
@@ -1399,6 +1407,7 @@ int rlo_posvel(rlo_model* m, int iline, int nx, int ny, double szx, double szy, 
     double *z0 = x0 + npix, *b = z0 + npix;
     int rc = rlo_pv_rays(m, nx, ny, szx, szy, phioff, xoff, yoff, addstar, x0, z0, b, info, dinfo);
     m->maser = 0;
+    m->overshoot = 0;
     double theta_saved = m->theta0;
     m->theta0 = dinfo[3];
     double rmax = RG(m, m->nr);
@@ -1454,6 +1463,7 @@ int rlo_image_to_spectrum(const rlo_model* m, const double* image, double* flux)
 }
 
 int rlo_masing(const rlo_model* m) { return m->maser; }
+long long rlo_overshoots(const rlo_model* m) { return m->overshoot; }
 
 int rlo_line_spectrum(rlo_model* m, int iline, double* flux, double* velo_kms, long long* counts) {
     size_t n = (size_t)m->nrays * m->nfr;

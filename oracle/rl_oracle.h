@@ -28,6 +28,10 @@ int rlo_hunt(const double* xx, int n, double x, int guess);
 /* 1 when the last line image, line spectrum or position-velocity cube met the masing
    test of charintline (telescope.F:4291-4297) */
 int rlo_masing(const rlo_model* m);
+/* formal-solution steps of the last line image, line spectrum or position-velocity cube
+   whose quadrature, before the bracket, exceeded twice the theoretical maximum
+   (transerr_overshoot, transfer.F:1548-1553) */
+long long rlo_overshoots(const rlo_model* m);
 #ifdef __cplusplus
 }
 #endif

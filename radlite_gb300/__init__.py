@@ -40,7 +40,7 @@ class Stats(C.Structure):
                 ("h2d_bytes", C.c_ulonglong), ("d2h_bytes", C.c_ulonglong), ("node_passes", C.c_ulonglong),
                 ("packed_passes", C.c_ulonglong), ("empty_steps", C.c_ulonglong),
                 ("refined_passes", C.c_ulonglong), ("sub_steps", C.c_ulonglong),
-                ("refined_channels", C.c_ulonglong)]
+                ("refined_channels", C.c_ulonglong), ("overshoots", C.c_ulonglong)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -89,7 +89,8 @@ class GenspecParams(C.Structure):
 
 
 EXPORTS = ["rl_create", "rl_destroy", "rl_last_error", "rl_load_dir", "rl_load_arrays", "rl_model_free",
-           "rl_model_get_info", "rl_set_camera", "rl_set_precision", "rl_line_spectrum", "rl_spectra",
+           "rl_model_get_info", "rl_set_camera", "rl_set_precision", "rl_set_checks", "rl_line_spectrum",
+           "rl_spectra",
            "rl_line_image", "rl_run_dir", "rl_debug_trajectory", "rl_measure_peaks",
            "rl_batch_create", "rl_batch_destroy", "rl_batch_add", "rl_batch_set_memory", "rl_batch_set_tiles",
            "rl_batch_get_tiles", "rl_batch_autotune", "rl_batch_use_graph", "rl_batch_flux_size",
@@ -123,6 +124,7 @@ def lib():
         L.rl_model_checksum.argtypes = [vp, C.POINTER(C.c_ulonglong)]
         L.rl_set_camera.argtypes = [vp, C.c_double, C.c_int, C.c_int, C.c_int]
         L.rl_set_precision.argtypes = [vp, C.c_int]
+        L.rl_set_checks.argtypes = [vp, C.c_int]
         L.rl_line_spectrum.argtypes = [vp, C.c_int, _D, _D, C.POINTER(Stats)]
         L.rl_spectra.argtypes = [vp, C.c_int, C.c_int, _D, C.POINTER(Stats)]
         L.rl_line_image.argtypes = [vp, C.c_int, _D, C.POINTER(Stats)]
@@ -339,6 +341,11 @@ class Model:
 
     def set_precision(self, precision: int):
         _check(lib().rl_set_precision(self.h, precision), self._ch)
+
+    def set_checks(self, overshoot: bool = True):
+        """Take the reference's overshoot test on every step of this model's line renders
+        and count the steps that fail it (stats["overshoots"]); results are unchanged."""
+        _check(lib().rl_set_checks(self.h, CHECK_OVERSHOOT if overshoot else 0), self._ch)
 
     def calc_line_spectrum(self, iline: int, stats: bool = False):
         """F_nu at 1 pc over the passband of line `iline` (1-based, moldata.dat order)."""
@@ -688,6 +695,7 @@ def load_dir_host(path: str) -> "Model":
 
 
 RUN_SAVE_IMCIR = 1
+CHECK_OVERSHOOT = 1
 
 
 def run_dir(path: str, device: int = 0, save_imcir: bool = False) -> dict:

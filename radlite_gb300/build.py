@@ -14,7 +14,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # host code: no FMA contraction, so that host arithmetic rounds alike on x86 and Arm
 COMMON = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-lineinfo"]
 SOURCES = ["rl_kernels.cu", "rl_adjoint.cu", "rl_host.cpp", "rl_capi.cpp", "rl_batch.cpp", "rl_diff.cpp",
-           "rl_noalloc.cu", "rl_posvel.cu", "rl_genspec.cu", "rl_walk_tau.cu"]
+           "rl_noalloc.cu", "rl_posvel.cu", "rl_genspec.cu", "rl_walk_tau.cu", "rl_walk_chk.cu"]
 
 
 def nvcc() -> str:

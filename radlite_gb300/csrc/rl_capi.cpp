@@ -268,7 +268,7 @@ static int run_lines(rl_model* md, int iline0, int nl, double* flux_out, double*
   P.list = md->dlist.as<unsigned short>();
   P.mask = mask_out ? md->dmask.as<unsigned char>() : nullptr;
   if (cam.ri[1] < m.rstar) return set_err(ctx, RL_ERR_ARG, "central beam smaller than the star");
-  CUDA_TRY(launch_walk<T>(P, cpl, ctx->nsm, s));
+  CUDA_TRY(launch_walk<T>(P, cpl, ctx->nsm, s, (md->checks & RL_CHECK_OVERSHOOT) != 0));
   CUDA_TRY(cudaEventRecord(ctx->ev[2], s));
   ReduceParams rp;
   rp.nrays = cam.nrays; rp.nfr = nfr; rp.nphi = cam.nphi; rp.nrr = cam.nrr; rp.nlines = nl;
@@ -319,6 +319,7 @@ static int run_lines(rl_model* md, int iline0, int nl, double* flux_out, double*
     st->steps += cnt[0]; st->integrated += cnt[1]; st->node_visits += cnt[2];
     st->node_passes += cnt[3]; st->packed_passes += cnt[4]; st->empty_steps += cnt[5];
     st->refined_passes += cnt[6]; st->sub_steps += cnt[7]; st->refined_channels += cnt[8];
+    st->overshoots += cnt[9];
     st->ray_channels += (unsigned long long)cam.nrays * nfr * nl;
     st->nrays = cam.nrays; st->nfr = nfr; st->kmax = md->kmax; st->nlines += nl;
   }
@@ -514,6 +515,13 @@ int rl_set_precision(rl_model* md, int precision) {
   return 0;
 }
 
+int rl_set_checks(rl_model* md, int flags) {
+  if (!md) return set_err(nullptr, RL_ERR_ARG, "rl_set_checks: null model");
+  if (flags & ~RL_CHECK_OVERSHOOT) return set_err(md->ctx, RL_ERR_ARG, "rl_set_checks: unknown flags");
+  md->checks = flags;
+  return 0;
+}
+
 int rl_line_spectrum(rl_model* md, int iline, double* flux_out, double* velo_out, rl_stats* st) {
   if (!md || !flux_out) return set_err(nullptr, RL_ERR_ARG, "rl_line_spectrum: null argument");
   rl_ctx* ctx = md->ctx;
@@ -573,28 +581,85 @@ int rl_line_image_mask(rl_model* md, int iline, double* image_out, unsigned char
 
 int rl_run_dir(const char* dir, int device, rl_stats* st) { return rl_run_dir_ex(dir, device, 0, st); }
 
-// radlite.log: the start and finish stamps the reference appends around the telescope
-// step (write_logmessage_start/_end, main.F:983-985, 1093-1095, 1119-1520; the list of
-// compile-time switches and the transfer warnings of the reference are not reproduced).
-static void run_log(const std::string& dir, bool start) {
-  FILE* fp = std::fopen((dir + "/radlite.log").c_str(), "a");
-  if (!fp) return;
+// radlite.log: the record the reference appends around the telescope step
+// (write_logmessage_start/_end, main.F:983-985, 1093-1095, 1121-1588), one line per
+// list-directed write (a leading blank, integers in 12 columns). The start record lists
+// the compile-time switches of the reference's spectrum build whose raytrace this library
+// reproduces (configure_spectrum.h; the short-characteristics, ALI and interpolation
+// switches of its level-population solver have no counterpart here), the precision of
+// this run, and the raytrace's part of the problem setup. The end record lists the
+// warnings the raytrace can raise: the overshoot warning (main.F:1547-1552).
+static void log_stamp(char* d, size_t nd, char* h, size_t nh) {
   const auto now = std::chrono::system_clock::now();
   const std::time_t t = std::chrono::system_clock::to_time_t(now);
   const int ms = (int)(std::chrono::duration_cast<std::chrono::milliseconds>(now.time_since_epoch()).count() % 1000);
   std::tm tmv;
   localtime_r(&t, &tmv);
+  std::snprintf(d, nd, "%02d-%02d-%04d", tmv.tm_mday, tmv.tm_mon + 1, tmv.tm_year + 1900);
+  std::snprintf(h, nh, "%02d:%02d:%02d.%03d", tmv.tm_hour, tmv.tm_min, tmv.tm_sec, ms);
+}
+
+static void run_log_start(const std::string& dir, const rl_model* md, int flags) {
+  FILE* fp = std::fopen((dir + "/radlite.log").c_str(), "a");
+  if (!fp) return;
   char d[32], h[32];
-  std::snprintf(d, sizeof d, "%02d-%02d-%04d", tmv.tm_mday, tmv.tm_mon + 1, tmv.tm_year + 1900);
-  std::snprintf(h, sizeof h, "%02d:%02d:%02d.%03d", tmv.tm_hour, tmv.tm_min, tmv.tm_sec, ms);
-  if (start)
-    std::fprintf(fp, "\n\n\n =========== RUN OF RADICAL ===========\n Action       : spectrum/image\n"
-                     " Starting Date: %s\n          Time: %s\n ......................................\n"
-                     "       COMPILATION OF CODE:            \n radlite_gb300 line raytrace (GB300, sm_103a)\n",
-                 d, h);
-  else
-    std::fprintf(fp, " ......................................\n Finished Date: %s\n          Time: %s\n", d, h);
+  log_stamp(d, sizeof d, h, sizeof h);
+  const Model& m = md->m;
+  std::fprintf(fp, "\n\n\n =========== RUN OF RADICAL ===========\n Action       : spectrum/image\n"
+                   " Starting Date: %s\n          Time: %s\n ......................................\n"
+                   "       COMPILATION OF CODE:            \n",
+               d, h);
+  std::fprintf(fp,
+               " Dimension = 2              (RADGRID_TWODIM)\n"
+               " Include lines              (INCLUDE_LINES)\n"
+               " Include dust continuum     (INCLUDE_DUST)\n"
+               " Mirror in Theta : yes      (MIRROR_THETA)\n"
+               " Quadrature                 (SRCQDR_PNT_2)\n"
+               " Line profile refinement    (SUBGRID)\n"
+               " Velocity window per ray    (NONREDUNDANT)\n"
+               " Star in the central beam   (CENTRAL_SOURCE)\n");
+  if (flags & RL_RUN_SAVE_IMCIR) std::fprintf(fp, " Circular images saved      (SAVE_IMCIR)\n");
+  std::fprintf(fp, " radlite_gb300 line raytrace (GB300, sm_103a): %s\n",
+               md->precision == RL_FP64 ? "FP64 transfer, FP64 crossings" : "FP32 transfer, FP64 crossings");
+  std::fprintf(fp, " \n ......................................\n           SETUP OF PROBLEM:           \n");
+  std::fprintf(fp, " frsize radius      = %12d\n frsize theta       = %12d\n bound cond outer   = %12d\n",
+               m.nr, m.nth, m.outer_bc);
+  std::fprintf(fp, " telescope nphi     = %12d\n telescope dbdr     = %12d\n telescope extra b  = %12d\n",
+               md->nphi, md->dbdr, md->nrext);
+  std::fprintf(fp, " \n");
   std::fclose(fp);
+}
+
+static void run_log_end(const std::string& dir, unsigned long long overshoots) {
+  FILE* fp = std::fopen((dir + "/radlite.log").c_str(), "a");
+  if (!fp) return;
+  char d[32], h[32];
+  log_stamp(d, sizeof d, h, sizeof h);
+  std::fprintf(fp, " ......................................\n Warnings:\n");
+  if (overshoots > 0)
+    std::fprintf(fp, " * During Short Characteristic integration     \n"
+                     "   there were overshoots in the quadrature.    \n"
+                     "   These have been corrected automatically,    \n"
+                     "   but they indicate poor grid resolution!     \n");
+  else
+    std::fprintf(fp, " <none>\n");
+  std::fprintf(fp, " ......................................\n Finishing Date: %s\n          Time: %s\n"
+                   " ========= END OF RUN RADLITE =========\n",
+               d, h);
+  std::fclose(fp);
+}
+
+// The warning make_freq_image_rectang prints after an image whose quadrature overshot
+// (telescope.F:2204-2213).
+static void warn_overshoot_image() {
+  std::printf(" \n -----------------------------------------------\n"
+              " |  WARNING:                                   |\n"
+              " |  While making the image there were serious  |\n"
+              " |  overshoots in the quadrature.              |\n"
+              " |  These have been corrected automatically,   |\n"
+              " |  but they indicate poor grid resolution!    |\n"
+              " -----------------------------------------------\n");
+  std::fflush(stdout);
 }
 
 // The reference's warning after each line whose render found masing: calc_line_spectrum
@@ -610,14 +675,21 @@ static void warn_masing(const rl_model* md, int iline0, int nl, bool posvel) {
   std::fflush(stdout);   // in order with the caller's own output
 }
 
-int rl_run_dir_ex(const char* dir, int device, int flags, rl_stats* st) {
+int rl_run_dir_ex(const char* dir, int device, int flags, rl_stats* st_out) {
   if (flags & ~RL_RUN_SAVE_IMCIR) return set_err(nullptr, RL_ERR_ARG, "rl_run_dir_ex: unknown flags");
+  rl_stats own;
+  rl_stats* st = st_out ? st_out : &own;   // the run's totals feed the log's warnings
+  std::memset(st, 0, sizeof *st);
+  unsigned long long last_over = 0;        // overshoots of the last rendered image
   rl_ctx* ctx = nullptr;
   int rc = rl_create(&ctx, device);
   if (rc) return rc;
   rl_model* md = nullptr;
   rc = rl_load_dir(ctx, dir, &md);
-  if (rc == 0) run_log(dir, true);
+  if (rc == 0) {
+    md->checks = RL_CHECK_OVERSHOOT;   // the reference's default build takes the test
+    run_log_start(dir, md, flags);
+  }
   if (rc == 0 && md->m.command == 2 && md->m.pv.sizespec == 0) {   // telescope.F:207-210
     std::printf(" While reading linespectrum.inp:\n Size specifier in arcsec not yet implemented\n");
     std::fflush(stdout);
@@ -637,8 +709,13 @@ int rl_run_dir_ex(const char* dir, int device, int flags, rl_stats* st) {
       const int nl = std::min(chunk, m.nlspec - l0);
       I.resize(per_line * nl);
       tau.resize(per_line * nl);
+      const unsigned long long over0 = st->overshoots;
       rc = dispatch_posvel(md, m.ilstart + l0, nl, I.data(), tau.data(), st);
       if (rc == 0) warn_masing(md, m.ilstart + l0, nl, true);
+      // the reference clears its counter per rectangular image (telescope.F:2094); a
+      // launch here renders the lines of one chunk
+      last_over = st->overshoots - over0;
+      if (rc == 0 && last_over > 0) warn_overshoot_image();
       for (int l = 0; l < nl && rc == 0; l++) {
         const int iline = m.ilstart + l0 + l;
         const std::string name = posvel_file_name(m, iline);
@@ -678,6 +755,7 @@ int rl_run_dir_ex(const char* dir, int device, int flags, rl_stats* st) {
         st->steps += one.steps; st->integrated += one.integrated; st->node_visits += one.node_visits;
         st->ray_channels += one.ray_channels; st->walk_ms += one.walk_ms; st->geometry_ms += one.geometry_ms;
         st->reduce_ms += one.reduce_ms; st->upload_ms += one.upload_ms; st->nlines += 1;
+        st->overshoots += one.overshoots;
         st->nrays = one.nrays; st->nfr = one.nfr; st->kmax = one.kmax;
       }
       const std::string name = imcir_file_name(m, iline);
@@ -713,7 +791,8 @@ int rl_run_dir_ex(const char* dir, int device, int flags, rl_stats* st) {
       }
     }
   }
-  if (rc == 0) run_log(dir, false);
+  // circular images never clear the counter: a spectrum run warns for any overshoot
+  if (rc == 0) run_log_end(dir, md->m.command == 2 ? last_over : st->overshoots);
   if (rc) g_last_error = ctx->err;
   rl_model_free(md);
   rl_destroy(ctx);

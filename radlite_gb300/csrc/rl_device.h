@@ -7,8 +7,8 @@ namespace rl {
 
 // Counters of a walk launch (flush_counters): steps, integrated pairs, node visits, node
 // passes, packed node passes, steps of empty segments, refined passes, their sub-steps,
-// their refined channels.
-constexpr int kWalkCounters = 9;
+// their refined channels, steps that failed the overshoot test (checking walks).
+constexpr int kWalkCounters = 10;
 // Walk launch shape: 4-warp blocks, at most this many per SM (sizes the list scratch).
 constexpr int kWalkBlocksPerSm = 4;
 constexpr int kWalkWarps = 4;

@@ -14,8 +14,10 @@ namespace rl {
 template <typename T>
 cudaError_t launch_geometry(const GeoParams& p, const NodeBuf<T>& nb, int ray0, int nray, TrajDebug* dbg,
                             cudaStream_t s);
+// check: count the steps that fail the reference's overshoot test in counters[9]
+// (the plain walk with P.tau unset only)
 template <typename T>
-cudaError_t launch_walk(const WalkParams<T>& P, int cpl, int nsm, cudaStream_t s);
+cudaError_t launch_walk(const WalkParams<T>& P, int cpl, int nsm, cudaStream_t s, bool check = false);
 template <typename T>
 cudaError_t launch_reduce(const ReduceParams& p, const T* img, double* ring, double* flux, cudaStream_t s);
 template <typename T>
@@ -164,6 +166,7 @@ struct rl_model {
   rl_ctx* ctx = nullptr;
   rl::Model m;
   int precision = RL_FP32;
+  int checks = 0;   // RL_CHECK_* diagnostics of the line renders
   // camera request
   double incl_rad = 0.0;
   int nphi = 0, dbdr = 1, nrext = 0;

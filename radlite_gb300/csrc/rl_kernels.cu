@@ -27,6 +27,9 @@ template <typename T>
 cudaError_t launch_walk_tau(const WalkParams<T>& P, int cpl, int nsm, cudaStream_t s);
 template <typename T>
 cudaError_t launch_walk_jobs_tau(const WalkJobs<T>& B, int cpl, int nsm, cudaStream_t s);
+// the walk instances that count the steps failing the overshoot test (rl_walk_chk.cu)
+template <typename T>
+cudaError_t launch_walk_chk(const WalkParams<T>& P, int cpl, int nsm, cudaStream_t s);
 
 // ------------------------------------------------------------------------------------
 // geometry
@@ -369,8 +372,9 @@ cudaError_t launch_geometry(const GeoParams& p, const NodeBuf<T>& nb, int ray0, 
 }
 
 template <typename T>
-cudaError_t launch_walk(const WalkParams<T>& P, int cpl, int nsm, cudaStream_t s) {
+cudaError_t launch_walk(const WalkParams<T>& P, int cpl, int nsm, cudaStream_t s, bool check) {
   if (P.tau) return launch_walk_tau<T>(P, cpl, nsm, s);   // rl_walk_tau.cu
+  if (check) return launch_walk_chk<T>(P, cpl, nsm, s);   // rl_walk_chk.cu
   return launch_walk_t<T, false>(P, cpl, nsm, s);
 }
 
@@ -418,8 +422,8 @@ cudaError_t launch_jobs(const JobLaunch<T>& L, cudaStream_t s) {
 
 template cudaError_t launch_geometry<float>(const GeoParams&, const NodeBuf<float>&, int, int, TrajDebug*, cudaStream_t);
 template cudaError_t launch_geometry<double>(const GeoParams&, const NodeBuf<double>&, int, int, TrajDebug*, cudaStream_t);
-template cudaError_t launch_walk<float>(const WalkParams<float>&, int, int, cudaStream_t);
-template cudaError_t launch_walk<double>(const WalkParams<double>&, int, int, cudaStream_t);
+template cudaError_t launch_walk<float>(const WalkParams<float>&, int, int, cudaStream_t, bool);
+template cudaError_t launch_walk<double>(const WalkParams<double>&, int, int, cudaStream_t, bool);
 template cudaError_t launch_reduce<float>(const ReduceParams&, const float*, double*, double*, cudaStream_t);
 template cudaError_t launch_reduce<double>(const ReduceParams&, const double*, double*, double*, cudaStream_t);
 template cudaError_t launch_gather_rows<float>(const float*, int, int, int, const int*, int, float*, cudaStream_t);

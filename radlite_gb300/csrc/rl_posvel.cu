@@ -8,7 +8,8 @@
 //   k_geometry    the circular image's node kernel over the traced rays.
 //   k_walk_pv     the circular image's walk with every channel of every ray integrated, no
 //                 star mixing (charintline with rbeam 0) and the line-of-sight optical depth
-//                 char_tau of each channel (Kahan-compensated in FP32).
+//                 char_tau of each channel (Kahan-compensated in FP32); it counts the steps
+//                 that fail the overshoot test (transfer.F:1548-1553) as well.
 //   k_posvel_cube image epilogue instead of the spectrum reduction: scatter the traced rays
 //                 into the [line][channel][iy][ix] cube in FP64, apply the intensity scale
 //                 and smear the unresolved star over the four central pixels
@@ -39,7 +40,7 @@ __global__ void __launch_bounds__(128, WalkMinBlocks<T>::value) k_walk_pv(WalkPa
     if (lane == 0) item = atomicAdd(P.work, 1);
     item = __shfl_sync(0xffffffffu, item, 0);
     if (item >= P.nitems) break;
-    walk_item<T, C, true>(P, item, *W.S, *W.SS, *W.SW, W.list, lane, steps);
+    walk_item<T, C, true, false, true>(P, item, *W.S, *W.SS, *W.SW, W.list, lane, steps);
   }
   flush_counters(steps, *W.SW, P.counters, lane);
 }
@@ -150,7 +151,7 @@ static int run_posvel(rl_model* md, int iline0, int nl, double* I_out, double* t
   CUDA_TRY(B.pix.ensure(sizeof(int) * npix));
   CUDA_TRY(B.scale.ensure(sizeof(double) * nl));
   float geo_ms = 0.f, walk_ms = 0.f, red_ms = 0.f, up_ms = 0.f;
-  unsigned long long cnt[4] = {0, 0, 0, 0};
+  unsigned long long cnt[kWalkCounters] = {};
   int kerr = 0;
   CUDA_TRY(cudaEventRecord(ctx->ev[0], s));
   CUDA_TRY(h2d(B.pix.p, pix.data(), sizeof(int) * npix, s));
@@ -259,6 +260,7 @@ static int run_posvel(rl_model* md, int iline0, int nl, double* I_out, double* t
   if (st) {
     st->upload_ms += up_ms; st->geometry_ms += geo_ms; st->walk_ms += walk_ms; st->reduce_ms += red_ms;
     st->steps += cnt[0]; st->integrated += cnt[1]; st->node_visits += cnt[2];
+    st->overshoots += cnt[9];
     st->ray_channels += (unsigned long long)ntr * nfr * nl;
     st->nrays = ntr; st->nfr = nfr; st->kmax = rlg::max_nodes(m.nr, m.nth); st->nlines += nl;
   }

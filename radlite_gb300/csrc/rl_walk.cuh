@@ -51,7 +51,7 @@ __device__ __forceinline__ SegGeom<T> seg_geom(T ds, T dvs, T rlw, T kq) {
 // zero a warp's launch totals (SubWork::ctr, rstat) before its first item
 template <typename T>
 __device__ __forceinline__ void zero_counters(SubWork<T>& SW, int lane) {
-  if (lane < 5) SW.ctr[lane] = 0;
+  if (lane < 6) SW.ctr[lane] = 0;
   if (lane < 3) SW.rstat[lane] = 0;
   __syncwarp();
 }
@@ -67,7 +67,9 @@ __device__ __forceinline__ void zero_counters(SubWork<T>& SW, int lane) {
 // line), so that entry line - lbase indexes the tile's staged lines 0..gl-1.
 // TAU (circular image): the slots' optical depth is kept as in the position-velocity walk
 // (for the gradient sweep of the differentiable path); nothing else changes.
-template <typename T, int C, bool PV = false, bool TAU = false>
+// CHK: every step also takes the reference's overshoot test (transfer.F:1548-1553), and the
+// steps that fail it are counted in SW.ctr[5]; the results are the same.
+template <typename T, int C, bool PV = false, bool TAU = false, bool CHK = false>
 __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<T, C>& SS, SubWork<T>& SW, int ray,
                               int K, int l0, int gl, const unsigned short* list, int nt, int lane, int lbase,
                               unsigned long long& steps_total) {
@@ -120,6 +122,7 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
   // per-call counts (32-bit: a call walks one tile of one ray): formal-solution steps, node
   // passes, of them on the general path and empty, and the steps of empty segments
   unsigned steps = 0, passes = 0, general = 0, emptyp = 0, skipped = 0;
+  int over = 0;   // CHK: this lane's steps that failed the overshoot test
   unsigned mbits = 0;   // tile lines whose line opacity x segment length fell below -0.01
   T lw_last = 0;
   bool pos_last = true, zero_last = false;
@@ -128,7 +131,7 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
       if (lane == 0) {
         S.vl[0] = S.vl[32]; S.hds[0] = S.hds[32]; S.ds[0] = S.ds[32]; S.rlw[0] = S.rlw[32];
         S.dvs[0] = S.dvs[32]; S.flags[0] = S.flags[32];
-        if constexpr (kFast) { S.hot[0][0] = S.hot[32][0]; S.hot[0][1] = S.hot[32][1]; }
+        if constexpr (kFast) { S.hot[0] = S.hot[32]; S.hrl[0] = S.hrl[32]; }
       }
       if (lane < gl) S.lv[lane][0] = S.lv[lane][32];
       __syncwarp();
@@ -182,8 +185,8 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
         // node values of the packed step, duplicated into pairs: {vl, vl, hds, hds},
         // {rl, rl} (the profile's 1/width)
         const float h = 0.5f * (float)ds;
-        S.hot[lane + 1][0] = make_float4((float)vl, (float)vl, h, h);
-        S.hot[lane + 1][1] = make_float4((float)rlw, (float)rlw, 0.f, 0.f);
+        S.hot[lane + 1] = make_float4((float)vl, (float)vl, h, h);
+        S.hrl[lane + 1] = make_float2((float)rlw, (float)rlw);
       }
       S.flags[lane + 1] = f;
     }
@@ -254,9 +257,9 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
             slow = __any_sync(0xffffffffu, any);
           }
           if (!slow) {
-            const float4 h0 = S.hot[n + 1][0], h1 = S.hot[n + 1][1];
+            const float4 h0 = S.hot[n + 1];
             const float2 vl2 = make_float2(h0.x, h0.y), hd2 = make_float2(h0.z, h0.w);
-            const float2 rl2 = make_float2(h1.x, h1.y);
+            const float2 rl2 = S.hrl[n + 1];
             float2 j1[kPass / 2], a1[kPass / 2], S1[kPass / 2], dt[kPass / 2], th[kPass / 2];
             bool ser = true, dir = true;
 #pragma unroll
@@ -300,6 +303,12 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
               const float2 Q = fma2(ca[p], make_float2(S0[2 * p], S0[2 * p + 1]), mul2(cb[p], S1[p]));
               const float2 thin = make_float2(__saturatef(fmaf(dt[p].x, -kThinScale, kThinBias)),
                                               __saturatef(fmaf(dt[p].y, -kThinScale, kThinBias)));
+              if constexpr (CHK) {
+                // before the bracket the quadrature is Q, or theo for an optically thin step
+                // (empty slots take discarded steps and are not counted)
+                over += (Ls[2 * p] >= 0 && (dt[p].x > 1.0e-9f ? Q.x > 2.f * th[p].x : th[p].x < 0.f)) ? 1 : 0;
+                over += (Ls[2 * p + 1] >= 0 && (dt[p].y > 1.0e-9f ? Q.y > 2.f * th[p].y : th[p].y < 0.f)) ? 1 : 0;
+              }
               const float2 Qb = fma2(thin, dup2(3.0e38f), Q);
               const float2 q = make_float2(fminf(Qb.x, th[p].x), fminf(Qb.y, th[p].y));
               const float2 In = fma2(make_float2(I[2 * p], I[2 * p + 1]), x[p], q);
@@ -374,6 +383,7 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
             const T src1 = a0[u] > (T)0 ? S0[u] : S1[u];
             const T src2 = a1[u] > (T)0 ? S1[u] : S0[u];
             T qv = dt[u] > (T)1.0e-9f ? fmadd(ca[u], src1, cb[u] * src2) : th[u];
+            if constexpr (CHK) over += (!ov[u] && Ls[u] >= 0 && qv > (T)2 * th[u]) ? 1 : 0;
             qv = qv < th[u] ? qv : th[u];
             if (!ov[u]) {
               I[u] = fmadd(I[u], x[u], qv);
@@ -402,12 +412,13 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
               const T wp = SW.w[p];
               const int lp = SW.l[p];
               const T s_c = sizeof(T) == 8 ? dsf * (wp - vl0) / dvsg : dsf * (wp - vl0) * G.idvs;
-              const SlotOutT<T, kTau> o = slot_sub<T, kTau>(wp, S.lv[lp][n], S.lv[lp][n + 1], vl0, vl1, rl, dsf, G.ids,
+              const SlotOutT<T, kTau, CHK> o = slot_sub<T, kTau, CHK>(wp, S.lv[lp][n], S.lv[lp][n + 1], vl0, vl1, rl, dsf, G.ids,
                                                         s_c - G.hw3, G.lg, G.ilg, SW.I[p], SW.j0[p], SW.a0[p], SW.S0[p]);
               SW.I[p] = o.I; SW.j0[p] = o.j0; SW.a0[p] = o.a0; SW.S0[p] = o.S0;
               if constexpr (kTau) SW.w[p] = o.dtau;   // the owner keeps w in a register
               steps += o.steps - 1;
               mysub += o.steps;
+              if constexpr (CHK) over += o.over;
             }
             // refinement statistics in shared memory (this path is rare; registers are not)
             mysub = __reduce_add_sync(0xffffffffu, mysub);
@@ -429,10 +440,11 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
 #pragma unroll
           for (int u = 0; u < kPass; u++) {
             if (Ls[u] < 0) continue;
-            const SlotOutT<T, kTau> o = slot_slow<T, kTau>(init, sub, w[u], S.lv[Ls[u]][n], S.lv[Ls[u]][n + 1], vl0, vl1,
+            const SlotOutT<T, kTau, CHK> o = slot_slow<T, kTau, CHK>(init, sub, w[u], S.lv[Ls[u]][n], S.lv[Ls[u]][n + 1], vl0, vl1,
                                                        rl, hds, G.q, dsf, dvs, G.ids, I[u], j0[u], a0[u], S0[u]);
             I[u] = o.I; j0[u] = o.j0; a0[u] = o.a0; S0[u] = o.S0; steps += o.steps - 1;
             if constexpr (kTau) add_tau(u, o.dtau);
+            if constexpr (CHK) over += o.over;
           }
         }
         if (P.maser) {
@@ -476,17 +488,19 @@ __device__ unsigned walk_ray(const WalkParams<T>& P, WarpStage<T>& S, SlotState<
     if (lane == 0)
       for (; mbits; mbits &= mbits - 1) atomicExch(&P.maser[l0 + __ffs(mbits) - 1], 1);
   }
+  if constexpr (CHK) over = __reduce_add_sync(0xffffffffu, over);
   if (lane == 0) {
     SW.ctr[2] += passes;
     SW.ctr[3] += kFast ? passes - general - emptyp : 0u;
     SW.ctr[4] += skipped;
+    if constexpr (CHK) SW.ctr[5] += (unsigned)over;
   }
   steps_total += steps;
   return steps;
 }
 
 // One work item: line group g of ray `ray`, item = g * nrays + ray.
-template <typename T, int C, bool PV = false, bool TAU = false>
+template <typename T, int C, bool PV = false, bool TAU = false, bool CHK = false>
 __device__ __forceinline__ void walk_item(const WalkParams<T>& P, int item, WarpStage<T>& S, SlotState<T, C>& SS,
                                           SubWork<T>& SW, unsigned short* list, int lane,
                                           unsigned long long& steps) {
@@ -574,7 +588,7 @@ __device__ __forceinline__ void walk_item(const WalkParams<T>& P, int item, Warp
     const int te = min(tb + 32 * C, S.lineoff[lcap]);
     const int nt = te - tb;
     const int lz = (int)(list[te - 1] >> kChBits);
-    walk_ray<T, C, PV, TAU>(P, S, SS, SW, ray, K, l0 + la, lz - la + 1, list + tb, nt, lane, la, steps);
+    walk_ray<T, C, PV, TAU, CHK>(P, S, SS, SW, ray, K, l0 + la, lz - la + 1, list + tb, nt, lane, la, steps);
     for (int j = 0; j < C; j++) {
       const int idx = j * 32 + lane;
       if (idx < nt) {
@@ -619,7 +633,7 @@ __device__ __forceinline__ void walk_item(const WalkParams<T>& P, int item, Warp
     __syncwarp();
     for (int tb = 0; tb < n2; tb += 32 * C) {
       const int nt = min(32 * C, n2 - tb);
-      walk_ray<T, C>(P, S, SS, SW, ray, K, l0 + l, 1, list + tb, nt, lane, l, steps);
+      walk_ray<T, C, false, false, CHK>(P, S, SS, SW, ray, K, l0 + l, 1, list + tb, nt, lane, l, steps);
       for (int j = 0; j < C; j++) {
         const int idx = j * 32 + lane;
         if (idx < nt) img[list[tb + idx] & (kMaxChannels - 1)] = SS.I[j][lane];
@@ -671,7 +685,8 @@ struct WarpSmem {
 // (pairs x nodes), [3] node passes of the walk (a pass = the tile's slots over one node),
 // [4] of them taken on the packed FP32 path, [5] steps of empty segments (counted in [0],
 // no arithmetic), [6] node passes with SUBGRID refinement, [7] the sub-steps of the refined
-// channels, [8] the refined channels of those passes. The buffers hold kWalkCounters values.
+// channels, [8] the refined channels of those passes, [9] steps that failed the overshoot
+// test (checking walks only). The buffers hold kWalkCounters values.
 template <typename T>
 __device__ __forceinline__ void flush_counters(unsigned long long steps, const SubWork<T>& SW,
                                                unsigned long long* counters, int lane) {
@@ -685,6 +700,7 @@ __device__ __forceinline__ void flush_counters(unsigned long long steps, const S
     atomicAdd(&counters[6], (unsigned long long)SW.rstat[0]);
     atomicAdd(&counters[7], (unsigned long long)SW.rstat[1]);
     atomicAdd(&counters[8], (unsigned long long)SW.rstat[2]);
+    atomicAdd(&counters[9], SW.ctr[5]);
   }
 }
 

@@ -154,8 +154,10 @@ __device__ __forceinline__ float profile<float>(float w, float vl, float rlw, fl
 // One application of the linear-source formal solution (qdr_src_2, transfer.F:1498-1571)
 // from point 0 (j0, a0, S0) to point 1 (j1, a1, S1) over half-length hds. Returns the
 // step's optical depth 0.5 (a0 + a1) ds, the increment of char_tau (line.F:4598).
-template <typename T>
-__device__ __forceinline__ T formal(T& I, T j0, T a0, T S0, T j1, T a1, T S1, T hds) {
+// CHK: counts in `over` the overshoot test of the reference (transfer.F:1548-1553): the
+// quadrature before the bracket above twice the theoretical maximum.
+template <typename T, bool CHK>
+__device__ __forceinline__ T formal_c(T& I, T j0, T a0, T S0, T j1, T a1, T S1, T hds, int& over) {
   const T dtau = (a0 + a1) * hds;
   const T theo = (j0 + j1) * hds;
   T x, a, b;
@@ -163,9 +165,15 @@ __device__ __forceinline__ T formal(T& I, T j0, T a0, T S0, T j1, T a1, T S1, T 
   const T src1 = a0 > (T)0 ? S0 : (a1 > (T)0 ? S1 : (T)0);
   const T src2 = a1 > (T)0 ? S1 : (a0 > (T)0 ? S0 : (T)0);
   T q = dtau > (T)1.0e-9f ? fmadd(a, src1, b * src2) : theo;
+  if constexpr (CHK) over += q > (T)2 * theo ? 1 : 0;
   q = q < theo ? q : theo;
   I = fmadd(I, x, q);
   return dtau;
+}
+template <typename T>
+__device__ __forceinline__ T formal(T& I, T j0, T a0, T S0, T j1, T a1, T S1, T hds) {
+  int unused = 0;
+  return formal_c<T, false>(I, j0, a0, S0, j1, a1, S1, hds, unused);
 }
 
 template <typename T>
@@ -198,7 +206,8 @@ struct WarpStage {
   LineVals<T> lv[kGroup][33];
   T vl[33], hds[33], ds[33], rlw[33], dvs[33];
   unsigned flags[33];
-  float4 hot[33][2];   // FP32 walk: per-node values of the packed step, as pairs
+  float4 hot[33];      // FP32 walk: per-node values of the packed step as pairs {vl, vl, hds, hds}
+  float2 hrl[33];      // and {1/width, 1/width}
   T contv[kItemLines];
   float mn[kItemLines], mx[kItemLines];
   int cont_ch[kItemLines];
@@ -212,9 +221,9 @@ struct SubWork {
   T I[128], j0[128], a0[128], S0[128], w[128];
   unsigned char l[128];
   // a warp's totals of a launch, kept here rather than in registers: integrated pairs, node
-  // visits, node passes, packed passes, steps of empty segments; refined passes, their
-  // sub-steps, their refined channels
-  unsigned long long ctr[5];
+  // visits, node passes, packed passes, steps of empty segments, overshooting steps (the
+  // checking walk); refined passes, their sub-steps, their refined channels
+  unsigned long long ctr[6];
   unsigned rstat[3];
 };
 
@@ -289,18 +298,21 @@ __device__ __forceinline__ T interp_1(const T* __restrict__ v, const Corners& c,
 
 template <typename T>
 struct SlotOutBase { T I, j0, a0, S0; int steps; };
-// TAU: the walk also accumulates the optical depth of the segment's steps
-template <typename T, bool TAU = false>
-struct SlotOutT : SlotOutBase<T> {};
-template <typename T>
-struct SlotOutT<T, true> : SlotOutBase<T> { T dtau; };
+// TAU: the walk also accumulates the optical depth of the segment's steps; CHK: it counts
+// the steps that fail the overshoot test
+template <typename T, bool TAU> struct SlotTau {};
+template <typename T> struct SlotTau<T, true> { T dtau; };
+template <bool CHK> struct SlotChk {};
+template <> struct SlotChk<true> { int over; };
+template <typename T, bool TAU = false, bool CHK = false>
+struct SlotOutT : SlotOutBase<T>, SlotTau<T, TAU>, SlotChk<CHK> {};
 
 // Segment with a state reset (first segment, central hole, star) or with SUBGRID
 // refinement (line.F:4703-4833): interior points i = ia..ib of the 31-point grid over
 // [s_c - 3 l, s_c + 3 l] strictly inside (0, ds), then the segment end. Kept out of line:
 // it is rare, and inlining it per slot overflows the instruction cache.
-template <typename T, bool TAU = false>
-__device__ __noinline__ SlotOutT<T, TAU> slot_slow(bool init, bool sub, T w, LineVals<T> v0, LineVals<T> v1, T vl0,
+template <typename T, bool TAU = false, bool CHK = false>
+__device__ __noinline__ SlotOutT<T, TAU, CHK> slot_slow(bool init, bool sub, T w, LineVals<T> v0, LineVals<T> v1, T vl0,
                                                T vl1, T rl, T hds, T q, T dsf, T dvs, T ids, T I, T j0, T a0, T S0) {
   const Pt<T> p0 = {v0.jd, v0.ad, v0.jf, v0.af, vl0};
   const Pt<T> p1 = {v1.jd, v1.ad, v1.jf, v1.af, vl1};
@@ -333,7 +345,7 @@ __device__ __noinline__ SlotOutT<T, TAU> slot_slow(bool init, bool sub, T w, Lin
       }
     }
   }
-  int steps = 0;
+  int steps = 0, over = 0;
   T sp = 0, tau = 0;
   for (int i = ia; i <= ib + 1; i++) {
     T s;
@@ -351,15 +363,16 @@ __device__ __noinline__ SlotOutT<T, TAU> slot_slow(bool init, bool sub, T w, Lin
     T j1, a1, S1;
     point_state(pq, ph, j1, a1, S1);
     const T h = (ia <= ib) ? (T)0.5 * (s - sp) : hds;
-    const T dt = formal(I, j0, a0, S0, j1, a1, S1, h);
+    const T dt = formal_c<T, CHK>(I, j0, a0, S0, j1, a1, S1, h, over);
     if constexpr (TAU) tau = tau + dt;
     j0 = j1; a0 = a1; S0 = S1;
     sp = s;
     steps++;
   }
-  SlotOutT<T, TAU> o;
+  SlotOutT<T, TAU, CHK> o;
   o.I = I; o.j0 = j0; o.a0 = a0; o.S0 = S0; o.steps = steps;
   if constexpr (TAU) o.dtau = tau;
+  if constexpr (CHK) o.over = over;
   return o;
 }
 
@@ -367,8 +380,8 @@ __device__ __noinline__ SlotOutT<T, TAU> slot_slow(bool init, bool sub, T w, Lin
 // overlaps it: interior points ia..ib of the grid s_i = sleft + i*lg, i = 0..30, that lie
 // strictly inside (0, ds), then the segment end (line.F:4769-4821). Called for those
 // channels only.
-template <typename T, bool TAU = false>
-__device__ __noinline__ SlotOutT<T, TAU> slot_sub(T w, LineVals<T> v0, LineVals<T> v1, T vl0, T vl1, T rl, T dsf, T ids,
+template <typename T, bool TAU = false, bool CHK = false>
+__device__ __noinline__ SlotOutT<T, TAU, CHK> slot_sub(T w, LineVals<T> v0, LineVals<T> v1, T vl0, T vl1, T rl, T dsf, T ids,
                                               T sleft, T lg, T ilg, T I, T j0, T a0, T S0) {
   int ia = 0;
   if (!(sleft > (T)0)) {
@@ -384,7 +397,7 @@ __device__ __noinline__ SlotOutT<T, TAU> slot_sub(T w, LineVals<T> v0, LineVals<
     while (ib < 30 && sleft + (T)(ib + 1) * lg < dsf) ib++;
     while (ib >= 0 && !(sleft + (T)ib * lg < dsf)) ib--;
   }
-  int steps = 0;
+  int steps = 0, over = 0;
   T sp = 0, tau = 0;
   for (int i = ia; i <= ib + 1; i++) {
     T s;
@@ -402,15 +415,16 @@ __device__ __noinline__ SlotOutT<T, TAU> slot_sub(T w, LineVals<T> v0, LineVals<
     const T ph = profile(w, pq.vl, rl, rl);
     T j1, a1, S1;
     point_state(pq, ph, j1, a1, S1);
-    const T dt = formal(I, j0, a0, S0, j1, a1, S1, (T)0.5 * (s - sp));
+    const T dt = formal_c<T, CHK>(I, j0, a0, S0, j1, a1, S1, (T)0.5 * (s - sp), over);
     if constexpr (TAU) tau = tau + dt;
     j0 = j1; a0 = a1; S0 = S1;
     sp = s;
     steps++;
   }
-  SlotOutT<T, TAU> o;
+  SlotOutT<T, TAU, CHK> o;
   o.I = I; o.j0 = j0; o.a0 = a0; o.S0 = S0; o.steps = steps;
   if constexpr (TAU) o.dtau = tau;
+  if constexpr (CHK) o.over = over;
   return o;
 }
 

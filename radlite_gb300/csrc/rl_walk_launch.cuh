@@ -1,8 +1,10 @@
 // rl_walk_launch.cuh -- the walk kernels (one model; many jobs from one queue) and their
 // launchers, templated on the channel slots per lane C and on TAU: whether the walk also
 // keeps each integrated channel's optical depth along the ray (compensated) in
-// WalkParams::tau / tauc, which the gradient sweep of the differentiable path reads. The
-// plain instances live in rl_kernels.cu, the TAU instances in rl_walk_tau.cu.
+// WalkParams::tau / tauc, which the gradient sweep of the differentiable path reads, and on
+// CHK: whether it counts the steps that fail the reference's overshoot test. The plain
+// instances live in rl_kernels.cu, the TAU instances in rl_walk_tau.cu, the CHK ones in
+// rl_walk_chk.cu.
 #pragma once
 #include <cuda_runtime.h>
 #include "rl_device.h"
@@ -10,7 +12,7 @@
 
 namespace rl {
 
-template <typename T, int C, bool TAU>
+template <typename T, int C, bool TAU, bool CHK = false>
 __global__ void __launch_bounds__(128, WalkMinBlocks<T>::value) k_walk(WalkParams<T> P) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -22,7 +24,7 @@ __global__ void __launch_bounds__(128, WalkMinBlocks<T>::value) k_walk(WalkParam
     if (lane == 0) item = atomicAdd(P.work, 1);
     item = __shfl_sync(0xffffffffu, item, 0);
     if (item >= P.nitems) break;
-    walk_item<T, C, false, TAU>(P, item, *W.S, *W.SS, *W.SW, W.list, lane, steps);
+    walk_item<T, C, false, TAU, CHK>(P, item, *W.S, *W.SS, *W.SW, W.list, lane, steps);
   }
   flush_counters(steps, *W.SW, P.counters, lane);
 }
@@ -61,16 +63,16 @@ __global__ void __launch_bounds__(128, WalkMinBlocks<T>::value) k_walk_jobs(Walk
   flush_counters(steps, *W.SW, B.counters, lane);
 }
 
-template <typename T, int C, bool TAU>
+template <typename T, int C, bool TAU, bool CHK = false>
 cudaError_t launch_walk_c(const WalkParams<T>& P, int nsm, cudaStream_t s) {
   const int warps = 4, threads = warps * 32;
   const int capp = (kItemLines * P.nfr + 7) & ~7;
   const size_t smem = (sizeof(WarpStage<T>) + sizeof(SlotState<T, C>) + sizeof(SubWork<T>)) * warps +
                       (kListInSmem ? sizeof(unsigned short) * (size_t)capp * warps : 0);
-  cudaError_t e = cudaFuncSetAttribute(k_walk<T, C, TAU>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = cudaFuncSetAttribute(k_walk<T, C, TAU, CHK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_walk<T, C, TAU>, threads, smem);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_walk<T, C, TAU, CHK>, threads, smem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
   if (per_sm > kWalkBlocksPerSm) per_sm = kWalkBlocksPerSm;   // the list scratch holds this many
@@ -78,7 +80,7 @@ cudaError_t launch_walk_c(const WalkParams<T>& P, int nsm, cudaStream_t s) {
   const long long need = ((long long)P.nitems + warps - 1) / warps;
   if (blocks > need) blocks = need;
   if (blocks < 1) blocks = 1;
-  k_walk<T, C, TAU><<<(unsigned)blocks, threads, smem, s>>>(P);
+  k_walk<T, C, TAU, CHK><<<(unsigned)blocks, threads, smem, s>>>(P);
   return cudaGetLastError();
 }
 
@@ -104,13 +106,13 @@ cudaError_t launch_walk_jobs_c(const WalkJobs<T>& B, int nsm, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-template <typename T, bool TAU>
+template <typename T, bool TAU, bool CHK = false>
 cudaError_t launch_walk_t(const WalkParams<T>& P, int cpl, int nsm, cudaStream_t s) {
   switch (cpl) {
-    case 1: return launch_walk_c<T, 1, TAU>(P, nsm, s);
-    case 2: return launch_walk_c<T, 2, TAU>(P, nsm, s);
-    case 4: return launch_walk_c<T, 4, TAU>(P, nsm, s);
-    default: return launch_walk_c<T, 8, TAU>(P, nsm, s);
+    case 1: return launch_walk_c<T, 1, TAU, CHK>(P, nsm, s);
+    case 2: return launch_walk_c<T, 2, TAU, CHK>(P, nsm, s);
+    case 4: return launch_walk_c<T, 4, TAU, CHK>(P, nsm, s);
+    default: return launch_walk_c<T, 8, TAU, CHK>(P, nsm, s);
   }
 }
 

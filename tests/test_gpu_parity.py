@@ -119,7 +119,7 @@ def test_executable(gpu_lib, model_dir, tmp_path):
     assert r.returncode == 0, r.stderr
     assert os.path.exists(os.path.join(d, "linespectrum_moldata.dat"))
     log = open(os.path.join(d, "radlite.log")).read()
-    assert "RUN OF RADICAL" in log and "Finished" in log
+    assert "RUN OF RADICAL" in log and "Finishing Date" in log and "END OF RUN RADLITE" in log
     # a SAVE_IMCIR build's circular images beside the spectrum
     r = subprocess.run([gpu_lib.EXE_PATH, "--save-imcir", d], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
