@@ -80,3 +80,14 @@ def test_batch_and_diff_entry_points_check_arguments(gpu_lib):
     assert L.rl_run_dir_ex(b".", 0, 8, None) == -1 and "unknown flags" in gpu_lib._err()
     assert L.rl_posvel(None, 1, 1, None, None, None) == -1
     assert L.rl_gen_spec(None, None, None, None, None, None, None, None, None) == -1
+
+
+def test_checks_setter(gpu_lib, model_dir):
+    """rl_set_checks takes RL_CHECK_OVERSHOOT or 0 on a host-only model and rejects unknown
+    flags and a null model (no GPU needed)."""
+    m = gpu_lib.load_dir_host(model_dir("tiny_line"))
+    m.set_checks(True)
+    m.set_checks(False)
+    L = gpu_lib.lib()
+    assert L.rl_set_checks(m.h, 2) == -1 and "unknown flags" in gpu_lib._err()
+    assert L.rl_set_checks(None, 1) == -1 and "null" in gpu_lib._err()
