@@ -91,3 +91,33 @@ def test_checks_setter(gpu_lib, model_dir):
     L = gpu_lib.lib()
     assert L.rl_set_checks(m.h, 2) == -1 and "unknown flags" in gpu_lib._err()
     assert L.rl_set_checks(None, 1) == -1 and "null" in gpu_lib._err()
+
+
+def _header_struct(name):
+    """Field (name, C type) pairs of `typedef struct name { ... } name;` in rlgpu.h."""
+    src = open(os.path.join(ROOT, "include", "rlgpu.h")).read()
+    body = re.search(r"typedef struct %s \{(.*?)\} %s;" % (name, name), src, flags=re.S).group(1)
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    out = []
+    for decl in body.split(";"):
+        decl = " ".join(decl.split())
+        if not decl:
+            continue
+        m = re.match(r"(unsigned long long|double|int|const double\*|const int\*|const char\*) (.*)", decl)
+        assert m, decl
+        out += [(f.strip(), m.group(1)) for f in m.group(2).split(",")]
+    return out
+
+
+@pytest.mark.parametrize("cname,pyname", [("rl_stats", "Stats"), ("rl_model_info", "ModelInfo"),
+                                          ("rl_model_arrays", "ModelArrays"), ("rl_posvel_spec", "PosvelSpec"),
+                                          ("rl_genspec_lines", "GenspecLines"),
+                                          ("rl_genspec_params", "GenspecParams")])
+def test_struct_mirrors_match_header(gpu_lib, cname, pyname):
+    """Each ctypes mirror of a structure of rlgpu.h has its fields, in order, with the same
+    types."""
+    import ctypes as C
+    ctype = {"unsigned long long": C.c_ulonglong, "double": C.c_double, "int": C.c_int,
+             "const double*": C.POINTER(C.c_double), "const int*": C.POINTER(C.c_int), "const char*": C.c_char_p}
+    want = [(n, ctype[t]) for n, t in _header_struct(cname)]
+    assert list(getattr(gpu_lib, pyname)._fields_) == want
