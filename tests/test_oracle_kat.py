@@ -117,3 +117,34 @@ def test_geometry_properties(oracle_lib, model_dir):
         assert np.all(t["r"] <= r[-1] * (1 + 1e-9)) and np.all(t["r"] >= r[0] * (1 - 1e-9))
         assert np.all((t["icr"] >= 1) & (t["icr"] <= 3))
         assert np.all(np.abs(t["mu"]) <= 1.0)
+
+
+def test_isothermal_lte_slab_law(oracle_lib, tmp_path):
+    """One gas temperature everywhere, LTE populations, no dust: the source function
+    j/alpha is the same at every node and every SUBGRID point (the interpolation keeps the
+    population ratio), and the linear-source step gives q = (1 - x) S exactly, which the
+    bracket at the theoretical maximum never clips (1 - e^-dtau <= dtau). Every ray and
+    channel then satisfies I = S (1 - e^-tau) with its own char_tau, however the walk
+    sub-steps, and S is the Planck function at the line frequency and that temperature
+    (to the 1e-5 of the physical constants' variants)."""
+    cfg = synth.config_by_name("tiny_line", t_pow=0.0, kappa_abs=0.0, nlines=1)
+    d = synth.write_model(cfg, str(tmp_path / "m"))
+    o = oracle_lib.Oracle(d)
+    x0, z0, _, _ = o.rays()
+    ratios, thick = [], 0
+    for k in range(0, len(x0), 23):
+        I, tau = o.ray_spectrum(cfg.ilinestart, x0[k], z0[k])
+        sel = tau > 1e-4
+        ratios.append(I[sel] / -np.expm1(-tau[sel]))
+        thick += int(np.sum(tau > 3.0))
+    r = np.concatenate(ratios)
+    assert r.size > 100 and thick > 0          # thin and thick channels both present
+    S = float(np.mean(r))
+    assert np.max(np.abs(r / S - 1.0)) <= 1e-7
+    f = synth.make_fields(cfg)
+    u, l, _ = f["lines"][cfg.ilinestart - 1]
+    E = np.round(f["E"], 4)                      # moldata.dat's F12.4 energies
+    nu = (E[u - 1] - E[l - 1]) * 2.99792458e10
+    h, kb, c = 6.62607015e-27, 1.380649e-16, 2.99792458e10
+    B = 2.0 * h * nu ** 3 / c ** 2 / math.expm1(h * nu / (kb * cfg.t0))
+    assert abs(S / B - 1.0) <= 1e-4
