@@ -125,7 +125,8 @@ int rl_model_get_info(rl_model* model, rl_model_info* info);
 int rl_set_camera(rl_model* model, double incl_deg, int nphi, int dbdr, int nrrayextra);
 /* RL_FP32 (default): FP64 geometry, FP32 transfer. RL_FP64: FP64 throughout. */
 int rl_set_precision(rl_model* model, int precision);
-/* Diagnostics of the model's line renders (spectra, images, image rows), off by default.
+/* Diagnostics of the model's own line renders (spectra, images, image rows), off by default;
+   batches (rl_batch_*) and the differentiable path (rl_diff_*) do not take them.
    RL_CHECK_OVERSHOOT: take the reference's overshoot test on every formal-solution step,
    the check its default build compiles in (transfer.F:1548-1553, not SRCQDR_NO_ERRCHECK),
    and count the steps that fail it in rl_stats.overshoots. The results are unchanged; the
