@@ -5,7 +5,7 @@ its own line-of-sight optical depth, whatever the walk's sub-stepping; S is the 
 the oracle's rays give (tests/test_oracle_kat.py pins it to the Planck function).
 
 Measured on a GB300 (1484 channels with tau > 1e-4, 116 of them with tau > 3): FP64 spread
-of I / (1 - e^-tau) 9.3e-9 and S 1e-10 from the oracle's; FP32 spread 4.2e-7 and S 6e-10
+of I / (1 - e^-tau) 9.3e-9 and S 1.4e-12 from the oracle's; FP32 spread 4.2e-7 and S 6.0e-10
 from it. Bounds: spread 1e-7 (FP64) and 4e-6 (FP32), S 1e-8 and 1e-6."""
 import numpy as np
 import pytest
